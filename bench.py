@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Cloth-step throughput of the GB300 engine.
+
+Workload (the batched forward workload): 256 independent cloths, each a
+square grid whose side is drawn from U{16..192} (seeded), per-cloth stiffness
+U[0.5, 1.0], constant wind U[-2, 2] m/s^2 on x and z, two pinned corners,
+10 solver iterations, dt = 1/60 s, self-collision on.  One "step" advances
+every cloth of the batch by one CudaDeformableBody::FixedUpdate.  value =
+cloth-steps/s = cloths x steps / device time.  With --gpus N (torchrun, one
+rank per GPU) every rank steps its own 256-cloth workload (seed + rank): weak
+scaling with no collective on the data path.
+
+Also reported: the plain path (the same engine stepping one cloth per call,
+on a seeded sample of the workload's cloths), e2e through the public API with
+the whole state uploaded from and downloaded to pinned host memory every
+step, the per-phase profile, the roofline of the dominant kernel, sampled SM
+clocks, and the CPU oracle port timed on the host cores.
+
+--impl reference times the reference scheme's CPU restatement (the oracle,
+OpenMP over cloths on every host core) on a bounded sample of the same
+workload: the reference has no CPU implementation of its GPU cloth step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cloth-steps/s, 256 uneven cloths (16..192 side) batched, 10 iterations, self-collision"
+UNIT = "cloth-steps/s"
+NCLOTH = 256
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(parts)
+            except ValueError:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if it covers this kernel/workload."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        t = json.loads(p.read_text())
+        e = t.get(kernel)
+        if e and e.get("workload") == workload:
+            return float(e["bytes_per_launch"])
+    except (ValueError, KeyError):
+        return None
+    return None
+
+
+def algorithmic_bytes(batch, specs, prof) -> dict:
+    """Compulsory DRAM bytes per launch of the hot kernels (the model is
+    written out in the design doc)."""
+    V = sum(s.num_vertices for s in specs)
+    T = sum(s.num_triangles for s in specs)
+    E = B = 0
+    for c in range(len(specs)):
+        e, b = batch.constraint_counts(c)
+        E += e
+        B += b
+    cnt = batch.counters()
+    P, C = cnt["pairs"], cnt["vf"] + cnt["ee"]
+    return {
+        # x read + x write (float4), 2 CSR offsets, one entry per incident
+        # constraint, each constraint record once, contact records + entries
+        "jacobi": 32 * V + 8 * V + 4 * (2 * E + 4 * B) + 16 * E + 20 * B + 16 * 4 * C + 32 * C + 16 * V,
+        # leaf box + pair writes + count, every node record once
+        "traverse": 32 * T + 4 * P + 4 * T + 48 * (2 * T - 1),
+        # pair read, counts + mask written, triangle records, per-vertex state once
+        "narrow": 18 * P + 20 * T + 48 * V,
+        "_sizes": dict(V=V, T=T, E=E, B=B, P=P, C=C),
+    }
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(specs, seed: int, cloths: int = 64, steps: int = 2) -> dict:
+    """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
+    cloths on every host core, on a seeded sample of the workload."""
+    from oracle.oracle_ffi import Oracle, max_threads
+    rng = np.random.default_rng(seed + 7)
+    pick = sorted(rng.choice(len(specs), size=min(cloths, len(specs)), replace=False).tolist())
+    o = Oracle([specs[i] for i in pick], fp64=False)
+    o.step(1)  # warm-up
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": len(pick) * steps / dt, "unit": UNIT, "cores": max_threads(), "kind": "port",
+            "sample": f"{len(pick)} of {len(specs)} cloths (seeded) x {steps} steps after 1 warm-up step, "
+                      f"FP32 oracle port, OpenMP over cloths", "seconds": dt}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from licenta_gb300 import scenes
+    from oracle.oracle_ffi import Oracle, max_threads
+    specs = scenes.batched_cloths(seed=args.seed)
+    rng = np.random.default_rng(args.seed + 11)
+    sample = 32
+    pick = sorted(rng.choice(len(specs), size=sample, replace=False).tolist())
+    o = Oracle([specs[i] for i in pick], fp64=False)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    value = sample * args.steps / dt
+    cores = max_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched-256-uneven", "cloths_per_step": sample, "iterations": 10},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} of 256 cloths (seeded) per step, FP32 restatement of the reference "
+                                   f"GPU scheme (the reference has no CPU implementation of it), OpenMP over cloths"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import torch
+    import torch.distributed as dist
+
+    from licenta_gb300 import ClothBatch, scenes
+
+    torch.cuda.set_device(local)
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    specs = scenes.batched_cloths(seed=args.seed + rank)
+    batch = ClothBatch(specs)
+    stream = torch.cuda.Stream()
+    batch.step(args.warmup, stream)
+    batch.sync()
+
+    # ---- device-timed region ------------------------------------------------
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    batch.step(args.steps, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    batch.sync()
+    value = world * NCLOTH * args.steps / (ms / 1000.0)
+
+    # ---- e2e through the public API: whole state host -> device -> host -----
+    V = sum(s.num_vertices for s in specs)
+    host = [torch.empty((V, 3), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+    batch.read_state(*(h.data_ptr() for h in host), True, stream)
+    torch.cuda.synchronize()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        batch.write_state(*(h.data_ptr() for h in host), True, stream)
+        batch.step(1, stream)
+        batch.read_state(*(h.data_ptr() for h in host), True, stream)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = max_over_ranks(f0.elapsed_time(f1))
+    batch.sync()
+    e2e = {"value": world * NCLOTH * args.steps / (ms_e2e / 1000.0), "unit": UNIT,
+           "h2d_bytes_per_step": 3 * 12 * V, "d2h_bytes_per_step": 3 * 12 * V,
+           "what": "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state"}
+
+    # ---- profile + roofline -------------------------------------------------
+    prof = batch.profile(2, stream)
+    alg = algorithmic_bytes(batch, specs, prof)
+    iters = 10
+    cands = {"jacobi": (prof["jacobi_ms"], prof["jacobi_ms"] * iters),
+             "traverse": (prof["traverse_ms"], prof["traverse_ms"]),
+             "narrow": (prof["narrow_ms"], prof["narrow_ms"])}
+    dom = max(cands, key=lambda k: cands[k][1])
+    launch_ms = cands[dom][0]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = alg[dom] / (launch_ms / 1000.0) / 1e9 if launch_ms > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
+            "traffic": ncu_traffic(dom, "batched-256-uneven"), "algorithmic_bytes_per_launch": alg[dom],
+            "launch_ms": launch_ms}
+
+    # ---- plain path: the same engine one cloth per call ---------------------
+    plain = None
+    if not args.no_plain:
+        rng = np.random.default_rng(args.seed + 3)
+        pick = rng.choice(len(specs), size=16, replace=False)
+        tot_ms = 0.0
+        for i in pick:
+            b1 = ClothBatch([specs[int(i)]])
+            b1.step(args.warmup, stream)
+            b1.sync()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            b1.step(args.steps, stream)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            tot_ms += g0.elapsed_time(g1)
+            b1.close()
+        plain_value = 16 * args.steps / (tot_ms / 1000.0)
+        plain = {"value": plain_value, "unit": UNIT, "sample": "16 of the 256 cloths (seeded), one cloth per step call",
+                 "batched_over_plain": (value / world) / plain_value}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(specs, args.seed)
+
+    T = sum(s.num_triangles for s in specs)
+    state_mb = (V * 16 * 5) / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded cloths, reference mesh topology)",
+        "config": {"workload": "batched-256-uneven", "global_batch": world * NCLOTH, "cloths_per_gpu": NCLOTH,
+                   "vertices_per_gpu": V, "triangles_per_gpu": T, "iterations": 10, "dt": 1.0 / 60.0,
+                   "parallelism": f"shard-by-cloth x{world}",
+                   "l2": f"inputs larger than L2 (vertex state {state_mb:.0f} MB + constraints + pair buffers)"},
+        "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "e2e": e2e,
+        "gpu_launches": int(prof["kernels_per_step"]) * args.steps,
+        "profile": {"phases_ms": prof["phases"], "jacobi_ms": prof["jacobi_ms"], "traverse_ms": prof["traverse_ms"],
+                    "narrow_ms": prof["narrow_ms"], "sort_ms": prof["sort_ms"], "kernels_per_step": prof["kernels_per_step"],
+                    "sizes": alg["_sizes"]},
+        "plain": plain,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

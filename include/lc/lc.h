@@ -1,0 +1,273 @@
+/*
+ * lc.h — C ABI of the GB300 cloth-step engine (PBD + LBVH self-collision).
+ *
+ * Every entry point replaces one piece of the reference's GPU cloth body
+ * (Tureyz/Licenta, paths relative to LicentaV2/LicentaV2/):
+ *
+ *   Physics::CudaDeformableBody ctor      Physics/CudaDeformableBody.h:23-24, .cpp:30-285
+ *   Physics::CudaDeformableBody::FixedUpdate   Physics/CudaDeformableBody.cpp:550-627
+ *   Physics::CudaDeformableBody::Update        Physics/CudaDeformableBody.cpp:629-638
+ *   Physics::CudaDeformableBody::SetSpherePos  Physics/CudaDeformableBody.cpp:640-643
+ *   CudaBVH::GenerateBVH2 / ComputeTreeAABBs / GetAABBCollisions
+ *                                          Collision/CudaBVH.cuh:15-33, Collision/CudaBVH.cu:9-188
+ *   DeformableUtils::CreateTriangleTests / CCDTriangleTests
+ *                                          Collision/CudaCollisionDetection.cuh:28-46
+ *
+ * Conventions: plain C PODs, explicit stream (a cudaStream_t passed as void*,
+ * NULL = legacy default stream), every call returns lc_status, no exception
+ * crosses the boundary.  A handle is thread-compatible (one host thread at a
+ * time), not thread-safe.  Device-side failures (capacity overflow, a
+ * traversal stack overflow) are latched in a device error word and reported
+ * by the next call that synchronises (lc_batch_sync, any *_get_* call).
+ */
+#ifndef LC_LC_H
+#define LC_LC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lc_status {
+    LC_OK = 0,
+    LC_ERR_INVALID_ARG = 1,
+    LC_ERR_OOM = 2,
+    LC_ERR_CAPACITY_OVERFLOW = 3,
+    LC_ERR_TIMEOUT = 4,
+    LC_ERR_CUDA = 5,
+    LC_ERR_NOT_SUPPORTED = 6,
+    LC_ERR_STACK_OVERFLOW = 7
+} lc_status;
+
+/* Morton encodings.  REF63: 21 bits per axis of x*2^21 clamped to
+ * [0, 2^21-1], the live encoder of Core/CudaUtils.cu:278-287,310-325.
+ * K30: 10 bits per axis (x*2^10 clamped to [0,1023]), the commented-out
+ * 30-bit encoder of Core/CudaUtils.cu:289-308. */
+enum { LC_MORTON_REF63 = 0, LC_MORTON_K30 = 1 };
+
+/*
+ * Cloth parameters.  The first block is field-for-field
+ * Physics::ClothParams (Physics/Structs.h:23-61) minus its device vector of
+ * pinned flags (passed in lc_cloth_desc.pinned instead); the second block
+ * holds what the reference hard-codes or leaves implicit.
+ */
+typedef struct lc_cloth_params {
+    float timestep;
+    float kFriction;
+    float kStretch;
+    float kShear;            /* stored, unused by the live step (as in the reference) */
+    float kBend;
+    float kDamp;
+    float kSpringDamp;       /* stored, unused by the live step */
+    float thickness;
+    float objectMass;
+    float globalVelDamp;
+    float strainLimit;
+    float gravity[3];
+    float minWindDir[3];
+    float startWindDir[3];
+    float maxWindDir[3];
+    float windMinVariation;
+    float windMaxVariation;
+    int32_t windOn;
+    float worldMin[3];
+    float worldMax[3];
+    int32_t dims[2];         /* informational; vertex count comes from the mesh */
+    int32_t solverIterations;
+    int32_t ccdIterations;   /* stored, unused by the live step */
+    int32_t BVHChunkSize;
+    uint64_t benchmarkSample;
+    int32_t useTriangleBending;
+    int32_t colorContacts;
+    int32_t useFriction;
+
+    /* --- not in ClothParams --- */
+    int32_t thicknessFromMesh;  /* 1: thickness = |x0 - x1| / 3 (Physics/CudaDeformableBody.cpp:86) */
+    int32_t mortonMode;         /* LC_MORTON_REF63 (default) or LC_MORTON_K30 */
+    int32_t refLeafAabbQuirk;   /* 1 (default): leaf k keeps the AABB of pre-sort slot k (reference behaviour) */
+    int32_t groundOn;           /* 1: ground constraints at worldMin.y + thickness (reference always on) */
+    float mortonOrigin[3];      /* Morton input = (p - origin) * scale; identity = (0,0,0), 1 */
+    float mortonScale;
+    uint64_t windSeed;          /* seeds the wind-variation draw that the reference takes from std::rand() */
+    int32_t sphereOn;           /* analytic sphere of CudaPBD::SetSpherePos (Physics/CudaPBD.cu:460-472) */
+    float spherePos[3];
+    float sphereRadius;
+} lc_cloth_params;
+
+/* One cloth: the constructor arguments of Physics::CudaDeformableBody. */
+typedef struct lc_cloth_desc {
+    int32_t num_vertices;
+    int32_t num_triangles;
+    const float *positions;   /* 3 * num_vertices, host memory */
+    const uint32_t *indices;  /* 3 * num_triangles, host memory */
+    const uint8_t *pinned;    /* num_vertices flags (fixedVerts), may be NULL */
+    lc_cloth_params params;
+} lc_cloth_desc;
+
+/* Capacities of the per-step device buffers; 0 picks the default. */
+typedef struct lc_batch_options {
+    uint64_t vf_capacity;     /* VF contacts kept per step over the whole batch (default 8 * total triangles) */
+    uint64_t ee_capacity;     /* EE contacts kept per step (default 8 * total triangles) */
+    int32_t use_graph;        /* 1 (default): capture one step in a CUDA graph and replay it */
+    int32_t debug_capture;    /* 1: keep intermediate buffers of the last step for lc_batch_debug_get */
+    int32_t solver_variant;   /* 0 = auto (cluster when every cloth fits on chip), 1 = per-vertex gather
+                                 over global memory, 2 = cluster on-chip */
+    int32_t block_size;       /* block size of the global-memory Jacobi kernel (0 = default) */
+    uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull (default 8 * total triangles) */
+} lc_batch_options;
+
+typedef struct lc_batch lc_batch;
+
+/* Fills the reference defaults of Managers/MastersSimulationManager.cpp:33-62
+ * (with gravity, dims and wind as that file sets them) plus the extension
+ * defaults above. */
+void lc_default_params(lc_cloth_params *out);
+void lc_default_options(lc_batch_options *out);
+
+/* Builds the device state of num_cloths independent cloths (constraints,
+ * LRA, feature ownership, initial triangles/normals) — the work of the
+ * CudaDeformableBody constructor and CudaPBD::Init (Physics/CudaPBD.cu:39-275)
+ * for each cloth, packed behind one offset table. */
+lc_status lc_batch_create(const lc_cloth_desc *descs, int32_t num_cloths,
+                          const lc_batch_options *opts, lc_batch **out);
+lc_status lc_batch_destroy(lc_batch *b);
+
+/* nsteps x CudaDeformableBody::FixedUpdate for every cloth of the batch, in
+ * one launch sequence per step (asynchronous on stream). */
+lc_status lc_batch_step(lc_batch *b, int32_t nsteps, void *stream);
+
+/* Waits for the stream work of the batch and reports latched device errors. */
+lc_status lc_batch_sync(lc_batch *b);
+
+lc_status lc_batch_num_cloths(const lc_batch *b, int32_t *out);
+lc_status lc_batch_cloth_sizes(const lc_batch *b, int32_t cloth, int32_t *num_vertices,
+                               int32_t *num_triangles);
+
+/* State of one cloth as float3 arrays (3 * V floats each); any pointer may be
+ * NULL.  x = m_dPositions, x_prev = m_dPrevPositions, v = m_dVelocities,
+ * vn = m_dAccumulatedVertexNormals.  *_host = 1 for host memory. */
+lc_status lc_batch_get_state(lc_batch *b, int32_t cloth, float *x, float *x_prev, float *v,
+                             float *vn, int32_t is_host);
+lc_status lc_batch_set_state(lc_batch *b, int32_t cloth, const float *x, const float *x_prev,
+                             const float *v, const float *vn, int32_t is_host);
+
+/* Triangle order (slot -> original triangle id) that persists between steps
+ * because the Morton sort permutes the triangle array in place
+ * (Physics/CudaDeformableUtils.cu:346-349). */
+lc_status lc_batch_get_triangle_order(lc_batch *b, int32_t cloth, uint32_t *perm);
+lc_status lc_batch_set_triangle_order(lc_batch *b, int32_t cloth, const uint32_t *perm);
+
+/* Positions of every cloth, packed in cloth order (3 floats per vertex) into
+ * host or device memory: the copy-out of CudaDeformableBody::Update /
+ * FinalVertUpdate (Physics/CudaDeformableBody.cpp:473-495), which publishes
+ * m_dPrevPositions.  Asynchronous on stream when dst is pinned or device memory. */
+lc_status lc_batch_read_positions(lc_batch *b, float *dst, int32_t is_host, void *stream);
+
+/* Whole-batch state in one call each way, packed in cloth order (3 floats
+ * per vertex per array; NULL arrays are skipped).  Asynchronous on stream;
+ * host memory should be pinned.  Used by callers that keep the cloth state on
+ * the host between steps. */
+lc_status lc_batch_write_state(lc_batch *b, const float *x, const float *x_prev, const float *v,
+                               int32_t is_host, void *stream);
+lc_status lc_batch_read_state(lc_batch *b, float *x, float *x_prev, float *v, int32_t is_host,
+                              void *stream);
+
+/* Per-phase timing of nsteps eager steps with CUDA events, using the seven
+ * phase labels of the reference's GPUBenchmark (Simulation/GPUBenchmark.cu:14-77,
+ * labels at Physics/CudaDeformableBody.cpp:556-594), plus the mean duration of
+ * single launches of the hot kernels.  All times in milliseconds per step or
+ * per launch. */
+typedef struct lc_profile {
+    float phase_ms[7];        /* 1 External, 2 Update Triangles, 3 Build BVH, 4 Create Triangle Tests,
+                                 5 Perform Triangle Tests, 6 PBD Solver, 7 PBD Integration */
+    float jacobi_ms;          /* one Jacobi iteration launch */
+    float traverse_ms;        /* one traversal launch */
+    float narrow_ms;          /* candidate + CCD count launch */
+    float sort_ms;            /* whole segmented sort */
+    float step_ms;            /* sum of the phases */
+    uint32_t kernels_per_step;
+    float solver_ms;          /* whole solver (set-up + iterations + integration on the cluster path) */
+    int32_t solver_variant;   /* 1 = per-vertex gather, 2 = cluster on-chip */
+    int32_t cluster_size;     /* CTAs per cloth on the cluster path */
+} lc_profile;
+lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile *out);
+
+/* CudaPBD::SetSpherePos for one cloth (Physics/CudaPBD.cu:460-472). */
+lc_status lc_batch_set_sphere(lc_batch *b, int32_t cloth, const float pos[3], float radius);
+
+/* Per-constraint stiffness override (stretch: E values, bend: B values). */
+lc_status lc_batch_set_stiffness(lc_batch *b, int32_t cloth, const float *k_stretch,
+                                 const float *k_bend);
+lc_status lc_batch_constraint_counts(const lc_batch *b, int32_t cloth, int32_t *num_stretch,
+                                     int32_t *num_bend);
+
+/* Intermediate buffers of the last step (needs options.debug_capture).
+ * Writes at most cap elements into dst (host memory) and the element count
+ * into *count. */
+enum {
+    LC_DBG_PRED_X = 1,        /* float3 per vertex: x after PBDStepExternal */
+    LC_DBG_PRED_XPREV = 2,    /* float3 per vertex: x_prev after PBDStepExternal */
+    LC_DBG_PRED_V = 3,        /* float3 per vertex: v after PBDStepExternal */
+    LC_DBG_PERM_BEFORE = 4,   /* u32 per slot: triangle order before the sort */
+    LC_DBG_MORTON = 5,        /* u64 per slot: sorted Morton codes */
+    LC_DBG_PERM = 6,          /* u32 per slot: triangle order after the sort */
+    LC_DBG_LEFTS = 7,         /* i32 per internal node */
+    LC_DBG_RIGHTS = 8,
+    LC_DBG_PARENTS = 9,       /* i32 per node (2T-1) */
+    LC_DBG_RML = 10,          /* i32 pair per internal node: rightmost leaf of left/right child */
+    LC_DBG_NODE_AABB = 11,    /* 6 floats per node: min xyz, max xyz */
+    LC_DBG_PAIRS = 12,        /* u32 pair per broadphase pair (leaf i, leaf j) */
+    LC_DBG_VF = 13,           /* lc_contact per vertex-face contact */
+    LC_DBG_EE = 14,           /* lc_contact per edge-edge contact */
+    LC_DBG_FEATURES = 15,     /* u8 per original triangle: ownership bits */
+    /* Discrete decisions of the last step, so that a checker can replay them
+     * (contact sets frozen): */
+    LC_DBG_GROUND = 16,       /* u8 per vertex: ground constraint created (Physics/CudaPBD.cu:1490) */
+    LC_DBG_GROUND_ACTIVE = 17,/* u32 per vertex: bit it = ground term counted in iteration it (:1612) */
+    LC_DBG_LRA = 18,          /* u8 per vertex x pinned vertex: attachment active (:1588) */
+    LC_DBG_DYN_ACTIVE = 19,   /* u8 per iteration x (VF contacts, then EE contacts) x 4 slots:
+                                 correction non-zero, i.e. counted (:1466) */
+    LC_DBG_SPHERE = 20        /* i8 per vertex: ray-sphere outcome -1/0/1 (:1523) */
+};
+
+/* A contact as the solver consumes it: the ids/weights of
+ * Physics::PrimitiveContact (Physics/Structs.h:106-129). */
+typedef struct lc_contact {
+    int32_t v[4];
+    float w[4];
+} lc_contact;
+
+lc_status lc_batch_debug_get(lc_batch *b, int32_t cloth, int32_t what, void *dst, uint64_t cap,
+                             uint64_t *count);
+
+/* Device counters of the last step: [0] pairs, [1] VF contacts, [2] EE
+ * contacts, [3] pairs dropped by the per-leaf chunk cap (the reference drops
+ * them silently, Collision/CudaBVH.cu:69-92). */
+lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]);
+
+/* ----- standalone LBVH (the GenerateBVH2 / ComputeTreeAABBs /
+ * GetAABBCollisions chain of Collision/CudaBVH.cu over caller triangles) --- */
+typedef struct lc_lbvh lc_lbvh;
+/* tri_min/tri_max: 3 * T floats each (device memory); builds Morton codes of
+ * the box midpoints, sorts, builds and refits the tree. */
+lc_status lc_lbvh_create(int32_t max_triangles, int32_t chunk_size, int32_t morton_mode,
+                         lc_lbvh **out);
+lc_status lc_lbvh_build(lc_lbvh *h, const float *tri_min, const float *tri_max,
+                        int32_t num_triangles, void *stream);
+/* Broadphase pairs (leaf i, leaf j), i < j, in the reference's order; pairs
+ * are indices into the sorted order.  out_pairs: device memory, 2 * cap u32. */
+lc_status lc_lbvh_pairs(lc_lbvh *h, uint32_t *out_pairs, uint64_t cap, uint64_t *count,
+                        void *stream);
+lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream);
+lc_status lc_lbvh_destroy(lc_lbvh *h);
+
+const char *lc_last_error_string(void);
+const char *lc_status_string(lc_status s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LC_LC_H */

@@ -1,0 +1,251 @@
+"""Python side of the engine: a batch of cloths, the reference's body
+interface on top of it, and the standalone LBVH.
+
+``CudaDeformableBody`` mirrors Physics::CudaDeformableBody
+(Physics/CudaDeformableBody.h:18-28): constructed from the vertex array, the
+index array, the parameters and the pinned flags; ``FixedUpdate`` runs one
+step (Physics/CudaDeformableBody.cpp:550-627) and ``Update`` writes the
+positions back into the caller's vertex array as FinalVertUpdate does
+(:473-495).  Every call goes through the C ABI of include/lc/lc.h; there is no
+CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _ffi
+from .scenes import ClothSpec
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _stream_handle(stream) -> C.c_void_p | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    h = getattr(stream, "cuda_stream", None)  # torch.cuda.Stream
+    return C.c_void_p(h) if h is not None else None
+
+
+class ClothBatch:
+    """Many independent cloths stepped together (one launch sequence per step)."""
+
+    def __init__(self, specs: Sequence[ClothSpec], *, use_graph: bool = True, debug_capture: bool = False,
+                 vf_capacity: int = 0, ee_capacity: int = 0, block_size: int = 0, solver_variant: int = 0):
+        L = _ffi.lib()
+        self.specs = list(specs)
+        self._keep = []
+        descs = (_ffi.ClothDesc * len(self.specs))()
+        for k, s in enumerate(self.specs):
+            pos = np.ascontiguousarray(s.positions, dtype=np.float32)
+            idx = np.ascontiguousarray(s.indices, dtype=np.uint32)
+            pin = np.ascontiguousarray(s.pinned, dtype=np.uint8)
+            self._keep += [pos, idx, pin]
+            descs[k].num_vertices = pos.shape[0]
+            descs[k].num_triangles = idx.shape[0]
+            descs[k].positions = pos.ctypes.data_as(C.POINTER(C.c_float))
+            descs[k].indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+            descs[k].pinned = pin.ctypes.data_as(C.POINTER(C.c_uint8))
+            descs[k].params = s.params
+        opt = _ffi.default_options()
+        opt.use_graph = 1 if use_graph else 0
+        opt.debug_capture = 1 if debug_capture else 0
+        opt.vf_capacity = vf_capacity
+        opt.ee_capacity = ee_capacity
+        opt.block_size = block_size
+        opt.solver_variant = solver_variant
+        h = C.c_void_p()
+        _ffi.check(L.lc_batch_create(descs, len(self.specs), C.byref(opt), C.byref(h)), "lc_batch_create")
+        self._h = h
+        self._keep.clear()
+        self.num_vertices = [s.num_vertices for s in self.specs]
+        self.num_triangles = [s.num_triangles for s in self.specs]
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _ffi.lib().lc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- stepping -----------------------------------------------------------
+    def step(self, nsteps: int = 1, stream=None) -> None:
+        _ffi.check(_ffi.lib().lc_batch_step(self._h, nsteps, _stream_handle(stream)), "lc_batch_step")
+
+    def sync(self) -> None:
+        _ffi.check(_ffi.lib().lc_batch_sync(self._h), "lc_batch_sync")
+
+    # -- state --------------------------------------------------------------
+    def get_state(self, cloth: int) -> dict:
+        V = self.num_vertices[cloth]
+        out = {k: np.empty((V, 3), dtype=np.float32) for k in ("x", "x_prev", "v", "vn")}
+        _ffi.check(_ffi.lib().lc_batch_get_state(self._h, cloth, _ptr(out["x"]), _ptr(out["x_prev"]), _ptr(out["v"]),
+                                                 _ptr(out["vn"]), 1), "lc_batch_get_state")
+        return out
+
+    def set_state(self, cloth: int, x=None, x_prev=None, v=None, vn=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (x, x_prev, v, vn)]
+        _ffi.check(_ffi.lib().lc_batch_set_state(self._h, cloth, *[_ptr(a) for a in arrs], 1), "lc_batch_set_state")
+
+    def triangle_order(self, cloth: int) -> np.ndarray:
+        out = np.empty(self.num_triangles[cloth], dtype=np.uint32)
+        _ffi.check(_ffi.lib().lc_batch_get_triangle_order(self._h, cloth, _ptr(out)), "get_triangle_order")
+        return out
+
+    def set_triangle_order(self, cloth: int, perm) -> None:
+        p = np.ascontiguousarray(perm, dtype=np.uint32)
+        _ffi.check(_ffi.lib().lc_batch_set_triangle_order(self._h, cloth, _ptr(p)), "set_triangle_order")
+
+    def read_positions(self, out: np.ndarray | None = None, stream=None) -> np.ndarray:
+        """Positions of every cloth, packed in cloth order (the Update() copy-out)."""
+        if out is None:
+            out = np.empty((sum(self.num_vertices), 3), dtype=np.float32)
+        _ffi.check(_ffi.lib().lc_batch_read_positions(self._h, _ptr(out), 1, _stream_handle(stream)),
+                   "lc_batch_read_positions")
+        return out
+
+    def read_positions_to(self, dst_ptr: int, is_host: bool, stream=None) -> None:
+        _ffi.check(_ffi.lib().lc_batch_read_positions(self._h, C.c_void_p(dst_ptr), 1 if is_host else 0,
+                                                      _stream_handle(stream)), "lc_batch_read_positions")
+
+    def write_state(self, x: int | None, x_prev: int | None, v: int | None, is_host: bool, stream=None) -> None:
+        """Upload the whole batch state from packed float3 arrays (raw pointers)."""
+        vp = lambda a: None if a is None else C.c_void_p(a)
+        _ffi.check(_ffi.lib().lc_batch_write_state(self._h, vp(x), vp(x_prev), vp(v), 1 if is_host else 0,
+                                                   _stream_handle(stream)), "lc_batch_write_state")
+
+    def read_state(self, x: int | None, x_prev: int | None, v: int | None, is_host: bool, stream=None) -> None:
+        vp = lambda a: None if a is None else C.c_void_p(a)
+        _ffi.check(_ffi.lib().lc_batch_read_state(self._h, vp(x), vp(x_prev), vp(v), 1 if is_host else 0,
+                                                  _stream_handle(stream)), "lc_batch_read_state")
+
+    def profile(self, nsteps: int = 1, stream=None) -> dict:
+        p = _ffi.Profile()
+        _ffi.check(_ffi.lib().lc_batch_profile(self._h, nsteps, _stream_handle(stream), C.byref(p)),
+                   "lc_batch_profile")
+        return dict(phases=dict(zip(_ffi.PHASES, list(p.phase_ms))), jacobi_ms=p.jacobi_ms,
+                    traverse_ms=p.traverse_ms, narrow_ms=p.narrow_ms, sort_ms=p.sort_ms, step_ms=p.step_ms,
+                    kernels_per_step=p.kernels_per_step, solver_ms=p.solver_ms, solver_variant=p.solver_variant,
+                    cluster_size=p.cluster_size)
+
+    def set_sphere(self, cloth: int, pos, radius: float) -> None:
+        p = (C.c_float * 3)(*[float(v) for v in pos])
+        _ffi.check(_ffi.lib().lc_batch_set_sphere(self._h, cloth, p, float(radius)), "lc_batch_set_sphere")
+
+    def constraint_counts(self, cloth: int) -> tuple[int, int]:
+        a, b = C.c_int32(), C.c_int32()
+        _ffi.check(_ffi.lib().lc_batch_constraint_counts(self._h, cloth, C.byref(a), C.byref(b)), "constraint_counts")
+        return a.value, b.value
+
+    def set_stiffness(self, cloth: int, k_stretch=None, k_bend=None) -> None:
+        ks = None if k_stretch is None else np.ascontiguousarray(k_stretch, dtype=np.float32)
+        kb = None if k_bend is None else np.ascontiguousarray(k_bend, dtype=np.float32)
+        _ffi.check(_ffi.lib().lc_batch_set_stiffness(self._h, cloth, _ptr(ks), _ptr(kb)), "lc_batch_set_stiffness")
+
+    def counters(self) -> dict:
+        out = (C.c_uint64 * 4)()
+        _ffi.check(_ffi.lib().lc_batch_counters(self._h, out), "lc_batch_counters")
+        return dict(pairs=out[0], vf=out[1], ee=out[2], dropped=out[3])
+
+    # -- debug dumps ----------------------------------------------------------
+    _DT = {1: (np.float32, 3), 2: (np.float32, 3), 3: (np.float32, 3), 4: (np.uint32, 1), 5: (np.uint64, 1),
+           6: (np.uint32, 1), 7: (np.int32, 1), 8: (np.int32, 1), 9: (np.int32, 1), 10: (np.int32, 2),
+           11: (np.float32, 6), 12: (np.uint32, 2), 15: (np.uint8, 1), 16: (np.uint8, 1), 17: (np.uint32, 1),
+           18: (np.uint8, 1), 19: (np.uint8, 1), 20: (np.int8, 1)}
+
+    def debug(self, cloth: int, what: str) -> np.ndarray:
+        sel = _ffi.DBG[what]
+        L = _ffi.lib()
+        n = C.c_uint64()
+        _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, None, 0, C.byref(n)), "lc_batch_debug_get")
+        if sel in (13, 14):
+            arr = (_ffi.Contact * max(n.value, 1))()
+            _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, arr, n.value, C.byref(n)), "lc_batch_debug_get")
+            v = np.array([list(arr[i].v) for i in range(n.value)], dtype=np.int32).reshape(-1, 4)
+            w = np.array([list(arr[i].w) for i in range(n.value)], dtype=np.float32).reshape(-1, 4)
+            return v, w
+        dt, width = self._DT[sel]
+        out = np.empty((n.value, width) if width > 1 else (n.value,), dtype=dt)
+        _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, _ptr(out), n.value, C.byref(n)), "lc_batch_debug_get")
+        return out
+
+
+class CudaDeformableBody:
+    """Physics::CudaDeformableBody on the GB300 engine (one-cloth batch).
+
+    verts: (V, 3) float array that ``Update`` writes the published positions
+    into (the reference writes m_dPrevPositions into its VertexFormat array).
+    """
+
+    def __init__(self, verts: np.ndarray, indices: np.ndarray, params: _ffi.ClothParams,
+                 fixed_verts: Iterable[bool], **batch_kw):
+        self.m_verts = verts
+        self.m_indices = np.asarray(indices, dtype=np.uint32).reshape(-1, 3)
+        pinned = np.asarray(list(fixed_verts), dtype=np.uint8)
+        spec = ClothSpec(np.asarray(verts, dtype=np.float32).reshape(-1, 3), self.m_indices, pinned, params)
+        self._batch = ClothBatch([spec], **batch_kw)
+
+    def FixedUpdate(self, stream=None) -> None:
+        self._batch.step(1, stream)
+
+    def Update(self) -> None:
+        self._batch.read_positions(self.m_verts.reshape(-1, 3) if self.m_verts.dtype == np.float32 else None)
+        self._batch.sync()
+
+    def SetSpherePos(self, pos, radius: float) -> None:
+        self._batch.set_sphere(0, pos, radius)
+
+    @property
+    def batch(self) -> ClothBatch:
+        return self._batch
+
+
+class Lbvh:
+    """Standalone LBVH over caller boxes (Collision/CudaBVH.cu chain)."""
+
+    def __init__(self, max_triangles: int, chunk_size: int = 64, morton_mode: int = _ffi.LC_MORTON_REF63):
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().lc_lbvh_create(max_triangles, chunk_size, morton_mode, C.byref(h)), "lc_lbvh_create")
+        self._h = h
+
+    def build(self, bmin_ptr: int, bmax_ptr: int, count: int, stream=None) -> None:
+        _ffi.check(_ffi.lib().lc_lbvh_build(self._h, C.c_void_p(bmin_ptr), C.c_void_p(bmax_ptr), count,
+                                            _stream_handle(stream)), "lc_lbvh_build")
+
+    def pairs(self, out_ptr: int | None, cap: int, stream=None) -> int:
+        n = C.c_uint64()
+        _ffi.check(_ffi.lib().lc_lbvh_pairs(self._h, None if out_ptr is None else C.c_void_p(out_ptr), cap,
+                                            C.byref(n), _stream_handle(stream)), "lc_lbvh_pairs")
+        return n.value
+
+    def sorted_ids(self, out_ptr: int, stream=None) -> None:
+        _ffi.check(_ffi.lib().lc_lbvh_sorted_ids(self._h, C.c_void_p(out_ptr), _stream_handle(stream)),
+                   "lc_lbvh_sorted_ids")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _ffi.lib().lc_lbvh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

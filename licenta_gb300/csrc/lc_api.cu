@@ -1,0 +1,1420 @@
+// lc_api.cu — host side of the engine behind the C ABI of include/lc/lc.h:
+// per-cloth construction (the work of the CudaDeformableBody constructor and
+// CudaPBD::Init), the packed multi-cloth device layout, the launch sequence
+// of one step (CudaDeformableBody::FixedUpdate) with every count kept on the
+// device, CUDA-graph capture/replay, state I/O and debug dumps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "lc_internal.cuh"
+
+namespace lc {
+// launchers (lc_lbvh.cu, lc_step.cu, lc_scan.cu)
+void launch_triangles(const DevPtrs &d, cudaStream_t st);
+void launch_leaves_from_boxes(const DevPtrs &d, const float *bmin, const float *bmax, int T, int mode,
+                              cudaStream_t st);
+void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream_t st);
+void launch_post_sort(const DevPtrs &d, cudaStream_t st);
+void launch_karras(const DevPtrs &d, cudaStream_t st);
+void launch_refit(const DevPtrs &d, cudaStream_t st);
+void launch_traverse(const DevPtrs &d, int block, cudaStream_t st);
+void launch_pair_compact(const DevPtrs &d, cudaStream_t st);
+void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncand, int grid, int stage,
+                   cudaStream_t st);
+void launch_wind(const DevPtrs &d, cudaStream_t st);
+void launch_external(const DevPtrs &d, cudaStream_t st);
+void launch_vertex_normals(const DevPtrs &d, cudaStream_t st);
+void launch_dyn(const DevPtrs &d, const uint32_t *nvf, const uint32_t *nee, int grid, int phase, cudaStream_t st);
+void launch_solver_setup(const DevPtrs &d, bool sphere, cudaStream_t st);
+void launch_jacobi(const DevPtrs &d, const float4 *xa, float4 *xb, int it, const uint32_t *nvf, int block,
+                   cudaStream_t st);
+void launch_integrate(const DevPtrs &d, const float4 *xs, cudaStream_t st);
+void scan_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, uint32_t n_static, uint32_t n_cap,
+              uint32_t *partial, uint32_t *total_out, unsigned long long *total_out64, cudaStream_t st);
+unsigned long long morton3_host(float x, float y, float z, int mode);
+struct ClusterArgs {
+    const int *cl_cloth;
+    const uint32_t *nvf;
+    int chunk_cap;
+};
+cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, int nclusters, cudaStream_t st);
+int cluster_chunk_cap();
+int cluster_max_active(int cs, int chunk_cap);
+}  // namespace lc
+
+using namespace lc;
+
+static thread_local std::string g_last_error;
+
+static lc_status fail(lc_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define LC_CUDA(call)                                                                               \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            return fail(e_ == cudaErrorMemoryAllocation ? LC_ERR_OOM : LC_ERR_CUDA,                 \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+        }                                                                                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Host-side construction of one cloth.
+// ---------------------------------------------------------------------------
+struct HostCloth {
+    int V = 0, T = 0;
+    lc_cloth_params p{};
+    float h = 0, vmass = 0;
+    std::vector<float> pos;
+    std::vector<uint32_t> idx;
+    std::vector<uint8_t> pinned;
+    std::vector<int2> s_ids;
+    std::vector<double> s_l0;
+    std::vector<int4> b_ids;
+    std::vector<int> soff;
+    std::vector<uint32_t> sent;  // kind<<31 | role<<29 | local constraint
+    std::vector<int> fixed;
+    std::vector<float> lra_l0;
+    std::vector<uint8_t> features;
+    std::vector<int> vt_off, vt_idx;
+    std::vector<float> vn0;  // initial vertex normals (3V)
+};
+
+static inline uint64_t ekey(int a, int b) {
+    const uint32_t lo = (uint32_t)std::min(a, b), hi = (uint32_t)std::max(a, b);
+    return ((uint64_t)lo << 32) | hi;
+}
+static inline double pdist(const std::vector<float> &p, int a, int b) {
+    const double dx = (double)p[3 * a] - p[3 * b], dy = (double)p[3 * a + 1] - p[3 * b + 1],
+                 dz = (double)p[3 * a + 2] - p[3 * b + 2];
+    return std::sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// Physics/CudaPBD.cu:289-346 — (p1, p2) shared, p3 / p4 opposite.  The
+// reference's first scan only breaks its inner loop, so p1 ends up as the
+// last vertex of t1 (in t1 order) that t2 shares.
+static void shared_edge(const int t1[3], const int t2[3], int &p1, int &p2, int &p3, int &p4) {
+    p1 = p2 = p3 = p4 = -1;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (t1[i] == t2[j]) { p1 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (t1[i] == t2[j] && t1[i] != p1) { p2 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        if (t1[i] != p1 && t1[i] != p2) { p3 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        if (t2[i] != p1 && t2[i] != p2) { p4 = t2[i]; break; }
+}
+
+static lc_status build_host_cloth(const lc_cloth_desc &d, HostCloth &hc) {
+    if (d.num_vertices < 2 || d.num_triangles < 1 || !d.positions || !d.indices)
+        return fail(LC_ERR_INVALID_ARG, "cloth needs >= 2 vertices, >= 1 triangle, positions and indices");
+    if (d.params.solverIterations < 1 || d.params.timestep <= 0.f || d.params.BVHChunkSize < 1)
+        return fail(LC_ERR_INVALID_ARG, "solverIterations, timestep and BVHChunkSize must be positive");
+    hc.V = d.num_vertices;
+    hc.T = d.num_triangles;
+    hc.p = d.params;
+    hc.pos.assign(d.positions, d.positions + 3 * (size_t)hc.V);
+    hc.idx.assign(d.indices, d.indices + 3 * (size_t)hc.T);
+    for (uint32_t v : hc.idx)
+        if (v >= (uint32_t)hc.V) return fail(LC_ERR_INVALID_ARG, "triangle index out of range");
+    hc.pinned.assign(hc.V, 0);
+    if (d.pinned)
+        for (int i = 0; i < hc.V; ++i) hc.pinned[i] = d.pinned[i] ? 1 : 0;
+    // Physics/CudaDeformableBody.cpp:52,86
+    hc.vmass = d.params.objectMass / (float)hc.V;
+    hc.h = d.params.thicknessFromMesh ? (float)(pdist(hc.pos, 0, 1) / 3.0) : d.params.thickness;
+
+    // Physics/CudaPBD.cu:111-142 — stretch on first sighting of an edge, bend
+    // on the second (which forgets the edge).
+    std::unordered_map<uint64_t, int> open;
+    open.reserve((size_t)hc.T * 2);
+    for (int t = 0; t < hc.T; ++t) {
+        const int tri[3] = {(int)hc.idx[3 * t], (int)hc.idx[3 * t + 1], (int)hc.idx[3 * t + 2]};
+        for (int j = 0; j < 3; ++j) {
+            const int a = tri[j], b = tri[(j + 1) % 3];
+            const uint64_t k = ekey(a, b);
+            auto it = open.find(k);
+            if (it != open.end()) {
+                const int o = it->second;
+                const int t1[3] = {(int)hc.idx[3 * o], (int)hc.idx[3 * o + 1], (int)hc.idx[3 * o + 2]};
+                int p1, p2, p3, p4;
+                shared_edge(t1, tri, p1, p2, p3, p4);
+                hc.b_ids.push_back(make_int4(p1, p2, p3, p4));
+                open.erase(it);
+            } else {
+                open[k] = t;
+                hc.s_ids.push_back(make_int2(a, b));
+                hc.s_l0.push_back(pdist(hc.pos, a, b));
+            }
+        }
+    }
+    const int E = (int)hc.s_ids.size(), B = (int)hc.b_ids.size();
+    for (const int4 &b : hc.b_ids)
+        if (b.x < 0 || b.y < 0 || b.z < 0 || b.w < 0)
+            return fail(LC_ERR_INVALID_ARG, "degenerate triangle pair (repeated vertex) in the mesh");
+    // Physics/CudaPBD.cu:146-233 — per-vertex slots, stretch first then bend.
+    std::vector<int> cnt(hc.V, 0);
+    for (const int2 &s : hc.s_ids) { cnt[s.x]++; cnt[s.y]++; }
+    for (const int4 &b : hc.b_ids) { cnt[b.x]++; cnt[b.y]++; cnt[b.z]++; cnt[b.w]++; }
+    hc.soff.assign(hc.V + 1, 0);
+    for (int i = 0; i < hc.V; ++i) hc.soff[i + 1] = hc.soff[i] + cnt[i];
+    hc.sent.assign(hc.soff[hc.V], 0);
+    std::fill(cnt.begin(), cnt.end(), 0);
+    auto put = [&](int v, uint32_t kind, uint32_t role, uint32_t c) {
+        hc.sent[hc.soff[v] + cnt[v]++] = (kind << 31) | (role << 29) | c;
+    };
+    for (int i = 0; i < E; ++i) { put(hc.s_ids[i].x, 0, 0, i); put(hc.s_ids[i].y, 0, 1, i); }
+    for (int i = 0; i < B; ++i) {
+        put(hc.b_ids[i].x, 1, 0, i); put(hc.b_ids[i].y, 1, 1, i);
+        put(hc.b_ids[i].z, 1, 2, i); put(hc.b_ids[i].w, 1, 3, i);
+    }
+    // Physics/CudaPBD.cu:48-81 — LRA to every pinned vertex.
+    for (int i = 0; i < hc.V; ++i)
+        if (hc.pinned[i]) hc.fixed.push_back(i);
+    const int F = (int)hc.fixed.size();
+    hc.lra_l0.assign((size_t)hc.V * F, 0.f);
+    for (int i = 0; i < hc.V; ++i)
+        for (int j = 0; j < F; ++j)
+            if (!hc.pinned[i])
+                hc.lra_l0[(size_t)i * F + j] =
+                    (float)(pdist(hc.pos, i, hc.fixed[j]) * (1.0 + (double)d.params.strainLimit));
+    // Collision/FeatureList.cu:84-132 — ownership: the reference races with
+    // atomicExch; here the lowest original triangle index owns a feature.
+    hc.features.assign(hc.T, 0);
+    std::vector<uint8_t> vt(hc.V, 0);
+    std::unordered_set<uint64_t> et;
+    et.reserve((size_t)hc.T * 2);
+    for (int t = 0; t < hc.T; ++t) {
+        const int v1 = hc.idx[3 * t], v2 = hc.idx[3 * t + 1], v3 = hc.idx[3 * t + 2];
+        uint8_t f = 0;
+        if (!vt[v1]) { vt[v1] = 1; f |= 1 << 5; }
+        if (!vt[v2]) { vt[v2] = 1; f |= 1 << 4; }
+        if (!vt[v3]) { vt[v3] = 1; f |= 1 << 3; }
+        if (et.insert(ekey(v1, v2)).second) f |= 1 << 2;
+        if (et.insert(ekey(v2, v3)).second) f |= 1 << 1;
+        if (et.insert(ekey(v3, v1)).second) f |= 1 << 0;
+        hc.features[t] = f;
+    }
+    // vertex -> triangles (for the running vertex normals)
+    std::vector<int> tc(hc.V, 0);
+    for (uint32_t v : hc.idx) tc[v]++;
+    hc.vt_off.assign(hc.V + 1, 0);
+    for (int i = 0; i < hc.V; ++i) hc.vt_off[i + 1] = hc.vt_off[i] + tc[i];
+    hc.vt_idx.assign(hc.vt_off[hc.V], 0);
+    std::fill(tc.begin(), tc.end(), 0);
+    for (int t = 0; t < hc.T; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const int v = hc.idx[3 * t + k];
+            hc.vt_idx[hc.vt_off[v] + tc[v]++] = t;
+        }
+    // Initial normals: Physics/CudaDeformableUtils.cu:37-64 (unnormalised face
+    // normals) accumulated and normalised (:190-249).
+    hc.vn0.assign(3 * (size_t)hc.V, 0.f);
+    for (int t = 0; t < hc.T; ++t) {
+        const float *a = &hc.pos[3 * hc.idx[3 * t]], *b = &hc.pos[3 * hc.idx[3 * t + 1]],
+                    *c = &hc.pos[3 * hc.idx[3 * t + 2]];
+        const float3 e1 = f3(b[0] - a[0], b[1] - a[1], b[2] - a[2]);
+        const float3 e2 = f3(c[0] - a[0], c[1] - a[1], c[2] - a[2]);
+        const float3 n = cross(e1, e2);
+        for (int k = 0; k < 3; ++k) {
+            float *o = &hc.vn0[3 * hc.idx[3 * t + k]];
+            o[0] += n.x; o[1] += n.y; o[2] += n.z;
+        }
+    }
+    for (int i = 0; i < hc.V; ++i) {
+        float *o = &hc.vn0[3 * i];
+        const float l = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+        o[0] /= l; o[1] /= l; o[2] /= l;
+    }
+    return LC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The batch.
+// ---------------------------------------------------------------------------
+struct DeviceArena {
+    std::vector<void *> ptrs;
+    ~DeviceArena() {
+        for (void *p : ptrs) cudaFree(p);
+    }
+    template <class T> lc_status alloc(T *&out, size_t n, const char *what) {
+        out = nullptr;
+        if (n == 0) n = 1;
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(LC_ERR_OOM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+        }
+        ptrs.push_back(p);
+        out = (T *)p;
+        return LC_OK;
+    }
+};
+
+#define LC_TRY(x)                     \
+    do {                              \
+        lc_status s_ = (x);           \
+        if (s_ != LC_OK) return s_;   \
+    } while (0)
+
+struct lc_batch {
+    int C = 0;
+    std::vector<HostCloth> hosts;
+    std::vector<ClothDev> cds;
+    lc_batch_options opt{};
+    DevPtrs d{};
+    DeviceArena arena;
+    ClothDev *cloth_dev = nullptr;
+    int *tile_first = nullptr;
+    uint32_t *npairs = nullptr, *nvf = nullptr, *nee = nullptr, *ncand = nullptr;
+    int max_iters = 1;
+    bool any_wind = false, any_sphere = false;
+    int sort_passes = 8;
+    int narrow_grid = 0;
+    int jacobi_block = 256, traverse_block = 128;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    cudaStream_t last_stream = nullptr;
+    std::vector<int> s_count, b_count;  // per cloth
+    std::vector<int> e_off, b_off;
+    // cluster-resident solver (lc_cluster.cu)
+    bool use_cluster = false;
+    int cluster_cs = 8;
+    ClusterArgs ca{};
+    // debug copies
+    float4 *dbg_x = nullptr, *dbg_xp = nullptr, *dbg_v = nullptr;
+    uint32_t *dbg_perm_before = nullptr;
+
+    // global indices of the VF / EE contacts of one cloth (contiguous ranges)
+    lc_status cloth_contacts(int c, bool vf, std::vector<uint64_t> &gidx, std::vector<int4> &iv,
+                             std::vector<float4> &wv);
+
+    ~lc_batch() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+    }
+
+    void invalidate_graph() {
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    }
+
+    lc_status enqueue_step(cudaStream_t st);
+    lc_status setup_cluster();
+
+    // profiling: when non-null, events are recorded at phase boundaries
+    cudaEvent_t *prof_ev = nullptr;    // 8 events per step
+    cudaEvent_t *kern_ev = nullptr;    // pairs around single kernels: [0,1] jacobi, [2,3] traverse, [4,5] narrow, [6,7] sort
+    uint32_t launches = 0;
+};
+
+static int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+static lc_status enqueue_cluster_solver(lc_batch *b, cudaStream_t st);
+
+#define LC_PHASE(k) do { if (prof_ev) LC_CUDA(cudaEventRecord(prof_ev[k], st)); } while (0)
+#define LC_KEV(k) do { if (kern_ev) LC_CUDA(cudaEventRecord(kern_ev[k], st)); } while (0)
+
+lc_status lc_batch::enqueue_step(cudaStream_t st) {
+    const bool dbg = opt.debug_capture != 0;
+    LC_PHASE(0);
+    LC_CUDA(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * 4, st));
+    // 1. PBD External
+    if (any_wind) launch_wind(d, st);
+    launch_external(d, st);
+    if (dbg) {
+        LC_CUDA(cudaMemcpyAsync(dbg_x, d.x, sizeof(float4) * d.Vtot, cudaMemcpyDeviceToDevice, st));
+        LC_CUDA(cudaMemcpyAsync(dbg_xp, d.xp, sizeof(float4) * d.Vtot, cudaMemcpyDeviceToDevice, st));
+        LC_CUDA(cudaMemcpyAsync(dbg_v, d.v, sizeof(float4) * d.Vtot, cudaMemcpyDeviceToDevice, st));
+        LC_CUDA(cudaMemcpyAsync(dbg_perm_before, d.perm, sizeof(uint32_t) * d.Ttot, cudaMemcpyDeviceToDevice, st));
+    }
+    LC_PHASE(1);
+    // 2. Update Triangles
+    launch_triangles(d, st);
+    if (any_wind) launch_vertex_normals(d, st);
+    LC_PHASE(2);
+    // 3. Build BVH
+    LC_KEV(6);
+    launch_sort(d, tile_first, sort_passes, st);
+    LC_KEV(7);
+    launch_post_sort(d, st);
+    LC_CUDA(cudaMemcpyAsync(d.perm, d.perm_alt, sizeof(uint32_t) * d.Ttot, cudaMemcpyDeviceToDevice, st));
+    LC_CUDA(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * (size_t)d.Ntot, st));
+    launch_karras(d, st);
+    launch_refit(d, st);
+    LC_PHASE(3);
+    // 4. Create Triangle Tests
+    LC_KEV(2);
+    launch_traverse(d, traverse_block, st);
+    LC_KEV(3);
+    scan_u32(d.pair_cnt, d.pair_off, nullptr, (uint32_t)d.Ttot, (uint32_t)d.Ttot, d.scan_tmp, npairs,
+             &d.counters[0], st);
+    launch_pair_compact(d, st);
+    LC_PHASE(4);
+    // 5. Perform Triangle Tests
+    LC_KEV(4);
+    launch_narrow(d, npairs, ncand, narrow_grid, 0, st);  // filter
+    scan_u32(d.pair_vf_cnt, d.pair_vf_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand, nullptr, st);
+    launch_narrow(d, npairs, ncand, narrow_grid, 1, st);  // expand
+    launch_narrow(d, npairs, ncand, narrow_grid, 2, st);  // CCD
+    LC_KEV(5);
+    scan_u32(d.cand_vf, d.cand_vf_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nvf, &d.counters[1], st);
+    scan_u32(d.cand_ee, d.cand_ee_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nee, &d.counters[2], st);
+    launch_narrow(d, npairs, ncand, narrow_grid, 3, st);  // write contacts
+    launch_narrow(d, npairs, ncand, narrow_grid, 4, st);  // per-cloth ranges
+    LC_PHASE(5);
+    // 6. PBD Solver (+ 7. integration fused on the cluster path)
+    LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
+    LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
+    launch_dyn(d, nvf, nee, narrow_grid, 0, st);
+    scan_u32(d.dyn_cnt, d.dyn_off, nullptr, (uint32_t)d.Vtot, (uint32_t)d.Vtot, d.scan_tmp, nullptr, nullptr, st);
+    launch_dyn(d, nvf, nee, narrow_grid, 1, st);
+    launch_dyn(d, nvf, nee, narrow_grid, 2, st);
+    if (use_cluster) {
+        LC_KEV(0);
+        LC_TRY(enqueue_cluster_solver(this, st));
+        LC_KEV(1);
+        LC_PHASE(6);
+        LC_PHASE(7);
+        LC_CUDA(cudaGetLastError());
+        return LC_OK;
+    }
+    launch_solver_setup(d, any_sphere, st);
+    float4 *a = d.x, *b = d.x2;
+    for (int it = 0; it < max_iters; ++it) {
+        if (it == 0) LC_KEV(0);
+        launch_jacobi(d, a, b, it, nvf, jacobi_block, st);
+        if (it == 0) LC_KEV(1);
+        std::swap(a, b);
+    }
+    LC_PHASE(6);
+    // 7. PBD Integration + WorldConstraints
+    launch_integrate(d, a, st);
+    LC_PHASE(7);
+    LC_CUDA(cudaGetLastError());
+    return LC_OK;
+}
+
+// Solver + integration on the cluster-resident path (one launch).
+static lc_status enqueue_cluster_solver(lc_batch *b, cudaStream_t st) {
+    LC_CUDA(launch_solve_cluster(b->d, b->ca, b->cluster_cs, b->C, st));
+    return LC_OK;
+}
+
+template <class T> static lc_status upload(T *dst, const std::vector<T> &src) {
+    if (!src.empty()) LC_CUDA(cudaMemcpy(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+    return LC_OK;
+}
+
+// Cluster-resident solver: picks the cluster size for the largest cloth and
+// the cluster -> cloth schedule (largest cloths first).  Leaves use_cluster
+// false when some cloth does not fit on chip.
+lc_status lc_batch::setup_cluster() {
+    use_cluster = false;
+    if (opt.solver_variant == 1) return LC_OK;
+    const int dev_cap = cluster_chunk_cap();
+    int vmax = 0;
+    bool ok = true;
+    for (int c = 0; c < C; ++c) {
+        vmax = std::max(vmax, hosts[c].V);
+        if (cds[c].F > 8) ok = false;
+    }
+    int cs = 0;
+    if (ok) {
+        if ((vmax + 7) / 8 <= dev_cap && cluster_max_active(8, (vmax + 7) / 8) > 0) cs = 8;
+        else if ((vmax + 15) / 16 <= dev_cap && cluster_max_active(16, (vmax + 15) / 16) > 0) cs = 16;
+    }
+    if (!cs) {
+        if (opt.solver_variant == 2) return fail(LC_ERR_NOT_SUPPORTED, "cluster solver: a cloth does not fit on chip");
+        return LC_OK;
+    }
+    cluster_cs = cs;
+    std::vector<int> order(C);
+    for (int c = 0; c < C; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hosts[x].V > hosts[y].V; });
+    int *clc;
+    LC_TRY(arena.alloc(clc, C, "cl_cloth"));
+    LC_TRY(upload(clc, order));
+    ca.cl_cloth = clc;
+    ca.nvf = nvf;
+    ca.chunk_cap = (vmax + cs - 1) / cs;
+    use_cluster = true;
+    return LC_OK;
+}
+
+static void fill_cloth_dev(const HostCloth &hc, ClothDev &cd) {
+    const lc_cloth_params &p = hc.p;
+    cd.chunk = std::min(p.BVHChunkSize, hc.T);
+    cd.iters = p.solverIterations;
+    cd.wind_on = p.windOn ? 1 : 0;
+    cd.ground_on = p.groundOn ? 1 : 0;
+    cd.sphere_on = p.sphereOn ? 1 : 0;
+    cd.morton_mode = p.mortonMode;
+    cd.leaf_quirk = p.refLeafAabbQuirk ? 1 : 0;
+    cd.dt = p.timestep;
+    cd.h = hc.h;
+    cd.kdamp = p.kDamp;
+    cd.kglobal = p.globalVelDamp;
+    for (int k = 0; k < 3; ++k) {
+        cd.g[k] = p.gravity[k];
+        cd.wmin[k] = p.worldMin[k];
+        cd.wmax[k] = p.worldMax[k];
+        cd.morton_origin[k] = p.mortonOrigin[k];
+        cd.sphere_pos[k] = p.spherePos[k];
+        cd.wind_start[k] = p.startWindDir[k];
+        cd.wind_min[k] = p.minWindDir[k];
+        cd.wind_max[k] = p.maxWindDir[k];
+    }
+    cd.ground_y = p.worldMin[1];
+    cd.morton_scale = p.mortonScale;
+    cd.sphere_r = p.sphereRadius;
+    cd.wind_var_min = p.windMinVariation;
+    cd.wind_var_max = p.windMaxVariation;
+}
+
+static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, const lc_batch_options &opt) {
+    b->C = n;
+    b->opt = opt;
+    b->hosts.resize(n);
+    for (int c = 0; c < n; ++c) LC_TRY(build_host_cloth(descs[c], b->hosts[c]));
+    // offsets
+    b->cds.resize(n);
+    int64_t V = 0, T = 0, N = 0, I = 0, F = 0, E = 0, B = 0, S = 0, VT = 0;
+    int64_t LRA = 0, PC = 0;
+    b->e_off.resize(n);
+    b->b_off.resize(n);
+    b->s_count.resize(n);
+    b->b_count.resize(n);
+    std::vector<int> tile_first(n + 1, 0), stile_cloth, stile_start, vblk_cloth, vblk_start, vb_first(n + 1, 0);
+    for (int c = 0; c < n; ++c) {
+        HostCloth &hc = b->hosts[c];
+        ClothDev &cd = b->cds[c];
+        std::memset(&cd, 0, sizeof(cd));
+        fill_cloth_dev(hc, cd);
+        cd.v_off = (int)V; cd.V = hc.V;
+        cd.t_off = (int)T; cd.T = hc.T;
+        cd.n_off = (int)N;
+        cd.i_off = (int)I;
+        cd.pc_off = PC;
+        cd.f_off = (int)F; cd.F = (int)hc.fixed.size();
+        cd.lra_off = LRA;
+        b->e_off[c] = (int)E; b->b_off[c] = (int)B;
+        b->s_count[c] = (int)hc.s_ids.size();
+        b->b_count[c] = (int)hc.b_ids.size();
+        tile_first[c] = (int)stile_cloth.size();
+        vb_first[c] = (int)vblk_cloth.size();
+        for (int s = 0; s < hc.T; s += kSortTile) { stile_cloth.push_back(c); stile_start.push_back((int)T + s); }
+        for (int s = 0; s < hc.V; s += kThreads) { vblk_cloth.push_back(c); vblk_start.push_back((int)V + s); }
+        V += hc.V; T += hc.T; N += 2 * hc.T - 1; I += hc.T - 1; F += cd.F;
+        E += hc.s_ids.size(); B += hc.b_ids.size(); S += hc.sent.size(); VT += hc.vt_idx.size();
+        LRA += (int64_t)hc.V * cd.F;
+        PC += (int64_t)hc.T * cd.chunk;
+        b->max_iters = std::max(b->max_iters, cd.iters);
+        b->any_wind |= cd.wind_on != 0;
+        b->any_sphere |= cd.sphere_on != 0;
+        if (hc.p.mortonMode != b->hosts[0].p.mortonMode)
+            return fail(LC_ERR_INVALID_ARG, "all cloths of a batch must use the same Morton mode");
+    }
+    tile_first[n] = (int)stile_cloth.size();
+    vb_first[n] = (int)vblk_cloth.size();
+    if (V > (1ll << 31) - 2 || T > (1ll << 31) - 2 || E + B >= (1ll << 29) || PC > 0xFFFFFFF0ll)
+        return fail(LC_ERR_INVALID_ARG, "batch too large for 32-bit indices");
+    b->sort_passes = b->hosts[0].p.mortonMode == LC_MORTON_K30 ? 4 : 8;
+
+    DevPtrs &d = b->d;
+    DeviceArena &A = b->arena;
+    d.C = n; d.Vtot = (int)V; d.Ttot = (int)T; d.Ntot = (int)N; d.Itot = (int)I;
+    d.nstiles = (int)stile_cloth.size();
+    d.nvblk = (int)vblk_cloth.size();
+    const uint64_t vf_cap = opt.vf_capacity ? opt.vf_capacity : std::max<uint64_t>(8 * (uint64_t)T, 4096);
+    const uint64_t ee_cap = opt.ee_capacity ? opt.ee_capacity : std::max<uint64_t>(8 * (uint64_t)T, 4096);
+    d.vf_cap = vf_cap; d.ee_cap = ee_cap;
+    d.pair_cap = (uint64_t)PC;
+    d.dyn_cap = 4 * (vf_cap + ee_cap);
+
+    ClothDev *cdev; ClothState *cst;
+    LC_TRY(A.alloc(cdev, n, "cloth table")); d.cloth = cdev; b->cloth_dev = cdev;
+    LC_TRY(A.alloc(cst, n, "cloth state")); d.cstate = cst;
+    int *vcl, *tcl; LC_TRY(A.alloc(vcl, V, "vcloth")); LC_TRY(A.alloc(tcl, T, "tcloth"));
+    d.vcloth = vcl; d.tcloth = tcl;
+    LC_TRY(A.alloc(d.x, V, "x")); LC_TRY(A.alloc(d.x2, V, "x2")); LC_TRY(A.alloc(d.xp, V, "xp"));
+    LC_TRY(A.alloc(d.v, V, "v")); LC_TRY(A.alloc(d.vn, V, "vn"));
+    int4 *tri; LC_TRY(A.alloc(tri, T, "tri")); d.tri = tri;
+    LC_TRY(A.alloc(d.perm, T, "perm")); LC_TRY(A.alloc(d.perm_alt, T, "perm_alt"));
+    LC_TRY(A.alloc(d.keys, T, "keys")); LC_TRY(A.alloc(d.keys_alt, T, "keys_alt"));
+    LC_TRY(A.alloc(d.payload, T, "payload")); LC_TRY(A.alloc(d.payload_alt, T, "payload_alt"));
+    LC_TRY(A.alloc(d.fn, T, "fn"));
+    int *vto, *vti; LC_TRY(A.alloc(vto, V + 1, "vt_off")); LC_TRY(A.alloc(vti, VT, "vt_idx"));
+    d.vt_off = vto; d.vt_idx = vti;
+    LC_TRY(A.alloc(d.nmin, N, "nmin")); LC_TRY(A.alloc(d.nmax, N, "nmax"));
+    LC_TRY(A.alloc(d.leaf_tmp_min, T, "leaf_tmp_min")); LC_TRY(A.alloc(d.leaf_tmp_max, T, "leaf_tmp_max"));
+    LC_TRY(A.alloc(d.parent, N, "parent")); LC_TRY(A.alloc(d.child, I, "child"));
+    LC_TRY(A.alloc(d.rml, I, "rml")); LC_TRY(A.alloc(d.visit, I, "visit"));
+    LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
+    LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
+    LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));
+    LC_TRY(A.alloc(d.pair_vf_cnt, PC, "pair_cand_cnt"));
+    LC_TRY(A.alloc(d.pair_vf_off, PC + 1, "pair_cand_off"));
+    d.cand_cap = opt.cand_capacity ? opt.cand_capacity : std::max<uint64_t>(8 * (uint64_t)T, 65536);
+    d.cand_cap = std::min<uint64_t>(d.cand_cap, 0xFFFFFFF0ull);
+    LC_TRY(A.alloc(d.cand, d.cand_cap, "candidates"));
+    LC_TRY(A.alloc(d.cand_vf, d.cand_cap, "cand_vf")); LC_TRY(A.alloc(d.cand_ee, d.cand_cap, "cand_ee"));
+    LC_TRY(A.alloc(d.cand_vf_off, d.cand_cap + 1, "cand_vf_off")); LC_TRY(A.alloc(d.cand_ee_off, d.cand_cap + 1, "cand_ee_off"));
+    LC_TRY(A.alloc(d.crange, n, "contact ranges"));
+    LC_TRY(A.alloc(d.vf_v, vf_cap, "vf_v")); LC_TRY(A.alloc(d.vf_w, vf_cap, "vf_w"));
+    LC_TRY(A.alloc(d.ee_v, ee_cap, "ee_v")); LC_TRY(A.alloc(d.ee_w, ee_cap, "ee_w"));
+    LC_TRY(A.alloc(d.dyn_cnt, V, "dyn_cnt")); LC_TRY(A.alloc(d.dyn_off, V + 1, "dyn_off"));
+    LC_TRY(A.alloc(d.dyn_cur, V, "dyn_cur")); LC_TRY(A.alloc(d.dyn_ent, d.dyn_cap, "dyn_ent"));
+    int *soff; uint32_t *sent; int2 *sids; float2 *spar; int4 *bids; float *bkp;
+    LC_TRY(A.alloc(soff, V + 1, "soff")); LC_TRY(A.alloc(sent, S, "sent"));
+    LC_TRY(A.alloc(sids, E, "s_ids")); LC_TRY(A.alloc(spar, E, "s_par"));
+    LC_TRY(A.alloc(bids, B, "b_ids")); LC_TRY(A.alloc(bkp, B, "b_kp"));
+    d.soff = soff; d.sent = sent; d.s_ids = sids; d.s_par = spar; d.b_ids = bids; d.b_kp = bkp;
+    int *fixed; float *lral0; LC_TRY(A.alloc(fixed, F, "fixed")); LC_TRY(A.alloc(lral0, LRA, "lra_l0"));
+    d.fixed = fixed; d.lra_l0 = lral0;
+    LC_TRY(A.alloc(d.lra_flag, LRA, "lra_flag"));
+    LC_TRY(A.alloc(d.ground_qc, V, "ground_qc"));
+    LC_TRY(A.alloc(d.damp, 16 * (size_t)n, "damp"));
+    LC_TRY(A.alloc(d.counters, 4, "counters"));
+    LC_TRY(A.alloc(d.err, 1, "err"));
+    LC_TRY(A.alloc(d.scan_tmp, kScanBlocks + 1, "scan_tmp"));
+    int *stc, *sts, *tf; LC_TRY(A.alloc(stc, stile_cloth.size(), "stile_cloth"));
+    LC_TRY(A.alloc(sts, stile_start.size(), "stile_start")); LC_TRY(A.alloc(tf, n + 1, "tile_first"));
+    d.stile_cloth = stc; d.stile_start = sts; b->tile_first = tf;
+    LC_TRY(A.alloc(d.shist, (size_t)stile_cloth.size() * kSortBuckets, "shist"));
+    int *vbc, *vbs, *vbf; LC_TRY(A.alloc(vbc, vblk_cloth.size(), "vblk_cloth")); LC_TRY(A.alloc(vbs, vblk_start.size(), "vblk_start"));
+    LC_TRY(A.alloc(vbf, vb_first.size(), "vb_first"));
+    d.vblk_cloth = vbc; d.vblk_start = vbs; d.vb_first = vbf;
+    LC_TRY(A.alloc(d.damp_part, 16 * vblk_cloth.size(), "damp_part"));
+    LC_TRY(A.alloc(b->npairs, 1, "npairs")); LC_TRY(A.alloc(b->nvf, 1, "nvf")); LC_TRY(A.alloc(b->nee, 1, "nee"));
+    LC_TRY(A.alloc(b->ncand, 1, "ncand"));
+    if (opt.debug_capture) {
+        LC_TRY(A.alloc(b->dbg_x, V, "dbg_x")); LC_TRY(A.alloc(b->dbg_xp, V, "dbg_xp"));
+        LC_TRY(A.alloc(b->dbg_v, V, "dbg_v")); LC_TRY(A.alloc(b->dbg_perm_before, T, "dbg_perm"));
+        LC_TRY(A.alloc(d.dbg_ground_it, V, "dbg_ground_it"));
+        LC_TRY(A.alloc(d.dbg_dyn_nz, (size_t)b->max_iters * d.dyn_cap, "dbg_dyn_nz"));
+        LC_TRY(A.alloc(d.dbg_sphere, V, "dbg_sphere"));
+        LC_CUDA(cudaMemset(d.dbg_sphere, 0, (size_t)V));
+    }
+    d.kpi_gap = (float)(3.14159265358979323846 - (double)kPi);
+
+    // host staging of the flat arrays
+    std::vector<int> hv_cloth(V), ht_cloth(T), hvt_off(V + 1, 0), hvt_idx(VT), hsoff(V + 1, 0), hfixed(F);
+    std::vector<float4> hx(V), hxp(V), hv(V, make_float4(0, 0, 0, 0)), hvn(V);
+    std::vector<int4> htri(T);
+    std::vector<uint32_t> hperm(T), hsent(S);
+    std::vector<int2> hsids(E);
+    std::vector<float2> hspar(E);
+    std::vector<int4> hbids(B);
+    std::vector<float> hbkp(B), hlra(LRA);
+    std::vector<ClothState> hst(n);
+    for (int c = 0; c < n; ++c) {
+        const HostCloth &hc = b->hosts[c];
+        const ClothDev &cd = b->cds[c];
+        const int vo = cd.v_off, to = cd.t_off, eo = b->e_off[c], bo = b->b_off[c];
+        const double iters = (double)hc.p.solverIterations;
+        const float kps = (float)(1.0 - std::pow(1.0 - (double)hc.p.kStretch, 1.0 / iters));
+        const float kpb = (float)(1.0 - std::pow(1.0 - (double)hc.p.kBend, 1.0 / iters));
+        for (int i = 0; i < hc.V; ++i) {
+            const float m = hc.pinned[i] ? 1000.f : hc.vmass;
+            const float w = hc.pinned[i] ? 0.f : 1.f / hc.vmass;
+            hx[vo + i] = make_float4(hc.pos[3 * i], hc.pos[3 * i + 1], hc.pos[3 * i + 2], w);
+            hxp[vo + i] = make_float4(hc.pos[3 * i], hc.pos[3 * i + 1], hc.pos[3 * i + 2], m);
+            hvn[vo + i] = make_float4(hc.vn0[3 * i], hc.vn0[3 * i + 1], hc.vn0[3 * i + 2], 0.f);
+            hv_cloth[vo + i] = c;
+        }
+        const int so = (int)hsoff[vo];
+        for (int i = 0; i <= hc.V; ++i) hsoff[vo + i] = so + hc.soff[i];
+        for (size_t k = 0; k < hc.sent.size(); ++k) {
+            const uint32_t e = hc.sent[k];
+            const uint32_t kind = e >> 31;
+            const uint32_t local = e & 0x1FFFFFFFu;
+            hsent[so + k] = (e & 0xE0000000u) | (local + (uint32_t)(kind ? bo : eo));
+        }
+        for (int t = 0; t < hc.T; ++t) {
+            htri[to + t] = make_int4(vo + (int)hc.idx[3 * t], vo + (int)hc.idx[3 * t + 1], vo + (int)hc.idx[3 * t + 2],
+                                     hc.features[t]);
+            hperm[to + t] = (uint32_t)(to + t);
+            ht_cloth[to + t] = c;
+        }
+        const int vto0 = hvt_off[vo];
+        for (int i = 0; i <= hc.V; ++i) hvt_off[vo + i] = vto0 + hc.vt_off[i];
+        for (size_t k = 0; k < hc.vt_idx.size(); ++k) hvt_idx[vto0 + k] = to + hc.vt_idx[k];
+        for (size_t k = 0; k < hc.s_ids.size(); ++k) {
+            hsids[eo + k] = make_int2(vo + hc.s_ids[k].x, vo + hc.s_ids[k].y);
+            hspar[eo + k] = make_float2((float)hc.s_l0[k], kps);
+        }
+        for (size_t k = 0; k < hc.b_ids.size(); ++k) {
+            const int4 q = hc.b_ids[k];
+            hbids[bo + k] = make_int4(vo + q.x, vo + q.y, vo + q.z, vo + q.w);
+            hbkp[bo + k] = kpb;
+        }
+        for (int j = 0; j < cd.F; ++j) hfixed[cd.f_off + j] = vo + hc.fixed[j];
+        for (size_t k = 0; k < hc.lra_l0.size(); ++k) hlra[cd.lra_off + k] = hc.lra_l0[k];
+        ClothState s{};
+        for (int k = 0; k < 3; ++k) s.wind[k] = hc.p.windOn ? hc.p.startWindDir[k] : 0.f;
+        s.rng = hc.p.windSeed ? hc.p.windSeed : 0x9E3779B97F4A7C15ull;
+        hst[c] = s;
+    }
+    LC_TRY(upload(cdev, b->cds));
+    LC_TRY(upload(cst, hst));
+    LC_TRY(upload(vcl, hv_cloth)); LC_TRY(upload(tcl, ht_cloth));
+    LC_TRY(upload(d.x, hx)); LC_TRY(upload(d.xp, hxp)); LC_TRY(upload(d.v, hv)); LC_TRY(upload(d.vn, hvn));
+    LC_TRY(upload(tri, htri)); LC_TRY(upload(d.perm, hperm));
+    LC_TRY(upload(vto, hvt_off)); LC_TRY(upload(vti, hvt_idx));
+    LC_TRY(upload(soff, hsoff)); LC_TRY(upload(sent, hsent));
+    LC_TRY(upload(sids, hsids)); LC_TRY(upload(spar, hspar));
+    LC_TRY(upload(bids, hbids)); LC_TRY(upload(bkp, hbkp));
+    LC_TRY(upload(fixed, hfixed)); LC_TRY(upload(lral0, hlra));
+    LC_TRY(upload(stc, stile_cloth)); LC_TRY(upload(sts, stile_start)); LC_TRY(upload(tf, tile_first));
+    LC_TRY(upload(vbc, vblk_cloth)); LC_TRY(upload(vbs, vblk_start)); LC_TRY(upload(vbf, vb_first));
+    LC_CUDA(cudaMemset(d.err, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(d.counters, 0, sizeof(unsigned long long) * 4));
+    LC_CUDA(cudaMemset(d.ground_qc, 0, sizeof(float4) * (size_t)std::max<int64_t>(V, 1)));
+    LC_CUDA(cudaMemset(d.dyn_off, 0, sizeof(uint32_t) * (size_t)(V + 1)));
+    LC_CUDA(cudaMemset(b->npairs, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(b->nvf, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(b->nee, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(b->ncand, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(d.crange, 0, sizeof(uint4) * (size_t)n));
+    LC_CUDA(cudaMemset(d.nmin, 0, sizeof(float4) * (size_t)N));
+    LC_CUDA(cudaMemset(d.nmax, 0, sizeof(float4) * (size_t)N));
+    b->narrow_grid = sm_count() * 8;
+    b->jacobi_block = opt.block_size > 0 ? opt.block_size : 256;
+    LC_TRY(b->setup_cluster());
+    LC_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    LC_CUDA(cudaDeviceSynchronize());
+    return LC_OK;
+}
+
+template <class T>
+static lc_status dump(const T *src, uint64_t n, void *dst, uint64_t cap, uint64_t *count) {
+    if (count) *count = n;
+    if (dst && n && cap) LC_CUDA(cudaMemcpy(dst, src, sizeof(T) * std::min(n, cap), cudaMemcpyDeviceToHost));
+    return LC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void lc_default_params(lc_cloth_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    // Managers/MastersSimulationManager.cpp:33-62
+    p->timestep = 1000.f / 60.f / 1000.f;  // Core/Utils.hpp:18-19
+    p->kFriction = 0.1f;
+    p->kStretch = 0.99f;
+    p->kShear = 0.7f;
+    p->kBend = 0.1f;
+    p->kDamp = 0.05f;
+    p->kSpringDamp = 0.2f;
+    p->thickness = 0.f;
+    p->objectMass = 0.525f;
+    p->globalVelDamp = 0.01f;
+    p->strainLimit = 0.15f;
+    p->gravity[0] = 0.f; p->gravity[1] = -0.0981f; p->gravity[2] = 0.f;
+    p->minWindDir[0] = -0.04f; p->minWindDir[1] = -0.1f; p->minWindDir[2] = -0.1f;
+    p->startWindDir[0] = 0.02f; p->startWindDir[1] = 0.095f; p->startWindDir[2] = 0.45f;
+    p->maxWindDir[0] = 0.04f; p->maxWindDir[1] = 0.135f; p->maxWindDir[2] = 0.4f;
+    p->windMinVariation = 0.f;
+    p->windMaxVariation = 0.2f;
+    p->windOn = 1;
+    p->worldMin[0] = p->worldMin[1] = p->worldMin[2] = 0.f;
+    p->worldMax[0] = p->worldMax[1] = p->worldMax[2] = 1.f;
+    p->dims[0] = p->dims[1] = 60;
+    p->solverIterations = 6;
+    p->ccdIterations = 5;
+    p->BVHChunkSize = 64;
+    p->benchmarkSample = 1000;
+    p->useTriangleBending = 0;
+    p->colorContacts = 0;
+    p->useFriction = 0;
+    p->thicknessFromMesh = 1;
+    p->mortonMode = LC_MORTON_REF63;
+    p->refLeafAabbQuirk = 1;
+    p->groundOn = 1;
+    p->mortonOrigin[0] = p->mortonOrigin[1] = p->mortonOrigin[2] = 0.f;
+    p->mortonScale = 1.f;
+    p->windSeed = 0;
+    p->sphereOn = 0;
+    p->sphereRadius = 0.f;
+}
+
+void lc_default_options(lc_batch_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->use_graph = 1;
+}
+
+const char *lc_last_error_string(void) { return g_last_error.c_str(); }
+
+const char *lc_status_string(lc_status s) {
+    switch (s) {
+        case LC_OK: return "ok";
+        case LC_ERR_INVALID_ARG: return "invalid argument";
+        case LC_ERR_OOM: return "out of device memory";
+        case LC_ERR_CAPACITY_OVERFLOW: return "contact capacity overflow";
+        case LC_ERR_TIMEOUT: return "timeout";
+        case LC_ERR_CUDA: return "CUDA error";
+        case LC_ERR_NOT_SUPPORTED: return "not supported";
+        case LC_ERR_STACK_OVERFLOW: return "BVH traversal stack overflow";
+    }
+    return "unknown";
+}
+
+uint64_t lc_morton3d(float x, float y, float z, int32_t mode) { return morton3_host(x, y, z, mode); }
+
+// Rendering/VisualBodyFactory.cpp:343-391 — grid triangles (alternating
+// diagonals); returns the triangle count, fills indices when non-NULL.
+int32_t lc_mesh_grid(int32_t rows, int32_t cols, uint32_t *indices) {
+    if (rows < 2 || cols < 2) return 0;
+    int32_t t = 0;
+    for (int i = 0; i < rows - 1; ++i)
+        for (int j = 0; j < cols - 1; ++j) {
+            uint32_t q[6];
+            if ((i + j) % 2 == 0) {
+                const uint32_t v[6] = {(uint32_t)(rows * i + j), (uint32_t)(rows * (i + 1) + j), (uint32_t)(rows * i + j + 1),
+                                       (uint32_t)(rows * i + j + 1), (uint32_t)(rows * (i + 1) + j),
+                                       (uint32_t)(rows * (i + 1) + j + 1)};
+                std::memcpy(q, v, sizeof(q));
+            } else {
+                const uint32_t v[6] = {(uint32_t)(rows * i + j), (uint32_t)(rows * (i + 1) + j),
+                                       (uint32_t)(rows * (i + 1) + j + 1), (uint32_t)(rows * (i + 1) + j + 1),
+                                       (uint32_t)(rows * i + j + 1), (uint32_t)(rows * i + j)};
+                std::memcpy(q, v, sizeof(q));
+            }
+            if (indices) std::memcpy(indices + 3 * t, q, sizeof(q));
+            t += 2;
+        }
+    return t;
+}
+
+// Rendering/VisualBodyFactory.cpp:259-341 — icosphere by midpoint
+// subdivision with unwelded vertices (6 per parent triangle per level).
+// Returns the triangle count; fills verts (3 per vertex, 18 * T / 4 floats)
+// and indices when non-NULL.
+int32_t lc_mesh_icosphere(int32_t depth, float *verts, uint32_t *indices) {
+    if (depth < 1 || depth > 8) return 0;
+    const float X = .525731112119133606f, Z = .850650808352039932f;
+    std::vector<float3> v = {f3(-X, 0, Z), f3(X, 0, Z), f3(-X, 0, -Z), f3(X, 0, -Z), f3(0, Z, X), f3(0, Z, -X),
+                             f3(0, -Z, X), f3(0, -Z, -X), f3(Z, X, 0), f3(-Z, X, 0), f3(Z, -X, 0), f3(-Z, -X, 0)};
+    std::vector<uint32_t> id = {0, 4, 1, 0, 9, 4, 9, 5, 4, 4, 5, 8, 4, 8, 1, 8, 10, 1, 8, 3, 10, 5, 3, 8, 5, 2, 3, 2, 7, 3,
+                                7, 10, 3, 7, 6, 10, 7, 11, 6, 11, 0, 6, 0, 1, 6, 6, 1, 10, 9, 0, 11, 9, 11, 2, 9, 2, 5, 7, 2, 11};
+    auto nrm = [](float3 a) {
+        const float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+        return f3(a.x / l, a.y / l, a.z / l);
+    };
+    for (int lvl = 0; lvl < depth; ++lvl) {
+        std::vector<float3> nv;
+        std::vector<uint32_t> ni;
+        nv.reserve(id.size() * 2);
+        ni.reserve(id.size() * 4);
+        for (size_t j = 0; j < id.size(); j += 3) {
+            const float3 a = v[id[j]], b = v[id[j + 1]], c = v[id[j + 2]];
+            const float3 ab = nrm(add(a, b)), bc = nrm(add(b, c)), ca = nrm(add(c, a));
+            const uint32_t base = (uint32_t)nv.size();
+            nv.push_back(a); nv.push_back(b); nv.push_back(c);
+            nv.push_back(ab); nv.push_back(bc); nv.push_back(ca);
+            const uint32_t t[12] = {base, base + 3, base + 5, base + 1, base + 4, base + 3,
+                                    base + 2, base + 5, base + 4, base + 3, base + 4, base + 5};
+            ni.insert(ni.end(), t, t + 12);
+        }
+        v.swap(nv);
+        id.swap(ni);
+    }
+    if (verts)
+        for (size_t i = 0; i < v.size(); ++i) { verts[3 * i] = v[i].x; verts[3 * i + 1] = v[i].y; verts[3 * i + 2] = v[i].z; }
+    if (indices) std::memcpy(indices, id.data(), id.size() * sizeof(uint32_t));
+    return (int32_t)(id.size() / 3);
+}
+
+lc_status lc_batch_create(const lc_cloth_desc *descs, int32_t num_cloths, const lc_batch_options *opts,
+                          lc_batch **out) {
+    if (!descs || num_cloths <= 0 || !out) return fail(LC_ERR_INVALID_ARG, "lc_batch_create: bad arguments");
+    *out = nullptr;
+    lc_batch_options o;
+    lc_default_options(&o);
+    if (opts) o = *opts;
+    std::unique_ptr<lc_batch> b(new lc_batch());
+    lc_status s = batch_build(b.get(), descs, num_cloths, o);
+    if (s != LC_OK) return s;
+    *out = b.release();
+    return LC_OK;
+}
+
+lc_status lc_batch_destroy(lc_batch *b) {
+    if (b) {
+        cudaDeviceSynchronize();
+        delete b;
+    }
+    return LC_OK;
+}
+
+lc_status lc_batch_step(lc_batch *b, int32_t nsteps, void *stream) {
+    if (!b || nsteps < 0) return fail(LC_ERR_INVALID_ARG, "lc_batch_step: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    b->last_stream = st;
+    if (!b->opt.use_graph || b->opt.debug_capture) {
+        for (int s = 0; s < nsteps; ++s) LC_TRY(b->enqueue_step(st));
+        return LC_OK;
+    }
+    if (!b->gexec) {
+        LC_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+        lc_status s = b->enqueue_step(b->cap_stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+        if (s != LC_OK) { if (g) cudaGraphDestroy(g); return s; }
+        LC_CUDA(e);
+        b->graph = g;
+        LC_CUDA(cudaGraphInstantiate(&b->gexec, g, 0));
+    }
+    for (int s = 0; s < nsteps; ++s) LC_CUDA(cudaGraphLaunch(b->gexec, st));
+    return LC_OK;
+}
+
+lc_status lc_batch_sync(lc_batch *b) {
+    if (!b) return fail(LC_ERR_INVALID_ARG, "lc_batch_sync: null batch");
+    LC_CUDA(cudaStreamSynchronize(b->last_stream));
+    LC_CUDA(cudaDeviceSynchronize());
+    uint32_t err = 0;
+    LC_CUDA(cudaMemcpy(&err, b->d.err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & (ERR_VF_OVERFLOW | ERR_EE_OVERFLOW | ERR_DYN_OVERFLOW | ERR_CAND_OVERFLOW)) {
+        cudaMemset(b->d.err, 0, sizeof(uint32_t));
+        return fail(LC_ERR_CAPACITY_OVERFLOW, (err & ERR_CAND_OVERFLOW)
+                                                  ? "narrowphase candidate capacity exceeded; raise lc_batch_options.cand_capacity"
+                                                  : "contact capacity exceeded; raise lc_batch_options.vf/ee_capacity");
+    }
+    if (err & ERR_STACK) {
+        cudaMemset(b->d.err, 0, sizeof(uint32_t));
+        return fail(LC_ERR_STACK_OVERFLOW, "BVH traversal stack (64) exceeded");
+    }
+    return LC_OK;
+}
+
+lc_status lc_batch_num_cloths(const lc_batch *b, int32_t *out) {
+    if (!b || !out) return fail(LC_ERR_INVALID_ARG, "null argument");
+    *out = b->C;
+    return LC_OK;
+}
+
+lc_status lc_batch_cloth_sizes(const lc_batch *b, int32_t c, int32_t *nv, int32_t *nt) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    if (nv) *nv = b->hosts[c].V;
+    if (nt) *nt = b->hosts[c].T;
+    return LC_OK;
+}
+
+lc_status lc_batch_constraint_counts(const lc_batch *b, int32_t c, int32_t *ns, int32_t *nb) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    if (ns) *ns = b->s_count[c];
+    if (nb) *nb = b->b_count[c];
+    return LC_OK;
+}
+
+static lc_status get3(const float4 *src, int n, float *dst, int is_host) {
+    if (!dst) return LC_OK;
+    LC_CUDA(cudaMemcpy2D(dst, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float), n,
+                         is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice));
+    return LC_OK;
+}
+static lc_status set3(float4 *dst, int n, const float *src, int is_host) {
+    if (!src) return LC_OK;
+    LC_CUDA(cudaMemcpy2D(dst, sizeof(float4), src, 3 * sizeof(float), 3 * sizeof(float), n,
+                         is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice));
+    return LC_OK;
+}
+
+lc_status lc_batch_get_state(lc_batch *b, int32_t c, float *x, float *xp, float *v, float *vn, int32_t is_host) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    LC_TRY(lc_batch_sync(b));
+    const ClothDev &cd = b->cds[c];
+    LC_TRY(get3(b->d.x + cd.v_off, cd.V, x, is_host));
+    LC_TRY(get3(b->d.xp + cd.v_off, cd.V, xp, is_host));
+    LC_TRY(get3(b->d.v + cd.v_off, cd.V, v, is_host));
+    LC_TRY(get3(b->d.vn + cd.v_off, cd.V, vn, is_host));
+    return LC_OK;
+}
+
+lc_status lc_batch_set_state(lc_batch *b, int32_t c, const float *x, const float *xp, const float *v, const float *vn,
+                             int32_t is_host) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    LC_CUDA(cudaDeviceSynchronize());
+    const ClothDev &cd = b->cds[c];
+    LC_TRY(set3(b->d.x + cd.v_off, cd.V, x, is_host));
+    LC_TRY(set3(b->d.xp + cd.v_off, cd.V, xp, is_host));
+    LC_TRY(set3(b->d.v + cd.v_off, cd.V, v, is_host));
+    LC_TRY(set3(b->d.vn + cd.v_off, cd.V, vn, is_host));
+    return LC_OK;
+}
+
+lc_status lc_batch_get_triangle_order(lc_batch *b, int32_t c, uint32_t *perm) {
+    if (!b || c < 0 || c >= b->C || !perm) return fail(LC_ERR_INVALID_ARG, "bad arguments");
+    LC_TRY(lc_batch_sync(b));
+    const ClothDev &cd = b->cds[c];
+    std::vector<uint32_t> tmp(cd.T);
+    LC_CUDA(cudaMemcpy(tmp.data(), b->d.perm + cd.t_off, sizeof(uint32_t) * cd.T, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < cd.T; ++i) perm[i] = tmp[i] - (uint32_t)cd.t_off;
+    return LC_OK;
+}
+
+lc_status lc_batch_set_triangle_order(lc_batch *b, int32_t c, const uint32_t *perm) {
+    if (!b || c < 0 || c >= b->C || !perm) return fail(LC_ERR_INVALID_ARG, "bad arguments");
+    const ClothDev &cd = b->cds[c];
+    std::vector<uint32_t> tmp(cd.T);
+    std::vector<char> seen(cd.T, 0);
+    for (int i = 0; i < cd.T; ++i) {
+        if (perm[i] >= (uint32_t)cd.T || seen[perm[i]]) return fail(LC_ERR_INVALID_ARG, "not a permutation");
+        seen[perm[i]] = 1;
+        tmp[i] = perm[i] + (uint32_t)cd.t_off;
+    }
+    LC_CUDA(cudaDeviceSynchronize());
+    LC_CUDA(cudaMemcpy(b->d.perm + cd.t_off, tmp.data(), sizeof(uint32_t) * cd.T, cudaMemcpyHostToDevice));
+    return LC_OK;
+}
+
+lc_status lc_batch_read_positions(lc_batch *b, float *dst, int32_t is_host, void *stream) {
+    if (!b || !dst) return fail(LC_ERR_INVALID_ARG, "bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    LC_CUDA(cudaMemcpy2DAsync(dst, 3 * sizeof(float), b->d.xp, sizeof(float4), 3 * sizeof(float), b->d.Vtot,
+                              is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    return LC_OK;
+}
+
+lc_status lc_batch_set_sphere(lc_batch *b, int32_t c, const float pos[3], float radius) {
+    if (!b || c < 0 || c >= b->C || !pos) return fail(LC_ERR_INVALID_ARG, "bad arguments");
+    ClothDev &cd = b->cds[c];
+    for (int k = 0; k < 3; ++k) cd.sphere_pos[k] = pos[k];
+    cd.sphere_r = radius;
+    const bool newly = !cd.sphere_on;
+    cd.sphere_on = 1;
+    b->hosts[c].p.sphereOn = 1;
+    LC_CUDA(cudaDeviceSynchronize());
+    LC_CUDA(cudaMemcpy(b->cloth_dev + c, &cd, sizeof(ClothDev), cudaMemcpyHostToDevice));
+    if (newly && !b->any_sphere) {
+        b->any_sphere = true;
+        b->invalidate_graph();
+    }
+    return LC_OK;
+}
+
+lc_status lc_batch_set_stiffness(lc_batch *b, int32_t c, const float *ks, const float *kb) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    const HostCloth &hc = b->hosts[c];
+    const double iters = (double)hc.p.solverIterations;
+    LC_CUDA(cudaDeviceSynchronize());
+    if (ks) {
+        std::vector<float2> par(hc.s_ids.size());
+        for (size_t k = 0; k < par.size(); ++k)
+            par[k] = make_float2((float)hc.s_l0[k], (float)(1.0 - std::pow(1.0 - (double)ks[k], 1.0 / iters)));
+        if (!par.empty())
+            LC_CUDA(cudaMemcpy((void *)(b->d.s_par + b->e_off[c]), par.data(), sizeof(float2) * par.size(),
+                               cudaMemcpyHostToDevice));
+    }
+    if (kb) {
+        std::vector<float> kp(hc.b_ids.size());
+        for (size_t k = 0; k < kp.size(); ++k) kp[k] = (float)(1.0 - std::pow(1.0 - (double)kb[k], 1.0 / iters));
+        if (!kp.empty())
+            LC_CUDA(cudaMemcpy((void *)(b->d.b_kp + b->b_off[c]), kp.data(), sizeof(float) * kp.size(),
+                               cudaMemcpyHostToDevice));
+    }
+    return LC_OK;
+}
+
+lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]) {
+    if (!b || !out) return fail(LC_ERR_INVALID_ARG, "bad arguments");
+    lc_status s = lc_batch_sync(b);
+    unsigned long long t[4];
+    LC_CUDA(cudaMemcpy(t, b->d.counters, sizeof(t), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 4; ++k) out[k] = t[k];
+    return s;
+}
+
+lc_status lc_batch::cloth_contacts(int c, bool vf, std::vector<uint64_t> &gidx, std::vector<int4> &iv,
+                                   std::vector<float4> &wv) {
+    const ClothDev &cd = cds[c];
+    uint32_t tot = 0;
+    LC_CUDA(cudaMemcpy(&tot, vf ? nvf : nee, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    const uint64_t n = std::min<uint64_t>(tot, vf ? d.vf_cap : d.ee_cap);
+    std::vector<int4> all_v(n);
+    std::vector<float4> all_w(n);
+    if (n) {
+        LC_CUDA(cudaMemcpy(all_v.data(), vf ? d.vf_v : d.ee_v, sizeof(int4) * n, cudaMemcpyDeviceToHost));
+        LC_CUDA(cudaMemcpy(all_w.data(), vf ? d.vf_w : d.ee_w, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    }
+    gidx.clear(); iv.clear(); wv.clear();
+    for (uint64_t i = 0; i < n; ++i) {
+        if (all_v[i].x < cd.v_off || all_v[i].x >= cd.v_off + cd.V) continue;
+        gidx.push_back(i);
+        iv.push_back(make_int4(all_v[i].x - cd.v_off, all_v[i].y - cd.v_off, all_v[i].z - cd.v_off, all_v[i].w - cd.v_off));
+        wv.push_back(all_w[i]);
+    }
+    return LC_OK;
+}
+
+lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, uint64_t cap, uint64_t *count) {
+    if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
+    LC_TRY(lc_batch_sync(b));
+    const ClothDev &cd = b->cds[c];
+    const DevPtrs &d = b->d;
+    const bool need_dbg = what == LC_DBG_PRED_X || what == LC_DBG_PRED_XPREV || what == LC_DBG_PRED_V ||
+                          what == LC_DBG_PERM_BEFORE;
+    if (need_dbg && !b->opt.debug_capture) return fail(LC_ERR_INVALID_ARG, "batch created without debug_capture");
+    switch (what) {
+        case LC_DBG_PRED_X: if (count) *count = cd.V; return get3(b->dbg_x + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PRED_XPREV: if (count) *count = cd.V; return get3(b->dbg_xp + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PRED_V: if (count) *count = cd.V; return get3(b->dbg_v + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PERM_BEFORE:
+        case LC_DBG_PERM: {
+            std::vector<uint32_t> t(cd.T);
+            LC_CUDA(cudaMemcpy(t.data(), (what == LC_DBG_PERM ? d.perm : b->dbg_perm_before) + cd.t_off,
+                               sizeof(uint32_t) * cd.T, cudaMemcpyDeviceToHost));
+            for (auto &v : t) v -= (uint32_t)cd.t_off;
+            if (count) *count = cd.T;
+            if (dst) std::memcpy(dst, t.data(), sizeof(uint32_t) * std::min<uint64_t>(cd.T, cap));
+            return LC_OK;
+        }
+        case LC_DBG_MORTON: return dump(d.keys + cd.t_off, (uint64_t)cd.T, dst, cap, count);
+        case LC_DBG_LEFTS:
+        case LC_DBG_RIGHTS: {
+            std::vector<int2> t(std::max(cd.T - 1, 0));
+            if (!t.empty())
+                LC_CUDA(cudaMemcpy(t.data(), d.child + cd.i_off, sizeof(int2) * t.size(), cudaMemcpyDeviceToHost));
+            if (count) *count = t.size();
+            if (dst)
+                for (size_t i = 0; i < std::min<uint64_t>(t.size(), cap); ++i)
+                    ((int *)dst)[i] = what == LC_DBG_LEFTS ? t[i].x : t[i].y;
+            return LC_OK;
+        }
+        case LC_DBG_PARENTS: return dump(d.parent + cd.n_off, (uint64_t)(2 * cd.T - 1), dst, cap, count);
+        case LC_DBG_RML: return dump(d.rml + cd.i_off, (uint64_t)std::max(cd.T - 1, 0), dst, cap, count);
+        case LC_DBG_NODE_AABB: {
+            const uint64_t n = 2 * (uint64_t)cd.T - 1;
+            std::vector<float4> mn(n), mx(n);
+            LC_CUDA(cudaMemcpy(mn.data(), d.nmin + cd.n_off, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+            LC_CUDA(cudaMemcpy(mx.data(), d.nmax + cd.n_off, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+            if (count) *count = n;
+            if (dst)
+                for (uint64_t i = 0; i < std::min(n, cap); ++i) {
+                    float *o = (float *)dst + 6 * i;
+                    o[0] = mn[i].x; o[1] = mn[i].y; o[2] = mn[i].z; o[3] = mx[i].x; o[4] = mx[i].y; o[5] = mx[i].z;
+                }
+            return LC_OK;
+        }
+        case LC_DBG_PAIRS: {
+            // pairs of this cloth: slots [t_off, t_off+T) own the range
+            std::vector<uint32_t> off(cd.T + 1);
+            LC_CUDA(cudaMemcpy(off.data(), d.pair_off + cd.t_off, sizeof(uint32_t) * (cd.T + 1), cudaMemcpyDeviceToHost));
+            const uint64_t n = off[cd.T] - off[0];
+            std::vector<uint2> t(n);
+            if (n) LC_CUDA(cudaMemcpy(t.data(), d.pairs + off[0], sizeof(uint2) * n, cudaMemcpyDeviceToHost));
+            if (count) *count = n;
+            if (dst)
+                for (uint64_t i = 0; i < std::min(n, cap); ++i) {
+                    ((uint32_t *)dst)[2 * i] = t[i].x - cd.t_off;
+                    ((uint32_t *)dst)[2 * i + 1] = t[i].y - cd.t_off;
+                }
+            return LC_OK;
+        }
+        case LC_DBG_VF:
+        case LC_DBG_EE: {
+            std::vector<uint64_t> gi;
+            std::vector<int4> iv;
+            std::vector<float4> wv;
+            LC_TRY(b->cloth_contacts(c, what == LC_DBG_VF, gi, iv, wv));
+            std::vector<lc_contact> outv(iv.size());
+            for (size_t i = 0; i < iv.size(); ++i) {
+                lc_contact &k = outv[i];
+                k.v[0] = iv[i].x; k.v[1] = iv[i].y; k.v[2] = iv[i].z; k.v[3] = iv[i].w;
+                k.w[0] = wv[i].x; k.w[1] = wv[i].y; k.w[2] = wv[i].z; k.w[3] = wv[i].w;
+            }
+            if (count) *count = outv.size();
+            if (dst && !outv.empty()) std::memcpy(dst, outv.data(), sizeof(lc_contact) * std::min<uint64_t>(outv.size(), cap));
+            return LC_OK;
+        }
+        case LC_DBG_GROUND: {
+            std::vector<float4> q(cd.V);
+            LC_CUDA(cudaMemcpy(q.data(), d.ground_qc + cd.v_off, sizeof(float4) * cd.V, cudaMemcpyDeviceToHost));
+            if (count) *count = cd.V;
+            if (dst)
+                for (uint64_t i = 0; i < std::min<uint64_t>(cd.V, cap); ++i) ((uint8_t *)dst)[i] = q[i].w != 0.f;
+            return LC_OK;
+        }
+        case LC_DBG_GROUND_ACTIVE:
+            if (!b->opt.debug_capture) return fail(LC_ERR_INVALID_ARG, "batch created without debug_capture");
+            return dump(d.dbg_ground_it + cd.v_off, (uint64_t)cd.V, dst, cap, count);
+        case LC_DBG_LRA: return dump(d.lra_flag + cd.lra_off, (uint64_t)cd.V * cd.F, dst, cap, count);
+        case LC_DBG_SPHERE:
+            if (!b->opt.debug_capture) return fail(LC_ERR_INVALID_ARG, "batch created without debug_capture");
+            return dump(d.dbg_sphere + cd.v_off, (uint64_t)cd.V, dst, cap, count);
+        case LC_DBG_DYN_ACTIVE: {
+            if (!b->opt.debug_capture) return fail(LC_ERR_INVALID_ARG, "batch created without debug_capture");
+            std::vector<uint64_t> gvf, gee;
+            std::vector<int4> iv;
+            std::vector<float4> wv;
+            LC_TRY(b->cloth_contacts(c, true, gvf, iv, wv));
+            LC_TRY(b->cloth_contacts(c, false, gee, iv, wv));
+            uint32_t nvf_tot = 0;
+            LC_CUDA(cudaMemcpy(&nvf_tot, b->nvf, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            nvf_tot = (uint32_t)std::min<uint64_t>(nvf_tot, d.vf_cap);
+            const int iters = b->cds[c].iters;
+            const size_t per = (gvf.size() + gee.size()) * 4;
+            std::vector<uint8_t> all((size_t)b->max_iters * d.dyn_cap);
+            if (!all.empty())
+                LC_CUDA(cudaMemcpy(all.data(), d.dbg_dyn_nz, all.size(), cudaMemcpyDeviceToHost));
+            std::vector<uint8_t> outv((size_t)iters * per);
+            for (int it = 0; it < iters; ++it) {
+                size_t o = (size_t)it * per;
+                for (uint64_t g : gvf)
+                    for (int s = 0; s < 4; ++s) outv[o++] = all[(size_t)it * d.dyn_cap + 4 * g + s];
+                for (uint64_t g : gee)
+                    for (int s = 0; s < 4; ++s) outv[o++] = all[(size_t)it * d.dyn_cap + 4 * (nvf_tot + g) + s];
+            }
+            if (count) *count = outv.size();
+            if (dst && !outv.empty()) std::memcpy(dst, outv.data(), std::min<uint64_t>(outv.size(), cap));
+            return LC_OK;
+        }
+        case LC_DBG_FEATURES: {
+            const HostCloth &hc = b->hosts[c];
+            if (count) *count = hc.features.size();
+            if (dst) std::memcpy(dst, hc.features.data(), std::min<uint64_t>(hc.features.size(), cap));
+            return LC_OK;
+        }
+        default: return fail(LC_ERR_INVALID_ARG, "unknown debug selector");
+    }
+}
+
+lc_status lc_batch_write_state(lc_batch *b, const float *x, const float *xp, const float *v, int32_t is_host,
+                               void *stream) {
+    if (!b) return fail(LC_ERR_INVALID_ARG, "null batch");
+    cudaStream_t st = (cudaStream_t)stream;
+    const cudaMemcpyKind k = is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    const int n = b->d.Vtot;
+    if (x) LC_CUDA(cudaMemcpy2DAsync(b->d.x, sizeof(float4), x, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
+    if (xp) LC_CUDA(cudaMemcpy2DAsync(b->d.xp, sizeof(float4), xp, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
+    if (v) LC_CUDA(cudaMemcpy2DAsync(b->d.v, sizeof(float4), v, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
+    return LC_OK;
+}
+
+lc_status lc_batch_read_state(lc_batch *b, float *x, float *xp, float *v, int32_t is_host, void *stream) {
+    if (!b) return fail(LC_ERR_INVALID_ARG, "null batch");
+    cudaStream_t st = (cudaStream_t)stream;
+    const cudaMemcpyKind k = is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    const int n = b->d.Vtot;
+    if (x) LC_CUDA(cudaMemcpy2DAsync(x, 3 * sizeof(float), b->d.x, sizeof(float4), 3 * sizeof(float), n, k, st));
+    if (xp) LC_CUDA(cudaMemcpy2DAsync(xp, 3 * sizeof(float), b->d.xp, sizeof(float4), 3 * sizeof(float), n, k, st));
+    if (v) LC_CUDA(cudaMemcpy2DAsync(v, 3 * sizeof(float), b->d.v, sizeof(float4), 3 * sizeof(float), n, k, st));
+    return LC_OK;
+}
+
+lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile *out) {
+    if (!b || !out || nsteps < 1) return fail(LC_ERR_INVALID_ARG, "lc_batch_profile: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<cudaEvent_t> pev(8 * (size_t)nsteps), kev(8 * (size_t)nsteps);
+    for (auto &e : pev) LC_CUDA(cudaEventCreate(&e));
+    for (auto &e : kev) LC_CUDA(cudaEventCreate(&e));
+    lc_status s = LC_OK;
+    for (int k = 0; k < nsteps && s == LC_OK; ++k) {
+        b->prof_ev = &pev[8 * (size_t)k];
+        b->kern_ev = &kev[8 * (size_t)k];
+        s = b->enqueue_step(st);
+    }
+    b->prof_ev = nullptr;
+    b->kern_ev = nullptr;
+    if (s == LC_OK) {
+        LC_CUDA(cudaStreamSynchronize(st));
+        std::memset(out, 0, sizeof(*out));
+        for (int k = 0; k < nsteps; ++k) {
+            float ms;
+            for (int p = 0; p < 7; ++p) {
+                cudaEventElapsedTime(&ms, pev[8 * k + p], pev[8 * k + p + 1]);
+                out->phase_ms[p] += ms / nsteps;
+            }
+            cudaEventElapsedTime(&ms, kev[8 * k + 0], kev[8 * k + 1]);
+            out->solver_ms += ms / nsteps;
+            out->jacobi_ms += (b->use_cluster ? ms / b->max_iters : ms) / nsteps;
+            cudaEventElapsedTime(&ms, kev[8 * k + 2], kev[8 * k + 3]); out->traverse_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, kev[8 * k + 4], kev[8 * k + 5]); out->narrow_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, kev[8 * k + 6], kev[8 * k + 7]); out->sort_ms += ms / nsteps;
+        }
+        for (int p = 0; p < 7; ++p) out->step_ms += out->phase_ms[p];
+        out->solver_variant = b->use_cluster ? 2 : 1;
+        out->cluster_size = b->use_cluster ? b->cluster_cs : 0;
+        if (!b->use_cluster) out->solver_ms = out->phase_ms[5];
+        // kernel launches per step, counted from the captured graph
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            lc_status s2 = b->enqueue_step(b->cap_stream);
+            if (cudaStreamEndCapture(b->cap_stream, &g) == cudaSuccess && g && s2 == LC_OK) {
+                size_t nn = 0;
+                cudaGraphGetNodes(g, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(g, nodes.data(), &nn);
+                uint32_t kn = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType t;
+                    cudaGraphNodeGetType(nd, &t);
+                    if (t == cudaGraphNodeTypeKernel) ++kn;
+                }
+                out->kernels_per_step = kn;
+            }
+            if (g) cudaGraphDestroy(g);
+        }
+    }
+    for (auto &e : pev) cudaEventDestroy(e);
+    for (auto &e : kev) cudaEventDestroy(e);
+    return s;
+}
+
+// ----- standalone LBVH ------------------------------------------------------
+struct lc_lbvh {
+    lc_batch b;  // one cloth whose triangles are the caller's boxes
+    int max_T = 0;
+    int T = 0;
+    int chunk_req = 64;
+};
+
+lc_status lc_lbvh_create(int32_t max_triangles, int32_t chunk_size, int32_t morton_mode, lc_lbvh **out) {
+    if (max_triangles < 1 || chunk_size < 1 || !out) return fail(LC_ERR_INVALID_ARG, "lc_lbvh_create: bad arguments");
+    *out = nullptr;
+    std::unique_ptr<lc_lbvh> h(new lc_lbvh());
+    lc_batch &b = h->b;
+    b.C = 1;
+    h->max_T = max_triangles;
+    h->chunk_req = chunk_size;
+    DevPtrs &d = b.d;
+    DeviceArena &A = b.arena;
+    const int64_t T = max_triangles, N = 2 * T - 1, I = T - 1, PC = T * std::min<int64_t>(chunk_size, T);
+    const int64_t tiles = (T + kSortTile - 1) / kSortTile;
+    b.cds.resize(1);
+    std::memset(&b.cds[0], 0, sizeof(ClothDev));
+    b.cds[0].chunk = (int)std::min<int64_t>(chunk_size, T);
+    b.cds[0].morton_mode = morton_mode;
+    b.cds[0].leaf_quirk = 0;
+    b.cds[0].morton_scale = 1.f;
+    b.sort_passes = morton_mode == LC_MORTON_K30 ? 4 : 8;
+    d.C = 1;
+    ClothDev *cdev;
+    LC_TRY(A.alloc(cdev, 1, "cloth table")); d.cloth = cdev; b.cloth_dev = cdev;
+    int *tcl; LC_TRY(A.alloc(tcl, T, "tcloth")); d.tcloth = tcl;
+    LC_CUDA(cudaMemset(tcl, 0, sizeof(int) * T));
+    LC_TRY(A.alloc(d.perm, T, "perm")); LC_TRY(A.alloc(d.perm_alt, T, "perm_alt"));
+    LC_TRY(A.alloc(d.keys, T, "keys")); LC_TRY(A.alloc(d.keys_alt, T, "keys_alt"));
+    LC_TRY(A.alloc(d.payload, T, "payload")); LC_TRY(A.alloc(d.payload_alt, T, "payload_alt"));
+    LC_TRY(A.alloc(d.nmin, N, "nmin")); LC_TRY(A.alloc(d.nmax, N, "nmax"));
+    LC_TRY(A.alloc(d.leaf_tmp_min, T, "leaf_tmp_min")); LC_TRY(A.alloc(d.leaf_tmp_max, T, "leaf_tmp_max"));
+    LC_TRY(A.alloc(d.parent, N, "parent")); LC_TRY(A.alloc(d.child, I, "child"));
+    LC_TRY(A.alloc(d.rml, I, "rml")); LC_TRY(A.alloc(d.visit, I, "visit"));
+    LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
+    LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
+    LC_TRY(A.alloc(d.counters, 4, "counters")); LC_TRY(A.alloc(d.err, 1, "err"));
+    LC_TRY(A.alloc(d.scan_tmp, kScanBlocks + 1, "scan_tmp"));
+    int *stc, *sts, *tf;
+    LC_TRY(A.alloc(stc, tiles, "stile_cloth")); LC_TRY(A.alloc(sts, tiles, "stile_start")); LC_TRY(A.alloc(tf, 2, "tile_first"));
+    d.stile_cloth = stc; d.stile_start = sts; b.tile_first = tf;
+    LC_TRY(A.alloc(d.shist, tiles * kSortBuckets, "shist"));
+    LC_TRY(A.alloc(b.npairs, 1, "npairs"));
+    d.pair_cap = (uint64_t)PC;
+    LC_CUDA(cudaMemset(d.err, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(stc, 0, sizeof(int) * tiles));
+    b.traverse_block = 128;
+    *out = h.release();
+    return LC_OK;
+}
+
+lc_status lc_lbvh_build(lc_lbvh *h, const float *tri_min, const float *tri_max, int32_t num_triangles, void *stream) {
+    if (!h || !tri_min || !tri_max || num_triangles < 1 || num_triangles > h->max_T)
+        return fail(LC_ERR_INVALID_ARG, "lc_lbvh_build: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    lc_batch &b = h->b;
+    DevPtrs &d = b.d;
+    const int T = num_triangles;
+    if (T != h->T) {
+        h->T = T;
+        ClothDev &cd = b.cds[0];
+        cd.T = T;
+        cd.chunk = std::min(h->chunk_req, T);
+        std::vector<int> starts;
+        for (int s = 0; s < T; s += kSortTile) starts.push_back(s);
+        const int tf[2] = {0, (int)starts.size()};
+        LC_CUDA(cudaStreamSynchronize(st));
+        LC_CUDA(cudaMemcpy((void *)d.stile_start, starts.data(), sizeof(int) * starts.size(), cudaMemcpyHostToDevice));
+        LC_CUDA(cudaMemcpy(b.tile_first, tf, sizeof(tf), cudaMemcpyHostToDevice));
+        LC_CUDA(cudaMemcpy(b.cloth_dev, &cd, sizeof(ClothDev), cudaMemcpyHostToDevice));
+        d.nstiles = (int)starts.size();
+    }
+    d.Ttot = T;
+    d.Ntot = 2 * T - 1;
+    d.Itot = T - 1;
+    LC_CUDA(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * 4, st));
+    launch_leaves_from_boxes(d, tri_min, tri_max, T, b.cds[0].morton_mode, st);
+    launch_sort(d, b.tile_first, b.sort_passes, st);
+    launch_post_sort(d, st);
+    LC_CUDA(cudaMemcpyAsync(d.perm, d.perm_alt, sizeof(uint32_t) * T, cudaMemcpyDeviceToDevice, st));
+    LC_CUDA(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * (size_t)d.Ntot, st));
+    launch_karras(d, st);
+    launch_refit(d, st);
+    LC_CUDA(cudaGetLastError());
+    return LC_OK;
+}
+
+lc_status lc_lbvh_pairs(lc_lbvh *h, uint32_t *out_pairs, uint64_t cap, uint64_t *count, void *stream) {
+    if (!h || !count) return fail(LC_ERR_INVALID_ARG, "lc_lbvh_pairs: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    lc_batch &b = h->b;
+    DevPtrs &d = b.d;
+    launch_traverse(d, b.traverse_block, st);
+    scan_u32(d.pair_cnt, d.pair_off, nullptr, (uint32_t)d.Ttot, (uint32_t)d.Ttot, d.scan_tmp, b.npairs,
+             &d.counters[0], st);
+    launch_pair_compact(d, st);
+    LC_CUDA(cudaGetLastError());
+    uint32_t n = 0;
+    LC_CUDA(cudaMemcpyAsync(&n, b.npairs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    LC_CUDA(cudaStreamSynchronize(st));
+    *count = n;
+    if (out_pairs && n)
+        LC_CUDA(cudaMemcpyAsync(out_pairs, d.pairs, sizeof(uint2) * std::min<uint64_t>(n, cap), cudaMemcpyDeviceToDevice, st));
+    uint32_t err = 0;
+    LC_CUDA(cudaMemcpy(&err, d.err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & ERR_STACK) return fail(LC_ERR_STACK_OVERFLOW, "BVH traversal stack (64) exceeded");
+    return LC_OK;
+}
+
+lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream) {
+    if (!h || !out_ids) return fail(LC_ERR_INVALID_ARG, "lc_lbvh_sorted_ids: bad arguments");
+    LC_CUDA(cudaMemcpyAsync(out_ids, h->b.d.perm, sizeof(uint32_t) * h->T, cudaMemcpyDeviceToDevice,
+                            (cudaStream_t)stream));
+    return LC_OK;
+}
+
+lc_status lc_lbvh_destroy(lc_lbvh *h) {
+    if (h) {
+        cudaDeviceSynchronize();
+        delete h;
+    }
+    return LC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,782 @@
+// lc_lbvh.cu — triangle boxes + Morton codes, segmented stable radix sort,
+// Karras hierarchy, bottom-up refit, leaf-vs-tree traversal, pair
+// compaction and the VF/EE narrowphase (feature AABB cull + CCD).
+//
+// Compiled with -fmad=false: every float expression here keeps the separate
+// roundings of the reference kernels, so Morton codes, tree topology, pair
+// lists and contact lists are bit-exact against the FP32 oracle for the
+// same input positions.
+#include "lc_internal.cuh"
+
+namespace lc {
+
+// ---------------------------------------------------------------------------
+// Morton encoding: Core/CudaUtils.cu:278-325 (REF63) and the commented 30-bit
+// variant at :289-308 (K30).  Bit k of an axis goes to bit 3k.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ unsigned long long spread21(unsigned long long v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+__host__ __device__ __forceinline__ unsigned long long spread10(unsigned long long v) {
+    v &= 0x3ffull;
+    v = (v | (v << 16)) & 0x30000ffull;
+    v = (v | (v << 8)) & 0x300f00full;
+    v = (v | (v << 4)) & 0x30c30c3ull;
+    v = (v | (v << 2)) & 0x9249249ull;
+    return v;
+}
+__host__ __device__ __forceinline__ unsigned long long morton3(float x, float y, float z, int mode) {
+    if (mode == LC_MORTON_K30) {
+        unsigned long long qx = (unsigned long long)fminf(fmaxf(x * 1024.f, 0.0f), 1023.0f);
+        unsigned long long qy = (unsigned long long)fminf(fmaxf(y * 1024.f, 0.0f), 1023.0f);
+        unsigned long long qz = (unsigned long long)fminf(fmaxf(z * 1024.f, 0.0f), 1023.0f);
+        return (spread10(qx) << 2) + (spread10(qy) << 1) + spread10(qz);
+    }
+    unsigned long long qx = (unsigned long long)fminf(fmaxf(x * 2097152.f, 0.0f), 2097151.0f);
+    unsigned long long qy = (unsigned long long)fminf(fmaxf(y * 2097152.f, 0.0f), 2097151.0f);
+    unsigned long long qz = (unsigned long long)fminf(fmaxf(z * 2097152.f, 0.0f), 2097151.0f);
+    return (spread21(qx) << 2) + (spread21(qy) << 1) + spread21(qz);
+}
+
+unsigned long long morton3_host(float x, float y, float z, int mode) { return morton3(x, y, z, mode); }
+
+// ---------------------------------------------------------------------------
+// Triangle update: Physics/CudaDeformableUtils.cu:120-151.  One thread per
+// slot; the swept, thickness-inflated box goes to leaf (T-1+slot) — the
+// pre-sort slot, which is the reference's leaf-AABB quirk — or to a
+// temporary that the post-sort gather places under the sorted leaf.
+// ---------------------------------------------------------------------------
+__global__ void k_triangles(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int local = s - cd.t_off;
+    const uint32_t orig = d.perm[s];
+    const int4 t = d.tri[orig];
+    const float3 a = xyz(d.x[t.x]), b = xyz(d.x[t.y]), cc = xyz(d.x[t.z]);
+    const float3 pa = xyz(d.xp[t.x]), pb = xyz(d.xp[t.y]), pc = xyz(d.xp[t.z]);
+    const float h = cd.h;
+    if (cd.wind_on) d.fn[orig] = f4(normalize(cross(sub(b, a), sub(cc, a))), 0.f);
+    const float3 mn = subc(min3(a, b, cc), h), mx = addc(max3(a, b, cc), h);
+    const float3 pmn = subc(min3(pa, pb, pc), h), pmx = addc(max3(pa, pb, pc), h);
+    const float3 smn = vmin(mn, pmn), smx = vmax(mx, pmx);
+    if (cd.leaf_quirk) {
+        const int node = cd.n_off + (cd.T - 1) + local;
+        d.nmin[node] = f4(smn, 0.f);
+        d.nmax[node] = f4(smx, 0.f);
+    } else {
+        d.leaf_tmp_min[s] = f4(smn, 0.f);
+        d.leaf_tmp_max[s] = f4(smx, 0.f);
+    }
+    const float3 mid = add(smn, dvs(sub(smx, smn), 2.f));
+    const float qx = (mid.x - cd.morton_origin[0]) * cd.morton_scale;
+    const float qy = (mid.y - cd.morton_origin[1]) * cd.morton_scale;
+    const float qz = (mid.z - cd.morton_origin[2]) * cd.morton_scale;
+    d.keys[s] = morton3(qx, qy, qz, cd.morton_mode);
+    d.payload[s] = (uint32_t)local;
+}
+
+// Standalone LBVH: leaf boxes supplied by the caller (one cloth, T slots).
+__global__ void k_leaves_from_boxes(DevPtrs d, const float *__restrict__ bmin, const float *__restrict__ bmax,
+                                    int T, int mode) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= T) return;
+    const float3 mn = f3(bmin[3 * s], bmin[3 * s + 1], bmin[3 * s + 2]);
+    const float3 mx = f3(bmax[3 * s], bmax[3 * s + 1], bmax[3 * s + 2]);
+    d.leaf_tmp_min[s] = f4(mn, 0.f);
+    d.leaf_tmp_max[s] = f4(mx, 0.f);
+    const float3 mid = add(mn, dvs(sub(mx, mn), 2.f));
+    d.keys[s] = morton3(mid.x, mid.y, mid.z, mode);
+    d.payload[s] = (uint32_t)s;
+    d.perm[s] = (uint32_t)s;
+}
+
+// ---------------------------------------------------------------------------
+// Segmented stable LSD radix sort of (u64 key, u32 payload), 8-bit digits.
+// Tiles never straddle cloths, so every pass ranks keys within their own
+// cloth: the result equals a stable sort of each cloth's slots by key, the
+// order CUB's SortPairs gives at Physics/CudaDeformableUtils.cu:346-349.
+// ---------------------------------------------------------------------------
+__global__ void k_sort_hist(DevPtrs d, const unsigned long long *__restrict__ keys, int shift) {
+    __shared__ uint32_t hist[kSortBuckets];
+    const int tile = blockIdx.x;
+    for (int i = threadIdx.x; i < kSortBuckets; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const int c = d.stile_cloth[tile];
+    const int start = d.stile_start[tile];
+    const ClothDev &cd = d.cloth[c];
+    const int end = min(start + kSortTile, cd.t_off + cd.T);
+    for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t dig = (uint32_t)(keys[i] >> shift) & (kSortBuckets - 1);
+        atomicAdd(&hist[dig], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSortBuckets; i += blockDim.x) d.shist[(size_t)tile * kSortBuckets + i] = hist[i];
+}
+
+// One block per cloth: turns the per-tile digit counts into global scatter
+// offsets (digit-major, tile-minor within the cloth).
+__global__ void k_sort_offsets(DevPtrs d, const int *__restrict__ tile_first) {
+    const int c = blockIdx.x;
+    const int d0 = threadIdx.x;  // one thread per digit (blockDim == kSortBuckets)
+    const int t0 = tile_first[c], t1 = tile_first[c + 1];
+    uint32_t tot = 0;
+    for (int t = t0; t < t1; ++t) tot += d.shist[(size_t)t * kSortBuckets + d0];
+    // exclusive scan of the 256 digit totals
+    __shared__ uint32_t s[kSortBuckets];
+    s[d0] = tot;
+    __syncthreads();
+    for (int o = 1; o < kSortBuckets; o <<= 1) {
+        uint32_t v = d0 >= o ? s[d0 - o] : 0u;
+        __syncthreads();
+        s[d0] += v;
+        __syncthreads();
+    }
+    uint32_t run = (uint32_t)d.cloth[c].t_off + s[d0] - tot;
+    for (int t = t0; t < t1; ++t) {
+        const size_t k = (size_t)t * kSortBuckets + d0;
+        const uint32_t n = d.shist[k];
+        d.shist[k] = run;
+        run += n;
+    }
+}
+
+__global__ void k_sort_scatter(DevPtrs d, const unsigned long long *__restrict__ kin,
+                               const uint32_t *__restrict__ pin, unsigned long long *__restrict__ kout,
+                               uint32_t *__restrict__ pout, int shift) {
+    constexpr int W = kThreads / 32;
+    __shared__ uint32_t base[kSortBuckets];
+    __shared__ uint32_t wcnt[W][kSortBuckets];
+    const int tile = blockIdx.x;
+    const int c = d.stile_cloth[tile];
+    const int start = d.stile_start[tile];
+    const ClothDev &cd = d.cloth[c];
+    const int end = min(start + kSortTile, cd.t_off + cd.T);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    base[threadIdx.x] = d.shist[(size_t)tile * kSortBuckets + threadIdx.x];
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (int r = 0; r < kSortTile / kThreads; ++r) {
+        const int i = start + r * kThreads + threadIdx.x;
+        const bool valid = i < end;
+        unsigned long long key = 0;
+        uint32_t pl = 0;
+        uint32_t dig = kSortBuckets;  // sentinel for empty lanes
+        if (valid) {
+            key = kin[i];
+            pl = pin[i];
+            dig = (uint32_t)(key >> shift) & (kSortBuckets - 1);
+        }
+        for (int k = threadIdx.x; k < W * kSortBuckets; k += kThreads) (&wcnt[0][0])[k] = 0;
+        __syncthreads();
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig);
+        const uint32_t rank = __popc(peers & lt_mask);
+        if (valid && rank == 0) wcnt[wid][dig] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t o = base[threadIdx.x];
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const uint32_t t = wcnt[w][threadIdx.x];
+                wcnt[w][threadIdx.x] = o;
+                o += t;
+            }
+            base[threadIdx.x] = o;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = wcnt[wid][dig] + rank;
+            kout[pos] = key;
+            pout[pos] = pl;
+        }
+        __syncthreads();
+    }
+}
+
+// After the sort: new triangle order and (fixed mode) leaf boxes gathered by
+// the permutation.
+__global__ void k_post_sort(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int src = cd.t_off + (int)d.payload[s];
+    d.perm_alt[s] = d.perm[src];
+    if (!cd.leaf_quirk) {
+        const int node = cd.n_off + (cd.T - 1) + (s - cd.t_off);
+        d.nmin[node] = d.leaf_tmp_min[src];
+        d.nmax[node] = d.leaf_tmp_max[src];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Karras hierarchy: Collision/CudaBVH.cu:163-242, Core/CudaUtils.cu:338-362.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int delta(const unsigned long long *__restrict__ m, int i, int j, int maxi) {
+    if (j < 0 || j > maxi) return -1;
+    const unsigned long long x = m[i] ^ m[j];
+    return x ? __clzll((long long)x) : __clzll((long long)((unsigned long long)i ^ (unsigned long long)j)) + 64;
+}
+__device__ __forceinline__ int sgn_ref(int a) { return signbit((float)a) ? -1 : 1; }
+
+__global__ void k_karras(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int id = s - cd.t_off;
+    const int In = cd.T - 1;
+    if (id >= In) return;
+    const unsigned long long *m = d.keys + cd.t_off;
+    // FindRange
+    const int dd = sgn_ref(delta(m, id, id + 1, In) - delta(m, id, id - 1, In));
+    const int delmin = delta(m, id, id - dd, In);
+    int lmax = 2;
+    while (delta(m, id, id + lmax * dd, In) > delmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(m, id, id + (l + t) * dd, In) > delmin) l += t;
+    const int j = id + l * dd;
+    const int first = min(id, j), last = max(id, j);
+    // FindSplit (code-only prefix)
+    int split;
+    const unsigned long long fc = m[first], lc = m[last];
+    if (fc == lc) {
+        split = (first + last) >> 1;
+    } else {
+        const int com = __clzll((long long)(fc ^ lc));
+        split = first;
+        int step = last - first;
+        do {
+            step = (step + 1) >> 1;
+            const int ns = split + step;
+            if (ns < last) {
+                if (__clzll((long long)(fc ^ m[ns])) > com) split = ns;
+            }
+        } while (step > 1);
+    }
+    const int left = split == first ? In + split : split;
+    const int right = split + 1 == last ? In + split + 1 : split + 1;
+    d.child[cd.i_off + id] = make_int2(left, right);
+    // An internal node that the refit never reaches (possible only when a run
+    // of >= 3 equal codes makes two nodes claim one child) keeps stale data in
+    // the reference; here it keeps zeros, deterministically.
+    d.nmin[cd.n_off + id] = make_float4(0.f, 0.f, 0.f, 0.f);
+    d.nmax[cd.n_off + id] = make_float4(0.f, 0.f, 0.f, 0.f);
+    d.rml[cd.i_off + id] = make_int2(0, 0);
+    // The reference's parents[] write race resolved as "largest parent wins".
+    atomicMax(&d.parent[cd.n_off + left], id);
+    atomicMax(&d.parent[cd.n_off + right], id);
+    d.visit[cd.i_off + id] = 0;
+}
+
+// Bottom-up refit: Collision/CudaBVH.cu:128-149.  The second arrival at a
+// node unions its children; a fence orders the child writes before the
+// arrival counter, and the children are re-read from L2.
+__global__ void k_refit(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int id = s - cd.t_off;
+    const int In = cd.T - 1;
+    if (In <= 0) return;
+    int pid = d.parent[cd.n_off + In + id];
+    for (int guard = 0; guard <= cd.T; ++guard) {
+        if (pid < 0 || pid >= In) {
+            if (pid != 0) atomicOr(d.err, ERR_TREE);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&d.visit[cd.i_off + pid], 1) == 0) return;
+        __threadfence();
+        const int2 ch = __ldcg(&d.child[cd.i_off + pid]);
+        const float4 lmn = __ldcg(&d.nmin[cd.n_off + ch.x]), lmx = __ldcg(&d.nmax[cd.n_off + ch.x]);
+        const float4 rmn = __ldcg(&d.nmin[cd.n_off + ch.y]), rmx = __ldcg(&d.nmax[cd.n_off + ch.y]);
+        d.nmin[cd.n_off + pid] = f4(vmin(xyz(lmn), xyz(rmn)), 0.f);
+        d.nmax[cd.n_off + pid] = f4(vmax(xyz(lmx), xyz(rmx)), 0.f);
+        int rl, rr;
+        if (ch.x >= In) rl = ch.x;
+        else { const int2 q = __ldcg(&d.rml[cd.i_off + ch.x]); rl = max(q.x, q.y); }
+        if (ch.y >= In) rr = ch.y;
+        else { const int2 q = __ldcg(&d.rml[cd.i_off + ch.y]); rr = max(q.x, q.y); }
+        d.rml[cd.i_off + pid] = make_int2(rl, rr);
+        if (pid == 0) return;
+        pid = __ldcg(&d.parent[cd.n_off + pid]);
+    }
+    atomicOr(d.err, ERR_TREE);
+}
+
+// Leaf-vs-tree traversal: Collision/CudaBVH.cu:23-113.  Pairs (i, j>i) in
+// left-first DFS order, at most `chunk` per leaf, the rest counted as dropped.
+__global__ void k_traverse(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int id = s - cd.t_off;
+    const int In = cd.T - 1;
+    if (In <= 0) { d.pair_cnt[s] = 0; return; }
+    const int me = In + id;
+    const int chunk = cd.chunk;
+    uint32_t *out = d.pair_chunk + cd.pc_off + (int64_t)id * chunk;
+    const float4 *nmin = d.nmin + cd.n_off, *nmax = d.nmax + cd.n_off;
+    const int2 *child = d.child + cd.i_off, *rml = d.rml + cd.i_off;
+    const float3 amin = xyz(nmin[me]), amax = xyz(nmax[me]);
+    int stack[kTraverseStack];
+    stack[0] = -1;
+    int top = 1, node = 0, got = 0;
+    uint32_t dropped = 0;
+    const int guard_max = 4 * cd.T + 64;
+    for (int guard = 0; guard < guard_max; ++guard) {
+        const int2 ch = __ldg(&child[node]);
+        const int2 rm = __ldg(&rml[node]);
+        bool ol = false, orr = false;
+        if (rm.x > me && overlap(amin, amax, xyz(__ldg(&nmin[ch.x])), xyz(__ldg(&nmax[ch.x])))) ol = true;
+        if (rm.y > me && overlap(amin, amax, xyz(__ldg(&nmin[ch.y])), xyz(__ldg(&nmax[ch.y])))) orr = true;
+        if (ol && ch.x >= In) {
+            if (got < chunk) out[got++] = (uint32_t)(ch.x - In);
+            else ++dropped;
+        }
+        if (orr && ch.y >= In) {
+            if (got < chunk) out[got++] = (uint32_t)(ch.y - In);
+            else ++dropped;
+        }
+        const bool tl = ol && ch.x < In, tr = orr && ch.y < In;
+        if (!tl && !tr) {
+            node = stack[--top];
+        } else {
+            node = tl ? ch.x : ch.y;
+            if (tl && tr) {
+                if (top >= kTraverseStack) { atomicOr(d.err, ERR_STACK); break; }
+                stack[top++] = ch.y;
+            }
+        }
+        if (top == 0) break;
+    }
+    d.pair_cnt[s] = (uint32_t)got;
+    if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
+}
+
+__global__ void k_pair_compact(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const uint32_t n = d.pair_cnt[s];
+    if (!n) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int id = s - cd.t_off;
+    const uint32_t *src = d.pair_chunk + cd.pc_off + (int64_t)id * cd.chunk;
+    const uint32_t o = d.pair_off[s];
+    for (uint32_t k = 0; k < n; ++k) d.pairs[o + k] = make_uint2((uint32_t)s, (uint32_t)cd.t_off + src[k]);
+}
+
+// ---------------------------------------------------------------------------
+// Narrowphase.  Candidate slots of Collision/CudaCollisionDetection.cu:53-189,
+// feature AABB cull of Collision/CudaPrimitiveTests.cu:427-490, CCD of
+// :109-238 with Physics/CudaCubicSolver.cu:5-153 and the tests at :252-425.
+// ---------------------------------------------------------------------------
+struct Wts { float w0, w1, w2, w3; };
+
+__device__ __forceinline__ float triple(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41,
+                                        float t) {
+    return dot(cross(add(x21, mul(v21, t)), add(x31, mul(v31, t))), add(x41, mul(v41, t)));
+}
+__device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41, float a, float b) {
+    float x0 = a, x1 = b;
+    for (int i = 0; i < 20; ++i) {
+        const float f0 = triple(x21, x31, x41, v21, v31, v41, x0);
+        const float f1 = triple(x21, x31, x41, v21, v31, v41, x1);
+        const float xc = (x0 * f1 - x1 * f0) / (f1 - f0);
+        if (fabsf(xc - x1) < kEpsCubic) return xc;
+        x0 = x1;
+        x1 = xc;
+    }
+    return -15.f;
+}
+// When only the second derivative root is in [0,1] the reference reads an
+// uninitialised slot; the found root is used instead (same as the oracle).
+__device__ int coplanarity_times(float3 x1, float3 x2, float3 x3, float3 x4, float3 v1, float3 v2, float3 v3,
+                                 float3 v4, float times[8]) {
+    const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
+    const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
+    const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
+                 x21x31 = cross(x21, x31);
+    const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
+                v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
+                v1x2x3 = dot(v21x31, x41);
+    const float a = v1v2v3, b = x1v2v3 + v1x2v3 + v1v2x3, c = x1x2v3 + x1v2x3 + v1x2x3;
+    const float ad = 3.f * a, bd = 2.f * b;
+    const float disc = 4.f * (b * b - ad * c);
+    const float sq = sqrtf(disc);
+    const float da = 2.f * ad;
+    const float t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
+    float ends[4];
+    int ne = 0;
+    ends[ne++] = 0.f;
+    if (disc >= kEpsCubic) {
+        if (between(t1, 0.f, 1.f)) ends[ne++] = t1;
+        if (between(t2, 0.f, 1.f)) ends[ne++] = t2;
+    } else if (fabsf(disc) < kEpsCubic) {
+        if (between(t1, 0.f, 1.f)) ends[ne++] = t1;
+    }
+    ends[ne++] = 1.f;
+    int n = 0;
+    for (int i = 0; i < ne - 1; ++i) {
+        const float ea = ends[i], eb = ends[i + 1];
+        const float fa = triple(x21, x31, x41, v21, v31, v41, ea);
+        const float fb = triple(x21, x31, x41, v21, v31, v41, eb);
+        if (fabsf(fa) < kEpsCubic) times[n++] = ea;
+        if (fa * fb < 0.f) {
+            const float t = secant(x21, x31, x41, v21, v31, v41, ea, eb);
+            if (t != -15.f) times[n++] = t;
+        }
+    }
+    return n;
+}
+
+__device__ __forceinline__ float3 project_on_line(float3 p, float3 e1, float3 e2) {
+    const float3 ab = sub(e2, e1), ap = sub(p, e1);
+    return add(e1, mul(ab, dot(ap, ab) / dot(ab, ab)));
+}
+__device__ __forceinline__ float3 clamp_on_line(float3 p, float3 e1, float3 e2) {
+    const float d1 = dist(p, e1), d2 = dist(p, e2);
+    if (fabsf(d1 + d2 - dist(e1, e2)) < kEpsPbd) return p;
+    return d1 < d2 ? e1 : e2;
+}
+
+__device__ bool test_vf(float3 x4, float3 x1, float3 x2, float3 x3, float th, Wts &w) {
+    const float3 x13 = sub(x1, x3), x23 = sub(x2, x3), x43 = sub(x4, x3);
+    const float3 crs = cross(sub(x2, x1), sub(x3, x1));
+    const float3 n = normalize(crs);
+    if (fabsf(dot(x43, n)) <= th) {
+        const float dt = dot(x13, x23);
+        const float m11 = dot(x13, x13), m12 = dt, m21 = dt, m22 = dot(x23, x23);
+        const float vr1 = dot(x13, x43), vr2 = dot(x23, x43);
+        const float w2 = (m11 * vr2 - m21 * vr1) / (m11 * m22 - m21 * m12);
+        const float w1 = (vr1 - m12 * w2) / m11;
+        const float w3 = 1.f - w1 - w2;
+        const float del = th / (len(x13) + len(x23) + len(sub(x1, x2)));
+        const float lo = 0.f, hi = 1.f + del;
+        if (between(w1, lo, hi) && between(w2, lo, hi) && between(w3, lo, hi)) {
+            w.w0 = 1.f; w.w1 = -w1; w.w2 = -w2; w.w3 = -w3;
+            return true;
+        }
+    }
+    return false;
+}
+
+__device__ bool test_ee(float3 x1, float3 x2, float3 x3, float3 x4, float th, Wts &w) {
+    const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x43 = sub(x4, x3);
+    const float3 crs = cross(x21, x43);
+    if (len(crs) < kEpsEE) {
+        const float3 m1 = add(x1, dvs(x21, 2.f)), m2 = add(x3, dvs(x43, 2.f));
+        if (dist(m1, m2) <= th) {
+            w.w0 = w.w1 = w.w2 = w.w3 = 0.5f;
+            return true;
+        }
+        return false;
+    }
+    if (is_zero(crs)) return false;
+    const float dt = dot(neg(x21), x43);
+    const float m11 = dot(x21, x21), m12 = dt, m21 = dt, m22 = dot(x43, x43);
+    const float vr1 = dot(x21, x31), vr2 = dot(neg(x43), x31);
+    float b = (m11 * vr2 - m21 * vr1) / (m11 * m22 - m21 * m12);
+    float a = (vr1 - m12 * b) / m11;
+    if (between(a, 0.f, 1.f) && between(b, 0.f, 1.f)) {
+        const float3 cp1 = add(x1, mul(x21, a)), cp2 = add(x3, mul(x43, a));
+        if (dist(cp1, cp2) <= th) {
+            w.w0 = 1.f - a; w.w1 = a; w.w2 = -(1.f - b); w.w3 = -b;
+            return true;
+        }
+    } else {
+        const float ac = clampf(a, 0.f, 1.f), bc = clampf(b, 0.f, 1.f);
+        const float d1 = fabsf(a - ac) * len(x21), d2 = fabsf(b - bc) * len(x43);
+        a = ac;
+        b = bc;
+        float3 cp1, cp2;
+        if (d1 > d2) {
+            cp1 = add(x1, mul(x21, a));
+            cp2 = clamp_on_line(project_on_line(cp1, x3, x4), x3, x4);
+        } else {
+            cp2 = add(x3, mul(x43, b));
+            cp1 = clamp_on_line(project_on_line(cp2, x1, x2), x1, x2);
+        }
+        if (dist(cp1, cp2) <= th) {
+            w.w0 = 1.f - a; w.w1 = a; w.w2 = -(1.f - b); w.w3 = -b;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Particle swept box of Collision/FeatureList.cu:134-148, recomputed from
+// x and x_prev (min/max are exact, so this equals the stored boxes).
+struct Box { float3 lo, hi; };
+__device__ __forceinline__ Box pbox(const DevPtrs &d, int v, float h) {
+    const float3 p = xyz(d.x[v]), q = xyz(d.xp[v]);
+    return Box{subc(vmin(p, q), h), addc(vmax(p, q), h)};
+}
+
+// CCD of one VF candidate (vertex p against face f1 f2 f3) on x_prev and v:
+// Collision/CudaPrimitiveTests.cu:128-184.
+__device__ bool vf_ccd(const DevPtrs &d, int p, int f1, int f2, int f3, float h, float dt, Wts &w) {
+    float3 x4 = xyz(d.xp[p]), x1 = xyz(d.xp[f1]), x2 = xyz(d.xp[f2]), x3 = xyz(d.xp[f3]);
+    const float3 v4 = xyz(d.v[p]), v1 = xyz(d.v[f1]), v2 = xyz(d.v[f2]), v3 = xyz(d.v[f3]);
+    float times[8];
+    const int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+    for (int i = 0; i < n; ++i) {
+        const float t = times[i] * dt;
+        x4 = add(x4, mul(v4, t));
+        x1 = add(x1, mul(v1, t));
+        x2 = add(x2, mul(v2, t));
+        x3 = add(x3, mul(v3, t));
+        if (test_vf(x4, x1, x2, x3, h, w)) return true;
+    }
+    return false;
+}
+
+// CCD of one EE candidate: Collision/CudaPrimitiveTests.cu:187-238.
+__device__ bool ee_ccd(const DevPtrs &d, int e1, int e2, int e3, int e4, float h, float dt, Wts &w) {
+    float3 x1 = xyz(d.xp[e1]), x2 = xyz(d.xp[e2]), x3 = xyz(d.xp[e3]), x4 = xyz(d.xp[e4]);
+    const float3 v1 = xyz(d.v[e1]), v2 = xyz(d.v[e2]), v3 = xyz(d.v[e3]), v4 = xyz(d.v[e4]);
+    float times[8];
+    const int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+    for (int i = 0; i < n; ++i) {
+        const float t = times[i] * dt;
+        x1 = add(x1, mul(v1, t));
+        x2 = add(x2, mul(v2, t));
+        x3 = add(x3, mul(v3, t));
+        x4 = add(x4, mul(v4, t));
+        if (test_ee(x1, x2, x3, x4, h, w)) return true;
+    }
+    return false;
+}
+
+// EE slot s: edge (s%3) of A x edge (s/3) of B; edge k of a triangle is
+// (v1,v2 | bit 2), (v1,v3 | bit 0), (v2,v3 | bit 1).
+__device__ __forceinline__ void edge_of(int k, int &a, int &b, int &bit) {
+    if (k == 0) { a = 0; b = 1; bit = 2; }
+    else if (k == 1) { a = 0; b = 2; bit = 0; }
+    else { a = 1; b = 2; bit = 1; }
+}
+
+// Vertex ids of candidate slot s of a pair (A, B): VF slots 0..5 are
+// (vertex s of A | face B) then (vertex s-3 of B | face A); EE slots 6..14 are
+// edge (s-6)%3 of A x edge (s-6)/3 of B (Collision/CudaCollisionDetection.cu:101-187).
+__device__ __forceinline__ int4 candidate_ids(const int vid[6], int s) {
+    if (s < 6) {
+        const int o = s < 3 ? 3 : 0;
+        return make_int4(vid[s], vid[o], vid[o + 1], vid[o + 2]);
+    }
+    int a0, a1, ab, b0, b1, bb;
+    edge_of((s - 6) % 3, a0, a1, ab);
+    edge_of((s - 6) / 3, b0, b1, bb);
+    return make_int4(vid[a0], vid[a1], vid[3 + b0], vid[3 + b1]);
+}
+
+// Stage 1 of the narrowphase: the candidates of one broadphase pair that
+// survive feature ownership, the shared-vertex sanity checks and the feature
+// AABB cull (Collision/CudaPrimitiveTests.cu:240-248, 427-490).  The checks
+// commute, so the surviving set is the reference's; the six vertex boxes are
+// built once per pair.
+__device__ uint16_t pair_filter(const DevPtrs &d, uint32_t p) {
+    const uint2 pr = d.pairs[p];
+    const int c = d.tcloth[pr.x];
+    const float h = d.cloth[c].h;
+    const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+    const int fa = A.w, fb = B.w;
+    const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
+    uint32_t want = 0;
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        const int f = s < 3 ? fa : fb;
+        if (!((f >> (5 - s % 3)) & 1)) continue;
+        const int pv = vid[s];
+        const int o = s < 3 ? 3 : 0;
+        if (pv == vid[o] || pv == vid[o + 1] || pv == vid[o + 2]) continue;
+        want |= 1u << s;
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        int a0, a1, ab, b0, b1, bb;
+        edge_of(s % 3, a0, a1, ab);
+        edge_of(s / 3, b0, b1, bb);
+        if (!(((fa >> ab) & 1) & ((fb >> bb) & 1))) continue;
+        const int e1 = vid[a0], e2 = vid[a1], e3 = vid[3 + b0], e4 = vid[3 + b1];
+        if (e1 == e3 || e1 == e4 || e2 == e3 || e2 == e4) continue;
+        want |= 1u << (6 + s);
+    }
+    if (!want) return 0;
+    Box bx[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) bx[k] = pbox(d, vid[k], h);
+    uint32_t mask = 0;
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        if (!((want >> s) & 1)) continue;
+        const int o = s < 3 ? 3 : 0;
+        const float3 flo = min3(bx[o].lo, bx[o + 1].lo, bx[o + 2].lo);
+        const float3 fhi = max3(bx[o].hi, bx[o + 1].hi, bx[o + 2].hi);
+        if (overlap(bx[s].lo, bx[s].hi, flo, fhi)) mask |= 1u << s;
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        if (!((want >> (6 + s)) & 1)) continue;
+        int a0, a1, ab, b0, b1, bb;
+        edge_of(s % 3, a0, a1, ab);
+        edge_of(s / 3, b0, b1, bb);
+        if (overlap(vmin(bx[a0].lo, bx[a1].lo), vmax(bx[a0].hi, bx[a1].hi), vmin(bx[3 + b0].lo, bx[3 + b1].lo),
+                    vmax(bx[3 + b0].hi, bx[3 + b1].hi)))
+            mask |= 1u << (6 + s);
+    }
+    return (uint16_t)mask;
+}
+
+__global__ void k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) {
+    const uint32_t n = *npairs;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint16_t m = pair_filter(d, p);
+        d.pair_mask[p] = m;
+        d.pair_vf_cnt[p] = (uint32_t)__popc((unsigned)m);
+    }
+}
+
+// Stage 2: one (pair, slot) entry per surviving candidate, in pair-then-slot
+// order — the order of the reference's compactions.
+__global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) {
+    const uint32_t n = *npairs;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t m = d.pair_mask[p];
+        uint64_t o = d.pair_vf_off[p];
+        while (m) {
+            const int s = __ffs(m) - 1;
+            m &= m - 1;
+            if (o < d.cand_cap) d.cand[o] = ((unsigned long long)p << 4) | (unsigned)s;
+            else atomicOr(d.err, ERR_CAND_OVERFLOW);
+            ++o;
+        }
+    }
+}
+
+__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long long q, int4 &ids, bool &isvf, Wts &w) {
+    const uint32_t p = (uint32_t)(q >> 4);
+    const int s = (int)(q & 15u);
+    const uint2 pr = d.pairs[p];
+    const ClothDev &cd = d.cloth[d.tcloth[pr.x]];
+    const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+    const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
+    ids = candidate_ids(vid, s);
+    isvf = s < 6;
+    return isvf ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
+                : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
+}
+
+// Stage 3: CCD of every candidate, one per thread
+// (Collision/CudaPrimitiveTests.cu:109-238).
+__global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
+    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        int4 ids;
+        bool isvf;
+        Wts w;
+        const bool hit = candidate_ccd(d, d.cand[q], ids, isvf, w);
+        d.cand_vf[q] = hit && isvf;
+        d.cand_ee[q] = hit && !isvf;
+    }
+}
+
+// Stage 4: contacts written in candidate order (the reference's compaction
+// order); the CCD of the few hits is evaluated again for their weights.
+__global__ void k_ccd_write(DevPtrs d, const uint32_t *__restrict__ ncand) {
+    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const bool hv = d.cand_vf[q] != 0, he = d.cand_ee[q] != 0;
+        if (!hv && !he) continue;
+        int4 ids;
+        bool isvf;
+        Wts w;
+        candidate_ccd(d, d.cand[q], ids, isvf, w);
+        if (hv) {
+            const uint32_t o = d.cand_vf_off[q];
+            if (o < d.vf_cap) { d.vf_v[o] = ids; d.vf_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
+            else atomicOr(d.err, ERR_VF_OVERFLOW);
+        } else {
+            const uint32_t o = d.cand_ee_off[q];
+            if (o < d.ee_cap) { d.ee_v[o] = ids; d.ee_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
+            else atomicOr(d.err, ERR_EE_OVERFLOW);
+        }
+    }
+}
+
+// Per-cloth contact ranges (the VF and the EE contacts of one cloth are
+// contiguous).
+__global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncand) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.C) return;
+    const ClothDev &cd = d.cloth[c];
+    const uint32_t nc = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const uint32_t p0 = d.pair_off[cd.t_off], p1 = d.pair_off[cd.t_off + cd.T];
+    const uint32_t q0 = min(d.pair_vf_off[p0], nc), q1 = min(d.pair_vf_off[p1], nc);
+    d.crange[c] = make_uint4((uint32_t)min((uint64_t)d.cand_vf_off[q0], d.vf_cap),
+                             (uint32_t)min((uint64_t)d.cand_vf_off[q1], d.vf_cap),
+                             (uint32_t)min((uint64_t)d.cand_ee_off[q0], d.ee_cap),
+                             (uint32_t)min((uint64_t)d.cand_ee_off[q1], d.ee_cap));
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+static inline int nblk(int64_t n, int b = kThreads) { return (int)((n + b - 1) / b); }
+
+void launch_triangles(const DevPtrs &d, cudaStream_t st) {
+    if (d.Ttot) k_triangles<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+}
+void launch_leaves_from_boxes(const DevPtrs &d, const float *bmin, const float *bmax, int T, int mode,
+                              cudaStream_t st) {
+    if (T) k_leaves_from_boxes<<<nblk(T), kThreads, 0, st>>>(d, bmin, bmax, T, mode);
+}
+void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream_t st) {
+    if (!d.nstiles) return;
+    for (int p = 0; p < passes; ++p) {
+        const bool even = (p & 1) == 0;
+        const unsigned long long *kin = even ? d.keys : d.keys_alt;
+        unsigned long long *kout = even ? d.keys_alt : d.keys;
+        const uint32_t *pin = even ? d.payload : d.payload_alt;
+        uint32_t *pout = even ? d.payload_alt : d.payload;
+        k_sort_hist<<<d.nstiles, kThreads, 0, st>>>(d, kin, p * kSortBits);
+        k_sort_offsets<<<d.C, kSortBuckets, 0, st>>>(d, tile_first);
+        k_sort_scatter<<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits);
+    }
+}
+void launch_post_sort(const DevPtrs &d, cudaStream_t st) {
+    if (d.Ttot) k_post_sort<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+}
+void launch_karras(const DevPtrs &d, cudaStream_t st) {
+    if (d.Ttot) k_karras<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+}
+void launch_refit(const DevPtrs &d, cudaStream_t st) {
+    if (d.Ttot) k_refit<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+}
+void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
+    if (d.Ttot) k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+}
+void launch_pair_compact(const DevPtrs &d, cudaStream_t st) {
+    if (d.Ttot) k_pair_compact<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+}
+void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncand, int grid, int stage,
+                   cudaStream_t st) {
+    if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs);
+    else if (stage == 1) k_narrow_expand<<<grid, kThreads, 0, st>>>(d, npairs);
+    else if (stage == 2) k_ccd<<<grid, kThreads, 0, st>>>(d, ncand);
+    else if (stage == 3) k_ccd_write<<<grid, kThreads, 0, st>>>(d, ncand);
+    else k_contact_ranges<<<nblk(d.C, 128), 128, 0, st>>>(d, ncand);
+}
+
+}  // namespace lc

@@ -1,0 +1,165 @@
+"""Seeded synthetic inputs of the five cloth workloads.
+
+The reference builds its cloth with VisualBodyFactory::CreateMeshProps
+(Rendering/VisualBodyFactory.cpp:343-391) and pins two corners
+(Managers/MastersSimulationManager.cpp:67-77); the triangle topology here is
+that generator's (lc_mesh_grid), placed as a 1 m x 1 m grid in the XZ plane at
+y = 1 m with a seeded uniform jitter on every coordinate.  Parameters the
+workloads leave open keep the reference defaults of
+Managers/MastersSimulationManager.cpp:33-62.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _ffi
+
+
+@dataclass
+class ClothSpec:
+    positions: np.ndarray      # (V, 3) float32
+    indices: np.ndarray        # (T, 3) uint32
+    pinned: np.ndarray         # (V,) uint8
+    params: _ffi.ClothParams
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def num_vertices(self) -> int:
+        return int(self.positions.shape[0])
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.indices.shape[0])
+
+
+def grid_indices(n: int) -> np.ndarray:
+    t = _ffi.lib().lc_mesh_grid(n, n, None)
+    out = np.empty((t, 3), dtype=np.uint32)
+    _ffi.lib().lc_mesh_grid(n, n, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def icosphere(depth: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """Rendering/VisualBodyFactory.cpp:259-341 (unwelded vertices)."""
+    t = _ffi.lib().lc_mesh_icosphere(depth, None, None)
+    v = np.empty((3 * t // 4 * 2, 3), dtype=np.float32)
+    idx = np.empty((t, 3), dtype=np.uint32)
+    _ffi.lib().lc_mesh_icosphere(depth, v.ctypes.data_as(C.c_void_p), idx.ctypes.data_as(C.c_void_p))
+    return v * np.float32(radius) + np.asarray(center, dtype=np.float32), idx
+
+
+def grid_positions(n: int, rng: np.random.Generator, jitter: float = 1e-4, y: float = 1.0,
+                   span: float = 1.0, origin=(0.0, 0.0)) -> np.ndarray:
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    p = np.stack([origin[0] + span * i / (n - 1), np.full(i.shape, y), origin[1] + span * j / (n - 1)], axis=-1)
+    p = p.reshape(-1, 3) + rng.uniform(-jitter, jitter, size=(n * n, 3))
+    return p.astype(np.float32)
+
+
+def corner_pins(n: int) -> np.ndarray:
+    """The two pinned vertices of Managers/MastersSimulationManager.cpp:67-77."""
+    p = np.zeros(n * n, dtype=np.uint8)
+    p[0] = 1
+    p[(n - 1) * n] = 1
+    return p
+
+
+def base_params(iterations: int, stiffness: float, dt: float = 1.0 / 60.0) -> _ffi.ClothParams:
+    p = _ffi.default_params()
+    p.timestep = dt
+    p.gravity[:] = (0.0, -9.81, 0.0)
+    p.solverIterations = iterations
+    p.kStretch = stiffness
+    p.kBend = stiffness
+    p.windOn = 0
+    return p
+
+
+def set_constant_wind(p: _ffi.ClothParams, wind) -> None:
+    """A constant wind: the reference update with zero variation clamped to itself."""
+    p.windOn = 1
+    p.startWindDir[:] = wind
+    p.minWindDir[:] = wind
+    p.maxWindDir[:] = wind
+    p.windMinVariation = 0.0
+    p.windMaxVariation = 0.0
+
+
+def small_cloth(seed: int = 0, n: int = 32, iterations: int = 10, stiffness: float = 0.9,
+                thickness: float = 0.01) -> ClothSpec:
+    """32x32 grid, two pinned corners, 10 iterations, stiffness 0.9, 0.01 m thickness."""
+    rng = np.random.default_rng(seed)
+    p = base_params(iterations, stiffness)
+    p.thicknessFromMesh = 0
+    p.thickness = thickness
+    p.dims[:] = (n, n)
+    return ClothSpec(grid_positions(n, rng), grid_indices(n), corner_pins(n), p,
+                     dict(workload="plain-small", n=n, steps=120))
+
+
+def large_cloth(seed: int = 0, n: int = 512, iterations: int = 20, stiffness: float = 0.9,
+                sphere_radius: float = 0.3) -> ClothSpec:
+    """512x512 grid centred over a sphere of radius 0.3 m at the origin,
+    dropped from y = 1 m (no pins), 20 iterations.  The sphere is the
+    reference's analytic sphere collider (CudaPBD::SetSpherePos)."""
+    rng = np.random.default_rng(seed)
+    p = base_params(iterations, stiffness)
+    p.dims[:] = (n, n)
+    p.worldMin[:] = (-1.0, -1.0, -1.0)
+    p.worldMax[:] = (1.0, 1.0, 1.0)
+    p.mortonOrigin[:] = (-1.0, -1.0, -1.0)
+    p.mortonScale = 0.5
+    p.sphereOn = 1
+    p.spherePos[:] = (0.0, 0.0, 0.0)
+    p.sphereRadius = sphere_radius
+    pos = grid_positions(n, rng, origin=(-0.5, -0.5))
+    return ClothSpec(pos, grid_indices(n), np.zeros(n * n, dtype=np.uint8), p,
+                     dict(workload="plain-large", n=n, steps=300))
+
+
+def batched_cloths(seed: int = 0, count: int = 256, n_min: int = 16, n_max: int = 192,
+                   iterations: int = 10) -> list[ClothSpec]:
+    """256 cloths, side drawn from U{16..192}, stiffness U[0.5, 1.0], constant
+    wind U[-2, 2] m/s^2 on x and z, two pinned corners each."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(n_min, n_max + 1, size=count)
+    ks = rng.uniform(0.5, 1.0, size=count)
+    winds = rng.uniform(-2.0, 2.0, size=(count, 2))
+    out = []
+    for c in range(count):
+        n = int(sides[c])
+        p = base_params(iterations, float(ks[c]))
+        p.dims[:] = (n, n)
+        set_constant_wind(p, (float(winds[c, 0]), 0.0, float(winds[c, 1])))
+        out.append(ClothSpec(grid_positions(n, rng), grid_indices(n), corner_pins(n), p,
+                             dict(workload="batched", n=n, k=float(ks[c]))))
+    return out
+
+
+def adjoint_cloth(seed: int = 0, n: int = 64, stiffness: float = 0.9, wind=(0.0, 0.0, 0.0)) -> ClothSpec:
+    """64x64 grid, 10 iterations (differentiable rollout workload)."""
+    rng = np.random.default_rng(seed)
+    p = base_params(10, stiffness)
+    p.dims[:] = (n, n)
+    if any(w != 0.0 for w in wind):
+        set_constant_wind(p, tuple(float(w) for w in wind))
+    return ClothSpec(grid_positions(n, rng), grid_indices(n), corner_pins(n), p,
+                     dict(workload="adjoint", n=n, steps=60))
+
+
+def random_triangle_boxes(count: int, seed: int = 0):
+    """LBVH microbenchmark input: first vertex uniform in the unit cube, two
+    edges of length U[1e-3, 5e-3] in uniformly random directions; returns the
+    (min, max) boxes, each (count, 3) float32."""
+    rng = np.random.default_rng(seed)
+    v0 = rng.uniform(0.0, 1.0, size=(count, 3))
+    dirs = rng.normal(size=(count, 2, 3))
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    lens = rng.uniform(1e-3, 5e-3, size=(count, 2, 1))
+    v1 = v0 + dirs[:, 0] * lens[:, 0]
+    v2 = v0 + dirs[:, 1] * lens[:, 1]
+    tri = np.stack([v0, v1, v2], axis=1).astype(np.float32)
+    return tri.min(axis=1), tri.max(axis=1)

@@ -1,0 +1,1099 @@
+// lc_oracle.hpp — CPU oracle of the reference's GPU cloth step.
+//
+// TEST INFRASTRUCTURE ONLY.  This file restates, in plain C++, the algorithm
+// of the reference's GPU cloth body (Tureyz/Licenta; paths relative to
+// LicentaV2/LicentaV2/) so that tests, smoke() and the CPU-baseline leg of
+// bench.py can check the CUDA engine against it.  Nothing in the product
+// (licenta_gb300/) includes, links or calls it.
+//
+// Parity status: the integer and contact stages (Morton codes, sort order,
+// Karras topology, refit, traversal pairs, feature AABB cull, CCD contacts)
+// are PINNED against the reference's own kernels (Core/CudaUtils.cu,
+// Collision/CudaBVH.cu, Collision/CudaPrimitiveTests.cu,
+// Physics/CudaCubicSolver.cu, Collision/FeatureList.cu built unmodified for
+// sm_103a and run on a GB300; fixtures under tests/golden/).  The PBD solver
+// half (Physics/CudaPBD.cu) cannot be built outside the reference's Windows/GL
+// project, so the solver restatement is "parity unpinned" by the reference:
+// it is checked by FP64-vs-FP32 agreement and the invariants in tests/.
+//
+// The class is templated on the real type R.  R = float is the FP32 mirror:
+// the same operation order as the reference kernels (no FMA contraction, the
+// build uses -ffp-contract=off), so integer/contact results are bit-exact for
+// identical inputs.  R = double is the FP64 oracle the positions are compared
+// against.  The vector length is sqrt(x*x+y*y+z*z) in both modes (the
+// reference's norm3df is CUDA library code and is not reproduced).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <utility>
+#include <vector>
+
+#include "../include/lc/lc.h"
+
+namespace lco {
+
+using u8 = uint8_t;
+using u32 = uint32_t;
+using u64 = uint64_t;
+
+// ---------------------------------------------------------------------------
+// float3 algebra — Core/CudaUtils.cu:32-107, 139-276 (operation order kept).
+// ---------------------------------------------------------------------------
+template <class R> struct V3 {
+    R x, y, z;
+};
+template <class R> inline V3<R> mk(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <class R> inline V3<R> operator+(V3<R> a, V3<R> b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <class R> inline V3<R> operator-(V3<R> a, V3<R> b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <class R> inline V3<R> operator-(V3<R> a) { return mk(-a.x, -a.y, -a.z); }
+template <class R> inline V3<R> operator*(V3<R> a, R s) { return mk(a.x * s, a.y * s, a.z * s); }
+template <class R> inline V3<R> operator*(R s, V3<R> a) { return mk(a.x * s, a.y * s, a.z * s); }
+template <class R> inline V3<R> operator/(V3<R> a, R s) { return mk(a.x / s, a.y / s, a.z / s); }
+template <class R> inline V3<R> addc(V3<R> a, R s) { return mk(a.x + s, a.y + s, a.z + s); }
+template <class R> inline V3<R> subc(V3<R> a, R s) { return mk(a.x - s, a.y - s, a.z - s); }
+template <class R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R> inline V3<R> cross(V3<R> a, V3<R> b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <class R> inline R len(V3<R> a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+template <class R> inline R dist(V3<R> a, V3<R> b) { return len(a - b); }
+template <class R> inline V3<R> normalize(V3<R> a) { return a / len(a); }
+template <class R> inline bool is_zero(V3<R> a) { return a.x == R(0) && a.y == R(0) && a.z == R(0); }
+template <class R> inline V3<R> vmin(V3<R> a, V3<R> b) { return mk(std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z)); }
+template <class R> inline V3<R> vmax(V3<R> a, V3<R> b) { return mk(std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z)); }
+template <class R> inline V3<R> min3(V3<R> a, V3<R> b, V3<R> c) { return vmin(a, vmin(b, c)); }
+template <class R> inline V3<R> max3(V3<R> a, V3<R> b, V3<R> c) { return vmax(a, vmax(b, c)); }
+template <class R> inline R clampf(R v, R lo, R hi) { return std::fmin(std::fmax(lo, v), hi); }
+template <class R> inline bool between(R v, R lo, R hi) { return v >= lo && v <= hi; }
+// Core/CudaUtils.cu:364-371 — closed-interval overlap.
+template <class R> inline bool overlap(V3<R> amin, V3<R> amax, V3<R> bmin, V3<R> bmax) {
+    bool a = amax.x < bmin.x || amin.x > bmax.x;
+    bool b = amax.y < bmin.y || amin.y > bmax.y;
+    bool c = amax.z < bmin.z || amin.z > bmax.z;
+    return !(a || b || c);
+}
+
+// Constants of the reference.
+static const double kEpsPbd = 0.00000001;      // Physics/CudaPBD.cu:33 (and Core/CudaUtils.cu:4)
+static const double kEpsCubic = 1.0 / 1000000;  // Physics/CudaCubicSolver.cuh:12
+static const double kEpsEE = 0.000000001;       // Collision/CudaPrimitiveTests.cu:124
+static const float kPi = 3.14159265359f;        // Physics/CudaPBD.cu:35
+
+// ---------------------------------------------------------------------------
+// Morton codes — Core/CudaUtils.cu:278-325 (REF63 live encoder) and the
+// commented-out 30-bit encoder at :289-308 (K30).  Bit k of each axis lands
+// at bit 3k (+2 for x, +1 for y), the interleave of ExpandBy2.
+// ---------------------------------------------------------------------------
+inline u64 spread_bits(u64 v, int nbits) {
+    u64 r = 0;
+    for (int k = 0; k < nbits; ++k)
+        if ((v >> k) & 1u) r |= u64(1) << (3 * k);
+    return r;
+}
+inline u64 quantize(float x, int mode) {
+    if (mode == LC_MORTON_K30) {
+        float q = std::fmin(std::fmax(x * 1024.f, 0.0f), 1023.0f);
+        return (u64)q;
+    }
+    float q = std::fmin(std::fmax(x * 2097152.f, 0.0f), 2097151.0f);
+    return (u64)q;
+}
+inline u64 morton3d(float x, float y, float z, int mode) {
+    int nb = mode == LC_MORTON_K30 ? 10 : 21;
+    return (spread_bits(quantize(x, mode), nb) << 2) + (spread_bits(quantize(y, mode), nb) << 1) +
+           spread_bits(quantize(z, mode), nb);
+}
+
+inline int clz64(u64 v) { return v ? __builtin_clzll(v) : 64; }
+
+// Core/CudaUtils.cu:338-351
+inline int delta(const u64 *m, int i, int j, int maxi) {
+    if (j < 0 || j > maxi) return -1;
+    u64 x = m[i] ^ m[j];
+    return x ? clz64(x) : clz64(u64(i) ^ u64(j)) + 64;
+}
+// Core/CudaUtils.cu:353-362 — sgn(0) = +1.
+inline int sgn(int a) { return std::signbit((float)a) ? -1 : 1; }
+
+// Collision/CudaBVH.cu:190-212
+inline void find_range(const u64 *m, int count, int id, int &first, int &last) {
+    int d = sgn(delta(m, id, id + 1, count) - delta(m, id, id - 1, count));
+    int delmin = delta(m, id, id - d, count);
+    int lmax = 2;
+    while (delta(m, id, id + lmax * d, count) > delmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(m, id, id + (l + t) * d, count) > delmin) l += t;
+    int j = id + l * d;
+    first = std::min(id, j);
+    last = std::max(id, j);
+}
+// Collision/CudaBVH.cu:214-242 — code-only prefix, no index tiebreak.
+inline int find_split(const u64 *m, int first, int last) {
+    u64 fc = m[first], lc = m[last];
+    if (fc == lc) return (first + last) >> 1;
+    int com = clz64(fc ^ lc);
+    int split = first, step = last - first;
+    do {
+        step = (step + 1) >> 1;
+        int ns = split + step;
+        if (ns < last) {
+            if (clz64(fc ^ m[ns]) > com) split = ns;
+        }
+    } while (step > 1);
+    return split;
+}
+
+// ---------------------------------------------------------------------------
+// Topology built once per cloth (constructor work).
+// ---------------------------------------------------------------------------
+struct Topology {
+    int V = 0, T = 0;
+    std::vector<u32> idx;        // 3T, original triangle order
+    std::vector<u8> pinned;      // V
+    std::vector<u8> features;    // T, per original triangle (bits 5..0)
+    std::vector<int> s1, s2;     // stretch constraints
+    std::vector<double> sl0;
+    std::vector<int> b1, b2, b3, b4;  // bend constraints (p1,p2 shared, p3,p4 opposite)
+    std::vector<int> soff;       // V+1 static CSR offsets (Physics/CudaPBD.cu:146-186)
+    std::vector<int> sent;       // entries: kind<<30 | role<<28 | constraint
+    std::vector<int> fixed;      // pinned ids (Physics/CudaPBD.cu:48-58)
+    std::vector<double> lra_l0;  // V*F
+    std::vector<double> kst, kbd;  // per-constraint stiffness
+    double vmass = 0;
+};
+
+enum { ENT_STRETCH = 0, ENT_BEND = 1 };
+
+// Rendering/VisualBodyFactory.cpp:343-391 topology (used by tests through
+// the C API); positions are supplied by the caller.
+inline void grid_indices(int rows, int cols, std::vector<u32> &out) {
+    out.clear();
+    for (int i = 0; i < rows - 1; ++i)
+        for (int j = 0; j < cols - 1; ++j) {
+            if ((i + j) % 2 == 0) {
+                u32 t[6] = {u32(rows * i + j), u32(rows * (i + 1) + j), u32(rows * i + j + 1),
+                            u32(rows * i + j + 1), u32(rows * (i + 1) + j), u32(rows * (i + 1) + j + 1)};
+                out.insert(out.end(), t, t + 6);
+            } else {
+                u32 t[6] = {u32(rows * i + j), u32(rows * (i + 1) + j), u32(rows * (i + 1) + j + 1),
+                            u32(rows * (i + 1) + j + 1), u32(rows * i + j + 1), u32(rows * i + j)};
+                out.insert(out.end(), t, t + 6);
+            }
+        }
+}
+
+inline double ddist(const float *p, int a, int b) {
+    double dx = (double)p[3 * a] - p[3 * b], dy = (double)p[3 * a + 1] - p[3 * b + 1],
+           dz = (double)p[3 * a + 2] - p[3 * b + 2];
+    return std::sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// Physics/CudaPBD.cu:289-370 — shared pair (p1,p2) and the opposite vertices.
+inline void bend_ids(const int t1[3], const int t2[3], int &p1, int &p2, int &p3, int &p4) {
+    p1 = p2 = p3 = p4 = -1;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (t1[i] == t2[j]) { p1 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (t1[i] == t2[j] && t1[i] != p1) { p2 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        if (t1[i] != p1 && t1[i] != p2) { p3 = t1[i]; break; }
+    for (int i = 0; i < 3; ++i)
+        if (t2[i] != p1 && t2[i] != p2) { p4 = t2[i]; break; }
+}
+
+inline void build_topology(const lc_cloth_desc &d, Topology &tp) {
+    tp.V = d.num_vertices;
+    tp.T = d.num_triangles;
+    tp.idx.assign(d.indices, d.indices + 3 * tp.T);
+    tp.pinned.assign(tp.V, 0);
+    if (d.pinned)
+        for (int i = 0; i < tp.V; ++i) tp.pinned[i] = d.pinned[i] ? 1 : 0;
+    const float *P = d.positions;
+    // Physics/CudaDeformableBody.cpp:52 — vertex mass = objectMass / vertex count.
+    tp.vmass = (double)(d.params.objectMass / (float)tp.V);
+
+    // Physics/CudaPBD.cu:111-142 — first sighting of an undirected edge makes a
+    // stretch constraint, the second makes a bend constraint and forgets it.
+    std::map<std::pair<int, int>, int> open;  // edge -> triangle index
+    for (int t = 0; t < tp.T; ++t) {
+        int tri[3] = {(int)tp.idx[3 * t], (int)tp.idx[3 * t + 1], (int)tp.idx[3 * t + 2]};
+        for (int j = 0; j < 3; ++j) {
+            int a = tri[j], b = tri[(j + 1) % 3];
+            std::pair<int, int> key(std::min(a, b), std::max(a, b));
+            auto it = open.find(key);
+            if (it != open.end()) {
+                int o = it->second;
+                int t1[3] = {(int)tp.idx[3 * o], (int)tp.idx[3 * o + 1], (int)tp.idx[3 * o + 2]};
+                int p1, p2, p3, p4;
+                bend_ids(t1, tri, p1, p2, p3, p4);
+                tp.b1.push_back(p1); tp.b2.push_back(p2); tp.b3.push_back(p3); tp.b4.push_back(p4);
+                open.erase(it);
+            } else {
+                open[key] = t;
+                tp.s1.push_back(a);
+                tp.s2.push_back(b);
+                tp.sl0.push_back(ddist(P, a, b));
+            }
+        }
+    }
+    int E = (int)tp.s1.size(), B = (int)tp.b1.size();
+    tp.kst.assign(E, d.params.kStretch);
+    tp.kbd.assign(B, d.params.kBend);
+    // Physics/CudaPBD.cu:146-233 — per-vertex slots, stretch first then bend.
+    std::vector<int> cnt(tp.V, 0);
+    for (int i = 0; i < E; ++i) { cnt[tp.s1[i]]++; cnt[tp.s2[i]]++; }
+    for (int i = 0; i < B; ++i) { cnt[tp.b1[i]]++; cnt[tp.b2[i]]++; cnt[tp.b3[i]]++; cnt[tp.b4[i]]++; }
+    tp.soff.assign(tp.V + 1, 0);
+    for (int i = 0; i < tp.V; ++i) tp.soff[i + 1] = tp.soff[i] + cnt[i];
+    tp.sent.assign(tp.soff[tp.V], 0);
+    std::fill(cnt.begin(), cnt.end(), 0);
+    auto put = [&](int v, int kind, int role, int c) {
+        tp.sent[tp.soff[v] + cnt[v]++] = (kind << 30) | (role << 28) | c;
+    };
+    for (int i = 0; i < E; ++i) { put(tp.s1[i], ENT_STRETCH, 0, i); put(tp.s2[i], ENT_STRETCH, 1, i); }
+    for (int i = 0; i < B; ++i) {
+        put(tp.b1[i], ENT_BEND, 0, i); put(tp.b2[i], ENT_BEND, 1, i);
+        put(tp.b3[i], ENT_BEND, 2, i); put(tp.b4[i], ENT_BEND, 3, i);
+    }
+    // Physics/CudaPBD.cu:48-81 — long-range attachments to every pinned vertex.
+    tp.fixed.clear();
+    for (int i = 0; i < tp.V; ++i)
+        if (tp.pinned[i]) tp.fixed.push_back(i);
+    int F = (int)tp.fixed.size();
+    tp.lra_l0.assign((size_t)tp.V * F, 0.0);
+    for (int i = 0; i < tp.V; ++i)
+        for (int j = 0; j < F; ++j)
+            if (!tp.pinned[i])
+                tp.lra_l0[(size_t)i * F + j] = ddist(P, i, tp.fixed[j]) * (1.0 + (double)d.params.strainLimit);
+    // Collision/FeatureList.cu:84-132 — feature ownership.  The reference
+    // decides it by an atomicExch race; here the lowest original triangle
+    // index wins, deterministically.
+    tp.features.assign(tp.T, 0);
+    std::vector<u8> vt(tp.V, 0);
+    std::map<std::pair<int, int>, int> et;
+    for (int t = 0; t < tp.T; ++t) {
+        int v1 = tp.idx[3 * t], v2 = tp.idx[3 * t + 1], v3 = tp.idx[3 * t + 2];
+        u8 f = 0;
+        if (!vt[v1]) { vt[v1] = 1; f |= 1 << 5; }
+        if (!vt[v2]) { vt[v2] = 1; f |= 1 << 4; }
+        if (!vt[v3]) { vt[v3] = 1; f |= 1 << 3; }
+        int e[3][2] = {{v1, v2}, {v2, v3}, {v3, v1}};
+        for (int k = 0; k < 3; ++k) {
+            std::pair<int, int> key(std::min(e[k][0], e[k][1]), std::max(e[k][0], e[k][1]));
+            if (!et.count(key)) { et[key] = t; f |= 1 << (2 - k); }
+        }
+        tp.features[t] = f;
+    }
+}
+
+// Thickness of Physics/CudaDeformableBody.cpp:86 (|x0 - x1| / 3).
+inline float mesh_thickness(const lc_cloth_desc &d) {
+    return (float)(ddist(d.positions, 0, 1) / 3.0);
+}
+
+struct Contact {
+    int v[4];
+    float w[4];
+};
+
+// ---------------------------------------------------------------------------
+// The cloth: state + one FixedUpdate (Physics/CudaDeformableBody.cpp:550-627).
+// ---------------------------------------------------------------------------
+template <class R> class Cloth {
+  public:
+    using V = V3<R>;
+    Topology tp;
+    lc_cloth_params prm;
+    float h = 0;  // thickness (float as the reference stores it)
+    std::vector<V> x, xp, v, vn;
+    std::vector<R> mass, invm;
+    std::vector<u32> perm;  // slot -> original triangle
+    V wind;                 // m_crtWindDir
+    u64 rng = 0;
+
+    // buffers of the last step (debug / parity)
+    std::vector<V> pred_x, pred_xp, pred_v;
+    std::vector<u32> perm_before;
+    std::vector<u64> morton;  // sorted
+    std::vector<int> lefts, rights, parents, rmll, rmlr;
+    std::vector<V> nmin, nmax;  // node AABBs (2T-1)
+    std::vector<u32> pairs;     // (i, j) flattened
+    std::vector<Contact> vf, ee;
+    std::vector<V> pmin, pmax;  // particle swept AABBs
+    u64 dropped = 0;
+    int stack_overflow = 0;
+
+    bool have_frozen = false;
+    std::vector<Contact> frozen_vf, frozen_ee;
+
+    // Discrete decisions replayed from another implementation for one step
+    // (ground / LRA / sphere activation, per-iteration counted terms), so that
+    // a comparison measures only the continuous arithmetic.
+    struct Forced {
+        bool on = false;
+        std::vector<u8> ground;     // V
+        std::vector<u32> ground_it; // V, bit per iteration
+        std::vector<u8> lra;        // V*F
+        std::vector<u8> dyn;        // iterations x (4 * contacts)
+        std::vector<int8_t> sphere; // V
+    } forced;
+
+    void init(const lc_cloth_desc &d) {
+        prm = d.params;
+        build_topology(d, tp);
+        h = prm.thicknessFromMesh ? mesh_thickness(d) : prm.thickness;
+        int Vn = tp.V;
+        x.resize(Vn); xp.resize(Vn); v.assign(Vn, mk<R>(0, 0, 0)); vn.assign(Vn, mk<R>(0, 0, 0));
+        mass.resize(Vn); invm.resize(Vn);
+        for (int i = 0; i < Vn; ++i) {
+            x[i] = mk<R>(d.positions[3 * i], d.positions[3 * i + 1], d.positions[3 * i + 2]);
+            xp[i] = x[i];
+            // Physics/CudaDeformableBody.cpp:80-82
+            float vm = prm.objectMass / (float)Vn;
+            mass[i] = tp.pinned[i] ? R(1000) : R(vm);
+            invm[i] = tp.pinned[i] ? R(0) : R(1.f / vm);
+        }
+        perm.resize(tp.T);
+        std::iota(perm.begin(), perm.end(), 0u);
+        // Physics/CudaPBD.cu:42 — current wind.
+        wind = prm.windOn ? mk<R>(prm.startWindDir[0], prm.startWindDir[1], prm.startWindDir[2]) : mk<R>(0, 0, 0);
+        rng = prm.windSeed ? prm.windSeed : 0x9E3779B97F4A7C15ull;
+        // Physics/CudaDeformableBody.cpp:214,269 with Physics/CudaDeformableUtils.cu:37-64
+        // and :190-249: initial vertex normals from the unnormalised face normals.
+        for (int t = 0; t < tp.T; ++t) {
+            V a = x[tp.idx[3 * t]], b = x[tp.idx[3 * t + 1]], c = x[tp.idx[3 * t + 2]];
+            V fn = cross(b - a, c - a);
+            for (int k = 0; k < 3; ++k) vn[tp.idx[3 * t + k]] = vn[tp.idx[3 * t + k]] + fn;
+        }
+        for (int i = 0; i < Vn; ++i) vn[i] = normalize(vn[i]);
+    }
+
+    R kp_of(double k) const {
+        return R(1.0 - std::pow(1.0 - k, 1.0 / (double)prm.solverIterations));
+    }
+
+    // Host wind update of Physics/CudaPBD.cu:613-619; the std::rand() draw is
+    // replaced by a seeded xorshift so that runs are reproducible.
+    double next_uniform() {
+        rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;
+        return (double)(rng >> 11) * (1.0 / 9007199254740992.0);
+    }
+    void update_wind() {
+        if (!prm.windOn) return;
+        u64 bit = (rng ^ (rng >> 29)) & 1;
+        double u = next_uniform();
+        double var = (double)prm.windMinVariation + u * ((double)prm.windMaxVariation - prm.windMinVariation);
+        float variation = (bit ? 1.f : -1.f) * (float)var;
+        V sw = mk<R>(prm.startWindDir[0], prm.startWindDir[1], prm.startWindDir[2]);
+        wind = wind + sw * R(variation);
+        wind = mk(clampf(wind.x, R(prm.minWindDir[0]), R(prm.maxWindDir[0])),
+                  clampf(wind.y, R(prm.minWindDir[1]), R(prm.maxWindDir[1])),
+                  clampf(wind.z, R(prm.minWindDir[2]), R(prm.maxWindDir[2])));
+    }
+
+    // ---- 1. PBDStepExternal (Physics/CudaPBD.cu:610-630) -------------------
+    void external() {
+        int Vn = tp.V;
+        update_wind();
+        R dt = R(prm.timestep);
+        V g = mk<R>(prm.gravity[0], prm.gravity[1], prm.gravity[2]);
+        // ApplyExternalForces, Physics/CudaPBD.cu:1992-2003
+        for (int i = 0; i < Vn; ++i) {
+            if (is_zero(wind))
+                v[i] = v[i] + dt * g;
+            else
+                v[i] = v[i] + dt * (g + vn[i] * dot(normalize(wind), vn[i]) * len(wind));
+        }
+        // DampVelocities, Physics/CudaPBD.cu:411-458 with kernels :1934-1990.
+        R kg = R(prm.globalVelDamp);
+        for (int i = 0; i < Vn; ++i) v[i] = v[i] * (R(1) - kg);
+        // Reductions in double (the reference reduces float3s with CUB).
+        double msum = 0, xm[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
+        for (int i = 0; i < Vn; ++i) {
+            double m = mass[i];
+            msum += m;
+            xm[0] += (double)(x[i].x * mass[i]); xm[1] += (double)(x[i].y * mass[i]); xm[2] += (double)(x[i].z * mass[i]);
+            vm[0] += (double)(v[i].x * mass[i]); vm[1] += (double)(v[i].y * mass[i]); vm[2] += (double)(v[i].z * mass[i]);
+        }
+        V xcm = mk<R>(R(xm[0] / msum), R(xm[1] / msum), R(xm[2] / msum));
+        V vcm = mk<R>(R(vm[0] / msum), R(vm[1] / msum), R(vm[2] / msum));
+        double L[3] = {0, 0, 0}, i1[3] = {0, 0, 0}, i2[3] = {0, 0, 0};
+        for (int i = 0; i < Vn; ++i) {
+            V ri = x[i] - xcm;
+            V l = cross(ri, v[i] * mass[i]);
+            L[0] += (double)l.x; L[1] += (double)l.y; L[2] += (double)l.z;
+            V a1 = mk(ri.x * ri.x, ri.y * ri.y, ri.z * ri.z) * mass[i];
+            V a2 = -mk(ri.x * ri.y, ri.x * ri.z, ri.y * ri.z) * mass[i];
+            i1[0] += (double)a1.x; i1[1] += (double)a1.y; i1[2] += (double)a1.z;
+            i2[0] += (double)a2.x; i2[1] += (double)a2.y; i2[2] += (double)a2.z;
+        }
+        double I[3][3] = {{i1[1] + i1[2], i2[0], i2[1]}, {i2[0], i1[0] + i1[2], i2[2]}, {i2[1], i2[2], i1[0] + i1[1]}};
+        double om[3];
+        solve3(I, L, om);
+        V omega = mk<R>(R(om[0]), R(om[1]), R(om[2]));
+        R kd = R(prm.kDamp);
+        for (int i = 0; i < Vn; ++i) {
+            V ri = x[i] - xcm;
+            V dv = vcm + cross(omega, ri) - v[i];
+            v[i] = v[i] + kd * dv;
+        }
+        // ExplicitEuler, Physics/CudaPBD.cu:2005-2012
+        for (int i = 0; i < Vn; ++i) x[i] = xp[i] + dt * v[i];
+    }
+
+    static void solve3(const double I[3][3], const double L[3], double out[3]) {
+        double a = I[0][0], b = I[0][1], c = I[0][2], d = I[1][0], e = I[1][1], f = I[1][2], g = I[2][0],
+               hh = I[2][1], k = I[2][2];
+        double A = e * k - f * hh, Bc = -(d * k - f * g), C = d * hh - e * g;
+        double det = a * A + b * Bc + c * C;
+        double inv[3][3] = {{A / det, -(b * k - c * hh) / det, (b * f - c * e) / det},
+                            {Bc / det, (a * k - c * g) / det, -(a * f - c * d) / det},
+                            {C / det, -(a * hh - b * g) / det, (a * e - b * d) / det}};
+        for (int r = 0; r < 3; ++r) out[r] = inv[r][0] * L[0] + inv[r][1] * L[1] + inv[r][2] * L[2];
+    }
+
+    // ---- 2-5. collision pipeline -------------------------------------------
+    // Runs on the current x, xp, v and perm; fills morton/perm/tree/pairs/
+    // contacts.  In FP32-mirror mode it is bit-exact with the GPU.
+    void collide() {
+        int Vn = tp.V, T = tp.T;
+        R hh = R(h);
+        // Collision/FeatureList.cu:134-148 — particle swept AABBs.
+        pmin.resize(Vn); pmax.resize(Vn);
+        for (int i = 0; i < Vn; ++i) {
+            pmin[i] = subc(vmin(x[i], xp[i]), hh);
+            pmax[i] = addc(vmax(x[i], xp[i]), hh);
+        }
+        // Physics/CudaDeformableUtils.cu:120-151 — per slot (pre-sort order).
+        int nodes = 2 * T - 1;
+        nmin.assign(std::max(nodes, 1), mk<R>(0, 0, 0));
+        nmax.assign(std::max(nodes, 1), mk<R>(0, 0, 0));
+        std::vector<u64> keys(T);
+        std::vector<V> fn(T);
+        perm_before = perm;
+        for (int s = 0; s < T; ++s) {
+            u32 t = perm[s];
+            int a = tp.idx[3 * t], b = tp.idx[3 * t + 1], c = tp.idx[3 * t + 2];
+            fn[s] = normalize(cross(x[b] - x[a], x[c] - x[a]));
+            V mn = subc(min3(x[a], x[b], x[c]), hh);
+            V mx = addc(max3(x[a], x[b], x[c]), hh);
+            V pmn = subc(min3(xp[a], xp[b], xp[c]), hh);
+            V pmx = addc(max3(xp[a], xp[b], xp[c]), hh);
+            V smn = vmin(mn, pmn), smx = vmax(mx, pmx);
+            nmin[T - 1 + s] = smn;
+            nmax[T - 1 + s] = smx;
+            V mid = smn + (smx - smn) / R(2);
+            float o0 = prm.mortonOrigin[0], o1 = prm.mortonOrigin[1], o2 = prm.mortonOrigin[2], sc = prm.mortonScale;
+            float qx = ((float)mid.x - o0) * sc, qy = ((float)mid.y - o1) * sc, qz = ((float)mid.z - o2) * sc;
+            keys[s] = morton3d(qx, qy, qz, prm.mortonMode);
+        }
+        // Physics/CudaDeformableUtils.cu:190-249 — running vertex normals
+        // (only read by the wind term).
+        for (int s = 0; s < T; ++s) {
+            u32 t = perm[s];
+            for (int k = 0; k < 3; ++k) vn[tp.idx[3 * t + k]] = vn[tp.idx[3 * t + k]] + fn[s];
+        }
+        for (int i = 0; i < Vn; ++i) vn[i] = normalize(vn[i]);
+        // Physics/CudaDeformableUtils.cu:346-349 — stable sort of the keys with
+        // the triangle payload; the AABBs stay where they are (quirk) unless
+        // refLeafAabbQuirk is 0.
+        std::vector<u32> order(T);
+        std::iota(order.begin(), order.end(), 0u);
+        std::stable_sort(order.begin(), order.end(), [&](u32 a, u32 b) { return keys[a] < keys[b]; });
+        morton.resize(T);
+        std::vector<u32> np(T);
+        for (int s = 0; s < T; ++s) { morton[s] = keys[order[s]]; np[s] = perm[order[s]]; }
+        if (!prm.refLeafAabbQuirk) {
+            std::vector<V> lm(T), lx(T);
+            for (int s = 0; s < T; ++s) { lm[s] = nmin[T - 1 + order[s]]; lx[s] = nmax[T - 1 + order[s]]; }
+            for (int s = 0; s < T; ++s) { nmin[T - 1 + s] = lm[s]; nmax[T - 1 + s] = lx[s]; }
+        }
+        perm = np;
+        build_tree();
+        refit();
+        traverse();
+        narrowphase();
+    }
+
+    // Collision/CudaBVH.cu:163-188.  Two internal nodes may claim the same
+    // child when a run of >= 3 equal codes meets FindSplit's midpoint rule;
+    // the reference's parents[] write race is resolved here as "largest
+    // parent index wins" (the GPU uses atomicMax).
+    void build_tree() {
+        int T = tp.T, In = T - 1;
+        lefts.assign(std::max(In, 0), 0);
+        rights.assign(std::max(In, 0), 0);
+        parents.assign(std::max(2 * T - 1, 1), -1);
+        for (int id = 0; id < In; ++id) {
+            int first, last;
+            find_range(morton.data(), In, id, first, last);
+            int split = find_split(morton.data(), first, last);
+            int l = split == first ? In + split : split;
+            int r = split + 1 == last ? In + split + 1 : split + 1;
+            lefts[id] = l;
+            rights[id] = r;
+            parents[l] = std::max(parents[l], id);
+            parents[r] = std::max(parents[r], id);
+        }
+    }
+
+    // Collision/CudaBVH.cu:128-149 — bottom-up union; the second arrival at a
+    // node proceeds.  rmll/rmlr: rightmost leaf node below each child.
+    void refit() {
+        int T = tp.T, In = T - 1;
+        rmll.assign(std::max(In, 0), 0);
+        rmlr.assign(std::max(In, 0), 0);
+        if (In <= 0) return;
+        std::vector<int> visited(In, 0);
+        for (int id = 0; id < T; ++id) {
+            int pid = parents[In + id];
+            for (int guard = 0; guard <= T && pid >= 0 && pid < In; ++guard) {
+                if (visited[pid]++ == 0) break;
+                int l = lefts[pid], r = rights[pid];
+                nmin[pid] = vmin(nmin[l], nmin[r]);
+                nmax[pid] = vmax(nmax[l], nmax[r]);
+                rmll[pid] = l >= In ? l : std::max(rmll[l], rmlr[l]);
+                rmlr[pid] = r >= In ? r : std::max(rmll[r], rmlr[r]);
+                if (pid == 0) break;
+                pid = parents[pid];
+            }
+        }
+    }
+
+    // Collision/CudaBVH.cu:23-113 — per-leaf DFS, pairs (i, j>i), at most
+    // chunk per leaf, overflow dropped; then the order-preserving compaction
+    // of Collision/CudaCollisionDetection.cu:17.
+    void traverse() {
+        int T = tp.T, In = T - 1;
+        pairs.clear();
+        dropped = 0;
+        stack_overflow = 0;
+        if (In <= 0) return;
+        int chunk = std::min(prm.BVHChunkSize, T);
+        for (int id = 0; id < T; ++id) {
+            int me = In + id;
+            int stack[64];
+            stack[0] = -1;
+            int top = 1, node = 0, got = 0;
+            V amin = nmin[me], amax = nmax[me];
+            do {
+                int l = lefts[node], r = rights[node];
+                bool ol = false, orr = false;
+                if (rmll[node] > me && overlap(amin, amax, nmin[l], nmax[l])) ol = true;
+                if (rmlr[node] > me && overlap(amin, amax, nmin[r], nmax[r])) orr = true;
+                if (ol && l >= In) {
+                    if (got < chunk) { pairs.push_back(id); pairs.push_back(l - In); ++got; }
+                    else ++dropped;
+                }
+                if (orr && r >= In) {
+                    if (got < chunk) { pairs.push_back(id); pairs.push_back(r - In); ++got; }
+                    else ++dropped;
+                }
+                bool tl = ol && l < In, tr = orr && r < In;
+                if (!tl && !tr) {
+                    node = stack[--top];
+                } else {
+                    node = tl ? l : r;
+                    if (tl && tr) {
+                        if (top >= 64) { stack_overflow = 1; break; }
+                        stack[top++] = r;
+                    }
+                }
+            } while (top != 0);
+        }
+    }
+
+    // ---- narrowphase --------------------------------------------------------
+    // Physics/CudaCubicSolver.cu:126-129
+    static R triple(V x21, V x31, V x41, V v21, V v31, V v41, R t) {
+        return dot(cross(x21 + t * v21, x31 + t * v31), x41 + t * v41);
+    }
+    // Physics/CudaCubicSolver.cu:131-153
+    static R secant(V x21, V x31, V x41, V v21, V v31, V v41, R a, R b, int maxit) {
+        R x0 = a, x1 = b;
+        for (int i = 0; i < maxit; ++i) {
+            R f0 = triple(x21, x31, x41, v21, v31, v41, x0);
+            R f1 = triple(x21, x31, x41, v21, v31, v41, x1);
+            R xc = (x0 * f1 - x1 * f0) / (f1 - f0);
+            if (std::fabs(xc - x1) < R(kEpsCubic)) return xc;
+            x0 = x1;
+            x1 = xc;
+        }
+        return R(-15);
+    }
+    // Physics/CudaCubicSolver.cu:69-124.  When only the second root lies in
+    // [0,1] the reference reads an uninitialised first slot; here the found
+    // root is used.
+    static int critical_points(V x21, V x31, V x41, V v21, V v31, V v41, R out[2]) {
+        V v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31), x21x31 = cross(x21, x31);
+        R v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
+          v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
+          v1x2x3 = dot(v21x31, x41);
+        R a = v1v2v3, b = x1v2v3 + v1x2v3 + v1v2x3, c = x1x2v3 + x1v2x3 + v1x2x3;
+        R ad = R(3) * a, bd = R(2) * b;
+        R disc = R(4) * (b * b - ad * c);
+        R sq = std::sqrt(disc);
+        R da = R(2) * ad;
+        R t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
+        int n = 0;
+        if (disc >= R(kEpsCubic)) {
+            if (between(t1, R(0), R(1))) out[n++] = t1;
+            if (between(t2, R(0), R(1))) out[n++] = t2;
+        } else if (std::fabs(disc) < R(kEpsCubic)) {
+            if (between(t1, R(0), R(1))) out[n++] = t1;
+        }
+        return n;
+    }
+    // Physics/CudaCubicSolver.cu:5-67
+    static int coplanarity_times(V x1, V x2, V x3, V x4, V v1, V v2, V v3, V v4, R times[8]) {
+        V x21 = x2 - x1, x31 = x3 - x1, x41 = x4 - x1, v21 = v2 - v1, v31 = v3 - v1, v41 = v4 - v1;
+        R cp[2];
+        int ncp = critical_points(x21, x31, x41, v21, v31, v41, cp);
+        R ends[4];
+        int ne = 0;
+        ends[ne++] = R(0);
+        for (int i = 0; i < ncp; ++i) ends[ne++] = cp[i];
+        ends[ne++] = R(1);
+        int n = 0;
+        for (int i = 0; i < ne - 1; ++i) {
+            R a = ends[i], b = ends[i + 1];
+            R fa = triple(x21, x31, x41, v21, v31, v41, a);
+            R fb = triple(x21, x31, x41, v21, v31, v41, b);
+            if (std::fabs(fa) < R(kEpsCubic)) times[n++] = a;
+            if (fa * fb < R(0)) {
+                R t = secant(x21, x31, x41, v21, v31, v41, a, b, 20);
+                if (t != R(-15)) times[n++] = t;
+            }
+        }
+        return n;
+    }
+    // Core/CudaUtils.cu:149-168
+    static V project_on_line(V p, V e1, V e2) {
+        V ab = e2 - e1, ap = p - e1;
+        return e1 + dot(ap, ab) / dot(ab, ab) * ab;
+    }
+    static V clamp_on_line(V p, V e1, V e2) {
+        R d1 = dist(p, e1), d2 = dist(p, e2);
+        if (std::fabs(d1 + d2 - dist(e1, e2)) < R(kEpsPbd)) return p;
+        return d1 < d2 ? e1 : e2;
+    }
+    // Collision/CudaPrimitiveTests.cu:348-406
+    static bool test_vf(V x4, V x1, V x2, V x3, Contact &c, R th) {
+        V x13 = x1 - x3, x23 = x2 - x3, x43 = x4 - x3;
+        V crs = cross(x2 - x1, x3 - x1);
+        V n = normalize(crs);
+        if (std::fabs(dot(x43, n)) <= th) {
+            R dt = dot(x13, x23);
+            R m11 = dot(x13, x13), m12 = dt, m21 = dt, m22 = dot(x23, x23);
+            R vr1 = dot(x13, x43), vr2 = dot(x23, x43);
+            R w2 = (m11 * vr2 - m21 * vr1) / (m11 * m22 - m21 * m12);
+            R w1 = (vr1 - m12 * w2) / m11;
+            R w3 = R(1) - w1 - w2;
+            R del = th / (len(x13) + len(x23) + len(x1 - x2));
+            R lo = R(0), hi = R(1) + del;
+            if (between(w1, lo, hi) && between(w2, lo, hi) && between(w3, lo, hi)) {
+                c.w[0] = 1.f; c.w[1] = (float)-w1; c.w[2] = (float)-w2; c.w[3] = (float)-w3;
+                return true;
+            }
+        }
+        return false;
+    }
+    // Collision/CudaPrimitiveTests.cu:408-425
+    static bool test_edge_degenerate(V x1, V x3, V x21, V x43, Contact &c, R th) {
+        V m1 = x1 + x21 / R(2), m2 = x3 + x43 / R(2);
+        if (dist(m1, m2) <= th) {
+            c.w[0] = c.w[1] = c.w[2] = c.w[3] = 0.5f;
+            return true;
+        }
+        return false;
+    }
+    // Collision/CudaPrimitiveTests.cu:252-346 (the in-range branch measures
+    // cp2 with a, not b, as the reference does).
+    static bool test_ee(V x1, V x2, V x3, V x4, Contact &c, R th) {
+        V x21 = x2 - x1, x31 = x3 - x1, x43 = x4 - x3;
+        V crs = cross(x21, x43);
+        if (len(crs) < R(kEpsEE)) return test_edge_degenerate(x1, x3, x21, x43, c, th);
+        if (is_zero(crs)) return false;
+        R dt = dot(-x21, x43);
+        R m11 = dot(x21, x21), m12 = dt, m21 = dt, m22 = dot(x43, x43);
+        R vr1 = dot(x21, x31), vr2 = dot(-x43, x31);
+        R b = (m11 * vr2 - m21 * vr1) / (m11 * m22 - m21 * m12);
+        R a = (vr1 - m12 * b) / m11;
+        if (between(a, R(0), R(1)) && between(b, R(0), R(1))) {
+            V cp1 = x1 + a * x21, cp2 = x3 + a * x43;
+            if (dist(cp1, cp2) <= th) {
+                c.w[0] = (float)(R(1) - a); c.w[1] = (float)a; c.w[2] = (float)(-(R(1) - b)); c.w[3] = (float)(-b);
+                return true;
+            }
+        } else {
+            R ac = clampf(a, R(0), R(1)), bc = clampf(b, R(0), R(1));
+            R d1 = std::fabs(a - ac) * len(x21), d2 = std::fabs(b - bc) * len(x43);
+            a = ac; b = bc;
+            V cp1, cp2;
+            if (d1 > d2) {
+                cp1 = x1 + a * x21;
+                cp2 = clamp_on_line(project_on_line(cp1, x3, x4), x3, x4);
+            } else {
+                cp2 = x3 + b * x43;
+                cp1 = clamp_on_line(project_on_line(cp2, x1, x2), x1, x2);
+            }
+            if (dist(cp1, cp2) <= th) {
+                c.w[0] = (float)(R(1) - a); c.w[1] = (float)a; c.w[2] = (float)(-(R(1) - b)); c.w[3] = (float)(-b);
+                return true;
+            }
+        }
+        return false;
+    }
+
+    // Collision/CudaCollisionDetection.cu:53-189 (candidate slots),
+    // Collision/CudaPrimitiveTests.cu:427-490 (feature AABB cull),
+    // :109-238 (CCD on x_prev and v), compactions at
+    // Collision/CudaCollisionDetection.cu:264-282.
+    void narrowphase() {
+        vf.clear();
+        ee.clear();
+        R th = R(h), dt = R(prm.timestep);
+        size_t P = pairs.size() / 2;
+        for (size_t p = 0; p < P; ++p) {
+            u32 ta = perm[pairs[2 * p]], tb = perm[pairs[2 * p + 1]];
+            int A[3] = {(int)tp.idx[3 * ta], (int)tp.idx[3 * ta + 1], (int)tp.idx[3 * ta + 2]};
+            int B[3] = {(int)tp.idx[3 * tb], (int)tp.idx[3 * tb + 1], (int)tp.idx[3 * tb + 2]};
+            u8 fa = tp.features[ta], fb = tp.features[tb];
+            for (int s = 0; s < 6; ++s) {
+                const int *P1 = s < 3 ? A : B, *F1 = s < 3 ? B : A;
+                u8 f = s < 3 ? fa : fb;
+                if (!((f >> (5 - s % 3)) & 1)) continue;
+                Contact c;
+                c.v[0] = P1[s % 3]; c.v[1] = F1[0]; c.v[2] = F1[1]; c.v[3] = F1[2];
+                c.w[0] = c.w[1] = c.w[2] = c.w[3] = -1.f;
+                if (vf_candidate(c, th, dt)) vf.push_back(c);
+            }
+            // EE slot k: edge ea of A x edge eb of B.
+            static const int ea_v[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+            static const int ea_bit[3] = {2, 0, 1};
+            for (int s = 0; s < 9; ++s) {
+                int ia = s % 3, ib = s / 3;
+                if (!(((fa >> ea_bit[ia]) & 1) & ((fb >> ea_bit[ib]) & 1))) continue;
+                Contact c;
+                c.v[0] = A[ea_v[ia][0]]; c.v[1] = A[ea_v[ia][1]];
+                c.v[2] = B[ea_v[ib][0]]; c.v[3] = B[ea_v[ib][1]];
+                c.w[0] = c.w[1] = c.w[2] = c.w[3] = -1.f;
+                if (ee_candidate(c, th, dt)) ee.push_back(c);
+            }
+        }
+    }
+
+    bool vf_candidate(Contact &c, R th, R dt) {
+        V tmin = min3(pmin[c.v[1]], pmin[c.v[2]], pmin[c.v[3]]);
+        V tmax = max3(pmax[c.v[1]], pmax[c.v[2]], pmax[c.v[3]]);
+        if (!overlap(pmin[c.v[0]], pmax[c.v[0]], tmin, tmax)) return false;
+        if (c.v[0] == c.v[1] || c.v[0] == c.v[2] || c.v[0] == c.v[3]) return false;
+        V x4 = xp[c.v[0]], x1 = xp[c.v[1]], x2 = xp[c.v[2]], x3 = xp[c.v[3]];
+        V v4 = v[c.v[0]], v1 = v[c.v[1]], v2 = v[c.v[2]], v3 = v[c.v[3]];
+        R times[8];
+        int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+        for (int i = 0; i < n; ++i) {
+            R t = times[i] * dt;
+            x4 = x4 + v4 * t; x1 = x1 + v1 * t; x2 = x2 + v2 * t; x3 = x3 + v3 * t;
+            if (test_vf(x4, x1, x2, x3, c, th)) return true;
+        }
+        return false;
+    }
+    bool ee_candidate(Contact &c, R th, R dt) {
+        V e1min = vmin(pmin[c.v[0]], pmin[c.v[1]]), e1max = vmax(pmax[c.v[0]], pmax[c.v[1]]);
+        V e2min = vmin(pmin[c.v[2]], pmin[c.v[3]]), e2max = vmax(pmax[c.v[2]], pmax[c.v[3]]);
+        if (!overlap(e1min, e1max, e2min, e2max)) return false;
+        if (c.v[0] == c.v[2] || c.v[0] == c.v[3] || c.v[1] == c.v[2] || c.v[1] == c.v[3]) return false;
+        V x1 = xp[c.v[0]], x2 = xp[c.v[1]], x3 = xp[c.v[2]], x4 = xp[c.v[3]];
+        V v1 = v[c.v[0]], v2 = v[c.v[1]], v3 = v[c.v[2]], v4 = v[c.v[3]];
+        R times[8];
+        int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+        for (int i = 0; i < n; ++i) {
+            R t = times[i] * dt;
+            x1 = x1 + v1 * t; x2 = x2 + v2 * t; x3 = x3 + v3 * t; x4 = x4 + v4 * t;
+            if (test_ee(x1, x2, x3, x4, c, th)) return true;
+        }
+        return false;
+    }
+
+    // ---- 6. PBDStepSolver (Physics/CudaPBD.cu:632-660) ----------------------
+    void solve(const std::vector<Contact> &cvf, const std::vector<Contact> &cee) {
+        int Vn = tp.V, F = (int)tp.fixed.size();
+        R th = R(h);
+        R gh = R(prm.worldMin[1]);
+        // Physics/CudaPBD.cu:1477-1507 — ground constraints.
+        std::vector<u8> gflag(Vn, 0);
+        std::vector<V> qc(Vn), nc(Vn);
+        if (prm.groundOn) {
+            for (int i = 0; i < Vn; ++i) {
+                V pos = x[i], prev = xp[i];
+                if (forced.on ? forced.ground[i] != 0 : pos.y <= gh + th) {
+                    V n = mk<R>(0, 1, 0);
+                    V p0 = mk<R>(1, gh + th, 1);
+                    V l = pos - prev;
+                    R d = dot(p0 - pos, n) / dot(l, n);
+                    qc[i] = d * l + pos;
+                    nc[i] = n;
+                    gflag[i] = 1;
+                }
+            }
+        }
+        // Physics/CudaPBD.cu:1571-1592 — LRA flags.
+        std::vector<u8> lflag((size_t)Vn * F, 0);
+        for (int i = 0; i < Vn; ++i) {
+            if (tp.pinned[i]) continue;
+            for (int j = 0; j < F; ++j) {
+                const size_t k = (size_t)i * F + j;
+                if (forced.on) lflag[k] = forced.lra[k];
+                else if (dist(x[i], x[tp.fixed[j]]) > R(tp.lra_l0[k])) lflag[k] = 1;
+            }
+        }
+        // Physics/CudaPBD.cu:1509-1569 — the analytic sphere projects x/x_prev
+        // directly (its flags are never set, so no iteration term).
+        if (prm.sphereOn) sphere_create(th);
+
+        // Dynamic entries grouped by vertex in entry order (the stable sort +
+        // RLE of Physics/CudaPBD.cu:711-721).
+        size_t nvf = cvf.size(), nee = cee.size();
+        std::vector<std::vector<u32>> dyn(Vn);
+        for (size_t c = 0; c < nvf + nee; ++c) {
+            const Contact &k = c < nvf ? cvf[c] : cee[c - nvf];
+            for (int s = 0; s < 4; ++s) dyn[k.v[s]].push_back(u32(c * 4 + s));
+        }
+        int E = (int)tp.s1.size(), Bn = (int)tp.b1.size();
+        std::vector<R> kps(E), kpb(Bn);
+        for (int i = 0; i < E; ++i) kps[i] = kp_of(tp.kst[i]);
+        for (int i = 0; i < Bn; ++i) kpb[i] = kp_of(tp.kbd[i]);
+
+        std::vector<V> corr_stat(tp.sent.size());
+        std::vector<V> corr_dyn((nvf + nee) * 4);
+        std::vector<V> acc(Vn);
+        std::vector<int> cnt(Vn);
+        for (int it = 0; it < prm.solverIterations; ++it) {
+            for (int i = 0; i < Vn; ++i) { acc[i] = mk<R>(0, 0, 0); cnt[i] = 0; }
+            // ground, Physics/CudaPBD.cu:1594-1629
+            for (int i = 0; i < Vn; ++i)
+                if (gflag[i]) {
+                    R cv = dot(x[i] - qc[i], nc[i]);
+                    bool take = forced.on ? ((forced.ground_it[i] >> it) & 1u) != 0 : cv < R(0);
+                    if (take) { acc[i] = acc[i] + (-cv) * nc[i]; cnt[i] += 1; }
+                }
+            // LRA, Physics/CudaPBD.cu:1656-1688
+            for (int i = 0; i < Vn; ++i) {
+                V a = mk<R>(0, 0, 0);
+                int c = 0;
+                for (int j = 0; j < F; ++j)
+                    if (lflag[(size_t)i * F + j]) {
+                        V diff = x[i] - x[tp.fixed[j]];
+                        R l = len(diff);
+                        V n = diff / l;
+                        a = a + (-(l - R(tp.lra_l0[(size_t)i * F + j]))) * n;
+                        ++c;
+                    }
+                acc[i] = acc[i] + a;
+                cnt[i] += c;
+            }
+            // static constraints into per-vertex slots, Physics/CudaPBD.cu:942-1147
+            for (int i = 0; i < Vn; ++i)
+                for (int e = tp.soff[i]; e < tp.soff[i + 1]; ++e) corr_stat[e] = static_corr(tp.sent[e], kps, kpb);
+            // Physics/CudaPBD.cu:1417-1446
+            for (int i = 0; i < Vn; ++i) {
+                V a = mk<R>(0, 0, 0);
+                for (int e = tp.soff[i]; e < tp.soff[i + 1]; ++e) a = a + corr_stat[e];
+                acc[i] = acc[i] + a;
+                cnt[i] += tp.soff[i + 1] - tp.soff[i];
+            }
+            // dynamic, Physics/CudaPBD.cu:1190-1415 and :1448-1475
+            for (size_t c = 0; c < nvf; ++c) vf_corr(cvf[c], th, &corr_dyn[c * 4]);
+            for (size_t c = 0; c < nee; ++c) ee_corr(cee[c], th, &corr_dyn[(nvf + c) * 4]);
+            for (int i = 0; i < Vn; ++i) {
+                if (dyn[i].empty()) continue;
+                V a = mk<R>(0, 0, 0);
+                int c = 0;
+                for (u32 e : dyn[i]) {
+                    bool take = forced.on ? forced.dyn[(size_t)it * corr_dyn.size() + e] != 0 : !is_zero(corr_dyn[e]);
+                    if (take) { a = a + corr_dyn[e]; ++c; }
+                }
+                acc[i] = acc[i] + a;
+                cnt[i] += c;
+            }
+            // Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
+            for (int i = 0; i < Vn; ++i) x[i] = x[i] + acc[i] / R(cnt[i]);
+        }
+    }
+
+    V static_corr(int ent, const std::vector<R> &kps, const std::vector<R> &kpb) const {
+        int kind = (ent >> 30) & 1, role = (ent >> 28) & 3, c = ent & 0x0FFFFFFF;
+        if (kind == ENT_STRETCH) {
+            // Physics/CudaPBD.cu:986-1022
+            R kp = kps[c];
+            int i1 = tp.s1[c], i2 = tp.s2[c];
+            R w1 = invm[i1], w2 = invm[i2], ws = w1 + w2;
+            if (ws == R(0)) return mk<R>(0, 0, 0);
+            V diff = x[i1] - x[i2];
+            R l = len(diff);
+            if (l <= R(kEpsPbd)) return mk<R>(0, 0, 0);
+            V n = diff / l;
+            V tt = (l - R(tp.sl0[c])) * n * kp / ws;
+            return role == 0 ? (-w1) * tt : w2 * tt;
+        }
+        // Physics/CudaPBD.cu:1024-1147 (raw positions, phi0 = PI)
+        R kp = kpb[c];
+        int id[4] = {tp.b1[c], tp.b2[c], tp.b3[c], tp.b4[c]};
+        R w[4] = {invm[id[0]], invm[id[1]], invm[id[2]], invm[id[3]]};
+        V p2 = x[id[1]], p3 = x[id[2]], p4 = x[id[3]];
+        V c23 = cross(p2, p3), c24 = cross(p2, p4);
+        R l23 = len(c23), l24 = len(c24);
+        if (l23 <= R(kEpsPbd) || l24 <= R(kEpsPbd)) return mk<R>(0, 0, 0);
+        V n1 = c23 / l23, n2 = c24 / l24;
+        R d = clampf(dot(n1, n2), R(-1), R(1));
+        R phi = std::acos(d);
+        R phi0 = R(kPi);
+        if (d == R(-1)) {
+            phi = R(kPi);
+            if (phi == phi0) return mk<R>(0, 0, 0);
+            if (role == 0) return n1 / R(100);
+            if (role == 1) return n2 / R(100);
+            return mk<R>(0, 0, 0);
+        }
+        if (d == R(1)) {
+            phi = R(0);
+            if (phi == phi0) return mk<R>(0, 0, 0);
+        }
+        V q3 = (cross(p2, n2) + (cross(n1, p2) * d)) / l23;
+        V q4 = (cross(p2, n1) + (cross(n2, p2) * d)) / l24;
+        V q2 = -((cross(p3, n2) + (cross(n1, p3) * d)) / l23) - ((cross(p4, n1) + (cross(n2, p4) * d)) / l24);
+        V q1 = -q2 - q3 - q4;
+        R term = std::sqrt(R(1) - d * d) * (phi - phi0) * kp;
+        R s1 = dot(q1, q1), s2 = dot(q2, q2), s3 = dot(q3, q3), s4 = dot(q4, q4);
+        R sf = w[0] * s1 + w[1] * s2 + w[2] * s3 + w[3] * s4;
+        if (sf <= R(kEpsPbd)) return mk<R>(0, 0, 0);
+        R ts = term / sf;
+        V q[4] = {q1, q2, q3, q4};
+        return (-(w[role] * ts)) * q[role];
+    }
+
+    // Physics/CudaPBD.cu:1212-1311
+    void vf_corr(const Contact &k, R th, V out[4]) const {
+        V p = x[k.v[0]], p0 = x[k.v[1]], p1 = x[k.v[2]], p2 = x[k.v[3]];
+        R b0 = clampf(R(-k.w[1]), R(0), R(1)), b1 = clampf(R(-k.w[2]), R(0), R(1)), b2 = clampf(R(-k.w[3]), R(0), R(1));
+        R w = invm[k.v[0]], w0 = invm[k.v[1]], w1 = invm[k.v[2]], w2 = invm[k.v[3]];
+        V q = p0 * b0 + p1 * b1 + p2 * b2;
+        V n = p - q;
+        R l = len(n);
+        n = n / l;
+        R c = l - th;
+        V g = n, g0 = -n * b0, g1 = -n * b1, g2 = -n * b2;
+        R s = w + w0 * b0 * b0 + w1 * b1 * b1 + w2 * b2 * b2;
+        if (s == R(0)) { out[0] = out[1] = out[2] = out[3] = mk<R>(0, 0, 0); return; }
+        s = c / s;
+        s = c < R(0) ? s : R(0);
+        out[0] = (-s * w) * g; out[1] = (-s * w0) * g0; out[2] = (-s * w1) * g1; out[3] = (-s * w2) * g2;
+    }
+    // Physics/CudaPBD.cu:1313-1415
+    void ee_corr(const Contact &k, R th, V out[4]) const {
+        V p0 = x[k.v[0]], p1 = x[k.v[1]], p2 = x[k.v[2]], p3 = x[k.v[3]];
+        R b0 = R(k.w[0]), b1 = R(k.w[1]), b2 = R(-k.w[2]), b3 = R(-k.w[3]);
+        R w0 = invm[k.v[0]], w1 = invm[k.v[1]], w2 = invm[k.v[2]], w3 = invm[k.v[3]];
+        V q0 = p0 * b0 + p1 * b1, q1 = p2 * b2 + p3 * b3;
+        V n = q0 - q1;
+        R l = len(n);
+        n = n / l;
+        R c = l - th;
+        V g0 = n * b0, g1 = n * b1, g2 = -n * b2, g3 = -n * b3;
+        R s = w0 * b0 * b0 + w1 * b1 * b1 + w2 * b2 * b2 + w3 * b3 * b3;
+        if (s == R(0)) { out[0] = out[1] = out[2] = out[3] = mk<R>(0, 0, 0); return; }
+        s = c / s;
+        s = c < R(0) ? s : R(0);
+        out[0] = (-s * w0) * g0; out[1] = (-s * w1) * g1; out[2] = (-s * w2) * g2; out[3] = (-s * w3) * g3;
+    }
+
+    // Physics/CudaPBD.cu:1509-1569 with Collision/CudaCollisionDetection.cu:529-567
+    void sphere_create(R th) {
+        V sc = mk<R>(prm.spherePos[0], prm.spherePos[1], prm.spherePos[2]);
+        R rad = R(prm.sphereRadius) + th;
+        for (int i = 0; i < tp.V; ++i) {
+            V pos = x[i], prev = xp[i];
+            V q;
+            int ret = ray_sphere(prev, pos, sc, rad, q);
+            if (forced.on) {
+                ret = forced.sphere[i];
+                if (ret != 0) {
+                    V dir = pos - prev;
+                    if (is_zero(dir)) continue;
+                    dir = dir / len(dir);
+                    V m = prev - sc;
+                    R b = dot(m, dir), c = dot(m, m) - rad * rad;
+                    R disc = std::fmax(b * b - c, R(0));
+                    q = prev + dir * (-b - std::sqrt(disc));
+                }
+            }
+            if (ret == -1) {
+                V qs = sc + normalize(q - sc) * rad;
+                V ns = normalize(qs - sc);
+                xp[i] = qs + ns * R(0.0001f);
+                x[i] = qs;
+            } else if (ret == 1) {
+                V ns = normalize(q - sc);
+                x[i] = q + ns * R(0.0001f);
+            }
+        }
+    }
+    static int ray_sphere(V p1, V p2, V c0, R rad, V &q) {
+        V dir = p2 - p1;
+        if (is_zero(dir)) return 0;
+        R l = len(dir);
+        dir = dir / l;
+        V m = p1 - c0;
+        R b = dot(m, dir);
+        R c = dot(m, m) - rad * rad;
+        if (c > R(0) && b > R(0)) return 0;
+        R disc = b * b - c;
+        if (disc < R(0)) return 0;
+        R t = -b - std::sqrt(disc);
+        if (t < R(0)) { q = p1 + dir * t; return -1; }
+        if (t > l) return 0;
+        q = p1 + dir * t;
+        return 1;
+    }
+
+    // ---- 7. PBDStepIntegration + WorldConstraints ---------------------------
+    void integrate() {
+        R dt = R(prm.timestep);
+        for (int i = 0; i < tp.V; ++i) {
+            // Physics/CudaPBD.cu:1916-1932
+            if (tp.pinned[i]) { v[i] = mk<R>(0, 0, 0); continue; }
+            v[i] = (x[i] - xp[i]) / dt;
+            xp[i] = x[i];
+        }
+        // Physics/CudaDeformableUtils.cu:260-269
+        for (int i = 0; i < tp.V; ++i) {
+            x[i] = mk(std::fmin(std::fmax(x[i].x, R(prm.worldMin[0])), R(prm.worldMax[0])),
+                      std::fmin(std::fmax(x[i].y, R(prm.worldMin[1])), R(prm.worldMax[1])),
+                      std::fmin(std::fmax(x[i].z, R(prm.worldMin[2])), R(prm.worldMax[2])));
+        }
+    }
+
+    void step() {
+        external();
+        pred_x = x; pred_xp = xp; pred_v = v;
+        collide();
+        if (have_frozen)
+            solve(frozen_vf, frozen_ee);
+        else
+            solve(vf, ee);
+        have_frozen = false;
+        forced.on = false;
+        integrate();
+    }
+};
+
+}  // namespace lco

@@ -1,0 +1,268 @@
+// lc_oracle_capi.cpp — C entry points of the CPU oracle (loaded with ctypes by
+// tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py).
+//
+// TEST INFRASTRUCTURE ONLY: the product never links or calls this library.
+// See lc_oracle.hpp for what is restated and how it is pinned.
+#include <omp.h>
+
+#include <memory>
+
+#include "lc_oracle.hpp"
+
+using namespace lco;
+
+struct lco_world {
+    int fp64 = 0;
+    std::vector<std::unique_ptr<Cloth<float>>> f32;
+    std::vector<std::unique_ptr<Cloth<double>>> f64;
+    int n() const { return fp64 ? (int)f64.size() : (int)f32.size(); }
+};
+
+template <class F> static int with_cloth(lco_world *w, int c, F &&fn) {
+    if (!w || c < 0 || c >= w->n()) return LC_ERR_INVALID_ARG;
+    if (w->fp64) return fn(*w->f64[c]);
+    return fn(*w->f32[c]);
+}
+
+template <class R> static void put3(const std::vector<V3<R>> &src, double *dst) {
+    if (!dst) return;
+    for (size_t i = 0; i < src.size(); ++i) {
+        dst[3 * i] = (double)src[i].x;
+        dst[3 * i + 1] = (double)src[i].y;
+        dst[3 * i + 2] = (double)src[i].z;
+    }
+}
+template <class R> static void get3(std::vector<V3<R>> &dst, const double *src) {
+    if (!src) return;
+    for (size_t i = 0; i < dst.size(); ++i) dst[i] = mk<R>(R(src[3 * i]), R(src[3 * i + 1]), R(src[3 * i + 2]));
+}
+template <class T> static int copy_out(const T *src, uint64_t n, void *dst, uint64_t cap, uint64_t *count) {
+    if (count) *count = n;
+    if (dst) std::memcpy(dst, src, sizeof(T) * std::min<uint64_t>(n, cap));
+    return LC_OK;
+}
+
+extern "C" {
+
+lco_world *lco_create(const lc_cloth_desc *descs, int n, int fp64) {
+    if (!descs || n <= 0) return nullptr;
+    auto *w = new lco_world();
+    w->fp64 = fp64 ? 1 : 0;
+    for (int i = 0; i < n; ++i) {
+        if (fp64) {
+            w->f64.emplace_back(new Cloth<double>());
+            w->f64.back()->init(descs[i]);
+        } else {
+            w->f32.emplace_back(new Cloth<float>());
+            w->f32.back()->init(descs[i]);
+        }
+    }
+    return w;
+}
+
+void lco_destroy(lco_world *w) { delete w; }
+
+int lco_num_cloths(lco_world *w) { return w ? w->n() : 0; }
+
+// nsteps FixedUpdates of every cloth; cloths run in parallel on nthreads
+// host threads (0 = all).
+int lco_step(lco_world *w, int nsteps, int nthreads) {
+    if (!w) return LC_ERR_INVALID_ARG;
+    int n = w->n();
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int c = 0; c < n; ++c) {
+        for (int s = 0; s < nsteps; ++s) {
+            if (w->fp64)
+                w->f64[c]->step();
+            else
+                w->f32[c]->step();
+        }
+    }
+    return LC_OK;
+}
+
+int lco_max_threads(void) { return omp_get_max_threads(); }
+
+int lco_sizes(lco_world *w, int c, int *nv, int *nt, int *ne, int *nb) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (nv) *nv = cl.tp.V;
+        if (nt) *nt = cl.tp.T;
+        if (ne) *ne = (int)cl.tp.s1.size();
+        if (nb) *nb = (int)cl.tp.b1.size();
+        return LC_OK;
+    });
+}
+
+int lco_get_state(lco_world *w, int c, double *x, double *xp, double *v, double *vn) {
+    return with_cloth(w, c, [&](auto &cl) {
+        put3(cl.x, x); put3(cl.xp, xp); put3(cl.v, v); put3(cl.vn, vn);
+        return LC_OK;
+    });
+}
+
+int lco_set_state(lco_world *w, int c, const double *x, const double *xp, const double *v, const double *vn) {
+    return with_cloth(w, c, [&](auto &cl) {
+        get3(cl.x, x); get3(cl.xp, xp); get3(cl.v, v); get3(cl.vn, vn);
+        return LC_OK;
+    });
+}
+
+int lco_get_perm(lco_world *w, int c, uint32_t *perm) {
+    return with_cloth(w, c, [&](auto &cl) {
+        std::memcpy(perm, cl.perm.data(), sizeof(uint32_t) * cl.perm.size());
+        return LC_OK;
+    });
+}
+
+int lco_set_perm(lco_world *w, int c, const uint32_t *perm) {
+    return with_cloth(w, c, [&](auto &cl) {
+        std::memcpy(cl.perm.data(), perm, sizeof(uint32_t) * cl.perm.size());
+        return LC_OK;
+    });
+}
+
+// Wind state (current wind vector and the variation RNG state).
+int lco_get_wind(lco_world *w, int c, double wind[3], uint64_t *rng) {
+    return with_cloth(w, c, [&](auto &cl) {
+        wind[0] = cl.wind.x; wind[1] = cl.wind.y; wind[2] = cl.wind.z;
+        if (rng) *rng = cl.rng;
+        return LC_OK;
+    });
+}
+int lco_set_wind(lco_world *w, int c, const double wind[3], uint64_t rng) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        cl.wind = mk<R>(R(wind[0]), R(wind[1]), R(wind[2]));
+        cl.rng = rng;
+        return LC_OK;
+    });
+}
+
+// Stage entry points for teacher-forced comparisons.
+int lco_external(lco_world *w, int c) {
+    return with_cloth(w, c, [&](auto &cl) { cl.external(); return LC_OK; });
+}
+int lco_collide(lco_world *w, int c) {
+    return with_cloth(w, c, [&](auto &cl) { cl.collide(); return LC_OK; });
+}
+int lco_step_one(lco_world *w, int c) {
+    return with_cloth(w, c, [&](auto &cl) { cl.step(); return LC_OK; });
+}
+
+// The next step of cloth c uses these contacts instead of the ones its own
+// collision stage finds (contact sets frozen for position comparisons).
+int lco_set_frozen_contacts(lco_world *w, int c, const lc_contact *vf, uint64_t nvf, const lc_contact *ee,
+                            uint64_t nee) {
+    return with_cloth(w, c, [&](auto &cl) {
+        cl.frozen_vf.resize(nvf);
+        cl.frozen_ee.resize(nee);
+        for (uint64_t i = 0; i < nvf; ++i) std::memcpy(&cl.frozen_vf[i], &vf[i], sizeof(Contact));
+        for (uint64_t i = 0; i < nee; ++i) std::memcpy(&cl.frozen_ee[i], &ee[i], sizeof(Contact));
+        cl.have_frozen = true;
+        return LC_OK;
+    });
+}
+
+// Replays discrete decisions for the next step of cloth c (see Cloth::Forced);
+// dyn holds iterations x (4 * (frozen VF + frozen EE contacts)) bytes.
+int lco_set_forced(lco_world *w, int c, const uint8_t *ground, const uint32_t *ground_it, const uint8_t *lra,
+                   const uint8_t *dyn, uint64_t dyn_len, const int8_t *sphere) {
+    return with_cloth(w, c, [&](auto &cl) {
+        const int V = cl.tp.V, F = (int)cl.tp.fixed.size();
+        cl.forced.ground.assign(ground, ground + V);
+        cl.forced.ground_it.assign(ground_it, ground_it + V);
+        cl.forced.lra.assign(lra, lra + (size_t)V * F);
+        cl.forced.dyn.assign(dyn, dyn + dyn_len);
+        if (sphere) cl.forced.sphere.assign(sphere, sphere + V);
+        else cl.forced.sphere.assign(V, 0);
+        cl.forced.on = true;
+        return LC_OK;
+    });
+}
+
+int lco_set_stiffness(lco_world *w, int c, const float *ks, const float *kb) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (ks) for (size_t i = 0; i < cl.tp.kst.size(); ++i) cl.tp.kst[i] = ks[i];
+        if (kb) for (size_t i = 0; i < cl.tp.kbd.size(); ++i) cl.tp.kbd[i] = kb[i];
+        return LC_OK;
+    });
+}
+
+int lco_thickness(lco_world *w, int c, float *h) {
+    return with_cloth(w, c, [&](auto &cl) { *h = cl.h; return LC_OK; });
+}
+
+int lco_counters(lco_world *w, int c, uint64_t out[4]) {
+    return with_cloth(w, c, [&](auto &cl) {
+        out[0] = cl.pairs.size() / 2;
+        out[1] = cl.vf.size();
+        out[2] = cl.ee.size();
+        out[3] = cl.dropped;
+        return cl.stack_overflow ? LC_ERR_STACK_OVERFLOW : LC_OK;
+    });
+}
+
+// Same selectors as lc_batch_debug_get (lc.h).
+int lco_debug_get(lco_world *w, int c, int what, void *dst, uint64_t cap, uint64_t *count) {
+    return with_cloth(w, c, [&](auto &cl) -> int {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        auto f3 = [&](const std::vector<V3<R>> &src) {
+            std::vector<float> tmp(3 * src.size());
+            for (size_t i = 0; i < src.size(); ++i) {
+                tmp[3 * i] = (float)src[i].x; tmp[3 * i + 1] = (float)src[i].y; tmp[3 * i + 2] = (float)src[i].z;
+            }
+            return copy_out(tmp.data(), tmp.size() / 3, dst, cap * 3, count), LC_OK;
+        };
+        switch (what) {
+            case LC_DBG_PRED_X: return f3(cl.pred_x);
+            case LC_DBG_PRED_XPREV: return f3(cl.pred_xp);
+            case LC_DBG_PRED_V: return f3(cl.pred_v);
+            case LC_DBG_PERM_BEFORE: return copy_out(cl.perm_before.data(), cl.perm_before.size(), dst, cap, count);
+            case LC_DBG_MORTON: return copy_out(cl.morton.data(), cl.morton.size(), dst, cap, count);
+            case LC_DBG_PERM: return copy_out(cl.perm.data(), cl.perm.size(), dst, cap, count);
+            case LC_DBG_LEFTS: return copy_out(cl.lefts.data(), cl.lefts.size(), dst, cap, count);
+            case LC_DBG_RIGHTS: return copy_out(cl.rights.data(), cl.rights.size(), dst, cap, count);
+            case LC_DBG_PARENTS: return copy_out(cl.parents.data(), cl.parents.size(), dst, cap, count);
+            case LC_DBG_RML: {
+                std::vector<int> t(2 * cl.rmll.size());
+                for (size_t i = 0; i < cl.rmll.size(); ++i) { t[2 * i] = cl.rmll[i]; t[2 * i + 1] = cl.rmlr[i]; }
+                if (count) *count = cl.rmll.size();
+                if (dst) std::memcpy(dst, t.data(), sizeof(int) * std::min<uint64_t>(t.size(), 2 * cap));
+                return LC_OK;
+            }
+            case LC_DBG_NODE_AABB: {
+                std::vector<float> t(6 * cl.nmin.size());
+                for (size_t i = 0; i < cl.nmin.size(); ++i) {
+                    t[6 * i] = (float)cl.nmin[i].x; t[6 * i + 1] = (float)cl.nmin[i].y; t[6 * i + 2] = (float)cl.nmin[i].z;
+                    t[6 * i + 3] = (float)cl.nmax[i].x; t[6 * i + 4] = (float)cl.nmax[i].y; t[6 * i + 5] = (float)cl.nmax[i].z;
+                }
+                if (count) *count = cl.nmin.size();
+                if (dst) std::memcpy(dst, t.data(), sizeof(float) * std::min<uint64_t>(t.size(), 6 * cap));
+                return LC_OK;
+            }
+            case LC_DBG_PAIRS: {
+                if (count) *count = cl.pairs.size() / 2;
+                if (dst) std::memcpy(dst, cl.pairs.data(), sizeof(uint32_t) * std::min<uint64_t>(cl.pairs.size(), 2 * cap));
+                return LC_OK;
+            }
+            case LC_DBG_VF: return copy_out(cl.vf.data(), cl.vf.size(), dst, cap, count);
+            case LC_DBG_EE: return copy_out(cl.ee.data(), cl.ee.size(), dst, cap, count);
+            case LC_DBG_FEATURES: return copy_out(cl.tp.features.data(), cl.tp.features.size(), dst, cap, count);
+            default: return LC_ERR_INVALID_ARG;
+        }
+    });
+}
+
+// Grid topology of Rendering/VisualBodyFactory.cpp:343-391.
+int lco_grid_indices(int rows, int cols, uint32_t *out) {
+    std::vector<u32> idx;
+    grid_indices(rows, cols, idx);
+    if (out) std::memcpy(out, idx.data(), idx.size() * sizeof(u32));
+    return (int)(idx.size() / 3);
+}
+
+// Morton code of one point, for golden-vector checks of the encoder.
+uint64_t lco_morton(float x, float y, float z, int mode) { return morton3d(x, y, z, mode); }
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+"""ctypes binding of oracle/liblc_oracle.so.
+
+TEST INFRASTRUCTURE ONLY (see oracle/lc_oracle.hpp): the checker for the CUDA
+engine, loaded by tests/, smoke() and bench.py's CPU-baseline leg.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from licenta_gb300 import _ffi
+from licenta_gb300.scenes import ClothSpec
+
+from . import build_oracle
+
+_lib = None
+VP = C.c_void_p
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(str(path))
+        sig = {
+            "lco_create": (VP, [C.POINTER(_ffi.ClothDesc), C.c_int, C.c_int]),
+            "lco_destroy": (None, [VP]),
+            "lco_num_cloths": (C.c_int, [VP]),
+            "lco_step": (C.c_int, [VP, C.c_int, C.c_int]),
+            "lco_max_threads": (C.c_int, []),
+            "lco_sizes": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+            "lco_get_state": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+            "lco_set_state": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+            "lco_get_perm": (C.c_int, [VP, C.c_int, VP]),
+            "lco_set_perm": (C.c_int, [VP, C.c_int, VP]),
+            "lco_get_wind": (C.c_int, [VP, C.c_int, VP, VP]),
+            "lco_set_wind": (C.c_int, [VP, C.c_int, VP, C.c_uint64]),
+            "lco_external": (C.c_int, [VP, C.c_int]),
+            "lco_collide": (C.c_int, [VP, C.c_int]),
+            "lco_step_one": (C.c_int, [VP, C.c_int]),
+            "lco_set_frozen_contacts": (C.c_int, [VP, C.c_int, VP, C.c_uint64, VP, C.c_uint64]),
+            "lco_set_stiffness": (C.c_int, [VP, C.c_int, VP, VP]),
+            "lco_set_forced": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
+            "lco_thickness": (C.c_int, [VP, C.c_int, VP]),
+            "lco_counters": (C.c_int, [VP, C.c_int, C.c_uint64 * 4]),
+            "lco_debug_get": (C.c_int, [VP, C.c_int, C.c_int, VP, C.c_uint64, C.POINTER(C.c_uint64)]),
+            "lco_grid_indices": (C.c_int, [C.c_int, C.c_int, VP]),
+            "lco_morton": (C.c_uint64, [C.c_float, C.c_float, C.c_float, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _chk(rc: int, where: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"oracle {where}: status {rc}")
+
+
+class Oracle:
+    """A batch of oracle cloths (fp64=True: FP64; False: FP32 mirror)."""
+
+    _DT = _ffi_DT = {1: (np.float32, 3), 2: (np.float32, 3), 3: (np.float32, 3), 4: (np.uint32, 1),
+                     5: (np.uint64, 1), 6: (np.uint32, 1), 7: (np.int32, 1), 8: (np.int32, 1), 9: (np.int32, 1),
+                     10: (np.int32, 2), 11: (np.float32, 6), 12: (np.uint32, 2), 15: (np.uint8, 1)}
+
+    def __init__(self, specs: Sequence[ClothSpec], fp64: bool = True):
+        keep = []
+        descs = (_ffi.ClothDesc * len(specs))()
+        for k, s in enumerate(specs):
+            pos = np.ascontiguousarray(s.positions, dtype=np.float32)
+            idx = np.ascontiguousarray(s.indices, dtype=np.uint32)
+            pin = np.ascontiguousarray(s.pinned, dtype=np.uint8)
+            keep += [pos, idx, pin]
+            descs[k].num_vertices = pos.shape[0]
+            descs[k].num_triangles = idx.shape[0]
+            descs[k].positions = pos.ctypes.data_as(C.POINTER(C.c_float))
+            descs[k].indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+            descs[k].pinned = pin.ctypes.data_as(C.POINTER(C.c_uint8))
+            descs[k].params = s.params
+        self._h = lib().lco_create(descs, len(specs), 1 if fp64 else 0)
+        if not self._h:
+            raise RuntimeError("oracle create failed")
+        self.fp64 = fp64
+        self.n = len(specs)
+        self.V = [s.num_vertices for s in specs]
+        self.T = [s.num_triangles for s in specs]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lco_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, nsteps: int = 1, threads: int = 0) -> None:
+        _chk(lib().lco_step(self._h, nsteps, threads), "step")
+
+    def step_one(self, c: int) -> None:
+        _chk(lib().lco_step_one(self._h, c), "step_one")
+
+    def external(self, c: int) -> None:
+        _chk(lib().lco_external(self._h, c), "external")
+
+    def collide(self, c: int) -> None:
+        _chk(lib().lco_collide(self._h, c), "collide")
+
+    def get_state(self, c: int) -> dict:
+        V = self.V[c]
+        out = {k: np.empty((V, 3), dtype=np.float64) for k in ("x", "x_prev", "v", "vn")}
+        _chk(lib().lco_get_state(self._h, c, _p(out["x"]), _p(out["x_prev"]), _p(out["v"]), _p(out["vn"])), "get_state")
+        return out
+
+    def set_state(self, c: int, x=None, x_prev=None, v=None, vn=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, x_prev, v, vn)]
+        _chk(lib().lco_set_state(self._h, c, *[_p(a) for a in arrs]), "set_state")
+
+    def perm(self, c: int) -> np.ndarray:
+        out = np.empty(self.T[c], dtype=np.uint32)
+        _chk(lib().lco_get_perm(self._h, c, _p(out)), "get_perm")
+        return out
+
+    def set_perm(self, c: int, perm) -> None:
+        p = np.ascontiguousarray(perm, dtype=np.uint32)
+        _chk(lib().lco_set_perm(self._h, c, _p(p)), "set_perm")
+
+    def wind(self, c: int):
+        w = np.empty(3, dtype=np.float64)
+        r = C.c_uint64()
+        _chk(lib().lco_get_wind(self._h, c, _p(w), C.byref(r)), "get_wind")
+        return w, r.value
+
+    def set_wind(self, c: int, wind, rng: int) -> None:
+        w = np.ascontiguousarray(wind, dtype=np.float64)
+        _chk(lib().lco_set_wind(self._h, c, _p(w), rng), "set_wind")
+
+    def freeze_contacts(self, c: int, vf: tuple, ee: tuple) -> None:
+        def pack(t):
+            v, w = t
+            arr = (_ffi.Contact * max(len(v), 1))()
+            for i in range(len(v)):
+                arr[i].v[:] = [int(q) for q in v[i]]
+                arr[i].w[:] = [float(q) for q in w[i]]
+            return arr, len(v)
+        a, na = pack(vf)
+        b, nb = pack(ee)
+        _chk(lib().lco_set_frozen_contacts(self._h, c, a, na, b, nb), "set_frozen_contacts")
+
+    def force_decisions(self, c: int, ground, ground_it, lra, dyn, sphere=None) -> None:
+        """Replay another implementation's discrete decisions in the next step."""
+        g = np.ascontiguousarray(ground, dtype=np.uint8)
+        gi = np.ascontiguousarray(ground_it, dtype=np.uint32)
+        la = np.ascontiguousarray(lra, dtype=np.uint8)
+        dy = np.ascontiguousarray(dyn, dtype=np.uint8)
+        sp = None if sphere is None else np.ascontiguousarray(sphere, dtype=np.int8)
+        _chk(lib().lco_set_forced(self._h, c, _p(g), _p(gi), _p(la), _p(dy), dy.size, _p(sp)), "set_forced")
+
+    def set_stiffness(self, c: int, k_stretch=None, k_bend=None) -> None:
+        ks = None if k_stretch is None else np.ascontiguousarray(k_stretch, dtype=np.float32)
+        kb = None if k_bend is None else np.ascontiguousarray(k_bend, dtype=np.float32)
+        _chk(lib().lco_set_stiffness(self._h, c, _p(ks), _p(kb)), "set_stiffness")
+
+    def thickness(self, c: int) -> float:
+        h = C.c_float()
+        _chk(lib().lco_thickness(self._h, c, C.byref(h)), "thickness")
+        return h.value
+
+    def counters(self, c: int) -> dict:
+        out = (C.c_uint64 * 4)()
+        rc = lib().lco_counters(self._h, c, out)
+        return dict(pairs=out[0], vf=out[1], ee=out[2], dropped=out[3], stack_overflow=rc != 0)
+
+    def debug(self, c: int, what: str):
+        sel = _ffi.DBG[what]
+        n = C.c_uint64()
+        _chk(lib().lco_debug_get(self._h, c, sel, None, 0, C.byref(n)), "debug_get")
+        if sel in (13, 14):
+            arr = (_ffi.Contact * max(n.value, 1))()
+            _chk(lib().lco_debug_get(self._h, c, sel, arr, n.value, C.byref(n)), "debug_get")
+            v = np.array([list(arr[i].v) for i in range(n.value)], dtype=np.int32).reshape(-1, 4)
+            w = np.array([list(arr[i].w) for i in range(n.value)], dtype=np.float32).reshape(-1, 4)
+            return v, w
+        dt, width = self._DT[sel]
+        out = np.empty((n.value, width) if width > 1 else (n.value,), dtype=dt)
+        _chk(lib().lco_debug_get(self._h, c, sel, _p(out), n.value, C.byref(n)), "debug_get")
+        return out
+
+
+def morton(x: float, y: float, z: float, mode: int = 0) -> int:
+    return int(lib().lco_morton(x, y, z, mode))
+
+
+def max_threads() -> int:
+    return int(lib().lco_max_threads())
