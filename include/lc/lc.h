@@ -112,8 +112,9 @@ typedef struct lc_batch_options {
     uint64_t ee_capacity;     /* EE contacts kept per step (default 8 * total triangles) */
     int32_t use_graph;        /* 1 (default): capture one step in a CUDA graph and replay it */
     int32_t debug_capture;    /* 1: keep intermediate buffers of the last step for lc_batch_debug_get */
-    int32_t solver_variant;   /* 0 = auto (cluster when every cloth fits on chip), 1 = per-vertex gather
-                                 over global memory, 2 = cluster on-chip */
+    int32_t solver_variant;   /* 0 = auto (cluster scatter when every cloth fits on chip, else 1),
+                                 1 = per-vertex gather over global memory, 2 = cluster on-chip gather,
+                                 3 = cluster on-chip scatter with fixed-point accumulators */
     int32_t block_size;       /* block size of the global-memory Jacobi kernel (0 = default) */
     uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull (default 8 * total triangles) */
 } lc_batch_options;

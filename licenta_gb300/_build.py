@@ -21,7 +21,14 @@ LIB = OUT / "liblicenta_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 SOURCES = ["lc_api.cu", "lc_lbvh.cu", "lc_step.cu", "lc_scan.cu", "lc_cluster.cu"]
-PER_FILE_FLAGS = {"lc_lbvh.cu": ["-fmad=false"]}
+# lc_lbvh.cu carries the bit-exact stages: no FMA contraction, IEEE div/sqrt.
+# The solver translation units are compared against FP64 within a tolerance
+# and use the approximate (2 ulp) division and square root.
+PER_FILE_FLAGS = {
+    "lc_lbvh.cu": ["-fmad=false"],
+    "lc_step.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "lc_cluster.cu": ["-prec-div=false", "-prec-sqrt=false"],
+}
 
 
 def nvcc() -> str:
@@ -60,16 +67,20 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         s = CSRC / src
         o = OUT / (s.stem + ".o")
         objs.append(o)
-        if not force and o.exists() and o.stat().st_mtime > max(s.stat().st_mtime, hdr):
-            continue
         cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
                "--expt-relaxed-constexpr", "-I", str(REPO / "include"), "-c", str(s), "-o", str(o)]
         cmd += PER_FILE_FLAGS.get(src, [])
-        jobs.append(cmd)
+        stamp = o.with_suffix(".flags")
+        if (not force and o.exists() and o.stat().st_mtime > max(s.stat().st_mtime, hdr)
+                and stamp.exists() and stamp.read_text() == " ".join(cmd)):
+            continue
+        jobs.append((cmd, stamp))
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
-            for f in [ex.submit(_run, j) for j in jobs]:
+            for f in [ex.submit(_run, j) for j, _ in jobs]:
                 f.result()
+        for cmd, stamp in jobs:
+            stamp.write_text(" ".join(cmd))
     if force or jobs or not LIB.exists():
         libdir = cuda_libdir()
         cmd = [nvcc(), ARCH, "-shared", "-o", str(LIB)] + [str(o) for o in objs] + [

@@ -28,8 +28,8 @@ void launch_karras(const DevPtrs &d, cudaStream_t st);
 void launch_refit(const DevPtrs &d, cudaStream_t st);
 void launch_traverse(const DevPtrs &d, int block, cudaStream_t st);
 void launch_pair_compact(const DevPtrs &d, cudaStream_t st);
-void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncand, int grid, int stage,
-                   cudaStream_t st);
+void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv, const uint32_t *nce, int grid,
+                   int stage, cudaStream_t st);
 void launch_wind(const DevPtrs &d, cudaStream_t st);
 void launch_external(const DevPtrs &d, cudaStream_t st);
 void launch_vertex_normals(const DevPtrs &d, cudaStream_t st);
@@ -46,9 +46,10 @@ struct ClusterArgs {
     const uint32_t *nvf;
     int chunk_cap;
 };
-cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, int nclusters, cudaStream_t st);
-int cluster_chunk_cap();
-int cluster_max_active(int cs, int chunk_cap);
+cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, bool scatter, int nclusters,
+                                 cudaStream_t st);
+int cluster_chunk_cap(bool scatter);
+int cluster_max_active(int cs, int chunk_cap, bool scatter);
 }  // namespace lc
 
 using namespace lc;
@@ -280,7 +281,7 @@ struct lc_batch {
     DeviceArena arena;
     ClothDev *cloth_dev = nullptr;
     int *tile_first = nullptr;
-    uint32_t *npairs = nullptr, *nvf = nullptr, *nee = nullptr, *ncand = nullptr;
+    uint32_t *npairs = nullptr, *nvf = nullptr, *nee = nullptr, *ncand = nullptr, *ncand_e = nullptr;
     int max_iters = 1;
     bool any_wind = false, any_sphere = false;
     int sort_passes = 8;
@@ -295,6 +296,7 @@ struct lc_batch {
     // cluster-resident solver (lc_cluster.cu)
     bool use_cluster = false;
     int cluster_cs = 8;
+    bool cluster_scatter = false;
     ClusterArgs ca{};
     // debug copies
     float4 *dbg_x = nullptr, *dbg_xp = nullptr, *dbg_v = nullptr;
@@ -374,15 +376,16 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     LC_PHASE(4);
     // 5. Perform Triangle Tests
     LC_KEV(4);
-    launch_narrow(d, npairs, ncand, narrow_grid, 0, st);  // filter
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 0, st);  // filter
     scan_u32(d.pair_vf_cnt, d.pair_vf_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand, nullptr, st);
-    launch_narrow(d, npairs, ncand, narrow_grid, 1, st);  // expand
-    launch_narrow(d, npairs, ncand, narrow_grid, 2, st);  // CCD
+    scan_u32(d.pair_ee_cnt, d.pair_ee_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand_e, nullptr, st);
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 1, st);  // expand
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 2, st);  // CCD
     LC_KEV(5);
     scan_u32(d.cand_vf, d.cand_vf_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nvf, &d.counters[1], st);
-    scan_u32(d.cand_ee, d.cand_ee_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nee, &d.counters[2], st);
-    launch_narrow(d, npairs, ncand, narrow_grid, 3, st);  // write contacts
-    launch_narrow(d, npairs, ncand, narrow_grid, 4, st);  // per-cloth ranges
+    scan_u32(d.cand_ee, d.cand_ee_off, ncand_e, 0, (uint32_t)d.cand_cap, d.scan_tmp, nee, &d.counters[2], st);
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 3, st);  // write contacts
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 4, st);  // per-cloth ranges
     LC_PHASE(5);
     // 6. PBD Solver (+ 7. integration fused on the cluster path)
     LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
@@ -418,7 +421,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
 
 // Solver + integration on the cluster-resident path (one launch).
 static lc_status enqueue_cluster_solver(lc_batch *b, cudaStream_t st) {
-    LC_CUDA(launch_solve_cluster(b->d, b->ca, b->cluster_cs, b->C, st));
+    LC_CUDA(launch_solve_cluster(b->d, b->ca, b->cluster_cs, b->cluster_scatter, b->C, st));
     return LC_OK;
 }
 
@@ -433,7 +436,10 @@ template <class T> static lc_status upload(T *dst, const std::vector<T> &src) {
 lc_status lc_batch::setup_cluster() {
     use_cluster = false;
     if (opt.solver_variant == 1) return LC_OK;
-    const int dev_cap = cluster_chunk_cap();
+    // the scatter form is the default on-chip solver (each constraint
+    // evaluated once per iteration); variant 2 selects the gather form
+    const bool scatter = opt.solver_variant != 2;
+    const int dev_cap = cluster_chunk_cap(scatter);
     int vmax = 0;
     bool ok = true;
     for (int c = 0; c < C; ++c) {
@@ -442,14 +448,15 @@ lc_status lc_batch::setup_cluster() {
     }
     int cs = 0;
     if (ok) {
-        if ((vmax + 7) / 8 <= dev_cap && cluster_max_active(8, (vmax + 7) / 8) > 0) cs = 8;
-        else if ((vmax + 15) / 16 <= dev_cap && cluster_max_active(16, (vmax + 15) / 16) > 0) cs = 16;
+        if ((vmax + 7) / 8 <= dev_cap && cluster_max_active(8, (vmax + 7) / 8, scatter) > 0) cs = 8;
+        else if ((vmax + 15) / 16 <= dev_cap && cluster_max_active(16, (vmax + 15) / 16, scatter) > 0) cs = 16;
     }
     if (!cs) {
-        if (opt.solver_variant == 2) return fail(LC_ERR_NOT_SUPPORTED, "cluster solver: a cloth does not fit on chip");
+        if (opt.solver_variant >= 2) return fail(LC_ERR_NOT_SUPPORTED, "cluster solver: a cloth does not fit on chip");
         return LC_OK;
     }
     cluster_cs = cs;
+    cluster_scatter = scatter;
     std::vector<int> order(C);
     for (int c = 0; c < C; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hosts[x].V > hosts[y].V; });
@@ -519,6 +526,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
         cd.pc_off = PC;
         cd.f_off = (int)F; cd.F = (int)hc.fixed.size();
         cd.lra_off = LRA;
+        cd.s_off = (int)E; cd.s_cnt = (int)hc.s_ids.size();
+        cd.b_off = (int)B; cd.b_cnt = (int)hc.b_ids.size();
         b->e_off[c] = (int)E; b->b_off[c] = (int)B;
         b->s_count[c] = (int)hc.s_ids.size();
         b->b_count[c] = (int)hc.b_ids.size();
@@ -574,11 +583,13 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));
-    LC_TRY(A.alloc(d.pair_vf_cnt, PC, "pair_cand_cnt"));
-    LC_TRY(A.alloc(d.pair_vf_off, PC + 1, "pair_cand_off"));
-    d.cand_cap = opt.cand_capacity ? opt.cand_capacity : std::max<uint64_t>(8 * (uint64_t)T, 65536);
+    LC_TRY(A.alloc(d.pair_vf_cnt, PC, "pair_vf_cnt")); LC_TRY(A.alloc(d.pair_ee_cnt, PC, "pair_ee_cnt"));
+    LC_TRY(A.alloc(d.pair_vf_off, PC + 1, "pair_vf_off")); LC_TRY(A.alloc(d.pair_ee_off, PC + 1, "pair_ee_off"));
+    // at most 15 candidates per pair; by default room for 32 per triangle
+    d.cand_cap = opt.cand_capacity ? opt.cand_capacity
+                                   : std::min<uint64_t>(15 * (uint64_t)PC, std::max<uint64_t>(32 * (uint64_t)T, 1u << 22));
     d.cand_cap = std::min<uint64_t>(d.cand_cap, 0xFFFFFFF0ull);
-    LC_TRY(A.alloc(d.cand, d.cand_cap, "candidates"));
+    LC_TRY(A.alloc(d.cand, d.cand_cap, "vf candidates")); LC_TRY(A.alloc(d.cand_e, d.cand_cap, "ee candidates"));
     LC_TRY(A.alloc(d.cand_vf, d.cand_cap, "cand_vf")); LC_TRY(A.alloc(d.cand_ee, d.cand_cap, "cand_ee"));
     LC_TRY(A.alloc(d.cand_vf_off, d.cand_cap + 1, "cand_vf_off")); LC_TRY(A.alloc(d.cand_ee_off, d.cand_cap + 1, "cand_ee_off"));
     LC_TRY(A.alloc(d.crange, n, "contact ranges"));
@@ -608,7 +619,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     d.vblk_cloth = vbc; d.vblk_start = vbs; d.vb_first = vbf;
     LC_TRY(A.alloc(d.damp_part, 16 * vblk_cloth.size(), "damp_part"));
     LC_TRY(A.alloc(b->npairs, 1, "npairs")); LC_TRY(A.alloc(b->nvf, 1, "nvf")); LC_TRY(A.alloc(b->nee, 1, "nee"));
-    LC_TRY(A.alloc(b->ncand, 1, "ncand"));
+    LC_TRY(A.alloc(b->ncand, 1, "ncand")); LC_TRY(A.alloc(b->ncand_e, 1, "ncand_e"));
     if (opt.debug_capture) {
         LC_TRY(A.alloc(b->dbg_x, V, "dbg_x")); LC_TRY(A.alloc(b->dbg_xp, V, "dbg_xp"));
         LC_TRY(A.alloc(b->dbg_v, V, "dbg_v")); LC_TRY(A.alloc(b->dbg_perm_before, T, "dbg_perm"));
@@ -697,6 +708,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_CUDA(cudaMemset(b->nvf, 0, sizeof(uint32_t)));
     LC_CUDA(cudaMemset(b->nee, 0, sizeof(uint32_t)));
     LC_CUDA(cudaMemset(b->ncand, 0, sizeof(uint32_t)));
+    LC_CUDA(cudaMemset(b->ncand_e, 0, sizeof(uint32_t)));
     LC_CUDA(cudaMemset(d.crange, 0, sizeof(uint4) * (size_t)n));
     LC_CUDA(cudaMemset(d.nmin, 0, sizeof(float4) * (size_t)N));
     LC_CUDA(cudaMemset(d.nmax, 0, sizeof(float4) * (size_t)N));
@@ -1260,7 +1272,7 @@ lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile
             cudaEventElapsedTime(&ms, kev[8 * k + 6], kev[8 * k + 7]); out->sort_ms += ms / nsteps;
         }
         for (int p = 0; p < 7; ++p) out->step_ms += out->phase_ms[p];
-        out->solver_variant = b->use_cluster ? 2 : 1;
+        out->solver_variant = b->use_cluster ? (b->cluster_scatter ? 3 : 2) : 1;
         out->cluster_size = b->use_cluster ? b->cluster_cs : 0;
         if (!b->use_cluster) out->solver_ms = out->phase_ms[5];
         // kernel launches per step, counted from the captured graph

@@ -55,8 +55,11 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
     float *gq = reinterpret_cast<float *>(smem4 + 2 * cap);
     uint8_t *lra = reinterpret_cast<uint8_t *>(gq + cap);
 
+    // owner CTA of local vertex li = li / chunk, as a multiply-high by
+    // ceil(2^32 / chunk): exact for li, chunk < 2^16
+    const uint32_t magic = (uint32_t)((0x100000000ull + chunk - 1) / chunk);
     auto X = [&](const float4 *xs, int li) -> float4 {
-        const int o = li / chunk;
+        const int o = (int)__umulhi((uint32_t)li, magic);
         if (o == r) return xs[li - lo];
         return cluster.map_shared_rank(xs, o)[li - o * chunk];
     };
@@ -249,75 +252,308 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
     }
 }
 
-size_t cluster_smem_bytes(int chunk_cap) { return (size_t)chunk_cap * kClusterBytesPerVertex + 64; }
+
+// ---------------------------------------------------------------------------
+// Scatter variant: every constraint is evaluated once per iteration by one
+// thread of the cluster, which adds its corrections to the owners'
+// accumulators (local or distributed shared memory).  Accumulators are 64-bit
+// fixed point (2^-32 m), so the sums are exact and independent of the order
+// the atomics land in, and results stay deterministic.
+// Shared memory per vertex: x (16) + 3 x s64 (24) + count (4) + ground (4) +
+// LRA flags (1).
+// ---------------------------------------------------------------------------
+constexpr int kScatterBytesPerVertex = 49;
+constexpr float kFix = 4294967296.f;           // 2^32
+constexpr float kFixInv = 1.f / 4294967296.f;  // exact power of two
+
+template <int CS>
+__global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevPtrs d, ClusterArgs a) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();
+    const int c = a.cl_cloth[blockIdx.x / CS];
+    const ClothDev &cd = d.cloth[c];
+    const int V = cd.V, vo = cd.v_off;
+    const int chunk = (V + CS - 1) / CS;
+    const int lo = r * chunk;
+    const int n_own = max(0, min(V, lo + chunk) - lo);
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const int cap = a.chunk_cap;
+    extern __shared__ float4 smem4[];
+    float4 *xs = smem4;
+    long long *ax = reinterpret_cast<long long *>(xs + cap);
+    long long *ay = ax + cap;
+    long long *az = ay + cap;
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(az + cap);
+    float *gq = reinterpret_cast<float *>(cnt + cap);
+    uint8_t *lra = reinterpret_cast<uint8_t *>(gq + cap);
+    const uint32_t magic = (uint32_t)((0x100000000ull + chunk - 1) / chunk);
+    auto owner = [&](int li) { return (int)__umulhi((uint32_t)li, magic); };
+    auto X = [&](int li) -> float4 {
+        const int o = owner(li);
+        if (o == r) return xs[li - lo];
+        return cluster.map_shared_rank(xs, o)[li - o * chunk];
+    };
+    auto add_corr = [&](int li, float3 v, bool count) {
+        const int o = owner(li);
+        const int k = li - o * chunk;
+        long long *px = o == r ? ax : cluster.map_shared_rank(ax, o);
+        long long *py = o == r ? ay : cluster.map_shared_rank(ay, o);
+        long long *pz = o == r ? az : cluster.map_shared_rank(az, o);
+        atomicAdd(reinterpret_cast<unsigned long long *>(px + k), (unsigned long long)__float2ll_rn(v.x * kFix));
+        atomicAdd(reinterpret_cast<unsigned long long *>(py + k), (unsigned long long)__float2ll_rn(v.y * kFix));
+        atomicAdd(reinterpret_cast<unsigned long long *>(pz + k), (unsigned long long)__float2ll_rn(v.z * kFix));
+        if (count) atomicAdd(o == r ? cnt + k : cluster.map_shared_rank(cnt, o) + k, 1u);
+    };
+    const float qnan = __int_as_float(0x7fc00000);
+    for (int i = tid; i < n_own; i += bs) {
+        const int g = vo + lo + i;
+        const float4 x4 = d.x[g];
+        xs[i] = x4;
+        ax[i] = ay[i] = az[i] = 0;
+        cnt[i] = 0;
+        lra[i] = 0;
+        float q = qnan;
+        float4 qdbg = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (cd.ground_on && x4.y <= cd.ground_y + cd.h) {
+            const float3 pos = xyz(x4);
+            const float3 nc = f3(0.f, 1.f, 0.f);
+            const float3 p0 = f3(1.f, cd.ground_y + cd.h, 1.f);
+            const float3 l = sub(pos, xyz(d.xp[g]));
+            const float dd = dot(sub(p0, pos), nc) / dot(l, nc);
+            const float3 qc = add(mul(l, dd), pos);
+            q = (isfinite(qc.x) && isfinite(qc.z)) ? qc.y : qnan;
+            qdbg = f4(qc, 1.f);
+        }
+        gq[i] = q;
+        if (d.dbg_ground_it) d.ground_qc[g] = qdbg;
+    }
+    cluster.sync();
+    if (cd.F) {
+        for (int i = tid; i < n_own; i += bs) {
+            const float4 x4 = xs[i];
+            uint8_t f = 0;
+            const int64_t base = cd.lra_off + (int64_t)(lo + i) * cd.F;
+            if (x4.w != 0.f)
+                for (int j = 0; j < cd.F; ++j)
+                    if (dist(xyz(x4), xyz(X(d.fixed[cd.f_off + j] - vo))) > d.lra_l0[base + j]) f |= (uint8_t)(1u << j);
+            lra[i] = f;
+            if (d.dbg_ground_it)
+                for (int j = 0; j < cd.F; ++j) d.lra_flag[base + j] = (f >> j) & 1u;
+        }
+        cluster.sync();
+    }
+    if (cd.sphere_on) {
+        const float3 sc = f3(cd.sphere_pos[0], cd.sphere_pos[1], cd.sphere_pos[2]);
+        const float rad = cd.sphere_r + cd.h;
+        for (int i = tid; i < n_own; i += bs) {
+            const int g = vo + lo + i;
+            const float4 x4 = xs[i], p4 = d.xp[g];
+            float3 dir = sub(xyz(x4), xyz(p4));
+            int ret = 0;
+            float3 q = f3(0.f, 0.f, 0.f);
+            if (!is_zero(dir)) {
+                const float l = len(dir);
+                dir = dvs(dir, l);
+                const float3 m = sub(xyz(p4), sc);
+                const float b = dot(m, dir);
+                const float cc = dot(m, m) - rad * rad;
+                if (!(cc > 0.f && b > 0.f)) {
+                    const float disc = b * b - cc;
+                    if (!(disc < 0.f)) {
+                        const float t = -b - sqrtf(disc);
+                        if (t < 0.f) { q = add(xyz(p4), mul(dir, t)); ret = -1; }
+                        else if (!(t > l)) { q = add(xyz(p4), mul(dir, t)); ret = 1; }
+                    }
+                }
+            }
+            if (d.dbg_sphere) d.dbg_sphere[g] = (int8_t)ret;
+            if (ret == -1) {
+                const float3 qs = add(sc, mul(normalize(sub(q, sc)), rad));
+                const float3 ns = normalize(sub(qs, sc));
+                d.xp[g] = f4(add(qs, mul(ns, 0.0001f)), p4.w);
+                xs[i] = f4(qs, x4.w);
+            } else if (ret == 1) {
+                const float3 ns = normalize(sub(q, sc));
+                xs[i] = f4(add(q, mul(ns, 0.0001f)), x4.w);
+            }
+        }
+        cluster.sync();
+    }
+    const uint4 cr = d.crange[c];
+    const uint32_t nvf_all = (uint32_t)min((uint64_t)*a.nvf, d.vf_cap);
+    const float h = cd.h;
+    // this CTA's share of the cloth's constraints (index order ~ vertex order)
+    const int s_per = (cd.s_cnt + CS - 1) / CS, b_per = (cd.b_cnt + CS - 1) / CS;
+    const int sb = cd.s_off + min(cd.s_cnt, r * s_per), se = cd.s_off + min(cd.s_cnt, (r + 1) * s_per);
+    const int bb = cd.b_off + min(cd.b_cnt, r * b_per), be = cd.b_off + min(cd.b_cnt, (r + 1) * b_per);
+    for (int it = 0; it < cd.iters; ++it) {
+        for (int k = sb + tid; k < se; k += bs) {
+            const int2 id = __ldg(&d.s_ids[k]);
+            const float2 par = __ldg(&d.s_par[k]);
+            const int i1 = id.x - vo, i2 = id.y - vo;
+            const float4 p1 = X(i1), p2 = X(i2);
+            add_corr(i1, stretch_corr_pos(p1, p2, par.x, par.y, 0), false);
+            add_corr(i2, stretch_corr_pos(p1, p2, par.x, par.y, 1), false);
+        }
+        for (int k = bb + tid; k < be; k += bs) {
+            const int4 id = __ldg(&d.b_ids[k]);
+            const float kp = __ldg(&d.b_kp[k]);
+            const int li[4] = {id.x - vo, id.y - vo, id.z - vo, id.w - vo};
+            const float4 p[4] = {X(li[0]), X(li[1]), X(li[2]), X(li[3])};
+            float3 q[4];
+            float s;
+            if (bend_all_pos(p[0], p[1], p[2], p[3], kp, d.kpi_gap, q, s)) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) add_corr(li[j], mul(q[j], -(p[j].w * s)), false);
+            }
+        }
+        const uint32_t nv = cr.y - cr.x, ncont = nv + (cr.w - cr.z);
+        for (uint32_t k = r * bs + tid; k < ncont; k += CS * bs) {
+            const bool isvf = k < nv;
+            const uint32_t gi = isvf ? cr.x + k : cr.z + (k - nv);
+            const int4 v = isvf ? d.vf_v[gi] : d.ee_v[gi];
+            const float4 w = isvf ? d.vf_w[gi] : d.ee_w[gi];
+            const int li[4] = {v.x - vo, v.y - vo, v.z - vo, v.w - vo};
+            const float4 P[4] = {X(li[0]), X(li[1]), X(li[2]), X(li[3])};
+            const uint32_t ent = 4u * (isvf ? gi : nvf_all + gi);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float3 corr = contact_corr_pos(P[0], P[1], P[2], P[3], w, isvf, h, j);
+                const bool nz = !is_zero(corr);
+                if (nz) add_corr(li[j], corr, true);
+                if (d.dbg_dyn_nz) d.dbg_dyn_nz[(size_t)it * d.dyn_cap + ent + j] = nz ? 1 : 0;
+            }
+        }
+        for (int i = tid; i < n_own; i += bs) {
+            const float4 x4 = xs[i];
+            const float cv = x4.y - gq[i];
+            const bool ground = cv < 0.f;
+            if (ground) {
+                atomicAdd(reinterpret_cast<unsigned long long *>(ay + i), (unsigned long long)__float2ll_rn(-cv * kFix));
+                atomicAdd(cnt + i, 1u);
+            }
+            if (d.dbg_ground_it) {
+                const uint32_t bit = ground ? (1u << it) : 0u;
+                d.dbg_ground_it[vo + lo + i] = it == 0 ? bit : (d.dbg_ground_it[vo + lo + i] | bit);
+            }
+            const uint8_t f = lra[i];
+            if (f) {
+                const int64_t base = cd.lra_off + (int64_t)(lo + i) * cd.F;
+                for (int j = 0; j < cd.F; ++j) {
+                    if (!((f >> j) & 1u)) continue;
+                    const float3 diff = sub(xyz(x4), xyz(X(d.fixed[cd.f_off + j] - vo)));
+                    const float l = len(diff);
+                    const float3 n = dvs(diff, l);
+                    add_corr(lo + i, mul(n, -(l - d.lra_l0[base + j])), true);
+                }
+            }
+        }
+        cluster.sync();
+        for (int i = tid; i < n_own; i += bs) {
+            const int g = vo + lo + i;
+            const float n = (float)(__ldg(&d.soff[g + 1]) - __ldg(&d.soff[g]) + (int)cnt[i]);
+            float4 x4 = xs[i];
+            x4.x += (__ll2float_rn(ax[i]) * kFixInv) / n;
+            x4.y += (__ll2float_rn(ay[i]) * kFixInv) / n;
+            x4.z += (__ll2float_rn(az[i]) * kFixInv) / n;
+            xs[i] = x4;
+            ax[i] = ay[i] = az[i] = 0;
+            cnt[i] = 0;
+        }
+        cluster.sync();
+    }
+    for (int i = tid; i < n_own; i += bs) {
+        const int g = vo + lo + i;
+        const float4 x4 = xs[i];
+        float3 p = xyz(x4);
+        if (x4.w == 0.f) {
+            d.v[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            const float4 p4 = d.xp[g];
+            d.v[g] = f4(dvs(sub(p, xyz(p4)), cd.dt), 0.f);
+            d.xp[g] = f4(p, p4.w);
+        }
+        p = f3(fminf(fmaxf(p.x, cd.wmin[0]), cd.wmax[0]), fminf(fmaxf(p.y, cd.wmin[1]), cd.wmax[1]),
+               fminf(fmaxf(p.z, cd.wmin[2]), cd.wmax[2]));
+        d.x[g] = f4(p, x4.w);
+    }
+}
+
+size_t cluster_smem_bytes(int chunk_cap, bool scatter) {
+    return (size_t)chunk_cap * (scatter ? kScatterBytesPerVertex : kClusterBytesPerVertex) + 128;
+}
 
 // Largest per-CTA vertex range the device's shared memory allows.
-int cluster_chunk_cap() {
+int cluster_chunk_cap(bool scatter) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (optin <= 0) optin = 48 * 1024;
-    return (optin - 128) / kClusterBytesPerVertex;
+    return (optin - 256) / (scatter ? kScatterBytesPerVertex : kClusterBytesPerVertex);
 }
 
-template <int CS>
-static cudaError_t launch_cs(const DevPtrs &d, const ClusterArgs &a, int nclusters, cudaStream_t st) {
-    const size_t smem = cluster_smem_bytes(a.chunk_cap);
-    cudaError_t e = cudaFuncSetAttribute(k_solve_cluster<CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int CS, bool SCATTER>
+static cudaError_t configure(size_t smem) {
+    auto k = SCATTER ? k_solve_cluster_scatter<CS> : k_solve_cluster<CS>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (CS > 8) {
-        e = cudaFuncSetAttribute(k_solve_cluster<CS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return e;
-    }
+    if (CS > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+static cudaLaunchConfig_t cluster_cfg(int cs, int nclusters, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nclusters * CS);
+    cfg.gridDim = dim3(nclusters * cs);
     cfg.blockDim = dim3(kClusterBlock);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_solve_cluster<CS>, d, a);
-}
-
-cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, int nclusters, cudaStream_t st) {
-    if (cs == 16) return launch_cs<16>(d, a, nclusters, st);
-    return launch_cs<8>(d, a, nclusters, st);
-}
-
-// How many clusters of cs CTAs the device can hold at once (0: unsupported).
-int cluster_max_active(int cs, int chunk_cap) {
-    const size_t smem = cluster_smem_bytes(chunk_cap);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cs * 64);
-    cfg.blockDim = dim3(kClusterBlock);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = cs;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    int n = 0;
-    cudaError_t e;
-    if (cs == 16) {
-        cudaFuncSetAttribute(k_solve_cluster<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_solve_cluster<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaOccupancyMaxActiveClusters(&n, k_solve_cluster<16>, &cfg);
-    } else {
-        cudaFuncSetAttribute(k_solve_cluster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        e = cudaOccupancyMaxActiveClusters(&n, k_solve_cluster<8>, &cfg);
+    return cfg;
+}
+
+template <int CS, bool SCATTER>
+static cudaError_t launch_cs(const DevPtrs &d, const ClusterArgs &a, int nclusters, cudaStream_t st) {
+    const size_t smem = cluster_smem_bytes(a.chunk_cap, SCATTER);
+    cudaError_t e = configure<CS, SCATTER>(smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(CS, nclusters, smem, st, attr);
+    return cudaLaunchKernelEx(&cfg, SCATTER ? k_solve_cluster_scatter<CS> : k_solve_cluster<CS>, d, a);
+}
+
+cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, bool scatter, int nclusters,
+                                 cudaStream_t st) {
+    if (cs == 16) return scatter ? launch_cs<16, true>(d, a, nclusters, st) : launch_cs<16, false>(d, a, nclusters, st);
+    return scatter ? launch_cs<8, true>(d, a, nclusters, st) : launch_cs<8, false>(d, a, nclusters, st);
+}
+
+template <int CS, bool SCATTER>
+static int max_active(int chunk_cap) {
+    const size_t smem = cluster_smem_bytes(chunk_cap, SCATTER);
+    if (configure<CS, SCATTER>(smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
     }
-    if (e != cudaSuccess) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(CS, 64, smem, nullptr, attr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, SCATTER ? k_solve_cluster_scatter<CS> : k_solve_cluster<CS>, &cfg) !=
+        cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
+}
+
+// How many clusters of cs CTAs the device can hold at once (0: unsupported).
+int cluster_max_active(int cs, int chunk_cap, bool scatter) {
+    if (cs == 16) return scatter ? max_active<16, true>(chunk_cap) : max_active<16, false>(chunk_cap);
+    return scatter ? max_active<8, true>(chunk_cap) : max_active<8, false>(chunk_cap);
 }
 
 }  // namespace lc

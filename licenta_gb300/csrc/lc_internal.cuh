@@ -50,6 +50,8 @@ struct ClothDev {
     float sphere_pos[3], sphere_r;
     float wind_start[3], wind_min[3], wind_max[3];
     float wind_var_min, wind_var_max;
+    int s_off, s_cnt;      // stretch constraints of the cloth (global range)
+    int b_off, b_cnt;      // bend constraints
 };
 
 // Mutable per-cloth state that kernels update on the device (wind + RNG).
@@ -92,10 +94,10 @@ struct DevPtrs {
     uint2 *pairs;          // compacted (global slot i, global slot j)
     uint64_t pair_cap;
     uint16_t *pair_mask;   // per pair: bits 0..5 VF, 6..14 EE candidates past the AABB cull
-    uint32_t *pair_vf_cnt; // per pair: candidate count
-    uint32_t *pair_vf_off; // per pair: first candidate (exclusive scan), total at [npairs]
-    unsigned long long *cand;  // candidate: pair << 4 | slot
-    uint64_t cand_cap;
+    uint32_t *pair_vf_cnt, *pair_ee_cnt;  // per pair: VF / EE candidate counts
+    uint32_t *pair_vf_off, *pair_ee_off;  // per pair: first candidate (exclusive scans), totals at [npairs]
+    unsigned long long *cand, *cand_e;    // VF / EE candidates: pair << 4 | slot
+    uint64_t cand_cap;                    // per list
     uint32_t *cand_vf, *cand_ee;          // per candidate: CCD hit flags
     uint32_t *cand_vf_off, *cand_ee_off;  // per candidate: output slot (exclusive scans)
     uint4 *crange;         // per cloth: [vf0, vf1) and [ee0, ee1) contact ranges

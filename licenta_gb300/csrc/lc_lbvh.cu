@@ -388,14 +388,18 @@ __device__ __forceinline__ float triple(float3 x21, float3 x31, float3 x41, floa
                                         float t) {
     return dot(cross(add(x21, mul(v21, t)), add(x31, mul(v31, t))), add(x41, mul(v41, t)));
 }
+// Physics/CudaCubicSolver.cu:131-153.  The reference evaluates f at both
+// ends every iteration; f(x0) of an iteration is f(x1) of the previous one
+// (same arguments, same bits), so it is carried over instead of recomputed.
 __device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41, float a, float b) {
     float x0 = a, x1 = b;
+    float f0 = triple(x21, x31, x41, v21, v31, v41, x0);
     for (int i = 0; i < 20; ++i) {
-        const float f0 = triple(x21, x31, x41, v21, v31, v41, x0);
         const float f1 = triple(x21, x31, x41, v21, v31, v41, x1);
         const float xc = (x0 * f1 - x1 * f0) / (f1 - f0);
         if (fabsf(xc - x1) < kEpsCubic) return xc;
         x0 = x1;
+        f0 = f1;
         x1 = xc;
     }
     return -15.f;
@@ -644,28 +648,37 @@ __global__ void k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) 
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint16_t m = pair_filter(d, p);
         d.pair_mask[p] = m;
-        d.pair_vf_cnt[p] = (uint32_t)__popc((unsigned)m);
+        d.pair_vf_cnt[p] = (uint32_t)__popc((unsigned)(m & 0x3Fu));
+        d.pair_ee_cnt[p] = (uint32_t)__popc((unsigned)(m >> 6));
     }
 }
 
-// Stage 2: one (pair, slot) entry per surviving candidate, in pair-then-slot
-// order — the order of the reference's compactions.
+// Stage 2: one (pair, slot) entry per surviving candidate, VF and EE in
+// separate lists, each in pair-then-slot order — the order of the
+// reference's compactions.
 __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) {
     const uint32_t n = *npairs;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         uint32_t m = d.pair_mask[p];
-        uint64_t o = d.pair_vf_off[p];
+        uint64_t ov = d.pair_vf_off[p], oe = d.pair_ee_off[p];
         while (m) {
             const int s = __ffs(m) - 1;
             m &= m - 1;
-            if (o < d.cand_cap) d.cand[o] = ((unsigned long long)p << 4) | (unsigned)s;
-            else atomicOr(d.err, ERR_CAND_OVERFLOW);
-            ++o;
+            const unsigned long long e = ((unsigned long long)p << 4) | (unsigned)s;
+            if (s < 6) {
+                if (ov < d.cand_cap) d.cand[ov] = e;
+                else atomicOr(d.err, ERR_CAND_OVERFLOW);
+                ++ov;
+            } else {
+                if (oe < d.cand_cap) d.cand_e[oe] = e;
+                else atomicOr(d.err, ERR_CAND_OVERFLOW);
+                ++oe;
+            }
         }
     }
 }
 
-__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long long q, int4 &ids, bool &isvf, Wts &w) {
+__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long long q, int4 &ids, Wts &w) {
     const uint32_t p = (uint32_t)(q >> 4);
     const int s = (int)(q & 15u);
     const uint2 pr = d.pairs[p];
@@ -673,42 +686,42 @@ __device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long lo
     const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
     const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
     ids = candidate_ids(vid, s);
-    isvf = s < 6;
-    return isvf ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
-                : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
+    return s < 6 ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
+                 : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
 }
 
-// Stage 3: CCD of every candidate, one per thread
+// Stage 3: CCD of every candidate of one kind, one per thread
 // (Collision/CudaPrimitiveTests.cu:109-238).
+template <bool VF>
 __global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const unsigned long long *list = VF ? d.cand : d.cand_e;
+    uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         int4 ids;
-        bool isvf;
         Wts w;
-        const bool hit = candidate_ccd(d, d.cand[q], ids, isvf, w);
-        d.cand_vf[q] = hit && isvf;
-        d.cand_ee[q] = hit && !isvf;
+        hit[q] = candidate_ccd(d, list[q], ids, w) ? 1u : 0u;
     }
 }
 
-// Stage 4: contacts written in candidate order (the reference's compaction
-// order); the CCD of the few hits is evaluated again for their weights.
+// Stage 4: contacts written in candidate order; the CCD of the few hits is
+// evaluated again for their weights.
+template <bool VF>
 __global__ void k_ccd_write(DevPtrs d, const uint32_t *__restrict__ ncand) {
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const unsigned long long *list = VF ? d.cand : d.cand_e;
+    const uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
+    const uint32_t *off = VF ? d.cand_vf_off : d.cand_ee_off;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const bool hv = d.cand_vf[q] != 0, he = d.cand_ee[q] != 0;
-        if (!hv && !he) continue;
+        if (!hit[q]) continue;
         int4 ids;
-        bool isvf;
         Wts w;
-        candidate_ccd(d, d.cand[q], ids, isvf, w);
-        if (hv) {
-            const uint32_t o = d.cand_vf_off[q];
+        candidate_ccd(d, list[q], ids, w);
+        const uint32_t o = off[q];
+        if (VF) {
             if (o < d.vf_cap) { d.vf_v[o] = ids; d.vf_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
             else atomicOr(d.err, ERR_VF_OVERFLOW);
         } else {
-            const uint32_t o = d.cand_ee_off[q];
             if (o < d.ee_cap) { d.ee_v[o] = ids; d.ee_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
             else atomicOr(d.err, ERR_EE_OVERFLOW);
         }
@@ -717,17 +730,18 @@ __global__ void k_ccd_write(DevPtrs d, const uint32_t *__restrict__ ncand) {
 
 // Per-cloth contact ranges (the VF and the EE contacts of one cloth are
 // contiguous).
-__global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncand) {
+__global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncv, const uint32_t *__restrict__ nce) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.C) return;
     const ClothDev &cd = d.cloth[c];
-    const uint32_t nc = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const uint32_t nv = (uint32_t)min((uint64_t)*ncv, d.cand_cap), ne = (uint32_t)min((uint64_t)*nce, d.cand_cap);
     const uint32_t p0 = d.pair_off[cd.t_off], p1 = d.pair_off[cd.t_off + cd.T];
-    const uint32_t q0 = min(d.pair_vf_off[p0], nc), q1 = min(d.pair_vf_off[p1], nc);
-    d.crange[c] = make_uint4((uint32_t)min((uint64_t)d.cand_vf_off[q0], d.vf_cap),
-                             (uint32_t)min((uint64_t)d.cand_vf_off[q1], d.vf_cap),
-                             (uint32_t)min((uint64_t)d.cand_ee_off[q0], d.ee_cap),
-                             (uint32_t)min((uint64_t)d.cand_ee_off[q1], d.ee_cap));
+    const uint32_t v0 = min(d.pair_vf_off[p0], nv), v1 = min(d.pair_vf_off[p1], nv);
+    const uint32_t e0 = min(d.pair_ee_off[p0], ne), e1 = min(d.pair_ee_off[p1], ne);
+    d.crange[c] = make_uint4((uint32_t)min((uint64_t)d.cand_vf_off[v0], d.vf_cap),
+                             (uint32_t)min((uint64_t)d.cand_vf_off[v1], d.vf_cap),
+                             (uint32_t)min((uint64_t)d.cand_ee_off[e0], d.ee_cap),
+                             (uint32_t)min((uint64_t)d.cand_ee_off[e1], d.ee_cap));
 }
 
 // ---------------------------------------------------------------------------
@@ -770,13 +784,19 @@ void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
 void launch_pair_compact(const DevPtrs &d, cudaStream_t st) {
     if (d.Ttot) k_pair_compact<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
 }
-void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncand, int grid, int stage,
-                   cudaStream_t st) {
+void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv, const uint32_t *nce, int grid,
+                   int stage, cudaStream_t st) {
     if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 1) k_narrow_expand<<<grid, kThreads, 0, st>>>(d, npairs);
-    else if (stage == 2) k_ccd<<<grid, kThreads, 0, st>>>(d, ncand);
-    else if (stage == 3) k_ccd_write<<<grid, kThreads, 0, st>>>(d, ncand);
-    else k_contact_ranges<<<nblk(d.C, 128), 128, 0, st>>>(d, ncand);
+    else if (stage == 2) {
+        k_ccd<true><<<grid, kThreads, 0, st>>>(d, ncv);
+        k_ccd<false><<<grid, kThreads, 0, st>>>(d, nce);
+    } else if (stage == 3) {
+        k_ccd_write<true><<<grid, kThreads, 0, st>>>(d, ncv);
+        k_ccd_write<false><<<grid, kThreads, 0, st>>>(d, nce);
+    } else {
+        k_contact_ranges<<<nblk(d.C, 128), 128, 0, st>>>(d, ncv, nce);
+    }
 }
 
 }  // namespace lc

@@ -58,6 +58,33 @@ __device__ __forceinline__ float3 bend_corr_pos(float4 a1, float4 a2, float4 a3,
     return mul(q, -(wr * ts));
 }
 
+// The same bend constraint evaluated once for all four vertices: q[j] and the
+// scale s such that vertex j's correction is -(w_j s) q[j].  Returns false
+// when the reference returns zero corrections.
+__device__ __forceinline__ bool bend_all_pos(float4 a1, float4 a2, float4 a3, float4 a4, float kp, float kpi_gap,
+                                             float3 q[4], float &s) {
+    const float3 p2 = xyz(a2), p3 = xyz(a3), p4 = xyz(a4);
+    const float3 c23 = cross(p2, p3), c24 = cross(p2, p4);
+    const float l23 = len(c23), l24 = len(c24);
+    if (l23 <= kEpsPbd || l24 <= kEpsPbd) return false;
+    const float3 n1 = dvs(c23, l23), n2 = dvs(c24, l24);
+    const float3 sv = add(n1, n2), tv = sub(n1, n2);
+    const float ss = dot(sv, sv), tt = dot(tv, tv);
+    if (ss == 0.f) return false;
+    const float opd = 0.5f * ss, omd = 0.5f * tt;
+    const float dphi = kpi_gap - 2.f * atan2f(sqrtf(ss), sqrtf(tt));
+    const float term = sqrtf(opd * omd) * dphi * kp;
+    const float3 u = sub(sv, mul(n1, opd)), w = sub(sv, mul(n2, opd));
+    q[2] = dvs(cross(p2, u), l23);
+    q[3] = dvs(cross(p2, w), l24);
+    q[1] = neg(add(dvs(cross(p3, u), l23), dvs(cross(p4, w), l24)));
+    q[0] = sub(sub(neg(q[1]), q[2]), q[3]);
+    const float sf = a1.w * dot(q[0], q[0]) + a2.w * dot(q[1], q[1]) + a3.w * dot(q[2], q[2]) + a4.w * dot(q[3], q[3]);
+    if (sf <= kEpsPbd) return false;
+    s = term / sf;
+    return true;
+}
+
 // Physics/CudaPBD.cu:1212-1415 — slot `slot` of a VF contact (vertex A, face
 // B C D, weights w = (1, -b0, -b1, -b2)) or an EE contact (edges A B and C D,
 // weights w = (b0, b1, -b2, -b3)).

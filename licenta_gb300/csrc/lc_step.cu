@@ -53,15 +53,13 @@ __device__ __forceinline__ void block_partials(float (&v)[N], double *dst) {
     }
 }
 
-// Cloth totals of partials [k0, k0+N) over the cloth's vertex blocks, summed
-// in a fixed order by every block that needs them.
-template <int N>
-__device__ __forceinline__ void cloth_totals(const DevPtrs &d, int c, int k0, double (&out)[N]) {
-    __shared__ double red[N][kThreads / 32];
-    __shared__ double tot[N];
+// Cloth totals of the block partials [k0, k0+N), one block per cloth, summed
+// in a fixed order (deterministic) into d.damp[c*16 + k].
+__global__ void k_cloth_totals(DevPtrs d, int k0, int N) {
+    const int c = blockIdx.x;
     const int b0 = d.vb_first[c], b1 = d.vb_first[c + 1];
+    __shared__ double red[16][kThreads / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
     for (int k = 0; k < N; ++k) {
         double s = 0;
         for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) s += d.damp_part[(size_t)b * 16 + k0 + k];
@@ -73,11 +71,8 @@ __device__ __forceinline__ void cloth_totals(const DevPtrs &d, int c, int k0, do
     if (threadIdx.x < N) {
         double t = 0;
         for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[threadIdx.x][w];
-        tot[threadIdx.x] = t;
+        d.damp[(size_t)c * 16 + k0 + threadIdx.x] = t;
     }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < N; ++k) out[k] = tot[k];
 }
 
 // ApplyExternalForces (Physics/CudaPBD.cu:1992-2003), GlobalVelDamp (:1934-1941)
@@ -116,8 +111,7 @@ __global__ void k_external(DevPtrs d) {
 __global__ void k_damp_moments(DevPtrs d) {
     const int c = d.vblk_cloth[blockIdx.x];
     const ClothDev &cd = d.cloth[c];
-    double t[7];
-    cloth_totals<7>(d, c, 0, t);
+    const double *t = d.damp + (size_t)c * 16;
     const int i = d.vblk_start[blockIdx.x] + threadIdx.x;
     const bool valid = i < cd.v_off + cd.V;
     float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -139,8 +133,7 @@ __global__ void k_damp_moments(DevPtrs d) {
 __global__ void k_damp_apply(DevPtrs d) {
     const int c = d.vblk_cloth[blockIdx.x];
     const ClothDev &cd = d.cloth[c];
-    double a[16];
-    cloth_totals<16>(d, c, 0, a);
+    const double *a = d.damp + (size_t)c * 16;
     __shared__ float sh[9];
     if (threadIdx.x == 0) {
         const double ms = a[0];
@@ -445,7 +438,9 @@ void launch_wind(const DevPtrs &d, cudaStream_t st) { k_wind<<<nblk(d.C, 128), 1
 void launch_external(const DevPtrs &d, cudaStream_t st) {
     if (d.nvblk) {
         k_external<<<d.nvblk, kThreads, 0, st>>>(d);
+        k_cloth_totals<<<d.C, kThreads, 0, st>>>(d, 0, 7);
         k_damp_moments<<<d.nvblk, kThreads, 0, st>>>(d);
+        k_cloth_totals<<<d.C, kThreads, 0, st>>>(d, 7, 9);
         k_damp_apply<<<d.nvblk, kThreads, 0, st>>>(d);
     }
 }

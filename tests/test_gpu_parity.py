@@ -41,7 +41,7 @@ def run_parity(specs, steps, check_every=1, variant=0):
     return worst, contacts
 
 
-@pytest.mark.parametrize("variant", [1, 2], ids=["gather", "cluster"])
+@pytest.mark.parametrize("variant", [1, 2, 3], ids=["gather", "cluster", "scatter"])
 def test_small_cloth_parity_through_contacts(variant):
     worst, contacts = run_parity([scenes.small_cloth(seed=0)], steps=60, variant=variant)
     assert contacts > 0, "the run should reach self-contact"
@@ -64,7 +64,7 @@ def test_k30_batch_parity():
     run_parity([a, b], steps=20)
 
 
-@pytest.mark.parametrize("variant", [1, 2], ids=["gather", "cluster"])
+@pytest.mark.parametrize("variant", [1, 2, 3], ids=["gather", "cluster", "scatter"])
 def test_sphere_and_mesh_thickness_parity(variant):
     s = scenes.large_cloth(seed=2, n=40)
     run_parity([s], steps=40, check_every=3, variant=variant)
@@ -104,7 +104,7 @@ def test_graph_replay_equals_eager():
     e.close()
 
 
-@pytest.mark.parametrize("variant", [1, 2], ids=["gather", "cluster"])
+@pytest.mark.parametrize("variant", [1, 2, 3], ids=["gather", "cluster", "scatter"])
 def test_runs_are_bitwise_reproducible(variant):
     specs = scenes.batched_cloths(seed=4, count=3, n_min=10, n_max=48)
     out = []
@@ -138,7 +138,7 @@ def test_cluster_profile_reports_variant():
     b = ClothBatch(specs)
     b.step(2)
     p = b.profile(1)
-    assert p["solver_variant"] == 2 and p["cluster_size"] in (8, 16)
+    assert p["solver_variant"] == 3 and p["cluster_size"] in (8, 16)
     assert p["kernels_per_step"] > 10 and p["step_ms"] > 0
     b.close()
 
