@@ -264,6 +264,31 @@ lc_status lc_lbvh_pairs(lc_lbvh *h, uint32_t *out_pairs, uint64_t cap, uint64_t 
 lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream);
 lc_status lc_lbvh_destroy(lc_lbvh *h);
 
+/* ----- allocation-free LBVH query ---------------------------------------
+ * No counterpart in the reference.  The same query as lc_lbvh_create +
+ * lc_lbvh_build + lc_lbvh_pairs (+ lc_lbvh_sorted_ids), for callers that
+ * cannot allocate device memory: code under a custom allocator or a fixed
+ * memory pool, plugins in a process that owns the device memory, real-time
+ * loops where an allocation and its implicit synchronisation are not allowed.
+ * Every intermediate buffer lives in one scratch array built into the library
+ * (about 0.9 MB of device memory on each GPU that loads it, kept until the
+ * process exits), so sizes are limited to LC_LBVH_STATIC_MAX_TRIANGLES
+ * triangles and LC_LBVH_STATIC_MAX_CHUNK pairs per leaf; larger requests
+ * return LC_ERR_INVALID_ARG.  The caller passes the boxes (device memory,
+ * 3 * n floats each), the pair output (device memory, 2 * cap u32; pairs
+ * beyond cap are not written and the call returns
+ * LC_ERR_CAPACITY_OVERFLOW with the full number in *count), *count (host) and
+ * optionally the sorted triangle ids (device memory, n u32).  The first call
+ * on a device looks up the scratch address and should come before any stream
+ * capture.  All calls share the scratch array and keep nothing between calls
+ * that they rely on; calls that overlap on the GPU race and must be
+ * serialised by the caller.  The call waits for its stream. */
+#define LC_LBVH_STATIC_MAX_TRIANGLES 2048
+#define LC_LBVH_STATIC_MAX_CHUNK 64
+lc_status lc_lbvh_pairs_static(const float *tri_min, const float *tri_max, int32_t num_triangles,
+                               int32_t chunk_size, int32_t morton_mode, uint32_t *out_pairs, uint64_t cap,
+                               uint64_t *count, uint32_t *out_sorted_ids, void *stream);
+
 const char *lc_last_error_string(void);
 const char *lc_status_string(lc_status s);
 

@@ -104,6 +104,8 @@ SIGNATURES = {
     "lc_lbvh_pairs": (C.c_int, [VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
     "lc_lbvh_sorted_ids": (C.c_int, [VP, VP, VP]),
     "lc_lbvh_destroy": (C.c_int, [VP]),
+    "lc_lbvh_pairs_static": (C.c_int, [VP, VP, C.c_int32, C.c_int32, C.c_int32, VP, C.c_uint64,
+                                       C.POINTER(C.c_uint64), VP, VP]),
     "lc_last_error_string": (C.c_char_p, []),
     "lc_status_string": (C.c_char_p, [C.c_int]),
     "lc_morton3d": (C.c_uint64, [C.c_float, C.c_float, C.c_float, C.c_int32]),

@@ -61,6 +61,10 @@ static lc_status fail(lc_status s, const std::string &msg) {
     return s;
 }
 
+namespace lc {
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace lc
+
 #define LC_CUDA(call)                                                                               \
     do {                                                                                            \
         cudaError_t e_ = (call);                                                                    \
