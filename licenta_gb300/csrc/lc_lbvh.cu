@@ -404,8 +404,10 @@ __device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v
     }
     return -15.f;
 }
-// When only the second derivative root is in [0,1] the reference reads an
-// uninitialised slot; the found root is used instead (same as the oracle).
+// Physics/CudaCubicSolver.cu:5-124.  When only the second root of the
+// derivative lies in [0,1], the reference reads its unset first critical
+// point; its kernels, built and run, behave as if that read returned the
+// first root t1 (outside [0,1]), so [0, t1] is searched: the same here.
 __device__ int coplanarity_times(float3 x1, float3 x2, float3 x3, float3 x4, float3 v1, float3 v2, float3 v3,
                                  float3 v4, float times[8]) {
     const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
@@ -425,8 +427,9 @@ __device__ int coplanarity_times(float3 x1, float3 x2, float3 x3, float3 x4, flo
     int ne = 0;
     ends[ne++] = 0.f;
     if (disc >= kEpsCubic) {
-        if (between(t1, 0.f, 1.f)) ends[ne++] = t1;
-        if (between(t2, 0.f, 1.f)) ends[ne++] = t2;
+        const bool in1 = between(t1, 0.f, 1.f), in2 = between(t2, 0.f, 1.f);
+        if (in1 || in2) ends[ne++] = t1;
+        if (in1 && in2) ends[ne++] = t2;
     } else if (fabsf(disc) < kEpsCubic) {
         if (between(t1, 0.f, 1.f)) ends[ne++] = t1;
     }

@@ -162,8 +162,13 @@ __global__ void k_damp_apply(DevPtrs d) {
     const float3 dv = sub(add(vcm, cross(omega, r)), vel);
     vel = add(vel, mul(dv, cd.kdamp));
     d.v[i] = f4(vel, 0.f);
+    // ExplicitEuler (Physics/CudaPBD.cu:2005-2012), rounded after the product
+    // and after the sum as the restatement does (no fused multiply-add), so
+    // the predicted positions the collision stages see are reproducible.
     const float4 p = d.xp[i];
-    d.x[i] = f4(add(xyz(p), mul(vel, cd.dt)), x4.w);
+    const float dt = cd.dt;
+    d.x[i] = make_float4(__fadd_rn(p.x, __fmul_rn(vel.x, dt)), __fadd_rn(p.y, __fmul_rn(vel.y, dt)),
+                         __fadd_rn(p.z, __fmul_rn(vel.z, dt)), x4.w);
 }
 
 // UpdateVertexNormals (Physics/CudaDeformableUtils.cu:190-249) as a gather

@@ -6,15 +6,18 @@
 // bench.py can check the CUDA engine against it.  Nothing in the product
 // (licenta_gb300/) includes, links or calls it.
 //
-// Parity status: the integer and contact stages (Morton codes, sort order,
-// Karras topology, refit, traversal pairs, feature AABB cull, CCD contacts)
-// are PINNED against the reference's own kernels (Core/CudaUtils.cu,
-// Collision/CudaBVH.cu, Collision/CudaPrimitiveTests.cu,
-// Physics/CudaCubicSolver.cu, Collision/FeatureList.cu built unmodified for
-// sm_103a and run on a GB300; fixtures under tests/golden/).  The PBD solver
-// half (Physics/CudaPBD.cu) cannot be built outside the reference's Windows/GL
-// project, so the solver restatement is "parity unpinned" by the reference:
-// it is checked by FP64-vs-FP32 agreement and the invariants in tests/.
+// Parity status.  The collision stages (Morton codes, stable sort, Karras
+// topology, refit boxes and rightmost leaves, traversal pairs, candidate
+// generation, feature AABB cull, CCD contacts) are PINNED against the
+// reference's own kernels: oracle/ref_pin/build_ref.py compiles the
+// reference's CUDA sources for sm_103a, oracle/ref_pin/refchain.py runs its
+// collision chain on a GPU, and the outputs are committed as golden vectors
+// under tests/golden/ (generator: tests/golden/make_golden.py), which this
+// restatement reproduces bit for bit.  The pin settled two points where the
+// reference's source alone is ambiguous: its refit races (see refit()) and
+// its unset critical point reads as the first root (see critical_points()).
+// The PBD solver half is checked FP32 against FP64 (same scheme, teacher
+// forced); it is not pinned against the reference's solver kernels.
 //
 // The class is templated on the real type R.  R = float is the FP32 mirror:
 // the same operation order as the reference kernels (no FMA contraction, the
@@ -546,7 +549,13 @@ template <class R> class Cloth {
     }
 
     // Collision/CudaBVH.cu:128-149 — bottom-up union; the second arrival at a
-    // node proceeds.  rmll/rmlr: rightmost leaf node below each child.
+    // node proceeds.  rmll/rmlr: rightmost leaf node below each child.  The
+    // reference writes a node's box and rightmost leaf without a fence before
+    // the atomicExch that lets its parent proceed; run on a GB300 its refit
+    // reads stale children at a few nodes per build (boxes with zero
+    // components, rightmost leaf 0).  The restatement computes the race-free
+    // result, which is what the reference's formulas give whenever the reads
+    // see the finished children.
     void refit() {
         int T = tp.T, In = T - 1;
         rmll.assign(std::max(In, 0), 0);
@@ -630,8 +639,12 @@ template <class R> class Cloth {
         return R(-15);
     }
     // Physics/CudaCubicSolver.cu:69-124.  When only the second root lies in
-    // [0,1] the reference reads an uninitialised first slot; here the found
-    // root is used.
+    // [0,1], FindCoplanarityTimes reads critPoint1, which FindCriticalPoints
+    // left unset (Physics/CudaCubicSolver.cu:19-33).  The reference's kernels,
+    // built and run (tests/golden), behave as if that read returned the first
+    // root t1 although it lies outside [0,1]: the interval [0, t1] is then
+    // searched, which is how the reference reports contacts at small
+    // negative times.  The restatement does the same.
     static int critical_points(V x21, V x31, V x41, V v21, V v31, V v41, R out[2]) {
         V v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31), x21x31 = cross(x21, x31);
         R v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
@@ -645,8 +658,9 @@ template <class R> class Cloth {
         R t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
         int n = 0;
         if (disc >= R(kEpsCubic)) {
-            if (between(t1, R(0), R(1))) out[n++] = t1;
-            if (between(t2, R(0), R(1))) out[n++] = t2;
+            const bool in1 = between(t1, R(0), R(1)), in2 = between(t2, R(0), R(1));
+            if (in1 || in2) out[n++] = t1;
+            if (in1 && in2) out[n++] = t2;
         } else if (std::fabs(disc) < R(kEpsCubic)) {
             if (between(t1, R(0), R(1))) out[n++] = t1;
         }

@@ -1,0 +1,322 @@
+"""The reference's collision chain, run with the reference's own kernels.
+
+TEST INFRASTRUCTURE ONLY: generates the golden vectors that pin the oracle
+(tests/golden/make_golden.py).  Nothing in the engine imports this module.
+
+oracle/_ref/ref_kernels.cubin (built by oracle/ref_pin/build_ref.py from the
+reference's sources) is loaded through the CUDA driver API (ctypes on
+libcuda) and its kernels are launched in the order and with the launch
+shapes of the reference's host code:
+
+  FeatureList::UpdateFeatureAABBs       Collision/FeatureList.cu:57-70
+  DeformableUtils::UpdateTrianglesContinuous
+                                        Physics/CudaDeformableUtils.cu:107-118
+  DeformableUtils::SortMortons          Physics/CudaDeformableUtils.cu:346-349
+  CudaBVH::GenerateBVH2                 Collision/CudaBVH.cu:152-161
+  CudaBVH::ComputeTreeAABBs             Collision/CudaBVH.cu:115-126
+  CudaDeformableBody::CreateTriangleTests
+                                        Physics/CudaDeformableBody.cpp:497-521
+  DeformableUtils::CreateTriangleTests  Collision/CudaCollisionDetection.cu:6-51
+  DeformableUtils::CCDTriangleTests     Collision/CudaCollisionDetection.cu:223-283
+
+Two host-side steps stand in for the reference's CUB calls: the stable radix
+sort of (Morton code, triangle) pairs (Core/CubWrappers.cuh:141-156) is a
+stable host sort of the same keys, whose result is unique, and
+cub::DeviceSelect::Flagged (Core/CubWrappers.cuh:84-88) is an order-preserving
+host compaction.  Device buffers are torch tensors; launches go to torch's
+current stream in torch's (primary) context.
+
+Before each kernel whose memory accesses depend on data, the inputs are
+checked on the host so that every access stays in bounds: the triangle
+indices, no run of three equal Morton codes (there the reference's parents[]
+has a write race and may leave a node without a parent, which its refit
+would then follow; the two triangles of a grid quad share a box and so a
+code, which its tie-break handles), a complete hierarchy in which every node
+has exactly one parent, and a depth well inside the traversal's 64-entry
+stack (Collision/CudaBVH.cu:38).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import gzip
+from pathlib import Path
+
+import numpy as np
+
+CUBIN = Path(__file__).resolve().parent.parent / "_ref" / "ref_kernels.cubin"
+THREADS = 256  # CudaUtils::THREADS_PER_BLOCK (Core/CudaUtils.cuh:87)
+MAX_DEPTH = 56
+
+# kernel key -> unqualified name in the reference
+KERNELS = {
+    "particle_aabbs": "UpdateParticleAABBs",
+    "edge_aabbs": "UpdateEdgeAABBs",
+    "tri_update": "_UpdateTrianglesContinuous",
+    "gen_bvh": "_GenerateBVH2",
+    "refit": "ComputeTreeAABBs",
+    "traverse": "_GetAABBCollisions",
+    "tri_tests": "CreateTriangleTests",
+    "feature_aabb": "FeatureAABBTests",
+    "ccd": "CCDTriangleTests",
+}
+
+
+class _Driver:
+    def __init__(self):
+        self.cu = C.CDLL("libcuda.so.1")
+        P = C.c_void_p
+        sig = {
+            "cuCtxGetCurrent": [C.POINTER(P)],
+            "cuModuleLoadData": [C.POINTER(P), P],
+            "cuModuleGetFunctionCount": [C.POINTER(C.c_uint), P],
+            "cuModuleEnumerateFunctions": [C.POINTER(P), C.c_uint, P],
+            "cuFuncGetName": [C.POINTER(C.c_char_p), P],
+            "cuLaunchKernel": [P, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, P,
+                               C.POINTER(P), C.POINTER(P)],
+            "cuModuleUnload": [P],
+        }
+        for name, args in sig.items():
+            f = getattr(self.cu, name)
+            f.argtypes = args
+            f.restype = C.c_int
+
+    def __call__(self, name, *args):
+        rc = getattr(self.cu, name)(*args)
+        if rc != 0:
+            raise RuntimeError(f"{name} failed with CUresult {rc}")
+
+
+class RefKernels:
+    """The reference kernels of the collision chain, loaded from the cubin."""
+
+    def __init__(self, cubin: Path = CUBIN):
+        import torch
+        gz = Path(str(cubin) + ".gz")
+        if cubin.exists():
+            image = cubin.read_bytes()
+        elif gz.exists():
+            image = gzip.decompress(gz.read_bytes())
+        else:
+            raise FileNotFoundError(f"{cubin} is missing: run python -m oracle.ref_pin.build_ref")
+        torch.cuda.init()
+        torch.empty(1, device="cuda")  # make torch's primary context current
+        self.torch = torch
+        self.drv = _Driver()
+        ctx = C.c_void_p()
+        self.drv("cuCtxGetCurrent", C.byref(ctx))
+        if not ctx.value:
+            raise RuntimeError("no current CUDA context")
+        self._image = C.create_string_buffer(image)
+        self.mod = C.c_void_p()
+        self.drv("cuModuleLoadData", C.byref(self.mod), C.cast(self._image, C.c_void_p))
+        n = C.c_uint()
+        self.drv("cuModuleGetFunctionCount", C.byref(n), self.mod)
+        funcs = (C.c_void_p * n.value)()
+        self.drv("cuModuleEnumerateFunctions", funcs, n.value, self.mod)
+        names = {}
+        for f in funcs:
+            s = C.c_char_p()
+            self.drv("cuFuncGetName", C.byref(s), f)
+            names[s.value.decode()] = f
+        self.names = sorted(names)
+        self.fn = {}
+        for key, ident in KERNELS.items():
+            tag = f"{len(ident)}{ident}"  # the identifier as it appears in a mangled name
+            hits = [m for m in names if tag in m]
+            if len(hits) != 1:
+                raise RuntimeError(f"kernel {ident}: {len(hits)} matches in the cubin: {hits}")
+            self.fn[key] = names[hits[0]]
+
+    def launch(self, key: str, n_threads: int, *args) -> None:
+        if n_threads <= 0:
+            return
+        vals = []
+        for a in args:
+            if isinstance(a, C._SimpleCData):
+                vals.append(a)
+            elif hasattr(a, "data_ptr"):
+                vals.append(C.c_void_p(a.data_ptr()))
+            elif a is None:
+                vals.append(C.c_void_p(0))
+            else:
+                raise TypeError(f"argument {a!r}: pass a ctypes scalar, a tensor or None")
+        params = (C.c_void_p * len(vals))(*[C.cast(C.pointer(v), C.c_void_p) for v in vals])
+        stream = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        blocks = (n_threads + THREADS - 1) // THREADS
+        self.drv("cuLaunchKernel", self.fn[key], blocks, 1, 1, THREADS, 1, 1, 0, stream, params, None)
+
+    # ------------------------------------------------------------------
+    def collide(self, x, x_prev, v, triangles, features, thickness: float, dt: float, chunk: int = 64,
+                prefill: dict | None = None) -> dict:
+        """One pass of the reference's collision stages.
+
+        x, x_prev, v: (V, 3) float32 predicted positions, previous positions
+        and velocities; triangles: (T, 3) vertex ids in the current slot
+        order; features: (T,) feature bytes of those triangles.  Returns the
+        sorted Morton codes, the sort order (new slot -> old slot), the
+        hierarchy, node boxes, rightmost leaves, broadphase pairs and the
+        compacted VF / EE contacts.
+
+        ComputeTreeAABBs (Collision/CudaBVH.cu:128-149) releases a parent with
+        atomicExch but writes the child's box and rightmost leaf without a
+        fence, so the second arrival at a node can read a child's box before
+        it is visible (stale zeros, or a float3 half written).  ``prefill``
+        (internal-node boxes ``node_min`` / ``node_max`` of shape (2T-1, 3)
+        and ``rmll`` / ``rmlr`` of shape (T-1,)) seeds the internal entries
+        before the refit runs: the kernel still computes and writes every
+        internal node, but a read that races now returns the seeded value.
+        Seeded with the restatement's values, an output node equal to the
+        seed shows that the reference's formula, applied to children that
+        already agree, gives the same value (induction from the leaves,
+        which the refit never writes).
+        """
+        torch = self.torch
+        f32, i32 = np.float32, np.int32
+        x = np.ascontiguousarray(x, f32)
+        xp = np.ascontiguousarray(x_prev, f32)
+        vel = np.ascontiguousarray(v, f32)
+        tris = np.ascontiguousarray(triangles, np.int64)
+        V, T = x.shape[0], tris.shape[0]
+        if T < 2 or V < 3 or V > 8192:
+            raise ValueError("need 2 <= T and 3 <= V <= 8192")
+        if tris.min() < 0 or tris.max() >= V:
+            raise ValueError("triangle index out of range")
+        chunk = min(chunk, T)  # Physics/CudaDeformableBody.cpp:233
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        h = C.c_float(thickness)
+
+        # Collision/FeatureList.cu:12-55 — unique edges and the V x V edge map.
+        emap = np.full(V * V, -1, dtype=i32)
+        e1, e2 = [], []
+        for t in range(T):
+            for j in range(3):
+                a, b = int(tris[t, j]), int(tris[t, (j + 1) % 3])
+                lo, hi = min(a, b), max(a, b)
+                if emap[lo * V + hi] == -1:
+                    emap[lo * V + hi] = len(e1)
+                    e1.append(lo)
+                    e2.append(hi)
+        E = len(e1)
+        d_x, d_xp, d_v = dev(x), dev(xp), dev(vel)
+        d_emap, d_e1, d_e2 = dev(emap), dev(np.array(e1, i32)), dev(np.array(e2, i32))
+        pmin = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        pmax = torch.zeros_like(pmin)
+        emin = torch.zeros((E, 3), dtype=torch.float32, device="cuda")
+        emax = torch.zeros_like(emin)
+        self.launch("particle_aabbs", V, C.c_int(V), d_x, d_xp, h, pmin, pmax)
+        self.launch("edge_aabbs", E, C.c_int(E), pmin, pmax, d_e1, d_e2, h, emin, emax)
+
+        # Physics/Structs.h:176-188 — CudaTriangle {int v1, v2, v3; char
+        # features; float3 normal} = 28 bytes, as 7 int32 words.
+        tri = np.zeros((T, 7), dtype=i32)
+        tri[:, :3] = tris
+        tri[:, 3] = np.asarray(features, np.uint8).astype(i32)
+        d_tri = dev(tri)
+        nodes = 2 * T - 1
+        mort = torch.zeros(T, dtype=torch.int64, device="cuda")
+        nmin = torch.zeros((nodes, 3), dtype=torch.float32, device="cuda")
+        nmax = torch.zeros_like(nmin)
+        self.launch("tri_update", T, C.c_int(T), d_x, d_xp, d_tri, mort, nmin, nmax, h)
+        torch.cuda.synchronize()
+
+        # Stable sort of the codes with the triangle payload; the boxes stay.
+        keys = mort.cpu().numpy().view(np.uint64)
+        order = np.argsort(keys, kind="stable")
+        skeys = keys[order]
+        if skeys.size > 2 and np.any((skeys[2:] == skeys[1:-1]) & (skeys[1:-1] == skeys[:-2])):
+            raise ValueError("three equal Morton codes in a row: the reference hierarchy would race")
+        tri_sorted = d_tri.cpu().numpy()[order]  # the payload carries the new face normals
+        d_tri = dev(tri_sorted)
+        d_keys = dev(skeys.view(np.int64))
+
+        In = T - 1
+        lefts = torch.zeros(In, dtype=torch.int32, device="cuda")
+        rights = torch.zeros_like(lefts)
+        parents = torch.zeros(nodes, dtype=torch.int32, device="cuda")
+        visited = torch.zeros(In, dtype=torch.int32, device="cuda")
+        self.launch("gen_bvh", In, C.c_int(In), d_keys, lefts, rights, parents, visited)
+        torch.cuda.synchronize()
+        L, R, Pa = lefts.cpu().numpy(), rights.cpu().numpy(), parents.cpu().numpy()
+        depth = _check_tree(L, R, Pa, T)
+        if depth > MAX_DEPTH:
+            raise ValueError(f"hierarchy depth {depth} too close to the 64-entry traversal stack")
+
+        rmll = torch.zeros(In, dtype=torch.int32, device="cuda")
+        rmlr = torch.zeros_like(rmll)
+        if prefill is not None:
+            nmin[:In] = torch.from_numpy(np.ascontiguousarray(prefill["node_min"][:In], f32)).cuda()
+            nmax[:In] = torch.from_numpy(np.ascontiguousarray(prefill["node_max"][:In], f32)).cuda()
+            rmll.copy_(torch.from_numpy(np.ascontiguousarray(prefill["rmll"], i32)))
+            rmlr.copy_(torch.from_numpy(np.ascontiguousarray(prefill["rmlr"], i32)))
+        self.launch("refit", T, C.c_int(T), lefts, rights, parents, visited, nmin, nmax, rmll, rmlr)
+
+        cols = torch.zeros((T * chunk, 2), dtype=torch.int32, device="cuda")
+        flags = torch.zeros(T * chunk, dtype=torch.uint8, device="cuda")
+        self.launch("traverse", T, C.c_int(T), lefts, rights, nmin, nmax, rmll, rmlr, cols, flags,
+                    C.c_int(chunk), C.c_uint64(1))
+        torch.cuda.synchronize()
+        pairs = cols[flags.bool()].contiguous()
+        P = pairs.shape[0]
+        if P and (int(pairs.min()) < 0 or int(pairs.max()) >= T):
+            raise RuntimeError("pair index out of range")
+
+        out = dict(morton=skeys, order=order.astype(i32), lefts=L, rights=R, parents=Pa,
+                   node_min=nmin.cpu().numpy(), node_max=nmax.cpu().numpy(),
+                   rmll=rmll.cpu().numpy(), rmlr=rmlr.cpu().numpy(), pairs=pairs.cpu().numpy())
+        if P == 0:
+            out["vf"] = out["ee"] = np.zeros((0, 12), i32)
+            return out
+
+        # PrimitiveContact {int v1..v4; float w1..w4, t; float3 n} = 12 words.
+        vf = torch.zeros((6 * P, 12), dtype=torch.int32, device="cuda")
+        ee = torch.zeros((9 * P, 12), dtype=torch.int32, device="cuda")
+        vff = torch.ones(6 * P, dtype=torch.uint8, device="cuda")
+        eef = torch.ones(9 * P, dtype=torch.uint8, device="cuda")
+        self.launch("tri_tests", P, C.c_int(P), d_tri, pairs, vf, vff, ee, eef)
+        self.launch("feature_aabb", 15 * P, C.c_int(V), pmin, pmax, d_emap, d_e1, d_e2, emin, emax, None, None, None,
+                    vf, vff, C.c_uint64(6 * P), ee, eef, C.c_uint64(9 * P))
+        torch.cuda.synchronize()
+        vf = vf[vff.bool()].contiguous()
+        ee = ee[eef.bool()].contiguous()
+        for c in (vf, ee):
+            if c.shape[0] and (int(c[:, :4].min()) < 0 or int(c[:, :4].max()) >= V):
+                raise RuntimeError("candidate vertex out of range")
+        nvf, nee = vf.shape[0], ee.shape[0]
+        vff = torch.zeros(max(nvf, 1), dtype=torch.uint8, device="cuda")
+        eef = torch.zeros(max(nee, 1), dtype=torch.uint8, device="cuda")
+        self.launch("ccd", nvf + nee, d_tri, d_xp, d_v, vf, vff, C.c_uint64(nvf), ee, eef, C.c_uint64(nee),
+                    h, C.c_float(dt))
+        torch.cuda.synchronize()
+        out["vf"] = vf[vff[:nvf].bool()].cpu().numpy()
+        out["ee"] = ee[eef[:nee].bool()].cpu().numpy()
+        return out
+
+
+def _check_tree(L, R, Pa, T) -> int:
+    """Every node below the root has its parent; returns the depth."""
+    In = T - 1
+    nodes = 2 * T - 1
+    if L.min() < 0 or R.min() < 0 or L.max() >= nodes or R.max() >= nodes:
+        raise ValueError("child index out of range")
+    seen = np.zeros(nodes, dtype=np.int32)
+    depth = np.zeros(nodes, dtype=np.int32)
+    stack = [0]
+    while stack:
+        n = stack.pop()
+        seen[n] += 1
+        if n < In:
+            for c in (int(L[n]), int(R[n])):
+                if Pa[c] != n:
+                    raise ValueError("parent link missing")
+                depth[c] = depth[n] + 1
+                stack.append(c)
+    if not np.all(seen == 1):
+        raise ValueError("hierarchy does not reach every node exactly once")
+    return int(depth.max())
+
+
+def contact_fields(c: np.ndarray):
+    """(ids (n,4) int32, weights (n,4) float32, t (n,) float32, normal (n,3))."""
+    c = np.ascontiguousarray(c, np.int32)
+    f = c.view(np.float32)
+    return c[:, :4].copy(), f[:, 4:8].copy(), f[:, 8].copy(), f[:, 9:12].copy()

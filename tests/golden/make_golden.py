@@ -1,0 +1,78 @@
+"""Generate the golden vectors of the collision stages from the reference's
+own kernels.
+
+Runs on a machine with a GPU, after ``python -m oracle.ref_pin.build_ref``
+has built oracle/_ref/ref_kernels.cubin from the reference checkout and
+``__graft_entry__.build()`` has built the engine and the oracle:
+
+    python tests/golden/make_golden.py OUTDIR
+
+Each case steps a seeded cloth with the FP32 oracle to a chosen step, takes
+the state the collision stages see at the next step (predicted positions,
+previous positions, velocities, the triangle order before the Morton sort)
+and runs the reference's collision chain on it (oracle/ref_pin/refchain.py).
+The inputs and the reference's outputs go to OUTDIR/<case>.npz; the tests
+hold the oracle (tests/test_golden_cpu.py) and the engine
+(tests/test_golden_gpu.py) to them bit for bit.  The script also prints how
+the FP32 oracle compares, so a run shows at once whether the pin holds.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "tests"))
+
+import golden_cases  # noqa: E402
+from oracle.oracle_ffi import Oracle  # noqa: E402
+from oracle.ref_pin.refchain import RefKernels  # noqa: E402
+
+
+def main(outdir: str) -> int:
+    out = Path(outdir)
+    out.mkdir(parents=True, exist_ok=True)
+    ref = RefKernels()
+    bad = 0
+    for case in golden_cases.CASES:
+        spec = golden_cases.make_spec(case)
+        o = Oracle([spec], fp64=False)
+        if case["steps"]:
+            o.step(case["steps"], threads=1)
+        o.step_one(0)
+        x, xp, v = o.debug(0, "PRED_X"), o.debug(0, "PRED_XPREV"), o.debug(0, "PRED_V")
+        perm = o.debug(0, "PERM_BEFORE").astype(np.int64)
+        feats = o.debug(0, "FEATURES")
+        h = o.thickness(0)
+        dt = float(spec.params.timestep)
+        chunk = int(spec.params.BVHChunkSize)
+        tris = spec.indices.astype(np.int64)[perm]
+        data = dict(x=x, x_prev=xp, v=v, perm_before=perm.astype(np.int32), features=feats,
+                    thickness=np.float32(h), dt=np.float32(dt), chunk=np.int32(chunk),
+                    meta=np.array(json.dumps(case)))
+        # As the reference runs: its refit may read a child before the
+        # child's box is visible (kept as evidence, not compared).
+        raw = ref.collide(x, xp, v, tris, feats[perm], h, dt, chunk)
+        data.update({"raw_" + k: raw[k] for k in ("node_min", "node_max", "rmll", "rmlr", "pairs")})
+        # With the internal nodes seeded so that a racing read is harmless.
+        r = ref.collide(x, xp, v, tris, feats[perm], h, dt, chunk, prefill=golden_cases.oracle_refit(spec, data))
+        data.update({"ref_" + k: val for k, val in r.items()})
+        raced = int(np.sum(np.any(raw["node_min"] != r["node_min"], axis=1) | np.any(raw["node_max"] != r["node_max"],
+                                                                                        axis=1)))
+        np.savez_compressed(out / f"{case['name']}.npz", **data)
+        o.close()
+        # how the FP32 oracle compares on the same inputs
+        diffs = golden_cases.compare_oracle(spec, data)
+        print(f"{case['name']}: T={len(perm)} pairs={len(r['pairs'])} vf={len(r['vf'])} ee={len(r['ee'])} "
+              f"nodes raced in the unseeded refit={raced} "
+              f"oracle {'agrees' if not diffs else 'DIFFERS: ' + ', '.join(diffs)}")
+        bad += bool(diffs)
+    return 1 if bad else 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else str(Path(__file__).resolve().parent)))
