@@ -108,15 +108,16 @@ typedef struct lc_cloth_desc {
 
 /* Capacities of the per-step device buffers; 0 picks the default. */
 typedef struct lc_batch_options {
-    uint64_t vf_capacity;     /* VF contacts kept per step over the whole batch (default 8 * total triangles) */
-    uint64_t ee_capacity;     /* EE contacts kept per step (default 8 * total triangles) */
+    uint64_t vf_capacity;     /* VF contacts kept per step over the whole batch (default max(8 * total triangles, 4096)) */
+    uint64_t ee_capacity;     /* EE contacts kept per step (default max(8 * total triangles, 4096)) */
     int32_t use_graph;        /* 1 (default): capture one step in a CUDA graph and replay it */
     int32_t debug_capture;    /* 1: keep intermediate buffers of the last step for lc_batch_debug_get */
     int32_t solver_variant;   /* 0 = auto (cluster scatter when every cloth fits on chip, else 1),
                                  1 = per-vertex gather over global memory, 2 = cluster on-chip gather,
                                  3 = cluster on-chip scatter with fixed-point accumulators */
     int32_t block_size;       /* block size of the global-memory Jacobi kernel (0 = default) */
-    uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull (default 8 * total triangles) */
+    uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull, per kind (VF, EE);
+                                 default min(15 * pair capacity, max(32 * total triangles, 4 Mi)) */
 } lc_batch_options;
 
 typedef struct lc_batch lc_batch;

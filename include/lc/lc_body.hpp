@@ -1,0 +1,109 @@
+/* lc_body.hpp — Physics::CudaDeformableBody on the licenta_gb300 engine, for
+ * C++ hosts.
+ *
+ * A header-only adapter over the C ABI of lc.h with the reference body's
+ * constructor arguments and methods (Physics/CudaDeformableBody.h:23-28):
+ *
+ *   CudaDeformableBody(std::vector<VertexT> *verts, std::vector<unsigned> *indices,
+ *                      const lc_cloth_params params, std::vector<bool> &fixedVerts)
+ *   FixedUpdate()  — one cloth step (Physics/CudaDeformableBody.cpp:550-627)
+ *   Update()       — publishes the positions into *verts
+ *                    (Physics/CudaDeformableBody.cpp:629-638, 473-495)
+ *   SetSpherePos(pos, radius)   (Physics/CudaDeformableBody.cpp:640-643)
+ *
+ * VertexT is any vertex record with a `m_position` member that has float x,
+ * y, z fields — Rendering::VertexFormat (glm::vec3 m_position) qualifies.
+ * As in the reference, the caller owns *verts and *indices and the body keeps
+ * the pointer to *verts, writing the published positions (the previous
+ * positions after the step, as the reference's FinalVertUpdate does) back
+ * into it on Update().  Errors throw lc::Error with the engine's message
+ * (the reference exits the process instead).
+ *
+ * The body steps on the default stream and waits for the step in Update();
+ * several bodies are better stepped together through lc_batch_* directly.
+ */
+#pragma once
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lc.h"
+
+namespace lc {
+
+struct Error : std::runtime_error {
+    lc_status status;
+    Error(lc_status s, const std::string &where)
+        : std::runtime_error(where + ": " + lc_status_string(s) + " (" + lc_last_error_string() + ")"), status(s) {}
+};
+
+inline void check(lc_status s, const char *where) {
+    if (s != LC_OK) throw Error(s, where);
+}
+
+template <class VertexT>
+class CudaDeformableBody {
+public:
+    CudaDeformableBody(std::vector<VertexT> *verts, std::vector<unsigned int> *indices, const lc_cloth_params params,
+                       std::vector<bool> &fixedVerts)
+        : m_verts(verts) {
+        if (!verts || !indices || indices->size() % 3 != 0 || fixedVerts.size() != verts->size())
+            throw std::invalid_argument("CudaDeformableBody: inconsistent vertices / indices / fixedVerts");
+        const size_t V = verts->size();
+        std::vector<float> pos(3 * V);
+        for (size_t i = 0; i < V; ++i) {
+            pos[3 * i] = (*verts)[i].m_position.x;
+            pos[3 * i + 1] = (*verts)[i].m_position.y;
+            pos[3 * i + 2] = (*verts)[i].m_position.z;
+        }
+        std::vector<uint8_t> pinned(V);
+        for (size_t i = 0; i < V; ++i) pinned[i] = fixedVerts[i] ? 1 : 0;
+        lc_cloth_desc d;
+        d.num_vertices = (int32_t)V;
+        d.num_triangles = (int32_t)(indices->size() / 3);
+        d.positions = pos.data();
+        d.indices = reinterpret_cast<const uint32_t *>(indices->data());
+        d.pinned = pinned.data();
+        d.params = params;
+        lc_batch_options o;
+        lc_default_options(&o);
+        check(lc_batch_create(&d, 1, &o, &m_batch), "lc_batch_create");
+        m_published.resize(3 * V);
+    }
+
+    CudaDeformableBody(const CudaDeformableBody &) = delete;
+    CudaDeformableBody &operator=(const CudaDeformableBody &) = delete;
+
+    virtual ~CudaDeformableBody() {
+        if (m_batch) lc_batch_destroy(m_batch);
+    }
+
+    virtual void FixedUpdate() { check(lc_batch_step(m_batch, 1, nullptr), "lc_batch_step"); }
+
+    virtual void Update() {
+        check(lc_batch_sync(m_batch), "lc_batch_sync");
+        check(lc_batch_read_positions(m_batch, m_published.data(), 1, nullptr), "lc_batch_read_positions");
+        check(lc_batch_sync(m_batch), "lc_batch_sync");
+        for (size_t i = 0; i < m_verts->size(); ++i) {
+            (*m_verts)[i].m_position.x = m_published[3 * i];
+            (*m_verts)[i].m_position.y = m_published[3 * i + 1];
+            (*m_verts)[i].m_position.z = m_published[3 * i + 2];
+        }
+    }
+
+    template <class Vec3>
+    void SetSpherePos(const Vec3 &pos, float radius) {
+        const float p[3] = {pos.x, pos.y, pos.z};
+        check(lc_batch_set_sphere(m_batch, 0, p, radius), "lc_batch_set_sphere");
+    }
+
+    lc_batch *batch() { return m_batch; }
+
+private:
+    std::vector<VertexT> *m_verts;
+    lc_batch *m_batch = nullptr;
+    std::vector<float> m_published;
+};
+
+}  // namespace lc
