@@ -349,6 +349,22 @@ template <class R> class Cloth {
         std::vector<int8_t> sphere; // V
     } forced;
 
+    // What one step decided and the intermediate states its adjoint needs
+    // (filled while `recording`; see backward()).
+    struct Record {
+        std::vector<Contact> vf, ee;
+        std::vector<u8> ground;      // V
+        std::vector<u32> ground_it;  // V
+        std::vector<u8> lra;         // V*F
+        std::vector<u8> dyn;         // iterations x 4*(vf+ee)
+        std::vector<V> x_in, v_b;    // damping inputs: state x, velocity after the global damping
+        std::vector<std::vector<V>> xk;  // solver iterates x^0 .. x^K
+        double M = 0, xcm[3] = {0, 0, 0}, vcm[3] = {0, 0, 0}, om[3] = {0, 0, 0}, I[3][3] = {};
+    };
+    bool recording = false;
+    Record rec;
+    std::vector<Record> records;  // one per recorded step of a rollout
+
     void init(const lc_cloth_desc &d) {
         prm = d.params;
         build_topology(d, tp);
@@ -418,6 +434,7 @@ template <class R> class Cloth {
         // DampVelocities, Physics/CudaPBD.cu:411-458 with kernels :1934-1990.
         R kg = R(prm.globalVelDamp);
         for (int i = 0; i < Vn; ++i) v[i] = v[i] * (R(1) - kg);
+        if (recording) { rec.x_in = x; rec.v_b = v; }
         // Reductions in double (the reference reduces float3s with CUB).
         double msum = 0, xm[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
         for (int i = 0; i < Vn; ++i) {
@@ -441,6 +458,13 @@ template <class R> class Cloth {
         double I[3][3] = {{i1[1] + i1[2], i2[0], i2[1]}, {i2[0], i1[0] + i1[2], i2[2]}, {i2[1], i2[2], i1[0] + i1[1]}};
         double om[3];
         solve3(I, L, om);
+        if (recording) {
+            rec.M = msum;
+            for (int k = 0; k < 3; ++k) {
+                rec.xcm[k] = xm[k] / msum; rec.vcm[k] = vm[k] / msum; rec.om[k] = om[k];
+                for (int l = 0; l < 3; ++l) rec.I[k][l] = I[k][l];
+            }
+        }
         V omega = mk<R>(R(om[0]), R(om[1]), R(om[2]));
         R kd = R(prm.kDamp);
         for (int i = 0; i < Vn; ++i) {
@@ -891,6 +915,13 @@ template <class R> class Cloth {
         std::vector<V> corr_dyn((nvf + nee) * 4);
         std::vector<V> acc(Vn);
         std::vector<int> cnt(Vn);
+        if (recording) {
+            rec.vf = cvf; rec.ee = cee;
+            rec.ground = gflag; rec.lra = lflag;
+            rec.ground_it.assign(Vn, 0u);
+            rec.dyn.assign((size_t)prm.solverIterations * corr_dyn.size(), 0);
+            rec.xk.assign(1, x);
+        }
         for (int it = 0; it < prm.solverIterations; ++it) {
             for (int i = 0; i < Vn; ++i) { acc[i] = mk<R>(0, 0, 0); cnt[i] = 0; }
             // ground, Physics/CudaPBD.cu:1594-1629
@@ -898,7 +929,11 @@ template <class R> class Cloth {
                 if (gflag[i]) {
                     R cv = dot(x[i] - qc[i], nc[i]);
                     bool take = forced.on ? ((forced.ground_it[i] >> it) & 1u) != 0 : cv < R(0);
-                    if (take) { acc[i] = acc[i] + (-cv) * nc[i]; cnt[i] += 1; }
+                    if (take) {
+                        acc[i] = acc[i] + (-cv) * nc[i];
+                        cnt[i] += 1;
+                        if (recording) rec.ground_it[i] |= 1u << it;
+                    }
                 }
             // LRA, Physics/CudaPBD.cu:1656-1688
             for (int i = 0; i < Vn; ++i) {
@@ -934,13 +969,18 @@ template <class R> class Cloth {
                 int c = 0;
                 for (u32 e : dyn[i]) {
                     bool take = forced.on ? forced.dyn[(size_t)it * corr_dyn.size() + e] != 0 : !is_zero(corr_dyn[e]);
-                    if (take) { a = a + corr_dyn[e]; ++c; }
+                    if (take) {
+                        a = a + corr_dyn[e];
+                        ++c;
+                        if (recording) rec.dyn[(size_t)it * corr_dyn.size() + e] = 1;
+                    }
                 }
                 acc[i] = acc[i] + a;
                 cnt[i] += c;
             }
             // Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
             for (int i = 0; i < Vn; ++i) x[i] = x[i] + acc[i] / R(cnt[i]);
+            if (recording) rec.xk.push_back(x);
         }
     }
 
@@ -1094,6 +1134,248 @@ template <class R> class Cloth {
                       std::fmin(std::fmax(x[i].y, R(prm.worldMin[1])), R(prm.worldMax[1])),
                       std::fmin(std::fmax(x[i].z, R(prm.worldMin[2])), R(prm.worldMax[2])));
         }
+    }
+
+    // ---- adjoint of one step ------------------------------------------------
+    // f(d) = (|d| - l0) d/|d| and its (symmetric) Jacobian applied to g: the
+    // shape shared by the stretch, LRA and contact corrections.
+    static V f_jac(V d, R l, R l0, V g) {
+        V n = d / l;
+        return g - (l0 / l) * (g - dot(n, g) * n);
+    }
+
+    // Reverse of the bend correction (Physics/CudaPBD.cu:1024-1147), written on
+    // the algebraically identical stable form: given the incoming gradients
+    // ub[j] of the four corrections, returns the gradients of p2, p3, p4 (the
+    // correction does not depend on p1) and of kp.
+    static void bend_vjp(V p2, V p3, V p4, const R w[4], R kp, R gap, const V ub[4], V &g2, V &g3, V &g4,
+                         R &gkp) {
+        g2 = g3 = g4 = mk<R>(0, 0, 0);
+        gkp = R(0);
+        V c23 = cross(p2, p3), c24 = cross(p2, p4);
+        R l23 = len(c23), l24 = len(c24);
+        if (l23 <= R(kEpsPbd) || l24 <= R(kEpsPbd)) return;
+        V n1 = c23 / l23, n2 = c24 / l24;
+        V sv = n1 + n2, tv = n1 - n2;
+        R ss = dot(sv, sv), tt = dot(tv, tv);
+        if (ss == R(0)) return;
+        R A = std::sqrt(ss), Bq = std::sqrt(tt);
+        R dphi = gap - R(2) * std::atan2(A, Bq);
+        R P = ss * tt / R(4), Rt = std::sqrt(P);
+        R term = Rt * dphi * kp;
+        R opd = ss / R(2);
+        V u = sv - n1 * opd, wv = sv - n2 * opd;
+        V a3 = cross(p2, u), a4 = cross(p2, wv), b3 = cross(p3, u), b4 = cross(p4, wv);
+        V q[4];
+        q[2] = a3 / l23;
+        q[3] = a4 / l24;
+        q[1] = -(b3 / l23 + b4 / l24);
+        q[0] = -q[1] - q[2] - q[3];
+        R sf = w[0] * dot(q[0], q[0]) + w[1] * dot(q[1], q[1]) + w[2] * dot(q[2], q[2]) + w[3] * dot(q[3], q[3]);
+        if (sf <= R(kEpsPbd)) return;
+        R sc = term / sf;
+        // corr_j = -w_j sc q_j
+        R gsc = 0;
+        V gq[4];
+        for (int j = 0; j < 4; ++j) { gsc += -w[j] * dot(q[j], ub[j]); gq[j] = ub[j] * (-w[j] * sc); }
+        R gterm = gsc / sf, gsf = -gsc * sc / sf;
+        for (int j = 0; j < 4; ++j) gq[j] = gq[j] + q[j] * (R(2) * w[j] * gsf);
+        gq[1] = gq[1] - gq[0]; gq[2] = gq[2] - gq[0]; gq[3] = gq[3] - gq[0];
+        V gb3 = -gq[1] / l23, gb4 = -gq[1] / l24;
+        R gl23 = dot(gq[1], b3) / (l23 * l23) - dot(gq[2], a3) / (l23 * l23);
+        R gl24 = dot(gq[1], b4) / (l24 * l24) - dot(gq[3], a4) / (l24 * l24);
+        V ga3 = gq[2] / l23, ga4 = gq[3] / l24;
+        V gu = mk<R>(0, 0, 0), gw = mk<R>(0, 0, 0);
+        g2 = g2 + cross(u, ga3); gu = gu + cross(ga3, p2);
+        g2 = g2 + cross(wv, ga4); gw = gw + cross(ga4, p2);
+        g3 = g3 + cross(u, gb3); gu = gu + cross(gb3, p3);
+        g4 = g4 + cross(wv, gb4); gw = gw + cross(gb4, p4);
+        V gsv = gu + gw, gn1 = -gu * opd, gn2 = -gw * opd;
+        R gss = -(dot(gu, n1) + dot(gw, n2)) / R(2), gtt = 0;
+        R gRt = gterm * dphi * kp, gdphi = gterm * Rt * kp;
+        gkp = gterm * Rt * dphi;
+        if (Rt > R(0)) { R gP = gRt / (R(2) * Rt); gss += gP * tt / R(4); gtt += gP * ss / R(4); }
+        R den = ss + tt;
+        R gA = R(-2) * Bq / den * gdphi, gB = R(2) * A / den * gdphi;
+        gss += gA / (R(2) * A);
+        if (Bq > R(0)) gtt += gB / (R(2) * Bq);
+        gsv = gsv + sv * (R(2) * gss);
+        V gtv = tv * (R(2) * gtt);
+        gn1 = gn1 + gsv + gtv; gn2 = gn2 + gsv - gtv;
+        V gc23 = gn1 / l23 + n1 * (gl23 - dot(gn1, c23) / (l23 * l23));
+        V gc24 = gn2 / l24 + n2 * (gl24 - dot(gn2, c24) / (l24 * l24));
+        g2 = g2 + cross(p3, gc23) + cross(p4, gc24);
+        g3 = g3 + cross(gc23, p2);
+        g4 = g4 + cross(gc24, p2);
+    }
+
+    // Reverse-mode derivative of step() with the decisions of `r` held fixed
+    // (contacts and their weights, ground / LRA activation, counted dynamic
+    // terms; the wind term's vertex normals are held fixed too).  gx, gxp, gv
+    // hold dL/d(x, x_prev, v) after the step and are overwritten with the
+    // gradients before it; dL/dk of every stretch and bend constraint is
+    // added to gks, gkb.  The analytic sphere is not differentiated.
+    void backward(const Record &r, std::vector<V> &gx, std::vector<V> &gxp, std::vector<V> &gv,
+                  std::vector<double> &gks, std::vector<double> &gkb) const {
+        const int Vn = tp.V, F = (int)tp.fixed.size(), K = prm.solverIterations;
+        const int E = (int)tp.s1.size(), Bn = (int)tp.b1.size();
+        const R dt = R(prm.timestep), th = R(h);
+        const V zero = mk<R>(0, 0, 0);
+        const std::vector<V> &xs = r.xk.back();
+        // integration and world clamp (Physics/CudaPBD.cu:1916-1932,
+        // Physics/CudaDeformableUtils.cu:260-269)
+        auto inside = [&](R v, int k) { return v > R(prm.worldMin[k]) && v < R(prm.worldMax[k]) ? R(1) : R(0); };
+        std::vector<V> a(Vn), gxp0(Vn, zero);
+        for (int i = 0; i < Vn; ++i) {
+            V gc = mk(gx[i].x * inside(xs[i].x, 0), gx[i].y * inside(xs[i].y, 1), gx[i].z * inside(xs[i].z, 2));
+            if (tp.pinned[i]) { a[i] = gc; gxp0[i] = gxp[i]; }
+            else { a[i] = gxp[i] + gv[i] / dt + gc; gxp0[i] = -gv[i] / dt; }
+        }
+        // Jacobi iterations in reverse (Physics/CudaPBD.cu:648-659)
+        std::vector<R> kps(E), kpb(Bn), dks(E), dkb(Bn);
+        auto dkp = [&](double k) { double K1 = (double)K; return (1.0 / K1) * std::pow(1.0 - k, 1.0 / K1 - 1.0); };
+        for (int i = 0; i < E; ++i) { kps[i] = kp_of(tp.kst[i]); dks[i] = R(dkp(tp.kst[i])); }
+        for (int i = 0; i < Bn; ++i) { kpb[i] = kp_of(tp.kbd[i]); dkb[i] = R(dkp(tp.kbd[i])); }
+        const size_t nvf = r.vf.size(), nee = r.ee.size(), ndyn = 4 * (nvf + nee);
+        std::vector<int> stat_cnt(Vn), lra_cnt(Vn, 0);
+        for (int i = 0; i < Vn; ++i) {
+            stat_cnt[i] = tp.soff[i + 1] - tp.soff[i];
+            for (int j = 0; j < F; ++j) lra_cnt[i] += r.lra[(size_t)i * F + j] ? 1 : 0;
+        }
+        const R gap = R(3.14159265358979323846) - R(kPi);
+        std::vector<V> u(Vn), g(Vn);
+        std::vector<int> cnt(Vn);
+        for (int it = K - 1; it >= 0; --it) {
+            const std::vector<V> &X = r.xk[it];
+            for (int i = 0; i < Vn; ++i) cnt[i] = stat_cnt[i] + lra_cnt[i] + (int)((r.ground_it[i] >> it) & 1u);
+            for (size_t c = 0; c < nvf + nee; ++c) {
+                const Contact &k = c < nvf ? r.vf[c] : r.ee[c - nvf];
+                for (int s2 = 0; s2 < 4; ++s2)
+                    if (r.dyn[(size_t)it * ndyn + c * 4 + s2]) cnt[k.v[s2]] += 1;
+            }
+            for (int i = 0; i < Vn; ++i) { u[i] = cnt[i] ? a[i] / R(cnt[i]) : zero; g[i] = a[i]; }
+            // ground (Physics/CudaPBD.cu:1594-1629): corr.y = -(x.y - (ground + h))
+            for (int i = 0; i < Vn; ++i)
+                if ((r.ground_it[i] >> it) & 1u) g[i].y -= u[i].y;
+            // LRA (Physics/CudaPBD.cu:1656-1688): corr = -f(x_i - x_fixed)
+            for (int i = 0; i < Vn; ++i)
+                for (int j = 0; j < F; ++j)
+                    if (r.lra[(size_t)i * F + j]) {
+                        int fj = tp.fixed[j];
+                        V d = X[i] - X[fj];
+                        R l = len(d);
+                        V dd = f_jac(d, l, R(tp.lra_l0[(size_t)i * F + j]), -u[i]);
+                        g[i] = g[i] + dd;
+                        g[fj] = g[fj] - dd;
+                    }
+            // stretch (Physics/CudaPBD.cu:986-1022)
+            for (int c = 0; c < E; ++c) {
+                int i1 = tp.s1[c], i2 = tp.s2[c];
+                R w1 = invm[i1], w2 = invm[i2], ws = w1 + w2;
+                if (ws == R(0)) continue;
+                V d = X[i1] - X[i2];
+                R l = len(d);
+                if (l <= R(kEpsPbd)) continue;
+                V comb = (u[i2] * w2 - u[i1] * w1) / ws;
+                V dd = f_jac(d, l, R(tp.sl0[c]), comb * kps[c]);
+                g[i1] = g[i1] + dd;
+                g[i2] = g[i2] - dd;
+                V fv = d - d * (R(tp.sl0[c]) / l);
+                gks[c] += double(dot(fv, comb) * dks[c]);
+            }
+            // bend (Physics/CudaPBD.cu:1024-1147)
+            for (int c = 0; c < Bn; ++c) {
+                int id[4] = {tp.b1[c], tp.b2[c], tp.b3[c], tp.b4[c]};
+                R w[4] = {invm[id[0]], invm[id[1]], invm[id[2]], invm[id[3]]};
+                V ub[4] = {u[id[0]], u[id[1]], u[id[2]], u[id[3]]};
+                V g2, g3, g4;
+                R gk;
+                bend_vjp(X[id[1]], X[id[2]], X[id[3]], w, kpb[c], gap, ub, g2, g3, g4, gk);
+                g[id[1]] = g[id[1]] + g2; g[id[2]] = g[id[2]] + g3; g[id[3]] = g[id[3]] + g4;
+                gkb[c] += double(gk * dkb[c]);
+            }
+            // contacts (Physics/CudaPBD.cu:1212-1415), taken entries only
+            for (size_t c = 0; c < nvf + nee; ++c) {
+                const bool isvf = c < nvf;
+                const Contact &k = isvf ? r.vf[c] : r.ee[c - nvf];
+                V ub[4];
+                bool any = false;
+                for (int s2 = 0; s2 < 4; ++s2) {
+                    bool t = r.dyn[(size_t)it * ndyn + c * 4 + s2] != 0;
+                    ub[s2] = t ? u[k.v[s2]] : zero;
+                    any = any || t;
+                }
+                if (!any) continue;
+                R wv[4] = {invm[k.v[0]], invm[k.v[1]], invm[k.v[2]], invm[k.v[3]]};
+                R b[4], sgn[4];
+                if (isvf) {
+                    b[0] = R(1);
+                    b[1] = clampf(R(-k.w[1]), R(0), R(1)); b[2] = clampf(R(-k.w[2]), R(0), R(1));
+                    b[3] = clampf(R(-k.w[3]), R(0), R(1));
+                    sgn[0] = R(1); sgn[1] = sgn[2] = sgn[3] = R(-1);
+                } else {
+                    b[0] = R(k.w[0]); b[1] = R(k.w[1]); b[2] = R(-k.w[2]); b[3] = R(-k.w[3]);
+                    sgn[0] = sgn[1] = R(1); sgn[2] = sgn[3] = R(-1);
+                }
+                // nvec = sum_s sgn_s b_s x_s ; corr_s = -(w_s sgn_s b_s / den) f(nvec)
+                R den = 0;
+                for (int s2 = 0; s2 < 4; ++s2) den += wv[s2] * b[s2] * b[s2];
+                if (den == R(0)) continue;
+                V nv = zero;
+                for (int s2 = 0; s2 < 4; ++s2) nv = nv + X[k.v[s2]] * (sgn[s2] * b[s2]);
+                R l = len(nv);
+                V comb = zero;
+                for (int s2 = 0; s2 < 4; ++s2) comb = comb - ub[s2] * (wv[s2] * sgn[s2] * b[s2] / den);
+                V dn = f_jac(nv, l, th, comb);
+                for (int s2 = 0; s2 < 4; ++s2) g[k.v[s2]] = g[k.v[s2]] + dn * (sgn[s2] * b[s2]);
+            }
+            a.swap(g);
+        }
+        // ExplicitEuler (Physics/CudaPBD.cu:2005-2012): x = x_prev + dt v
+        std::vector<V> gvc(Vn);
+        for (int i = 0; i < Vn; ++i) { gxp0[i] = gxp0[i] + a[i]; gvc[i] = a[i] * dt; }
+        // DampVelocities (Physics/CudaPBD.cu:411-458): v_c = v_b + kd (vcm + w x r - v_b)
+        const double kd = prm.kDamp, kg = prm.globalVelDamp, M = r.M;
+        double S1[3] = {0, 0, 0}, S2[3] = {0, 0, 0};
+        auto dv3 = [](double a0, double a1, double a2) { return mk<double>(a0, a1, a2); };
+        const V3<double> xcm = dv3(r.xcm[0], r.xcm[1], r.xcm[2]), om = dv3(r.om[0], r.om[1], r.om[2]);
+        for (int i = 0; i < Vn; ++i) {
+            V3<double> ri = dv3(r.x_in[i].x, r.x_in[i].y, r.x_in[i].z) - xcm;
+            V3<double> gi = dv3(gvc[i].x, gvc[i].y, gvc[i].z);
+            V3<double> cr = cross(ri, gi);
+            S1[0] += gi.x; S1[1] += gi.y; S1[2] += gi.z;
+            S2[0] += cr.x; S2[1] += cr.y; S2[2] += cr.z;
+        }
+        double omb[3] = {kd * S2[0], kd * S2[1], kd * S2[2]}, Lb[3];
+        solve3(r.I, omb, Lb);  // I is symmetric: I^-T omb = I^-1 omb
+        const V3<double> Lbar = dv3(Lb[0], Lb[1], Lb[2]);
+        double Ib[3][3];
+        for (int p = 0; p < 3; ++p)
+            for (int q2 = 0; q2 < 3; ++q2) Ib[p][q2] = -Lb[p] * r.om[q2];
+        const double trI = Ib[0][0] + Ib[1][1] + Ib[2][2];
+        const V3<double> vcmbar = dv3(kd * S1[0], kd * S1[1], kd * S1[2]);
+        std::vector<V3<double>> rbar(Vn);
+        V3<double> rsum = dv3(0, 0, 0);
+        for (int i = 0; i < Vn; ++i) {
+            const double m = (double)mass[i];
+            V3<double> ri = dv3(r.x_in[i].x, r.x_in[i].y, r.x_in[i].z) - xcm;
+            V3<double> gi = dv3(gvc[i].x, gvc[i].y, gvc[i].z);
+            V3<double> vb = dv3(r.v_b[i].x, r.v_b[i].y, r.v_b[i].z);
+            V3<double> gvb = gi * (1.0 - kd) + vcmbar * (m / M) + cross(Lbar, ri) * m;
+            V3<double> Isr = dv3((Ib[0][0] + Ib[0][0]) * ri.x + (Ib[0][1] + Ib[1][0]) * ri.y + (Ib[0][2] + Ib[2][0]) * ri.z,
+                                 (Ib[1][0] + Ib[0][1]) * ri.x + (Ib[1][1] + Ib[1][1]) * ri.y + (Ib[1][2] + Ib[2][1]) * ri.z,
+                                 (Ib[2][0] + Ib[0][2]) * ri.x + (Ib[2][1] + Ib[1][2]) * ri.y + (Ib[2][2] + Ib[2][2]) * ri.z);
+            rbar[i] = cross(gi, om) * kd + cross(vb, Lbar) * m + (ri * (2.0 * trI) - Isr) * m;
+            rsum = rsum + rbar[i];
+            // v_b = (v + dt g_ext) (1 - kg)
+            V3<double> gvn = gvb * (1.0 - kg);
+            gv[i] = mk<R>(R(gvn.x), R(gvn.y), R(gvn.z));
+        }
+        for (int i = 0; i < Vn; ++i) {
+            V3<double> gxi = rbar[i] - rsum * ((double)mass[i] / M);
+            gx[i] = mk<R>(R(gxi.x), R(gxi.y), R(gxi.z));
+        }
+        gxp.swap(gxp0);
     }
 
     void step() {

@@ -266,3 +266,84 @@ int lco_grid_indices(int rows, int cols, uint32_t *out) {
 uint64_t lco_morton(float x, float y, float z, int mode) { return morton3d(x, y, z, mode); }
 
 }  // extern "C"
+
+// ---- adjoint of the step (FP64 oracle) -------------------------------------
+// Steps cloth c nsteps times, recording after each step its decisions and the
+// intermediate states its adjoint needs (Cloth::Record).
+extern "C" int lco_adj_record(lco_world *w, int c, int nsteps) {
+    return with_cloth(w, c, [&](auto &cl) {
+        for (int s = 0; s < nsteps; ++s) {
+            cl.recording = true;
+            cl.step();
+            cl.recording = false;
+            cl.records.push_back(cl.rec);
+        }
+        return LC_OK;
+    });
+}
+
+// Steps cloth c nsteps times with the decisions recorded for steps
+// [first, first + nsteps) imposed (the piecewise-smooth branch a finite
+// difference of the recorded rollout has to stay on).
+extern "C" int lco_adj_replay(lco_world *w, int c, int first, int nsteps) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (first < 0 || first + nsteps > (int)cl.records.size()) return (int)LC_ERR_INVALID_ARG;
+        for (int s = 0; s < nsteps; ++s) {
+            const auto &r = cl.records[first + s];
+            cl.frozen_vf = r.vf;
+            cl.frozen_ee = r.ee;
+            cl.have_frozen = true;
+            cl.forced.ground = r.ground;
+            cl.forced.ground_it = r.ground_it;
+            cl.forced.lra = r.lra;
+            cl.forced.dyn = r.dyn;
+            cl.forced.sphere.assign(cl.tp.V, 0);
+            cl.forced.on = true;
+            cl.step();
+        }
+        return (int)LC_OK;
+    });
+}
+
+// Reverse pass over every recorded step, last first.  gx, gxp, gv (3V
+// doubles each) hold dL/d(x, x_prev, v) after the last recorded step and
+// receive the gradients before the first; gks (stretch count) and gkb (bend
+// count) accumulate dL/dk.
+extern "C" int lco_adj_backward(lco_world *w, int c, double *gx, double *gxp, double *gv, double *gks,
+                                double *gkb) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using Cl = std::remove_reference_t<decltype(cl)>;
+        using V = typename Cl::V;
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        const int Vn = cl.tp.V;
+        std::vector<V> ax(Vn), axp(Vn), av(Vn);
+        for (int i = 0; i < Vn; ++i) {
+            ax[i] = mk<R>(R(gx[3 * i]), R(gx[3 * i + 1]), R(gx[3 * i + 2]));
+            axp[i] = mk<R>(R(gxp[3 * i]), R(gxp[3 * i + 1]), R(gxp[3 * i + 2]));
+            av[i] = mk<R>(R(gv[3 * i]), R(gv[3 * i + 1]), R(gv[3 * i + 2]));
+        }
+        std::vector<double> ks(cl.tp.s1.size(), 0.0), kb(cl.tp.b1.size(), 0.0);
+        for (int s = (int)cl.records.size() - 1; s >= 0; --s) cl.backward(cl.records[s], ax, axp, av, ks, kb);
+        for (int i = 0; i < Vn; ++i) {
+            gx[3 * i] = ax[i].x; gx[3 * i + 1] = ax[i].y; gx[3 * i + 2] = ax[i].z;
+            gxp[3 * i] = axp[i].x; gxp[3 * i + 1] = axp[i].y; gxp[3 * i + 2] = axp[i].z;
+            gv[3 * i] = av[i].x; gv[3 * i + 1] = av[i].y; gv[3 * i + 2] = av[i].z;
+        }
+        for (size_t i = 0; i < ks.size(); ++i) gks[i] += ks[i];
+        for (size_t i = 0; i < kb.size(); ++i) gkb[i] += kb[i];
+        return (int)LC_OK;
+    });
+}
+
+extern "C" int lco_adj_clear(lco_world *w, int c) {
+    return with_cloth(w, c, [&](auto &cl) { cl.records.clear(); return (int)LC_OK; });
+}
+
+// Per-constraint stiffness in double (finite differences need more than float).
+extern "C" int lco_set_stiffness_d(lco_world *w, int c, const double *ks, const double *kb) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (ks) for (size_t i = 0; i < cl.tp.kst.size(); ++i) cl.tp.kst[i] = ks[i];
+        if (kb) for (size_t i = 0; i < cl.tp.kbd.size(); ++i) cl.tp.kbd[i] = kb[i];
+        return (int)LC_OK;
+    });
+}

@@ -49,6 +49,11 @@ def lib() -> C.CDLL:
             "lco_debug_get": (C.c_int, [VP, C.c_int, C.c_int, VP, C.c_uint64, C.POINTER(C.c_uint64)]),
             "lco_grid_indices": (C.c_int, [C.c_int, C.c_int, VP]),
             "lco_morton": (C.c_uint64, [C.c_float, C.c_float, C.c_float, C.c_int]),
+            "lco_adj_record": (C.c_int, [VP, C.c_int, C.c_int]),
+            "lco_adj_replay": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
+            "lco_adj_backward": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, VP]),
+            "lco_adj_clear": (C.c_int, [VP, C.c_int]),
+            "lco_set_stiffness_d": (C.c_int, [VP, C.c_int, VP, VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -173,6 +178,39 @@ class Oracle:
         ks = None if k_stretch is None else np.ascontiguousarray(k_stretch, dtype=np.float32)
         kb = None if k_bend is None else np.ascontiguousarray(k_bend, dtype=np.float32)
         _chk(lib().lco_set_stiffness(self._h, c, _p(ks), _p(kb)), "set_stiffness")
+
+    def sizes(self, c: int):
+        """(vertices, triangles, stretch constraints, bend constraints) of cloth c."""
+        out = [C.c_int() for _ in range(4)]
+        _chk(lib().lco_sizes(self._h, c, *[C.byref(o) for o in out]), "sizes")
+        return tuple(o.value for o in out)
+
+    # ---- adjoint (FP64 oracle) ------------------------------------------
+    def adj_record(self, c: int, nsteps: int) -> None:
+        """Step cloth c, recording each step's decisions for the adjoint."""
+        _chk(lib().lco_adj_record(self._h, c, nsteps), "adj_record")
+
+    def adj_replay(self, c: int, first: int, nsteps: int) -> None:
+        """Step cloth c with the decisions recorded for steps [first, first + nsteps)."""
+        _chk(lib().lco_adj_replay(self._h, c, first, nsteps), "adj_replay")
+
+    def adj_backward(self, c: int, gx, gxp, gv):
+        """Reverse over the recorded steps.  Returns dL/d(x, x_prev, v) of the
+        state before the first recorded step and dL/dk of every stretch and
+        bend constraint, given dL/d(x, x_prev, v) after the last."""
+        nv, nt, ne, nb = self.sizes(c)
+        arrs = [np.ascontiguousarray(a, np.float64).reshape(nv, 3).copy() for a in (gx, gxp, gv)]
+        gks, gkb = np.zeros(ne), np.zeros(nb)
+        _chk(lib().lco_adj_backward(self._h, c, *[_p(a) for a in arrs], _p(gks), _p(gkb)), "adj_backward")
+        return arrs[0], arrs[1], arrs[2], gks, gkb
+
+    def adj_clear(self, c: int) -> None:
+        _chk(lib().lco_adj_clear(self._h, c), "adj_clear")
+
+    def set_stiffness_d(self, c: int, k_stretch=None, k_bend=None) -> None:
+        ks = None if k_stretch is None else np.ascontiguousarray(k_stretch, np.float64)
+        kb = None if k_bend is None else np.ascontiguousarray(k_bend, np.float64)
+        _chk(lib().lco_set_stiffness_d(self._h, c, _p(ks), _p(kb)), "set_stiffness_d")
 
     def thickness(self, c: int) -> float:
         h = C.c_float()

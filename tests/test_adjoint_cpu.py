@@ -1,0 +1,114 @@
+"""The FP64 adjoint of the cloth step (oracle/lc_oracle.hpp, Cloth::backward)
+against central finite differences of the FP64 oracle.
+
+The step is piecewise smooth: contacts, ground / LRA activation and which
+contact terms count change discretely.  The rollout is recorded once and every
+finite-difference evaluation replays its decisions (Oracle.adj_replay), so
+both sides differentiate the same branch.  The loss is the summed squared
+distance of the final positions (x_prev after the last step, the positions the
+reference publishes) to a target.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from licenta_gb300 import scenes
+from oracle.oracle_ffi import Oracle
+
+
+class Rollout:
+    def __init__(self, spec, warm_steps=0, seed=0, v_scale=0.0):
+        self.o = Oracle([spec], fp64=True)
+        self.nv, _, self.ne, self.nb = self.o.sizes(0)
+        if warm_steps:
+            self.o.step(warm_steps, threads=1)
+        self.st0 = self.o.get_state(0)
+        self.perm0 = self.o.perm(0)
+        rng = np.random.default_rng(seed)
+        self.v0 = self.st0["v"] + rng.normal(scale=v_scale, size=(self.nv, 3)) * (spec.pinned == 0)[:, None]
+        self.ks0 = 0.9 + rng.uniform(-0.1, 0.05, self.ne)
+        self.kb0 = 0.9 + rng.uniform(-0.1, 0.05, self.nb)
+        self.target = self.st0["x_prev"] + rng.normal(scale=0.05, size=(self.nv, 3))
+
+    def reset(self, x=None, xp=None, v=None, ks=None, kb=None):
+        st = self.st0
+        self.o.set_state(0, x=st["x"] if x is None else x, x_prev=st["x_prev"] if xp is None else xp,
+                         v=self.v0 if v is None else v, vn=st["vn"])
+        self.o.set_perm(0, self.perm0)
+        self.o.set_stiffness_d(0, self.ks0 if ks is None else ks, self.kb0 if kb is None else kb)
+
+    def loss(self):
+        return float(((self.o.get_state(0)["x_prev"] - self.target) ** 2).sum())
+
+    def record(self, steps):
+        self.steps = steps
+        self.reset()
+        self.o.adj_clear(0)
+        self.o.adj_record(0, steps)
+        xp = self.o.get_state(0)["x_prev"]
+        z = np.zeros((self.nv, 3))
+        return self.o.adj_backward(0, z, 2 * (xp - self.target), z)
+
+    def fd(self, **perturbed):
+        vals = []
+        for sgn in (1, -1):
+            self.reset(**{k: f(sgn) for k, f in perturbed.items()})
+            self.o.adj_replay(0, 0, self.steps)
+            vals.append(self.loss())
+        self.reset()
+        return vals
+
+
+def check(ad, fd_vals, eps, rtol=1e-3, atol=1e-6):
+    """Relative 1e-3, with an absolute floor: a folded rollout amplifies the
+    loss's rounding, which puts about 1e-7..1e-6 of noise on a difference
+    quotient (the gradients checked are 1e-4..1e-1)."""
+    fd = (fd_vals[0] - fd_vals[1]) / (2 * eps)
+    assert abs(ad - fd) <= rtol * abs(fd) + atol, f"adjoint {ad:.8g} vs finite difference {fd:.8g}"
+
+
+def test_adjoint_matches_finite_differences_hanging_cloth():
+    spec = scenes.small_cloth(seed=1, n=10)
+    r = Rollout(spec, v_scale=0.3)
+    gx, gxp, gv, gks, gkb = r.record(8)
+    rng = np.random.default_rng(5)
+    eps = 1e-3
+    for c in rng.choice(r.ne, 4, replace=False):
+        check(gks[c], r.fd(ks=lambda s, c=c: r.ks0 + s * eps * (np.arange(r.ne) == c)), eps)
+    for c in rng.choice(r.nb, 4, replace=False):
+        check(gkb[c], r.fd(kb=lambda s, c=c: r.kb0 + s * eps * (np.arange(r.nb) == c)), eps)
+    free = np.where(spec.pinned == 0)[0]
+    for i in rng.choice(free, 3, replace=False):
+        for d in range(3):
+            e = np.zeros((r.nv, 3)); e[i, d] = eps
+            check(gv[i, d], r.fd(v=lambda s, e=e: r.v0 + s * e), eps)
+    # a pinned vertex: its position enters x and x_prev (kept off the world
+    # clamp at z = 0 by a step smaller than its jitter)
+    p = int(np.where(spec.pinned)[0][0])
+    for d, e_d in ((0, 1e-3), (1, 1e-3), (2, 1e-6)):
+        e = np.zeros((r.nv, 3)); e[p, d] = e_d
+        x0 = r.st0["x"]
+        vals = r.fd(x=lambda s, e=e: x0 + s * e, xp=lambda s, e=e: x0 + s * e)
+        check(gx[p, d] + gxp[p, d], vals, e_d)
+
+
+def test_adjoint_matches_finite_differences_through_contacts():
+    spec = scenes.small_cloth(seed=0, n=20)
+    r = Rollout(spec, warm_steps=55, seed=1)
+    gx, gxp, gv, gks, gkb = r.record(6)
+    rng = np.random.default_rng(2)
+    eps = 1e-3
+    for c in rng.choice(r.ne, 5, replace=False):
+        check(gks[c], r.fd(ks=lambda s, c=c: r.ks0 + s * eps * (np.arange(r.ne) == c)), eps)
+    for c in rng.choice(r.nb, 5, replace=False):
+        check(gkb[c], r.fd(kb=lambda s, c=c: r.kb0 + s * eps * (np.arange(r.nb) == c)), eps)
+    free = np.where(spec.pinned == 0)[0]
+    for i in rng.choice(free, 3, replace=False):
+        for d in range(3):
+            e = np.zeros((r.nv, 3)); e[i, d] = eps
+            check(gv[i, d], r.fd(v=lambda s, e=e: r.v0 + s * e), eps)
+            # positions: a step well below a millimetre, so that no vertex
+            # crosses the world clamp (many lie outside the unit box here)
+            e = np.zeros((r.nv, 3)); e[i, d] = 1e-6
+            check(gxp[i, d], r.fd(xp=lambda s, e=e: r.st0["x_prev"] + s * e), 1e-6)
