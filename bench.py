@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cloths", type=int, default=NCLOTH,
                     help="cloths per GPU (the workload has 256; fewer only for small profiling cases)")
     return ap.parse_args()
@@ -170,6 +171,59 @@ def algorithmic_bytes(batch, specs, prof) -> dict:
 
 
 # ---------------------------------------------------------------------------
+def adjoint_timing(seed: int) -> dict:
+    """The differentiable-rollout workload: a 64x64 cloth, 60 steps, 10
+    iterations, checkpoints every 10 steps, loss = summed squared distance of
+    the final positions to a target.  Times the forward rollout and its
+    backward pass (re-running each segment from its checkpoint, then the
+    reverse of every step) with CUDA events, and the plain forward step of
+    the same cloth on the default solver."""
+    import torch
+    from licenta_gb300 import ClothBatch, scenes
+    from licenta_gb300.adjoint import ClothRollout, DiffCloth
+
+    steps, every = 60, 10
+    spec = scenes.adjoint_cloth(seed=seed)
+    cloth = DiffCloth([spec], checkpoint_every=every)
+    ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
+    kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
+    x0 = torch.tensor(spec.positions, device="cuda", requires_grad=True)
+    v0 = torch.zeros_like(x0, requires_grad=True)
+    target = x0.detach() - torch.tensor([0.0, 0.3, 0.0], device="cuda")
+
+    def once():
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        out = ClothRollout.apply(cloth, steps, ks, kb, x0, v0)
+        loss = ((out - target) ** 2).sum()
+        e[1].record()
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+
+    for _ in range(2):
+        once()
+    runs = [once() for _ in range(3)]
+    fwd = float(np.median([r[0] for r in runs])) / steps
+    bwd = float(np.median([r[1] for r in runs])) / steps
+    cloth.close()
+    b = ClothBatch([spec])
+    b.step(3)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    b.step(steps)
+    g1.record()
+    torch.cuda.synchronize()
+    plain = g0.elapsed_time(g1) / steps
+    b.close()
+    return {"workload": "differentiable rollout: 64x64 cloth, 60 steps, 10 iterations, checkpoints every 10",
+            "forward_ms_per_step": fwd, "backward_ms_per_step": bwd, "adjoint_over_forward": bwd / fwd,
+            "forward_default_solver_ms_per_step": plain, "adjoint_over_default_forward": bwd / plain,
+            "what": "backward = segment re-run from checkpoints + recorded step + reverse pass, per step"}
+
+
 def cpu_baseline(specs, seed: int, cloths: int = 64, steps: int = 2) -> dict:
     """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
     cloths on every host core, on a seeded sample of the workload."""
@@ -321,6 +375,10 @@ def run_ours(args, world, rank, local):
         plain = {"value": plain_value, "unit": UNIT, "sample": "16 of the 256 cloths (seeded), one cloth per step call",
                  "batched_over_plain": (value / world) / plain_value}
 
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        adj = adjoint_timing(args.seed)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(specs, args.seed)
@@ -342,6 +400,7 @@ def run_ours(args, world, rank, local):
                     "narrow_ms": prof["narrow_ms"], "sort_ms": prof["sort_ms"], "kernels_per_step": prof["kernels_per_step"],
                     "sizes": alg["_sizes"]},
         "plain": plain,
+        "adjoint": adj,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

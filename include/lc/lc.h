@@ -118,6 +118,7 @@ typedef struct lc_batch_options {
     int32_t block_size;       /* block size of the global-memory Jacobi kernel (0 = default) */
     uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull, per kind (VF, EE);
                                  default min(15 * pair capacity, max(32 * total triangles, 4 Mi)) */
+    int32_t adjoint;          /* 1: keep the tape lc_batch_adjoint_step needs (implies solver_variant 1) */
 } lc_batch_options;
 
 typedef struct lc_batch lc_batch;
@@ -248,6 +249,33 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t cloth, int32_t what, void *dst
  * contacts, [3] pairs dropped by the per-leaf chunk cap (the reference drops
  * them silently, Collision/CudaBVH.cu:69-92). */
 lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]);
+
+/* ---- differentiation (no counterpart in the reference) -------------------
+ * Per-constraint stiffness of the whole batch in the global constraint order
+ * (cloth 0 first; lc_batch_constraint_counts gives each cloth's share), host
+ * or device arrays; either may be NULL. */
+lc_status lc_batch_set_constraint_stiffness(lc_batch *b, const float *k_stretch, const float *k_bend,
+                                            int32_t is_host);
+
+/* The dynamic state every later step reads (x, x_prev, v, running normals,
+ * triangle order, wind state) saved to / restored from one device buffer of
+ * lc_batch_state_size bytes, on stream: checkpoints of a rollout. */
+lc_status lc_batch_state_size(const lc_batch *b, uint64_t *bytes);
+lc_status lc_batch_save_state(lc_batch *b, void *dst, void *stream);
+lc_status lc_batch_load_state(lc_batch *b, const void *src, void *stream);
+
+/* Reverse pass of one step.  The batch (created with options.adjoint = 1)
+ * must hold the state S_n before the step; the call steps it to S_{n+1}
+ * exactly as lc_batch_step does, recording the step's solver iterates and
+ * decisions, then runs the adjoint with those decisions held fixed (contacts
+ * and their weights, ground / LRA activation, the contact terms counted in
+ * each iteration; the analytic sphere and the wind's vertex normals are held
+ * fixed).  gx, gx_prev, gv: device arrays, 3 floats per vertex packed in cloth
+ * order, holding dL/d(x, x_prev, v) of S_{n+1} on entry and of S_n on return.
+ * gk_stretch / gk_bend (device, global constraint order, may be NULL)
+ * accumulate dL/dk. */
+lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gx_prev, float *gv, float *gk_stretch,
+                                float *gk_bend, void *stream);
 
 /* ----- standalone LBVH (the GenerateBVH2 / ComputeTreeAABBs /
  * GetAABBCollisions chain of Collision/CudaBVH.cu over caller triangles) --- */

@@ -56,7 +56,7 @@ class BatchOptions(C.Structure):
     _fields_ = [
         ("vf_capacity", C.c_uint64), ("ee_capacity", C.c_uint64), ("use_graph", C.c_int32),
         ("debug_capture", C.c_int32), ("solver_variant", C.c_int32), ("block_size", C.c_int32),
-        ("cand_capacity", C.c_uint64),
+        ("cand_capacity", C.c_uint64), ("adjoint", C.c_int32),
     ]
 
 
@@ -81,6 +81,11 @@ SIGNATURES = {
     "lc_default_params": (None, [C.POINTER(ClothParams)]),
     "lc_default_options": (None, [C.POINTER(BatchOptions)]),
     "lc_batch_create": (C.c_int, [C.POINTER(ClothDesc), C.c_int32, C.POINTER(BatchOptions), C.POINTER(VP)]),
+    "lc_batch_set_constraint_stiffness": (C.c_int, [VP, VP, VP, C.c_int32]),
+    "lc_batch_state_size": (C.c_int, [VP, C.POINTER(C.c_uint64)]),
+    "lc_batch_save_state": (C.c_int, [VP, VP, VP]),
+    "lc_batch_load_state": (C.c_int, [VP, VP, VP]),
+    "lc_batch_adjoint_step": (C.c_int, [VP, VP, VP, VP, VP, VP, VP]),
     "lc_batch_destroy": (C.c_int, [VP]),
     "lc_batch_step": (C.c_int, [VP, C.c_int32, VP]),
     "lc_batch_sync": (C.c_int, [VP]),

@@ -1,0 +1,143 @@
+"""Differentiable cloth rollouts: the engine's reverse pass behind a
+torch.autograd.Function.
+
+``ClothRollout`` steps a batch of cloths for a fixed number of steps from
+given initial positions and velocities with given per-constraint
+stiffnesses, and returns the published positions after the last step (the
+x_prev array the reference's Update() copies out).  Its backward pass returns
+dL/d(stretch stiffness), dL/d(bend stiffness), dL/d(initial velocities) and
+dL/d(initial positions) (for a pinned vertex, the gradient with respect to its
+fixed position).
+
+Memory: the forward pass keeps a checkpoint of the full dynamic state every
+``checkpoint_every`` steps; the backward pass re-runs each segment from its
+checkpoint, keeping the segment's states, and runs the adjoint of every step
+(lc_batch_adjoint_step: the step re-run with its solver iterates recorded,
+then reversed with its discrete decisions held fixed).  Peak memory is about
+(steps / checkpoint_every + checkpoint_every) states plus one step's tape.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _ffi
+from .cloth import ClothBatch
+from .scenes import ClothSpec
+
+
+def _p(t: torch.Tensor | None):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class DiffCloth:
+    """A batch prepared for differentiable rollouts (adjoint tape kept)."""
+
+    def __init__(self, specs: Sequence[ClothSpec], checkpoint_every: int = 10, **batch_kw):
+        self.batch = ClothBatch(specs, adjoint=True, use_graph=True, **batch_kw)
+        self.h = self.batch._h
+        self.every = max(1, int(checkpoint_every))
+        L = _ffi.lib()
+        n = C.c_uint64()
+        _ffi.check(L.lc_batch_state_size(self.h, C.byref(n)), "lc_batch_state_size")
+        self.state_bytes = n.value
+        self.V = sum(self.batch.num_vertices)
+        counts = [self.batch.constraint_counts(c) for c in range(len(specs))]
+        self.E = sum(e for e, _ in counts)
+        self.B = sum(b for _, b in counts)
+        self.initial = self.new_state()
+        self.save(self.initial)
+        torch.cuda.synchronize()
+
+    # -- state buffers ---------------------------------------------------------
+    def new_state(self) -> torch.Tensor:
+        return torch.empty(self.state_bytes, dtype=torch.uint8, device="cuda")
+
+    @staticmethod
+    def _stream():
+        return torch.cuda.current_stream()
+
+    @staticmethod
+    def _sp():
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def save(self, buf: torch.Tensor) -> None:
+        _ffi.check(_ffi.lib().lc_batch_save_state(self.h, _p(buf), self._sp()), "lc_batch_save_state")
+
+    def load(self, buf: torch.Tensor) -> None:
+        _ffi.check(_ffi.lib().lc_batch_load_state(self.h, _p(buf), self._sp()), "lc_batch_load_state")
+
+    def step(self, n: int = 1) -> None:
+        self.batch.step(n, self._stream())
+
+    def set_stiffness(self, ks: torch.Tensor, kb: torch.Tensor) -> None:
+        ks = ks.detach().to("cuda", torch.float32).contiguous()
+        kb = kb.detach().to("cuda", torch.float32).contiguous()
+        _ffi.check(_ffi.lib().lc_batch_set_constraint_stiffness(self.h, _p(ks), _p(kb), 0),
+                   "lc_batch_set_constraint_stiffness")
+
+    def set_initial(self, x0: torch.Tensor, v0: torch.Tensor) -> None:
+        """The initial state with positions x0 (x and x_prev) and velocities v0."""
+        self.load(self.initial)
+        x0 = x0.detach().to("cuda", torch.float32).contiguous()
+        v0 = v0.detach().to("cuda", torch.float32).contiguous()
+        self.batch.write_state(x0.data_ptr(), x0.data_ptr(), v0.data_ptr(), False, self._stream())
+
+    def positions(self) -> torch.Tensor:
+        out = torch.empty((self.V, 3), dtype=torch.float32, device="cuda")
+        self.batch.read_state(None, out.data_ptr(), None, False, self._stream())
+        return out
+
+    def adjoint_step(self, gx, gxp, gv, gks, gkb) -> None:
+        _ffi.check(_ffi.lib().lc_batch_adjoint_step(self.h, _p(gx), _p(gxp), _p(gv), _p(gks), _p(gkb),
+                                                    self._sp()), "lc_batch_adjoint_step")
+
+    def close(self) -> None:
+        self.batch.close()
+
+
+class ClothRollout(torch.autograd.Function):
+    """final_positions = ClothRollout.apply(cloth, steps, k_stretch, k_bend, x0, v0)"""
+
+    @staticmethod
+    def forward(ctx, cloth: DiffCloth, steps: int, ks, kb, x0, v0):
+        cloth.set_stiffness(ks, kb)
+        cloth.set_initial(x0, v0)
+        ckpts = []
+        for n in range(steps):
+            if n % cloth.every == 0:
+                buf = cloth.new_state()
+                cloth.save(buf)
+                ckpts.append(buf)
+            cloth.step(1)
+        ctx.cloth, ctx.steps, ctx.ckpts = cloth, steps, ckpts
+        ctx.params = (ks.detach().clone(), kb.detach().clone())
+        return cloth.positions()
+
+    @staticmethod
+    def backward(ctx, g_out):
+        cloth, steps = ctx.cloth, ctx.steps
+        cloth.set_stiffness(*ctx.params)
+        V = cloth.V
+        gx = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        gxp = g_out.detach().to(torch.float32).contiguous().clone()
+        gv = torch.zeros_like(gx)
+        gks = torch.zeros(cloth.E, dtype=torch.float32, device="cuda")
+        gkb = torch.zeros(cloth.B, dtype=torch.float32, device="cuda")
+        for seg in range(len(ctx.ckpts) - 1, -1, -1):
+            first = seg * cloth.every
+            last = min(steps, first + cloth.every)
+            states = [ctx.ckpts[seg]]
+            cloth.load(ctx.ckpts[seg])
+            for _ in range(first, last - 1):
+                cloth.step(1)
+                buf = cloth.new_state()
+                cloth.save(buf)
+                states.append(buf)
+            for n in range(last - 1, first - 1, -1):
+                cloth.load(states[n - first])
+                cloth.adjoint_step(gx, gxp, gv, gks, gkb)
+        return None, None, gks, gkb, gx + gxp, gv

@@ -37,7 +37,8 @@ class ClothBatch:
     """Many independent cloths stepped together (one launch sequence per step)."""
 
     def __init__(self, specs: Sequence[ClothSpec], *, use_graph: bool = True, debug_capture: bool = False,
-                 vf_capacity: int = 0, ee_capacity: int = 0, block_size: int = 0, solver_variant: int = 0):
+                 vf_capacity: int = 0, ee_capacity: int = 0, block_size: int = 0, solver_variant: int = 0,
+                 adjoint: bool = False, cand_capacity: int = 0):
         L = _ffi.lib()
         self.specs = list(specs)
         self._keep = []
@@ -60,6 +61,8 @@ class ClothBatch:
         opt.ee_capacity = ee_capacity
         opt.block_size = block_size
         opt.solver_variant = solver_variant
+        opt.adjoint = 1 if adjoint else 0
+        opt.cand_capacity = cand_capacity
         h = C.c_void_p()
         _ffi.check(L.lc_batch_create(descs, len(self.specs), C.byref(opt), C.byref(h)), "lc_batch_create")
         self._h = h

@@ -31,7 +31,11 @@ void launch_pair_compact(const DevPtrs &d, cudaStream_t st);
 void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv, const uint32_t *nce, int grid,
                    int stage, cudaStream_t st);
 void launch_wind(const DevPtrs &d, cudaStream_t st);
-void launch_external(const DevPtrs &d, cudaStream_t st);
+void launch_external(const DevPtrs &d, cudaStream_t st, float4 *save_x = nullptr, float4 *save_v = nullptr);
+void launch_adj_unpack(const float *src, float4 *dst, int n, cudaStream_t st);
+void launch_adj_pack(const float4 *src, float *dst, int n, cudaStream_t st);
+void launch_adjoint(const DevPtrs &d, const AdjPtrs &A, float4 *a, float4 *g, const uint32_t *nvf, const uint32_t *nee,
+                    int grid, int nfixed, float *gk_stretch, float *gk_bend, cudaStream_t st);
 void launch_vertex_normals(const DevPtrs &d, cudaStream_t st);
 void launch_dyn(const DevPtrs &d, const uint32_t *nvf, const uint32_t *nee, int grid, int phase, cudaStream_t st);
 void launch_solver_setup(const DevPtrs &d, bool sphere, cudaStream_t st);
@@ -302,6 +306,12 @@ struct lc_batch {
     int cluster_cs = 8;
     bool cluster_scatter = false;
     ClusterArgs ca{};
+    // adjoint (lc_batch_adjoint_step): the tape of one recorded step
+    bool recording = false;
+    AdjPtrs adj{};
+    float4 *tape_x = nullptr, *tape_xin = nullptr, *tape_vb = nullptr;
+    float4 *adj_a = nullptr, *adj_g = nullptr;
+    int nfixed = 0;
     // debug copies
     float4 *dbg_x = nullptr, *dbg_xp = nullptr, *dbg_v = nullptr;
     uint32_t *dbg_perm_before = nullptr;
@@ -348,7 +358,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     LC_CUDA(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * 4, st));
     // 1. PBD External
     if (any_wind) launch_wind(d, st);
-    launch_external(d, st);
+    launch_external(d, st, recording ? tape_xin : nullptr, recording ? tape_vb : nullptr);
     if (dbg) {
         LC_CUDA(cudaMemcpyAsync(dbg_x, d.x, sizeof(float4) * d.Vtot, cudaMemcpyDeviceToDevice, st));
         LC_CUDA(cudaMemcpyAsync(dbg_xp, d.xp, sizeof(float4) * d.Vtot, cudaMemcpyDeviceToDevice, st));
@@ -409,11 +419,17 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     }
     launch_solver_setup(d, any_sphere, st);
     float4 *a = d.x, *b = d.x2;
+    if (recording) {  // iterates go to the tape: x^0 = prediction, x^{it+1} after iteration it
+        LC_CUDA(cudaMemcpyAsync(tape_x, d.x, sizeof(float4) * (size_t)d.Vtot, cudaMemcpyDeviceToDevice, st));
+        a = tape_x;
+    }
     for (int it = 0; it < max_iters; ++it) {
+        if (recording) b = tape_x + (size_t)(it + 1) * d.Vtot;
         if (it == 0) LC_KEV(0);
         launch_jacobi(d, a, b, it, nvf, jacobi_block, st);
         if (it == 0) LC_KEV(1);
-        std::swap(a, b);
+        if (recording) a = b;
+        else std::swap(a, b);
     }
     LC_PHASE(6);
     // 7. PBD Integration + WorldConstraints
@@ -504,7 +520,13 @@ static void fill_cloth_dev(const HostCloth &hc, ClothDev &cd) {
     cd.wind_var_max = p.windMaxVariation;
 }
 
-static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, const lc_batch_options &opt) {
+static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, const lc_batch_options &opt_in) {
+    lc_batch_options opt = opt_in;
+    if (opt.adjoint) {
+        // the reverse pass replays the global-memory Jacobi iterations
+        if (opt.solver_variant >= 2) return fail(LC_ERR_NOT_SUPPORTED, "adjoint: needs solver_variant 0 or 1");
+        opt.solver_variant = 1;
+    }
     b->C = n;
     b->opt = opt;
     b->hosts.resize(n);
@@ -627,6 +649,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     if (opt.debug_capture) {
         LC_TRY(A.alloc(b->dbg_x, V, "dbg_x")); LC_TRY(A.alloc(b->dbg_xp, V, "dbg_xp"));
         LC_TRY(A.alloc(b->dbg_v, V, "dbg_v")); LC_TRY(A.alloc(b->dbg_perm_before, T, "dbg_perm"));
+    }
+    if (opt.debug_capture || opt.adjoint) {  // the decisions the reverse pass replays
         LC_TRY(A.alloc(d.dbg_ground_it, V, "dbg_ground_it"));
         LC_TRY(A.alloc(d.dbg_dyn_nz, (size_t)b->max_iters * d.dyn_cap, "dbg_dyn_nz"));
         LC_TRY(A.alloc(d.dbg_sphere, V, "dbg_sphere"));
@@ -716,6 +740,36 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_CUDA(cudaMemset(d.crange, 0, sizeof(uint4) * (size_t)n));
     LC_CUDA(cudaMemset(d.nmin, 0, sizeof(float4) * (size_t)N));
     LC_CUDA(cudaMemset(d.nmax, 0, sizeof(float4) * (size_t)N));
+    if (opt.adjoint) {
+        AdjPtrs &J = b->adj;
+        LC_TRY(A.alloc(b->tape_x, (size_t)(b->max_iters + 1) * V, "tape_x"));
+        LC_TRY(A.alloc(b->tape_xin, V, "tape_xin")); LC_TRY(A.alloc(b->tape_vb, V, "tape_vb"));
+        LC_TRY(A.alloc(b->adj_a, V, "adj_a")); LC_TRY(A.alloc(b->adj_g, V, "adj_g"));
+        LC_TRY(A.alloc(J.u, V, "adj_u"));
+        LC_TRY(A.alloc(J.gx, V, "adj_gx")); LC_TRY(A.alloc(J.gxp, V, "adj_gxp")); LC_TRY(A.alloc(J.gv, V, "adj_gv"));
+        LC_TRY(A.alloc(J.slot, std::max<int64_t>(S, 1), "adj_slot"));
+        LC_TRY(A.alloc(J.dyn, std::max<uint64_t>(d.dyn_cap, 1), "adj_dyn"));
+        LC_TRY(A.alloc(J.fixed, 3 * std::max<int64_t>(F, 1), "adj_fixed"));
+        LC_CUDA(cudaMemset(J.fixed, 0, sizeof(float) * 3 * std::max<int64_t>(F, 1)));
+        LC_TRY(A.alloc(J.red, 8 * (vblk_cloth.size() + (size_t)n), "adj_red"));
+        // static CSR entry of every (constraint, role): where a constraint's
+        // reverse contribution to each of its vertices goes
+        std::vector<int> sslot(std::max<int64_t>(2 * E, 1), 0), bslot(std::max<int64_t>(4 * B, 1), 0);
+        for (int64_t e = 0; e < S; ++e) {
+            const uint32_t ent = hsent[e], k = ent & 0x1FFFFFFFu, role = (ent >> 29) & 3u;
+            if (ent >> 31) bslot[4 * (size_t)k + role] = (int)e;
+            else sslot[2 * (size_t)k + role] = (int)e;
+        }
+        int *ds, *db;
+        LC_TRY(A.alloc(ds, sslot.size(), "s_slot")); LC_TRY(A.alloc(db, bslot.size(), "b_slot"));
+        LC_TRY(upload(ds, sslot)); LC_TRY(upload(db, bslot));
+        J.s_slot = ds; J.b_slot = db;
+        J.tape_x = b->tape_x; J.tape_xin = b->tape_xin; J.tape_vb = b->tape_vb;
+        J.nvblk_red = (int)vblk_cloth.size();
+        J.K = b->max_iters;
+        J.E = (int)E; J.B = (int)B;
+        b->nfixed = (int)F;
+    }
     b->narrow_grid = sm_count() * 8;
     b->jacobi_block = opt.block_size > 0 ? opt.block_size : 256;
     LC_TRY(b->setup_cluster());
@@ -1056,6 +1110,103 @@ lc_status lc_batch_set_stiffness(lc_batch *b, int32_t c, const float *ks, const 
             LC_CUDA(cudaMemcpy((void *)(b->d.b_kp + b->b_off[c]), kp.data(), sizeof(float) * kp.size(),
                                cudaMemcpyHostToDevice));
     }
+    return LC_OK;
+}
+
+// All stretch and bend stiffnesses of the batch in the global constraint
+// order (cloth 0's constraints first), as lc_batch_set_stiffness converts them.
+lc_status lc_batch_set_constraint_stiffness(lc_batch *b, const float *ks, const float *kb, int32_t is_host) {
+    if (!b) return fail(LC_ERR_INVALID_ARG, "lc_batch_set_constraint_stiffness: null batch");
+    std::vector<float> hs, hb;
+    size_t E = 0, B = 0;
+    for (int c = 0; c < b->C; ++c) { E += b->hosts[c].s_ids.size(); B += b->hosts[c].b_ids.size(); }
+    LC_CUDA(cudaDeviceSynchronize());
+    if (ks) {
+        hs.resize(E);
+        if (E) LC_CUDA(cudaMemcpy(hs.data(), ks, sizeof(float) * E, is_host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost));
+    }
+    if (kb) {
+        hb.resize(B);
+        if (B) LC_CUDA(cudaMemcpy(hb.data(), kb, sizeof(float) * B, is_host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost));
+    }
+    for (int c = 0; c < b->C; ++c)
+        LC_TRY(lc_batch_set_stiffness(b, c, ks ? hs.data() + b->e_off[c] : nullptr, kb ? hb.data() + b->b_off[c] : nullptr));
+    return LC_OK;
+}
+
+// Dynamic state of the batch (everything a later step reads from an earlier
+// one): x, x_prev, v, running normals, the triangle order and the per-cloth
+// wind state, packed into one device buffer.
+static size_t al256(size_t n) { return (n + 255) & ~size_t(255); }
+static void state_layout(const lc_batch *b, size_t off[6]) {
+    const size_t V = (size_t)b->d.Vtot, T = (size_t)b->d.Ttot;
+    off[0] = 0;
+    off[1] = off[0] + al256(sizeof(float4) * V);
+    off[2] = off[1] + al256(sizeof(float4) * V);
+    off[3] = off[2] + al256(sizeof(float4) * V);
+    off[4] = off[3] + al256(sizeof(float4) * V);
+    off[5] = off[4] + al256(sizeof(uint32_t) * T);
+}
+lc_status lc_batch_state_size(const lc_batch *b, uint64_t *bytes) {
+    if (!b || !bytes) return fail(LC_ERR_INVALID_ARG, "lc_batch_state_size: bad arguments");
+    size_t off[6];
+    state_layout(b, off);
+    *bytes = off[5] + al256(sizeof(ClothState) * (size_t)b->C);
+    return LC_OK;
+}
+lc_status lc_batch_save_state(lc_batch *b, void *dst, void *stream) {
+    if (!b || !dst) return fail(LC_ERR_INVALID_ARG, "lc_batch_save_state: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t V = (size_t)b->d.Vtot, T = (size_t)b->d.Ttot;
+    size_t off[6];
+    state_layout(b, off);
+    char *p = static_cast<char *>(dst);
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    LC_CUDA(cudaMemcpyAsync(p + off[0], b->d.x, sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(p + off[1], b->d.xp, sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(p + off[2], b->d.v, sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(p + off[3], b->d.vn, sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(p + off[4], b->d.perm, sizeof(uint32_t) * T, k, st));
+    LC_CUDA(cudaMemcpyAsync(p + off[5], b->d.cstate, sizeof(ClothState) * (size_t)b->C, k, st));
+    return LC_OK;
+}
+lc_status lc_batch_load_state(lc_batch *b, const void *src, void *stream) {
+    if (!b || !src) return fail(LC_ERR_INVALID_ARG, "lc_batch_load_state: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t V = (size_t)b->d.Vtot, T = (size_t)b->d.Ttot;
+    size_t off[6];
+    state_layout(b, off);
+    const char *p = static_cast<const char *>(src);
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    LC_CUDA(cudaMemcpyAsync(b->d.x, p + off[0], sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(b->d.xp, p + off[1], sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(b->d.v, p + off[2], sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(b->d.vn, p + off[3], sizeof(float4) * V, k, st));
+    LC_CUDA(cudaMemcpyAsync(b->d.perm, p + off[4], sizeof(uint32_t) * T, k, st));
+    LC_CUDA(cudaMemcpyAsync(b->d.cstate, p + off[5], sizeof(ClothState) * (size_t)b->C, k, st));
+    return LC_OK;
+}
+
+// One step forward (recorded) and its reverse pass; see lc.h.
+lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, float *gk_stretch, float *gk_bend,
+                                void *stream) {
+    if (!b || !gx || !gxp || !gv) return fail(LC_ERR_INVALID_ARG, "lc_batch_adjoint_step: bad arguments");
+    if (!b->opt.adjoint) return fail(LC_ERR_INVALID_ARG, "lc_batch_adjoint_step: batch created without the adjoint option");
+    cudaStream_t st = (cudaStream_t)stream;
+    b->last_stream = st;
+    b->recording = true;
+    const lc_status s = b->enqueue_step(st);
+    b->recording = false;
+    if (s != LC_OK) return s;
+    const int V = b->d.Vtot;
+    launch_adj_unpack(gx, b->adj.gx, V, st);
+    launch_adj_unpack(gxp, b->adj.gxp, V, st);
+    launch_adj_unpack(gv, b->adj.gv, V, st);
+    launch_adjoint(b->d, b->adj, b->adj_a, b->adj_g, b->nvf, b->nee, b->narrow_grid, b->nfixed, gk_stretch, gk_bend, st);
+    launch_adj_pack(b->adj.gx, gx, V, st);
+    launch_adj_pack(b->adj.gxp, gxp, V, st);
+    launch_adj_pack(b->adj.gv, gv, V, st);
+    LC_CUDA(cudaGetLastError());
     return LC_OK;
 }
 

@@ -140,6 +140,25 @@ struct DevPtrs {
     float kpi_gap;            // pi - (float)3.14159265359f, rest-angle offset of the bend term
 };
 
+// Reverse pass of one step (lc_adjoint.cu): the recorded step's tape and the
+// work buffers of the reverse sweep.  Gradient buffers are float4 (w unused).
+struct AdjPtrs {
+    const float4 *tape_x;    // (K+1) x Vtot: solver iterates x^0 (prediction) .. x^K
+    const float4 *tape_xin;  // state x at the start of the step (damping input)
+    const float4 *tape_vb;   // velocity after the global damping (damping input)
+    const int *s_slot;       // 2 per stretch constraint: static CSR entry of (constraint, role)
+    const int *b_slot;       // 4 per bend constraint
+    float4 *slot;            // per static CSR entry: the constraint's contribution to that vertex
+    float4 *dyn;             // per dynamic entry (contact * 4 + vertex)
+    float *fixed;            // 3 per pinned vertex: LRA contributions (block sums + atomics)
+    float4 *u;               // dL/dx^{k+1} / count, per vertex
+    float4 *gx, *gxp, *gv;   // state gradients: after the step on entry, before it on exit
+    double *red;             // 8 per vertex block (partials), then 8 per cloth (totals)
+    int nvblk_red;           // offset of the cloth totals in red
+    int K;                   // solver iterations of the recorded step (max over cloths)
+    int E, B;                // stretch / bend constraints of the batch
+};
+
 // ---------------------------------------------------------------------------
 // float3 algebra in the operation order of Core/CudaUtils.cu:32-276.
 // ---------------------------------------------------------------------------

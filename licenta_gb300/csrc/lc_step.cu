@@ -440,12 +440,16 @@ __global__ void k_integrate(DevPtrs d, const float4 *__restrict__ xs) {
 static inline int nblk(int64_t n, int b = kThreads) { return (int)((n + b - 1) / b); }
 
 void launch_wind(const DevPtrs &d, cudaStream_t st) { k_wind<<<nblk(d.C, 128), 128, 0, st>>>(d); }
-void launch_external(const DevPtrs &d, cudaStream_t st) {
+// save_x / save_v (may be null): copies of the damping inputs (state x and the
+// velocity after the global damping) for the reverse pass.
+void launch_external(const DevPtrs &d, cudaStream_t st, float4 *save_x, float4 *save_v) {
     if (d.nvblk) {
         k_external<<<d.nvblk, kThreads, 0, st>>>(d);
         k_cloth_totals<<<d.C, kThreads, 0, st>>>(d, 0, 7);
         k_damp_moments<<<d.nvblk, kThreads, 0, st>>>(d);
         k_cloth_totals<<<d.C, kThreads, 0, st>>>(d, 7, 9);
+        if (save_x) cudaMemcpyAsync(save_x, d.x, sizeof(float4) * (size_t)d.Vtot, cudaMemcpyDeviceToDevice, st);
+        if (save_v) cudaMemcpyAsync(save_v, d.v, sizeof(float4) * (size_t)d.Vtot, cudaMemcpyDeviceToDevice, st);
         k_damp_apply<<<d.nvblk, kThreads, 0, st>>>(d);
     }
 }

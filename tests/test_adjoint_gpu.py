@@ -1,0 +1,116 @@
+"""The engine's reverse pass (lc_batch_adjoint_step / ClothRollout) against
+the FP64 adjoint of the oracle, whose own gradients are checked by finite
+differences in tests/test_adjoint_cpu.py.
+
+Both sides differentiate the same rollout: the engine in FP32 on its own
+trajectory, the oracle in FP64 on its own; the rollouts are short and the
+comparisons are on the whole gradient vector (relative L2 error), so that
+the FP32 / FP64 difference of the trajectories stays well inside the bound.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from licenta_gb300 import scenes
+from licenta_gb300.adjoint import ClothRollout, DiffCloth
+from oracle.oracle_ffi import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def engine_grads(spec, steps, ks, kb, v0, target, every):
+    cloth = DiffCloth([spec], checkpoint_every=every)
+    ks_t = torch.tensor(ks, dtype=torch.float32, device="cuda", requires_grad=True)
+    kb_t = torch.tensor(kb, dtype=torch.float32, device="cuda", requires_grad=True)
+    x0 = torch.tensor(spec.positions, dtype=torch.float32, device="cuda", requires_grad=True)
+    v0_t = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    out = ClothRollout.apply(cloth, steps, ks_t, kb_t, x0, v0_t)
+    loss = ((out - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    res = dict(loss=float(loss.detach()), ks=ks_t.grad.cpu().numpy(), kb=kb_t.grad.cpu().numpy(),
+               x0=x0.grad.cpu().numpy(), v0=v0_t.grad.cpu().numpy(), final=out.detach().cpu().numpy())
+    cloth.close()
+    return res
+
+
+def oracle_grads(spec, steps, ks, kb, v0, target):
+    o = Oracle([spec], fp64=True)
+    st = o.get_state(0)
+    o.set_state(0, x=st["x"], x_prev=st["x"], v=v0, vn=st["vn"])
+    o.set_stiffness_d(0, ks, kb)
+    o.adj_record(0, steps)
+    xp = o.get_state(0)["x_prev"]
+    z = np.zeros_like(xp)
+    gx, gxp, gv, gks, gkb = o.adj_backward(0, z, 2 * (xp - target), z)
+    o.close()
+    return dict(loss=float(((xp - target) ** 2).sum()), ks=gks, kb=gkb, x0=gx + gxp, v0=gv, final=xp)
+
+
+def case(seed, n, steps, v_scale):
+    spec = scenes.small_cloth(seed=seed, n=n)
+    o = Oracle([spec], fp64=True)
+    _, _, ne, nb = o.sizes(0)
+    o.close()
+    rng = np.random.default_rng(seed)
+    ks = 0.9 + rng.uniform(-0.1, 0.05, ne)
+    kb = 0.9 + rng.uniform(-0.1, 0.05, nb)
+    v0 = rng.normal(scale=v_scale, size=(spec.num_vertices, 3)) * (spec.pinned == 0)[:, None]
+    target = spec.positions + rng.normal(scale=0.05, size=(spec.num_vertices, 3)) - np.array([0.0, 0.2, 0.0])
+    return spec, ks, kb, v0, target
+
+
+def test_engine_adjoint_matches_fp64_adjoint():
+    spec, ks, kb, v0, target = case(1, 12, 10, 0.3)
+    g = engine_grads(spec, 10, ks, kb, v0, target, every=4)
+    r = oracle_grads(spec, 10, ks, kb, v0, target)
+    assert np.abs(g["final"] - r["final"]).max() < 1e-5
+    for k in ("ks", "kb", "v0", "x0"):
+        assert rel_l2(g[k], r[k]) < 2e-3, f"{k}: relative error {rel_l2(g[k], r[k]):.2e}"
+
+
+def test_checkpointing_does_not_change_gradients():
+    spec, ks, kb, v0, target = case(3, 14, 12, 0.2)
+    a = engine_grads(spec, 12, ks, kb, v0, target, every=12)
+    b = engine_grads(spec, 12, ks, kb, v0, target, every=5)
+    for k in ("ks", "kb", "v0", "x0"):
+        assert rel_l2(b[k], a[k]) < 1e-6, k
+
+
+def test_stiffness_recovered_by_gradient_descent():
+    """The differentiable-rollout workload in small: the target comes from a
+    rollout with stiffness 0.7 and wind; starting from 0.9, a few steps of
+    gradient descent on the per-constraint stiffness lower the loss."""
+    spec = scenes.small_cloth(seed=6, n=16)
+    tgt_spec = scenes.small_cloth(seed=6, n=16, stiffness=0.7)
+    scenes.set_constant_wind(tgt_spec.params, (1.5, 0.0, 0.5))
+    steps = 20
+    o = Oracle([tgt_spec], fp64=False)
+    o.step(steps, threads=1)
+    target = torch.tensor(o.get_state(0)["x_prev"], dtype=torch.float32, device="cuda")
+    o.close()
+    cloth = DiffCloth([spec], checkpoint_every=5)
+    ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
+    kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
+    x0 = torch.tensor(spec.positions, device="cuda")
+    v0 = torch.zeros_like(x0)
+    losses = []
+    for _ in range(4):
+        out = ClothRollout.apply(cloth, steps, ks, kb, x0, v0)
+        loss = ((out - target) ** 2).sum()
+        losses.append(float(loss))
+        ks.grad = kb.grad = None
+        loss.backward()
+        with torch.no_grad():
+            for p in (ks, kb):
+                p -= 0.5 * p.grad / (p.grad.abs().max() + 1e-12) * 0.02
+                p.clamp_(0.05, 0.99)
+    cloth.close()
+    assert losses[-1] < losses[0], losses
