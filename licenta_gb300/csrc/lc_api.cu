@@ -605,7 +605,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.nmin, N, "nmin")); LC_TRY(A.alloc(d.nmax, N, "nmax"));
     LC_TRY(A.alloc(d.leaf_tmp_min, T, "leaf_tmp_min")); LC_TRY(A.alloc(d.leaf_tmp_max, T, "leaf_tmp_max"));
     LC_TRY(A.alloc(d.parent, N, "parent")); LC_TRY(A.alloc(d.child, I, "child"));
-    LC_TRY(A.alloc(d.rml, I, "rml")); LC_TRY(A.alloc(d.visit, I, "visit"));
+    LC_TRY(A.alloc(d.rml, I, "rml"));
+    LC_TRY(A.alloc(d.wnode, 4 * std::max<int64_t>(I, 1), "wnode")); LC_TRY(A.alloc(d.visit, I, "visit"));
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));

@@ -88,6 +88,7 @@ struct DevPtrs {
     int2 *child;
     int2 *rml;
     int *visit;
+    float4 *wnode;         // 4 per internal node: {lmin, left} {lmax, rmll} {rmin, right} {rmax, rmlr} (may be null)
     uint32_t *pair_cnt;    // per slot
     uint32_t *pair_off;    // per slot (exclusive scan), + total at [Ttot]
     uint32_t *pair_chunk;  // chunk area: j leaf (local) per entry
@@ -96,7 +97,7 @@ struct DevPtrs {
     uint16_t *pair_mask;   // per pair: bits 0..5 VF, 6..14 EE candidates past the AABB cull
     uint32_t *pair_vf_cnt, *pair_ee_cnt;  // per pair: VF / EE candidate counts
     uint32_t *pair_vf_off, *pair_ee_off;  // per pair: first candidate (exclusive scans), totals at [npairs]
-    unsigned long long *cand, *cand_e;    // VF / EE candidates: pair << 4 | slot
+    int4 *cand, *cand_e;                  // VF / EE candidates: their four vertex ids, in candidate order
     uint64_t cand_cap;                    // per list
     uint32_t *cand_vf, *cand_ee;          // per candidate: CCD hit flags
     uint32_t *cand_vf_off, *cand_ee_off;  // per candidate: output slot (exclusive scans)

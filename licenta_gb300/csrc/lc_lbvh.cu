@@ -364,6 +364,75 @@ __global__ void k_traverse(DevPtrs d) {
     if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
 }
 
+// Wide node records for the traversal: per internal node both children's
+// boxes, with the child ids and rightmost leaves in the w lanes, so that one
+// node visit is one contiguous 64-byte read instead of six dependent ones.
+__global__ void k_pack_nodes(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const ClothDev &cd = d.cloth[d.tcloth[s]];
+    const int k = s - cd.t_off;
+    if (k >= cd.T - 1) return;
+    const int2 ch = d.child[cd.i_off + k], rm = d.rml[cd.i_off + k];
+    const float4 *nmin = d.nmin + cd.n_off, *nmax = d.nmax + cd.n_off;
+    const float4 a = nmin[ch.x], b = nmax[ch.x], c = nmin[ch.y], e = nmax[ch.y];
+    float4 *w = d.wnode + 4 * (size_t)(cd.i_off + k);
+    w[0] = make_float4(a.x, a.y, a.z, __int_as_float(ch.x));
+    w[1] = make_float4(b.x, b.y, b.z, __int_as_float(rm.x));
+    w[2] = make_float4(c.x, c.y, c.z, __int_as_float(ch.y));
+    w[3] = make_float4(e.x, e.y, e.z, __int_as_float(rm.y));
+}
+
+// k_traverse on the wide node records: the same tests in the same order.
+__global__ void k_traverse_wide(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const int c = d.tcloth[s];
+    const ClothDev &cd = d.cloth[c];
+    const int id = s - cd.t_off;
+    const int In = cd.T - 1;
+    if (In <= 0) { d.pair_cnt[s] = 0; return; }
+    const int me = In + id;
+    const int chunk = cd.chunk;
+    uint32_t *out = d.pair_chunk + cd.pc_off + (int64_t)id * chunk;
+    const float4 *W = d.wnode + 4 * (size_t)cd.i_off;
+    const float3 amin = xyz(d.nmin[cd.n_off + me]), amax = xyz(d.nmax[cd.n_off + me]);
+    int stack[kTraverseStack];
+    stack[0] = -1;
+    int top = 1, node = 0, got = 0;
+    uint32_t dropped = 0;
+    const int guard_max = 4 * cd.T + 64;
+    for (int guard = 0; guard < guard_max; ++guard) {
+        const float4 *r = W + 4 * (size_t)node;
+        const float4 l0 = __ldg(r), l1 = __ldg(r + 1), r0 = __ldg(r + 2), r1 = __ldg(r + 3);
+        const int chx = __float_as_int(l0.w), rmx = __float_as_int(l1.w);
+        const int chy = __float_as_int(r0.w), rmy = __float_as_int(r1.w);
+        const bool ol = rmx > me && overlap(amin, amax, xyz(l0), xyz(l1));
+        const bool orr = rmy > me && overlap(amin, amax, xyz(r0), xyz(r1));
+        if (ol && chx >= In) {
+            if (got < chunk) out[got++] = (uint32_t)(chx - In);
+            else ++dropped;
+        }
+        if (orr && chy >= In) {
+            if (got < chunk) out[got++] = (uint32_t)(chy - In);
+            else ++dropped;
+        }
+        const bool tl = ol && chx < In, tr = orr && chy < In;
+        if (!tl && !tr) {
+            node = stack[--top];
+        } else {
+            node = tl ? chx : chy;
+            if (tl && tr) {
+                if (top >= kTraverseStack) { atomicOr(d.err, ERR_STACK); break; }
+                stack[top++] = chy;
+            }
+        }
+        if (top == 0) break;
+    }
+    d.pair_cnt[s] = (uint32_t)got;
+    if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
+}
+
 __global__ void k_pair_compact(DevPtrs d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.Ttot) return;
@@ -391,11 +460,14 @@ __device__ __forceinline__ float triple(float3 x21, float3 x31, float3 x41, floa
 // Physics/CudaCubicSolver.cu:131-153.  The reference evaluates f at both
 // ends every iteration; f(x0) of an iteration is f(x1) of the previous one
 // (same arguments, same bits), so it is carried over instead of recomputed.
-__device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41, float a, float b) {
+// fa, fb: f(a), f(b) as the caller evaluated them (the same arguments, so
+// the same bits as the reference's first-iteration evaluations).
+__device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41, float a, float b,
+                        float fa, float fb) {
     float x0 = a, x1 = b;
-    float f0 = triple(x21, x31, x41, v21, v31, v41, x0);
+    float f0 = fa;
     for (int i = 0; i < 20; ++i) {
-        const float f1 = triple(x21, x31, x41, v21, v31, v41, x1);
+        const float f1 = i == 0 ? fb : triple(x21, x31, x41, v21, v31, v41, x1);
         const float xc = (x0 * f1 - x1 * f0) / (f1 - f0);
         if (fabsf(xc - x1) < kEpsCubic) return xc;
         x0 = x1;
@@ -404,50 +476,6 @@ __device__ float secant(float3 x21, float3 x31, float3 x41, float3 v21, float3 v
     }
     return -15.f;
 }
-// Physics/CudaCubicSolver.cu:5-124.  When only the second root of the
-// derivative lies in [0,1], the reference reads its unset first critical
-// point; its kernels, built and run, behave as if that read returned the
-// first root t1 (outside [0,1]), so [0, t1] is searched: the same here.
-__device__ int coplanarity_times(float3 x1, float3 x2, float3 x3, float3 x4, float3 v1, float3 v2, float3 v3,
-                                 float3 v4, float times[8]) {
-    const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
-    const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
-    const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
-                 x21x31 = cross(x21, x31);
-    const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
-                v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
-                v1x2x3 = dot(v21x31, x41);
-    const float a = v1v2v3, b = x1v2v3 + v1x2v3 + v1v2x3, c = x1x2v3 + x1v2x3 + v1x2x3;
-    const float ad = 3.f * a, bd = 2.f * b;
-    const float disc = 4.f * (b * b - ad * c);
-    const float sq = sqrtf(disc);
-    const float da = 2.f * ad;
-    const float t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
-    float ends[4];
-    int ne = 0;
-    ends[ne++] = 0.f;
-    if (disc >= kEpsCubic) {
-        const bool in1 = between(t1, 0.f, 1.f), in2 = between(t2, 0.f, 1.f);
-        if (in1 || in2) ends[ne++] = t1;
-        if (in1 && in2) ends[ne++] = t2;
-    } else if (fabsf(disc) < kEpsCubic) {
-        if (between(t1, 0.f, 1.f)) ends[ne++] = t1;
-    }
-    ends[ne++] = 1.f;
-    int n = 0;
-    for (int i = 0; i < ne - 1; ++i) {
-        const float ea = ends[i], eb = ends[i + 1];
-        const float fa = triple(x21, x31, x41, v21, v31, v41, ea);
-        const float fb = triple(x21, x31, x41, v21, v31, v41, eb);
-        if (fabsf(fa) < kEpsCubic) times[n++] = ea;
-        if (fa * fb < 0.f) {
-            const float t = secant(x21, x31, x41, v21, v31, v41, ea, eb);
-            if (t != -15.f) times[n++] = t;
-        }
-    }
-    return n;
-}
-
 __device__ __forceinline__ float3 project_on_line(float3 p, float3 e1, float3 e2) {
     const float3 ab = sub(e2, e1), ap = sub(p, e1);
     return add(e1, mul(ab, dot(ap, ab) / dot(ab, ab)));
@@ -531,39 +559,76 @@ __device__ __forceinline__ Box pbox(const DevPtrs &d, int v, float h) {
     return Box{subc(vmin(p, q), h), addc(vmax(p, q), h)};
 }
 
-// CCD of one VF candidate (vertex p against face f1 f2 f3) on x_prev and v:
-// Collision/CudaPrimitiveTests.cu:128-184.
-__device__ bool vf_ccd(const DevPtrs &d, int p, int f1, int f2, int f3, float h, float dt, Wts &w) {
-    float3 x4 = xyz(d.xp[p]), x1 = xyz(d.xp[f1]), x2 = xyz(d.xp[f2]), x3 = xyz(d.xp[f3]);
-    const float3 v4 = xyz(d.v[p]), v1 = xyz(d.v[f1]), v2 = xyz(d.v[f2]), v3 = xyz(d.v[f3]);
-    float times[8];
-    const int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
-    for (int i = 0; i < n; ++i) {
-        const float t = times[i] * dt;
-        x4 = add(x4, mul(v4, t));
-        x1 = add(x1, mul(v1, t));
-        x2 = add(x2, mul(v2, t));
-        x3 = add(x3, mul(v3, t));
-        if (test_vf(x4, x1, x2, x3, h, w)) return true;
+// CCD of one candidate on x_prev and v (Collision/CudaPrimitiveTests.cu:
+// 128-238 with Physics/CudaCubicSolver.cu:5-124).  VF: vertex x4 against the
+// face x1 x2 x3; EE: edges x1 x2 and x3 x4.  The reference first collects
+// every coplanarity time of [0,1] (FindCoplanarityTimes) and then advances the
+// four positions by v t dt for each time in turn, testing after each advance
+// until one test hits.  Computing the times has no side effects, so each time
+// is tested as soon as it is found: the same tests on the same positions, in
+// the same order, and the search stops at the first hit.
+template <bool VF>
+__device__ bool ccd_scan(float3 x1, float3 x2, float3 x3, float3 x4, float3 v1, float3 v2, float3 v3, float3 v4,
+                         float h, float dt, Wts &w) {
+    const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
+    const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
+    const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
+                 x21x31 = cross(x21, x31);
+    const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
+                v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
+                v1x2x3 = dot(v21x31, x41);
+    const float a3 = v1v2v3, b3 = x1v2v3 + v1x2v3 + v1v2x3, c3 = x1x2v3 + x1v2x3 + v1x2x3;
+    const float ad = 3.f * a3, bd = 2.f * b3;
+    const float disc = 4.f * (b3 * b3 - ad * c3);
+    const float sq = sqrtf(disc);
+    const float da = 2.f * ad;
+    const float t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
+    // interval ends 0, [t1], [t2], 1.  When only the second root of the
+    // derivative lies in [0,1], the reference reads its unset first critical
+    // point (Physics/CudaCubicSolver.cu:19-33); its kernels, built and run,
+    // behave as if that read returned t1 (outside [0,1]), so [0, t1] is
+    // searched: the same here.
+    int ncp = 0;
+    if (disc >= kEpsCubic) {
+        const bool in1 = between(t1, 0.f, 1.f), in2 = between(t2, 0.f, 1.f);
+        ncp = (in1 || in2) ? ((in1 && in2) ? 2 : 1) : 0;
+    } else if (fabsf(disc) < kEpsCubic) {
+        ncp = between(t1, 0.f, 1.f) ? 1 : 0;
+    }
+    const float e1 = ncp >= 1 ? t1 : 1.f, e2 = ncp == 2 ? t2 : 1.f;
+    auto hit = [&](float t) {
+        const float tt = t * dt;
+        x1 = add(x1, mul(v1, tt));
+        x2 = add(x2, mul(v2, tt));
+        x3 = add(x3, mul(v3, tt));
+        x4 = add(x4, mul(v4, tt));
+        return VF ? test_vf(x4, x1, x2, x3, h, w) : test_ee(x1, x2, x3, x4, h, w);
+    };
+    float a = 0.f, fa = triple(x21, x31, x41, v21, v31, v41, 0.f);
+#pragma unroll
+    for (int i = 0; i <= 2; ++i) {
+        if (i > ncp) break;
+        const float b = i == ncp ? 1.f : (i == 0 ? e1 : e2);
+        const float fb = triple(x21, x31, x41, v21, v31, v41, b);
+        if (fabsf(fa) < kEpsCubic && hit(a)) return true;
+        if (fa * fb < 0.f) {
+            const float t = secant(x21, x31, x41, v21, v31, v41, a, b, fa, fb);
+            if (t != -15.f && hit(t)) return true;
+        }
+        a = b;
+        fa = fb;
     }
     return false;
 }
 
-// CCD of one EE candidate: Collision/CudaPrimitiveTests.cu:187-238.
+__device__ bool vf_ccd(const DevPtrs &d, int p, int f1, int f2, int f3, float h, float dt, Wts &w) {
+    return ccd_scan<true>(xyz(d.xp[f1]), xyz(d.xp[f2]), xyz(d.xp[f3]), xyz(d.xp[p]), xyz(d.v[f1]), xyz(d.v[f2]),
+                          xyz(d.v[f3]), xyz(d.v[p]), h, dt, w);
+}
+
 __device__ bool ee_ccd(const DevPtrs &d, int e1, int e2, int e3, int e4, float h, float dt, Wts &w) {
-    float3 x1 = xyz(d.xp[e1]), x2 = xyz(d.xp[e2]), x3 = xyz(d.xp[e3]), x4 = xyz(d.xp[e4]);
-    const float3 v1 = xyz(d.v[e1]), v2 = xyz(d.v[e2]), v3 = xyz(d.v[e3]), v4 = xyz(d.v[e4]);
-    float times[8];
-    const int n = coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
-    for (int i = 0; i < n; ++i) {
-        const float t = times[i] * dt;
-        x1 = add(x1, mul(v1, t));
-        x2 = add(x2, mul(v2, t));
-        x3 = add(x3, mul(v3, t));
-        x4 = add(x4, mul(v4, t));
-        if (test_ee(x1, x2, x3, x4, h, w)) return true;
-    }
-    return false;
+    return ccd_scan<false>(xyz(d.xp[e1]), xyz(d.xp[e2]), xyz(d.xp[e3]), xyz(d.xp[e4]), xyz(d.v[e1]), xyz(d.v[e2]),
+                           xyz(d.v[e3]), xyz(d.v[e4]), h, dt, w);
 }
 
 // EE slot s: edge (s%3) of A x edge (s/3) of B; edge k of a triangle is
@@ -659,21 +724,27 @@ __global__ void k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) 
 // Stage 2: one (pair, slot) entry per surviving candidate, VF and EE in
 // separate lists, each in pair-then-slot order — the order of the
 // reference's compactions.
+// Stage 2: the surviving candidates written in the reference's order (pair,
+// then slot) as the four vertex ids the CCD needs.
 __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) {
     const uint32_t n = *npairs;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         uint32_t m = d.pair_mask[p];
+        if (!m) continue;
         uint64_t ov = d.pair_vf_off[p], oe = d.pair_ee_off[p];
+        const uint2 pr = d.pairs[p];
+        const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+        const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
         while (m) {
             const int s = __ffs(m) - 1;
             m &= m - 1;
-            const unsigned long long e = ((unsigned long long)p << 4) | (unsigned)s;
+            const int4 ids = candidate_ids(vid, s);
             if (s < 6) {
-                if (ov < d.cand_cap) d.cand[ov] = e;
+                if (ov < d.cand_cap) d.cand[ov] = ids;
                 else atomicOr(d.err, ERR_CAND_OVERFLOW);
                 ++ov;
             } else {
-                if (oe < d.cand_cap) d.cand_e[oe] = e;
+                if (oe < d.cand_cap) d.cand_e[oe] = ids;
                 else atomicOr(d.err, ERR_CAND_OVERFLOW);
                 ++oe;
             }
@@ -681,16 +752,11 @@ __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) 
     }
 }
 
-__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long long q, int4 &ids, Wts &w) {
-    const uint32_t p = (uint32_t)(q >> 4);
-    const int s = (int)(q & 15u);
-    const uint2 pr = d.pairs[p];
-    const ClothDev &cd = d.cloth[d.tcloth[pr.x]];
-    const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
-    const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
-    ids = candidate_ids(vid, s);
-    return s < 6 ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
-                 : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
+template <bool VF>
+__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, const int4 ids, Wts &w) {
+    const ClothDev &cd = d.cloth[d.vcloth[ids.x]];
+    return VF ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
+              : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
 }
 
 // Stage 3: CCD of every candidate of one kind, one per thread
@@ -698,12 +764,11 @@ __device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, unsigned long lo
 template <bool VF>
 __global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
-    const unsigned long long *list = VF ? d.cand : d.cand_e;
+    const int4 *list = VF ? d.cand : d.cand_e;
     uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        int4 ids;
         Wts w;
-        hit[q] = candidate_ccd(d, list[q], ids, w) ? 1u : 0u;
+        hit[q] = candidate_ccd<VF>(d, list[q], w) ? 1u : 0u;
     }
 }
 
@@ -712,14 +777,14 @@ __global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
 template <bool VF>
 __global__ void k_ccd_write(DevPtrs d, const uint32_t *__restrict__ ncand) {
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
-    const unsigned long long *list = VF ? d.cand : d.cand_e;
+    const int4 *list = VF ? d.cand : d.cand_e;
     const uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
     const uint32_t *off = VF ? d.cand_vf_off : d.cand_ee_off;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         if (!hit[q]) continue;
-        int4 ids;
+        const int4 ids = list[q];
         Wts w;
-        candidate_ccd(d, list[q], ids, w);
+        candidate_ccd<VF>(d, ids, w);
         const uint32_t o = off[q];
         if (VF) {
             if (o < d.vf_cap) { d.vf_v[o] = ids; d.vf_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
@@ -782,7 +847,13 @@ void launch_refit(const DevPtrs &d, cudaStream_t st) {
     if (d.Ttot) k_refit<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
 }
 void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
-    if (d.Ttot) k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+    if (!d.Ttot) return;
+    if (d.wnode) {
+        k_pack_nodes<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+        k_traverse_wide<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+    } else {
+        k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+    }
 }
 void launch_pair_compact(const DevPtrs &d, cudaStream_t st) {
     if (d.Ttot) k_pair_compact<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
