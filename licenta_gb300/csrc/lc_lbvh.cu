@@ -433,17 +433,39 @@ __global__ void k_traverse_wide(DevPtrs d) {
     if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
 }
 
+// Order-preserving compaction of the per-leaf chunks into the pair list:
+// each warp takes 32 consecutive leaves and copies them one leaf at a time
+// with all 32 lanes, so reads and writes are coalesced.
 __global__ void k_pair_compact(DevPtrs d) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.Ttot) return;
-    const uint32_t n = d.pair_cnt[s];
-    if (!n) return;
-    const int c = d.tcloth[s];
-    const ClothDev &cd = d.cloth[c];
-    const int id = s - cd.t_off;
-    const uint32_t *src = d.pair_chunk + cd.pc_off + (int64_t)id * cd.chunk;
-    const uint32_t o = d.pair_off[s];
-    for (uint32_t k = 0; k < n; ++k) d.pairs[o + k] = make_uint2((uint32_t)s, (uint32_t)cd.t_off + src[k]);
+    const int lane = threadIdx.x & 31;
+    const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp0 * 32; base < d.Ttot; base += nwarps * 32) {
+        const int s = base + lane;
+        uint32_t n = 0, o = 0;
+        int t0 = 0;
+        const uint32_t *src = nullptr;
+        if (s < d.Ttot) {
+            n = d.pair_cnt[s];
+            if (n) {
+                const ClothDev &cd = d.cloth[d.tcloth[s]];
+                o = d.pair_off[s];
+                t0 = cd.t_off;
+                src = d.pair_chunk + cd.pc_off + (int64_t)(s - cd.t_off) * cd.chunk;
+            }
+        }
+        unsigned live = __ballot_sync(0xffffffffu, n != 0);
+        while (live) {
+            const int j = __ffs(live) - 1;
+            live &= live - 1;
+            const uint32_t nj = __shfl_sync(0xffffffffu, n, j), oj = __shfl_sync(0xffffffffu, o, j);
+            const int tj = __shfl_sync(0xffffffffu, t0, j);
+            const uint32_t *sj = reinterpret_cast<const uint32_t *>(
+                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), j));
+            for (uint32_t k = lane; k < nj; k += 32)
+                d.pairs[oj + k] = make_uint2((uint32_t)(base + j), (uint32_t)tj + sj[k]);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -772,6 +794,138 @@ __global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
     }
 }
 
+// Stage 3 with the secant solves spread over the warp.  Each warp takes 32
+// candidates at a time: (1) every lane sets up its candidate's cubic, finds
+// the interval ends and evaluates f there, and queues the intervals whose
+// ends differ in sign; (2) the warp runs the queued secant solves, one per
+// lane; (3) every lane tests its roots in interval order with the cumulative
+// advance and stops at the first hit.  Each piece is the arithmetic of
+// ccd_scan on the same operands, so the decisions are the same bits; only
+// the assignment of work to lanes differs (and secants after a hit are
+// computed and not used).
+constexpr int kCcdWarps = 8;
+struct CcdJob { float a, b, fa, fb; };
+
+template <bool VF>
+__global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const uint32_t *__restrict__ ncand) {
+    __shared__ float geom[kCcdWarps][18][33];     // x21 x31 x41 v21 v31 v41 per lane (padded)
+    __shared__ CcdJob jobs[kCcdWarps][96];
+    __shared__ uint8_t job_owner[kCcdWarps][96];  // lane << 2 | interval
+    __shared__ float roots[kCcdWarps][3][32];
+    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const int4 *list = VF ? d.cand : d.cand_e;
+    uint32_t *hitout = VF ? d.cand_vf : d.cand_ee;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    const uint32_t nwarps = gridDim.x * kCcdWarps;
+    for (uint32_t base = (blockIdx.x * kCcdWarps + w) * 32u; base < n; base += nwarps * 32u) {
+        const uint32_t q = base + lane;
+        const bool valid = q < n;
+        int4 ids = make_int4(0, 0, 0, 0);
+        int ncp = -1;
+        float e1 = 1.f, e2 = 1.f;
+        unsigned imm = 0, sec = 0;
+        float fv[4] = {0.f, 0.f, 0.f, 0.f};
+        if (valid) {
+            ids = list[q];
+            // VF: face ids.y ids.z ids.w, vertex ids.x (x4); EE: x1..x4 = ids
+            const int i1 = VF ? ids.y : ids.x, i2 = VF ? ids.z : ids.y, i3 = VF ? ids.w : ids.z, i4 = VF ? ids.x : ids.w;
+            const float3 x1 = xyz(d.xp[i1]), x2 = xyz(d.xp[i2]), x3 = xyz(d.xp[i3]), x4 = xyz(d.xp[i4]);
+            const float3 v1 = xyz(d.v[i1]), v2 = xyz(d.v[i2]), v3 = xyz(d.v[i3]), v4 = xyz(d.v[i4]);
+            const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
+            const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
+            const float g[18] = {x21.x, x21.y, x21.z, x31.x, x31.y, x31.z, x41.x, x41.y, x41.z,
+                                 v21.x, v21.y, v21.z, v31.x, v31.y, v31.z, v41.x, v41.y, v41.z};
+#pragma unroll
+            for (int k = 0; k < 18; ++k) geom[w][k][lane] = g[k];
+            const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
+                         x21x31 = cross(x21, x31);
+            const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
+                        v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
+                        v1x2x3 = dot(v21x31, x41);
+            const float a3 = v1v2v3, b3 = x1v2v3 + v1x2v3 + v1v2x3, c3 = x1x2v3 + x1v2x3 + v1x2x3;
+            const float ad = 3.f * a3, bd = 2.f * b3;
+            const float disc = 4.f * (b3 * b3 - ad * c3);
+            const float sq = sqrtf(disc);
+            const float da = 2.f * ad;
+            const float t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
+            ncp = 0;
+            if (disc >= kEpsCubic) {
+                const bool in1 = between(t1, 0.f, 1.f), in2 = between(t2, 0.f, 1.f);
+                ncp = (in1 || in2) ? ((in1 && in2) ? 2 : 1) : 0;
+            } else if (fabsf(disc) < kEpsCubic) {
+                ncp = between(t1, 0.f, 1.f) ? 1 : 0;
+            }
+            e1 = ncp >= 1 ? t1 : 1.f;
+            e2 = ncp == 2 ? t2 : 1.f;
+            fv[0] = triple(x21, x31, x41, v21, v31, v41, 0.f);
+#pragma unroll
+            for (int i = 0; i <= 2; ++i) {
+                if (i > ncp) break;
+                const float b = i == ncp ? 1.f : (i == 0 ? e1 : e2);
+                fv[i + 1] = triple(x21, x31, x41, v21, v31, v41, b);
+                if (fabsf(fv[i]) < kEpsCubic) imm |= 1u << i;
+                if (fv[i] * fv[i + 1] < 0.f) sec |= 1u << i;
+            }
+        }
+        // queue the secant solves of the warp
+        int njobs = 0;
+#pragma unroll
+        for (int i = 0; i <= 2; ++i) {
+            const bool want = (sec >> i) & 1u;
+            const unsigned m = __ballot_sync(full, want);
+            if (want) {
+                const int pos = njobs + __popc(m & ((1u << lane) - 1u));
+                const float a = i == 0 ? 0.f : (i == 1 ? e1 : e2);
+                const float b = i == ncp ? 1.f : (i == 0 ? e1 : e2);
+                jobs[w][pos] = CcdJob{a, b, fv[i], fv[i + 1]};
+                job_owner[w][pos] = (uint8_t)(lane << 2 | i);
+            }
+            njobs += __popc(m);
+        }
+        __syncwarp();
+        for (int j = lane; j < njobs; j += 32) {
+            const CcdJob jb = jobs[w][j];
+            const int own = job_owner[w][j] >> 2, iv = job_owner[w][j] & 3;
+            const float3 x21 = f3(geom[w][0][own], geom[w][1][own], geom[w][2][own]);
+            const float3 x31 = f3(geom[w][3][own], geom[w][4][own], geom[w][5][own]);
+            const float3 x41 = f3(geom[w][6][own], geom[w][7][own], geom[w][8][own]);
+            const float3 v21 = f3(geom[w][9][own], geom[w][10][own], geom[w][11][own]);
+            const float3 v31 = f3(geom[w][12][own], geom[w][13][own], geom[w][14][own]);
+            const float3 v41 = f3(geom[w][15][own], geom[w][16][own], geom[w][17][own]);
+            roots[w][iv][own] = secant(x21, x31, x41, v21, v31, v41, jb.a, jb.b, jb.fa, jb.fb);
+        }
+        __syncwarp();
+        if (valid) {
+            const ClothDev &cd = d.cloth[d.vcloth[ids.x]];
+            const int i1 = VF ? ids.y : ids.x, i2 = VF ? ids.z : ids.y, i3 = VF ? ids.w : ids.z, i4 = VF ? ids.x : ids.w;
+            float3 x1 = xyz(d.xp[i1]), x2 = xyz(d.xp[i2]), x3 = xyz(d.xp[i3]), x4 = xyz(d.xp[i4]);
+            const float3 v1 = xyz(d.v[i1]), v2 = xyz(d.v[i2]), v3 = xyz(d.v[i3]), v4 = xyz(d.v[i4]);
+            const float h = cd.h, dt = cd.dt;
+            Wts wt;
+            bool found = false;
+            auto hit = [&](float t) {
+                const float tt = t * dt;
+                x1 = add(x1, mul(v1, tt));
+                x2 = add(x2, mul(v2, tt));
+                x3 = add(x3, mul(v3, tt));
+                x4 = add(x4, mul(v4, tt));
+                return VF ? test_vf(x4, x1, x2, x3, h, wt) : test_ee(x1, x2, x3, x4, h, wt);
+            };
+            for (int i = 0; i <= ncp && !found; ++i) {
+                const float a = i == 0 ? 0.f : (i == 1 ? e1 : e2);
+                if (((imm >> i) & 1u) && hit(a)) { found = true; break; }
+                if ((sec >> i) & 1u) {
+                    const float t = roots[w][i][lane];
+                    if (t != -15.f && hit(t)) { found = true; break; }
+                }
+            }
+            hitout[q] = found ? 1u : 0u;
+        }
+        __syncwarp();
+    }
+}
+
 // Stage 4: contacts written in candidate order; the CCD of the few hits is
 // evaluated again for their weights.
 template <bool VF>
@@ -856,15 +1010,15 @@ void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
     }
 }
 void launch_pair_compact(const DevPtrs &d, cudaStream_t st) {
-    if (d.Ttot) k_pair_compact<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+    if (d.Ttot) k_pair_compact<<<nblk(d.Ttot), kThreads, 0, st>>>(d);  // one warp per 32 leaves
 }
 void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv, const uint32_t *nce, int grid,
                    int stage, cudaStream_t st) {
     if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 1) k_narrow_expand<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 2) {
-        k_ccd<true><<<grid, kThreads, 0, st>>>(d, ncv);
-        k_ccd<false><<<grid, kThreads, 0, st>>>(d, nce);
+        k_ccd_warp<true><<<grid, kCcdWarps * 32, 0, st>>>(d, ncv);
+        k_ccd_warp<false><<<grid, kCcdWarps * 32, 0, st>>>(d, nce);
     } else if (stage == 3) {
         k_ccd_write<true><<<grid, kThreads, 0, st>>>(d, ncv);
         k_ccd_write<false><<<grid, kThreads, 0, st>>>(d, nce);
