@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-lbvh", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cloths", type=int, default=NCLOTH,
                     help="cloths per GPU (the workload has 256; fewer only for small profiling cases)")
     return ap.parse_args()
@@ -224,6 +226,52 @@ def adjoint_timing(seed: int) -> dict:
             "what": "backward = segment re-run from checkpoints + recorded step + reverse pass, per step"}
 
 
+def lbvh_timing(seed: int, count: int = 1_000_000) -> dict:
+    """The LBVH-only microbenchmark: 1M random triangles (first vertex uniform
+    in the unit cube, two edges of length U[1e-3, 5e-3]), their boxes resident
+    on the device; one build = Morton codes + stable 63-bit radix sort + Karras
+    hierarchy + refit (lc_lbvh_build), one query = traversal + compaction
+    (lc_lbvh_pairs).  CUDA events on the launching stream; the inputs (24 MB
+    of boxes) and the hierarchy (~150 MB) exceed nothing, so L2 is flushed
+    between timed builds by a 256 MB write."""
+    import torch
+    from licenta_gb300 import Lbvh, scenes
+    lo, hi = scenes.random_triangle_boxes(count, seed=seed)
+    lo_t, hi_t = torch.from_numpy(lo).cuda(), torch.from_numpy(hi).cuda()
+    h = Lbvh(count, chunk_size=64)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        h.build(lo_t.data_ptr(), hi_t.data_ptr(), count, stream)
+    torch.cuda.synchronize()
+    b_ms, q_ms = [], []
+    npairs = 0
+    for _ in range(10):
+        flush.fill_(1.0)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        h.build(lo_t.data_ptr(), hi_t.data_ptr(), count, stream)
+        e[1].record()
+        npairs = h.pairs(None, 0, stream)
+        e[2].record()
+        torch.cuda.synchronize()
+        b_ms.append(e[0].elapsed_time(e[1]))
+        q_ms.append(e[1].elapsed_time(e[2]))
+    h.close()
+    build = float(np.median(b_ms))
+    # algorithmic bytes of one build: boxes read + key/slot written (32 T),
+    # 8 sort passes of (key, payload) read + written (8 x 24 T), hierarchy
+    # written (20 T: children, parents), refit (56 T: node boxes read/written)
+    alg = (32 + 8 * 24 + 20 + 56) * count
+    peak, kind = measured_peak_gbs()
+    return {"workload": f"LBVH build over {count} random triangles (63-bit Morton)", "builds_per_s": 1000.0 / build,
+            "build_ms": build, "query_ms": float(np.median(q_ms)), "pairs": int(npairs),
+            "roofline": {"bound": "hbm", "achieved": alg / (build / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (build / 1000.0) / 1e9 / peak, "algorithmic_bytes_per_build": alg,
+                         "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({kind})"},
+            "l2": "flushed by a 256 MB write before each timed build"}
+
+
 def cpu_baseline(specs, seed: int, cloths: int = 64, steps: int = 2) -> dict:
     """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
     cloths on every host core, on a seeded sample of the workload."""
@@ -297,6 +345,16 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.Stream()
     batch.step(args.warmup, stream)
     batch.sync()
+    tuning = None
+    if not args.no_autotune:
+        # launch shapes picked by the project's autotuner on this state (each
+        # candidate timed from the same saved state; the state is restored)
+        from licenta_gb300 import autotune
+        with torch.cuda.stream(stream):
+            tuned = autotune.autotune(batch, steps=2, warmup=1, cache=None,
+                                      space={"traverse_block": (64, 128, 256), "jacobi_block": (256,),
+                                             "narrow_blocks_per_sm": (4, 8, 16), "solver_variant": (1, 3)})
+        tuning = {"config": tuned["config"], "candidates": len(tuned["tried"])}
 
     # ---- device-timed region ------------------------------------------------
     clocks = ClockSampler(local)
@@ -378,6 +436,9 @@ def run_ours(args, world, rank, local):
     adj = None
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_timing(args.seed)
+    lbvh = None
+    if rank == 0 and not args.no_lbvh:
+        lbvh = lbvh_timing(args.seed)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -401,6 +462,8 @@ def run_ours(args, world, rank, local):
                     "sizes": alg["_sizes"]},
         "plain": plain,
         "adjoint": adj,
+        "lbvh": lbvh,
+        "tuning": tuning,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

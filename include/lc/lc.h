@@ -250,6 +250,20 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t cloth, int32_t what, void *dst
  * them silently, Collision/CudaBVH.cu:69-92). */
 lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]);
 
+/* ---- launch tuning (no counterpart in the reference) ---------------------
+ * Block and grid sizes of the batch's kernels and the Jacobi solver variant;
+ * picked by licenta_gb300/autotune.py.  Block and grid sizes never change
+ * results; the solver variant sums the Jacobi corrections differently (all
+ * variants stay within the FP64 tolerance). */
+typedef struct lc_tuning {
+    int32_t traverse_block;        /* threads per block of the BVH traversal (32..1024, multiple of 32) */
+    int32_t jacobi_block;          /* threads per block of the global-memory Jacobi kernel */
+    int32_t narrow_blocks_per_sm;  /* grid of the narrowphase and contact kernels, in blocks per SM */
+    int32_t solver_variant;        /* 1, 2 or 3 as lc_batch_options.solver_variant (2, 3 need every cloth on chip) */
+} lc_tuning;
+lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t);
+lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t);
+
 /* ---- differentiation (no counterpart in the reference) -------------------
  * Per-constraint stiffness of the whole batch in the global constraint order
  * (cloth 0 first; lc_batch_constraint_counts gives each cloth's share), host

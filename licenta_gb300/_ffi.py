@@ -60,6 +60,11 @@ class BatchOptions(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("traverse_block", C.c_int32), ("jacobi_block", C.c_int32), ("narrow_blocks_per_sm", C.c_int32),
+                ("solver_variant", C.c_int32)]
+
+
 class Profile(C.Structure):
     _fields_ = [("phase_ms", C.c_float * 7), ("jacobi_ms", C.c_float), ("traverse_ms", C.c_float),
                 ("narrow_ms", C.c_float), ("sort_ms", C.c_float), ("step_ms", C.c_float),
@@ -82,6 +87,8 @@ SIGNATURES = {
     "lc_default_options": (None, [C.POINTER(BatchOptions)]),
     "lc_batch_create": (C.c_int, [C.POINTER(ClothDesc), C.c_int32, C.POINTER(BatchOptions), C.POINTER(VP)]),
     "lc_batch_set_constraint_stiffness": (C.c_int, [VP, VP, VP, C.c_int32]),
+    "lc_batch_get_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
+    "lc_batch_set_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
     "lc_batch_state_size": (C.c_int, [VP, C.POINTER(C.c_uint64)]),
     "lc_batch_save_state": (C.c_int, [VP, VP, VP]),
     "lc_batch_load_state": (C.c_int, [VP, VP, VP]),

@@ -998,6 +998,41 @@ lc_status lc_batch_cloth_sizes(const lc_batch *b, int32_t c, int32_t *nv, int32_
     return LC_OK;
 }
 
+// Launch shapes (results do not depend on them, except solver_variant which
+// picks a different summation of the Jacobi corrections).
+lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t) {
+    if (!b || !t) return fail(LC_ERR_INVALID_ARG, "lc_batch_get_tuning: bad arguments");
+    t->traverse_block = b->traverse_block;
+    t->jacobi_block = b->jacobi_block;
+    t->narrow_blocks_per_sm = b->narrow_grid / sm_count();
+    t->solver_variant = b->use_cluster ? (b->cluster_scatter ? 3 : 2) : 1;
+    return LC_OK;
+}
+
+lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
+    if (!b || !t) return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: bad arguments");
+    auto ok_block = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
+    if (!ok_block(t->traverse_block) || !ok_block(t->jacobi_block) || t->narrow_blocks_per_sm < 1 ||
+        t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3)
+        return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: value out of range");
+    if (b->opt.adjoint && t->solver_variant != 1)
+        return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_tuning: an adjoint batch keeps solver variant 1");
+    LC_CUDA(cudaDeviceSynchronize());
+    b->traverse_block = t->traverse_block;
+    b->jacobi_block = t->jacobi_block;
+    b->narrow_grid = sm_count() * t->narrow_blocks_per_sm;
+    const int prev = b->opt.solver_variant;
+    b->opt.solver_variant = t->solver_variant;
+    const lc_status s = b->setup_cluster();
+    if (s != LC_OK) {
+        b->opt.solver_variant = prev;
+        b->setup_cluster();
+        return s;
+    }
+    b->invalidate_graph();
+    return LC_OK;
+}
+
 lc_status lc_batch_constraint_counts(const lc_batch *b, int32_t c, int32_t *ns, int32_t *nb) {
     if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
     if (ns) *ns = b->s_count[c];

@@ -262,9 +262,11 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
 // Shared memory per vertex: x (16) + 3 x s64 (24) + count (4) + ground (4) +
 // LRA flags (1).
 // ---------------------------------------------------------------------------
-constexpr int kScatterBytesPerVertex = 49;
-constexpr float kFix = 4294967296.f;           // 2^32
-constexpr float kFixInv = 1.f / 4294967296.f;  // exact power of two
+// Correction sums in 32-bit fixed point: 2^25 per metre, i.e. 3e-8 m steps
+// (finer than a float's spacing at 1 m) and +-64 m of range.
+constexpr int kScatterBytesPerVertex = 37;
+constexpr float kFix = 33554432.f;           // 2^25
+constexpr float kFixInv = 1.f / 33554432.f;  // exact power of two
 
 template <int CS>
 __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevPtrs d, ClusterArgs a) {
@@ -280,9 +282,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevP
     const int cap = a.chunk_cap;
     extern __shared__ float4 smem4[];
     float4 *xs = smem4;
-    long long *ax = reinterpret_cast<long long *>(xs + cap);
-    long long *ay = ax + cap;
-    long long *az = ay + cap;
+    int *ax = reinterpret_cast<int *>(xs + cap);
+    int *ay = ax + cap;
+    int *az = ay + cap;
     uint32_t *cnt = reinterpret_cast<uint32_t *>(az + cap);
     float *gq = reinterpret_cast<float *>(cnt + cap);
     uint8_t *lra = reinterpret_cast<uint8_t *>(gq + cap);
@@ -296,12 +298,12 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevP
     auto add_corr = [&](int li, float3 v, bool count) {
         const int o = owner(li);
         const int k = li - o * chunk;
-        long long *px = o == r ? ax : cluster.map_shared_rank(ax, o);
-        long long *py = o == r ? ay : cluster.map_shared_rank(ay, o);
-        long long *pz = o == r ? az : cluster.map_shared_rank(az, o);
-        atomicAdd(reinterpret_cast<unsigned long long *>(px + k), (unsigned long long)__float2ll_rn(v.x * kFix));
-        atomicAdd(reinterpret_cast<unsigned long long *>(py + k), (unsigned long long)__float2ll_rn(v.y * kFix));
-        atomicAdd(reinterpret_cast<unsigned long long *>(pz + k), (unsigned long long)__float2ll_rn(v.z * kFix));
+        int *px = o == r ? ax : cluster.map_shared_rank(ax, o);
+        int *py = o == r ? ay : cluster.map_shared_rank(ay, o);
+        int *pz = o == r ? az : cluster.map_shared_rank(az, o);
+        atomicAdd(px + k, __float2int_rn(v.x * kFix));
+        atomicAdd(py + k, __float2int_rn(v.y * kFix));
+        atomicAdd(pz + k, __float2int_rn(v.z * kFix));
         if (count) atomicAdd(o == r ? cnt + k : cluster.map_shared_rank(cnt, o) + k, 1u);
     };
     const float qnan = __int_as_float(0x7fc00000);
@@ -429,7 +431,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevP
             const float cv = x4.y - gq[i];
             const bool ground = cv < 0.f;
             if (ground) {
-                atomicAdd(reinterpret_cast<unsigned long long *>(ay + i), (unsigned long long)__float2ll_rn(-cv * kFix));
+                atomicAdd(ay + i, __float2int_rn(-cv * kFix));
                 atomicAdd(cnt + i, 1u);
             }
             if (d.dbg_ground_it) {
@@ -453,9 +455,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevP
             const int g = vo + lo + i;
             const float n = (float)(__ldg(&d.soff[g + 1]) - __ldg(&d.soff[g]) + (int)cnt[i]);
             float4 x4 = xs[i];
-            x4.x += (__ll2float_rn(ax[i]) * kFixInv) / n;
-            x4.y += (__ll2float_rn(ay[i]) * kFixInv) / n;
-            x4.z += (__ll2float_rn(az[i]) * kFixInv) / n;
+            x4.x += (__int2float_rn(ax[i]) * kFixInv) / n;
+            x4.y += (__int2float_rn(ay[i]) * kFixInv) / n;
+            x4.z += (__int2float_rn(az[i]) * kFixInv) / n;
             xs[i] = x4;
             ax[i] = ay[i] = az[i] = 0;
             cnt[i] = 0;
