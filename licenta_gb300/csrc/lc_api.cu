@@ -401,13 +401,17 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 3, st);  // write contacts
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 4, st);  // per-cloth ranges
     LC_PHASE(5);
-    // 6. PBD Solver (+ 7. integration fused on the cluster path)
-    LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
-    LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
-    launch_dyn(d, nvf, nee, narrow_grid, 0, st);
-    scan_u32(d.dyn_cnt, d.dyn_off, nullptr, (uint32_t)d.Vtot, (uint32_t)d.Vtot, d.scan_tmp, nullptr, nullptr, st);
-    launch_dyn(d, nvf, nee, narrow_grid, 1, st);
-    launch_dyn(d, nvf, nee, narrow_grid, 2, st);
+    // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
+    // per-vertex contact CSR feeds the gather solvers; the scatter solver
+    // walks the cloth's contact ranges instead.
+    if (!(use_cluster && cluster_scatter)) {
+        LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
+        LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
+        launch_dyn(d, nvf, nee, narrow_grid, 0, st);
+        scan_u32(d.dyn_cnt, d.dyn_off, nullptr, (uint32_t)d.Vtot, (uint32_t)d.Vtot, d.scan_tmp, nullptr, nullptr, st);
+        launch_dyn(d, nvf, nee, narrow_grid, 1, st);
+        launch_dyn(d, nvf, nee, narrow_grid, 2, st);
+    }
     if (use_cluster) {
         LC_KEV(0);
         LC_TRY(enqueue_cluster_solver(this, st));
@@ -622,6 +626,9 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.crange, n, "contact ranges"));
     LC_TRY(A.alloc(d.vf_v, vf_cap, "vf_v")); LC_TRY(A.alloc(d.vf_w, vf_cap, "vf_w"));
     LC_TRY(A.alloc(d.ee_v, ee_cap, "ee_v")); LC_TRY(A.alloc(d.ee_w, ee_cap, "ee_w"));
+    LC_TRY(A.alloc(d.hit_q[0], vf_cap, "hit_q_vf")); LC_TRY(A.alloc(d.hit_w[0], vf_cap, "hit_w_vf"));
+    LC_TRY(A.alloc(d.hit_q[1], ee_cap, "hit_q_ee")); LC_TRY(A.alloc(d.hit_w[1], ee_cap, "hit_w_ee"));
+    LC_TRY(A.alloc(d.hit_n, 2, "hit_n"));
     LC_TRY(A.alloc(d.dyn_cnt, V, "dyn_cnt")); LC_TRY(A.alloc(d.dyn_off, V + 1, "dyn_off"));
     LC_TRY(A.alloc(d.dyn_cur, V, "dyn_cur")); LC_TRY(A.alloc(d.dyn_ent, d.dyn_cap, "dyn_ent"));
     int *soff; uint32_t *sent; int2 *sids; float2 *spar; int4 *bids; float *bkp;

@@ -100,6 +100,9 @@ struct DevPtrs {
     int4 *cand, *cand_e;                  // VF / EE candidates: their four vertex ids, in candidate order
     uint64_t cand_cap;                    // per list
     uint32_t *cand_vf, *cand_ee;          // per candidate: CCD hit flags
+    uint32_t *hit_q[2];                   // VF / EE hits in any order: candidate index ...
+    float4 *hit_w[2];                     // ... and contact weights (capacity vf_cap / ee_cap)
+    uint32_t *hit_n;                      // [2] hit counts of the step
     uint32_t *cand_vf_off, *cand_ee_off;  // per candidate: output slot (exclusive scans)
     uint4 *crange;         // per cloth: [vf0, vf1) and [ee0, ee1) contact ranges
     int4 *vf_v; float4 *vf_w;   // VF contacts (ids, weights)

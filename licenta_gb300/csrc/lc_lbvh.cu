@@ -581,78 +581,6 @@ __device__ __forceinline__ Box pbox(const DevPtrs &d, int v, float h) {
     return Box{subc(vmin(p, q), h), addc(vmax(p, q), h)};
 }
 
-// CCD of one candidate on x_prev and v (Collision/CudaPrimitiveTests.cu:
-// 128-238 with Physics/CudaCubicSolver.cu:5-124).  VF: vertex x4 against the
-// face x1 x2 x3; EE: edges x1 x2 and x3 x4.  The reference first collects
-// every coplanarity time of [0,1] (FindCoplanarityTimes) and then advances the
-// four positions by v t dt for each time in turn, testing after each advance
-// until one test hits.  Computing the times has no side effects, so each time
-// is tested as soon as it is found: the same tests on the same positions, in
-// the same order, and the search stops at the first hit.
-template <bool VF>
-__device__ bool ccd_scan(float3 x1, float3 x2, float3 x3, float3 x4, float3 v1, float3 v2, float3 v3, float3 v4,
-                         float h, float dt, Wts &w) {
-    const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
-    const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
-    const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
-                 x21x31 = cross(x21, x31);
-    const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
-                v1v2x3 = dot(v21v31, x41), x1x2v3 = dot(x21x31, v41), x1v2x3 = dot(x21v31, x41),
-                v1x2x3 = dot(v21x31, x41);
-    const float a3 = v1v2v3, b3 = x1v2v3 + v1x2v3 + v1v2x3, c3 = x1x2v3 + x1v2x3 + v1x2x3;
-    const float ad = 3.f * a3, bd = 2.f * b3;
-    const float disc = 4.f * (b3 * b3 - ad * c3);
-    const float sq = sqrtf(disc);
-    const float da = 2.f * ad;
-    const float t1 = (-bd + sq) / da, t2 = (-bd - sq) / da;
-    // interval ends 0, [t1], [t2], 1.  When only the second root of the
-    // derivative lies in [0,1], the reference reads its unset first critical
-    // point (Physics/CudaCubicSolver.cu:19-33); its kernels, built and run,
-    // behave as if that read returned t1 (outside [0,1]), so [0, t1] is
-    // searched: the same here.
-    int ncp = 0;
-    if (disc >= kEpsCubic) {
-        const bool in1 = between(t1, 0.f, 1.f), in2 = between(t2, 0.f, 1.f);
-        ncp = (in1 || in2) ? ((in1 && in2) ? 2 : 1) : 0;
-    } else if (fabsf(disc) < kEpsCubic) {
-        ncp = between(t1, 0.f, 1.f) ? 1 : 0;
-    }
-    const float e1 = ncp >= 1 ? t1 : 1.f, e2 = ncp == 2 ? t2 : 1.f;
-    auto hit = [&](float t) {
-        const float tt = t * dt;
-        x1 = add(x1, mul(v1, tt));
-        x2 = add(x2, mul(v2, tt));
-        x3 = add(x3, mul(v3, tt));
-        x4 = add(x4, mul(v4, tt));
-        return VF ? test_vf(x4, x1, x2, x3, h, w) : test_ee(x1, x2, x3, x4, h, w);
-    };
-    float a = 0.f, fa = triple(x21, x31, x41, v21, v31, v41, 0.f);
-#pragma unroll
-    for (int i = 0; i <= 2; ++i) {
-        if (i > ncp) break;
-        const float b = i == ncp ? 1.f : (i == 0 ? e1 : e2);
-        const float fb = triple(x21, x31, x41, v21, v31, v41, b);
-        if (fabsf(fa) < kEpsCubic && hit(a)) return true;
-        if (fa * fb < 0.f) {
-            const float t = secant(x21, x31, x41, v21, v31, v41, a, b, fa, fb);
-            if (t != -15.f && hit(t)) return true;
-        }
-        a = b;
-        fa = fb;
-    }
-    return false;
-}
-
-__device__ bool vf_ccd(const DevPtrs &d, int p, int f1, int f2, int f3, float h, float dt, Wts &w) {
-    return ccd_scan<true>(xyz(d.xp[f1]), xyz(d.xp[f2]), xyz(d.xp[f3]), xyz(d.xp[p]), xyz(d.v[f1]), xyz(d.v[f2]),
-                          xyz(d.v[f3]), xyz(d.v[p]), h, dt, w);
-}
-
-__device__ bool ee_ccd(const DevPtrs &d, int e1, int e2, int e3, int e4, float h, float dt, Wts &w) {
-    return ccd_scan<false>(xyz(d.xp[e1]), xyz(d.xp[e2]), xyz(d.xp[e3]), xyz(d.xp[e4]), xyz(d.v[e1]), xyz(d.v[e2]),
-                           xyz(d.v[e3]), xyz(d.v[e4]), h, dt, w);
-}
-
 // EE slot s: edge (s%3) of A x edge (s/3) of B; edge k of a triangle is
 // (v1,v2 | bit 2), (v1,v3 | bit 0), (v2,v3 | bit 1).
 __device__ __forceinline__ void edge_of(int k, int &a, int &b, int &bit) {
@@ -708,27 +636,33 @@ __device__ uint16_t pair_filter(const DevPtrs &d, uint32_t p) {
         want |= 1u << (6 + s);
     }
     if (!want) return 0;
+    // the six vertex boxes, the two face boxes and the six edge boxes once
+    // (min / max are exact, so any grouping gives the reference's boxes)
     Box bx[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) bx[k] = pbox(d, vid[k], h);
+    Box face[2], edge[6];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        face[t] = Box{min3(bx[3 * t].lo, bx[3 * t + 1].lo, bx[3 * t + 2].lo),
+                      max3(bx[3 * t].hi, bx[3 * t + 1].hi, bx[3 * t + 2].hi)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int a0, a1, ab;
+            edge_of(k, a0, a1, ab);
+            edge[3 * t + k] = Box{vmin(bx[3 * t + a0].lo, bx[3 * t + a1].lo), vmax(bx[3 * t + a0].hi, bx[3 * t + a1].hi)};
+        }
+    }
     uint32_t mask = 0;
 #pragma unroll
     for (int s = 0; s < 6; ++s) {
-        if (!((want >> s) & 1)) continue;
-        const int o = s < 3 ? 3 : 0;
-        const float3 flo = min3(bx[o].lo, bx[o + 1].lo, bx[o + 2].lo);
-        const float3 fhi = max3(bx[o].hi, bx[o + 1].hi, bx[o + 2].hi);
-        if (overlap(bx[s].lo, bx[s].hi, flo, fhi)) mask |= 1u << s;
+        const Box &f = face[s < 3 ? 1 : 0];
+        if (((want >> s) & 1) && overlap(bx[s].lo, bx[s].hi, f.lo, f.hi)) mask |= 1u << s;
     }
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
-        if (!((want >> (6 + s)) & 1)) continue;
-        int a0, a1, ab, b0, b1, bb;
-        edge_of(s % 3, a0, a1, ab);
-        edge_of(s / 3, b0, b1, bb);
-        if (overlap(vmin(bx[a0].lo, bx[a1].lo), vmax(bx[a0].hi, bx[a1].hi), vmin(bx[3 + b0].lo, bx[3 + b1].lo),
-                    vmax(bx[3 + b0].hi, bx[3 + b1].hi)))
-            mask |= 1u << (6 + s);
+        const Box &ea = edge[s % 3], &eb = edge[3 + s / 3];
+        if (((want >> (6 + s)) & 1) && overlap(ea.lo, ea.hi, eb.lo, eb.hi)) mask |= 1u << (6 + s);
     }
     return (uint16_t)mask;
 }
@@ -743,66 +677,84 @@ __global__ void k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) 
     }
 }
 
-// Stage 2: one (pair, slot) entry per surviving candidate, VF and EE in
-// separate lists, each in pair-then-slot order — the order of the
-// reference's compactions.
 // Stage 2: the surviving candidates written in the reference's order (pair,
-// then slot) as the four vertex ids the CCD needs.
-__global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) {
-    const uint32_t n = *npairs;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        uint32_t m = d.pair_mask[p];
-        if (!m) continue;
-        uint64_t ov = d.pair_vf_off[p], oe = d.pair_ee_off[p];
-        const uint2 pr = d.pairs[p];
-        const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
-        const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
-        while (m) {
-            const int s = __ffs(m) - 1;
-            m &= m - 1;
-            const int4 ids = candidate_ids(vid, s);
-            if (s < 6) {
-                if (ov < d.cand_cap) d.cand[ov] = ids;
-                else atomicOr(d.err, ERR_CAND_OVERFLOW);
-                ++ov;
-            } else {
-                if (oe < d.cand_cap) d.cand_e[oe] = ids;
-                else atomicOr(d.err, ERR_CAND_OVERFLOW);
-                ++oe;
-            }
+// then slot) as the four vertex ids the CCD needs.  A warp takes 32
+// consecutive pairs, whose outputs are contiguous; the warp's candidates are
+// spread over all lanes (output j belongs to the last pair whose prefix count
+// is <= j), so every lane writes and the writes are coalesced.
+template <bool VF>
+__device__ __forceinline__ void expand_kind(const DevPtrs &d, uint32_t bits, const int vid[6], uint64_t base_off) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t cnt = __popc(bits);
+    uint32_t ex = cnt;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(full, ex, o);
+        if (lane >= o) ex += t;
+    }
+    const uint32_t total = __shfl_sync(full, ex, 31);
+    ex -= cnt;  // exclusive
+    int4 *out = VF ? d.cand : d.cand_e;
+    for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        int L = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int cand = L + step;
+            const uint32_t e = __shfl_sync(full, ex, cand & 31);
+            if (cand < 32 && e <= j) L = cand;
+        }
+        const uint32_t exL = __shfl_sync(full, ex, L);
+        const uint32_t bL = __shfl_sync(full, bits, L);
+        int v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __shfl_sync(full, vid[k], L);
+        if (j < total) {
+            uint32_t m = bL;
+            for (uint32_t k = j - exL; k > 0; --k) m &= m - 1;
+            const int s = (__ffs(m) - 1) + (VF ? 0 : 6);
+            const uint64_t o = base_off + j;
+            if (o < d.cand_cap) out[o] = candidate_ids(v, s);
+            else atomicOr(d.err, ERR_CAND_OVERFLOW);
         }
     }
 }
 
-template <bool VF>
-__device__ __forceinline__ bool candidate_ccd(const DevPtrs &d, const int4 ids, Wts &w) {
-    const ClothDev &cd = d.cloth[d.vcloth[ids.x]];
-    return VF ? vf_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w)
-              : ee_ccd(d, ids.x, ids.y, ids.z, ids.w, cd.h, cd.dt, w);
-}
-
-// Stage 3: CCD of every candidate of one kind, one per thread
-// (Collision/CudaPrimitiveTests.cu:109-238).
-template <bool VF>
-__global__ void k_ccd(DevPtrs d, const uint32_t *__restrict__ ncand) {
-    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
-    const int4 *list = VF ? d.cand : d.cand_e;
-    uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        Wts w;
-        hit[q] = candidate_ccd<VF>(d, list[q], w) ? 1u : 0u;
+__global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) {
+    const uint32_t n = *npairs;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warp0 * 32u; base < n; base += nwarps * 32u) {
+        const uint32_t p = base + lane;
+        const uint32_t m = p < n ? d.pair_mask[p] : 0u;
+        int vid[6] = {0, 0, 0, 0, 0, 0};
+        if (m) {
+            const uint2 pr = d.pairs[p];
+            const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+            vid[0] = A.x; vid[1] = A.y; vid[2] = A.z; vid[3] = B.x; vid[4] = B.y; vid[5] = B.z;
+        }
+        if (!__any_sync(0xffffffffu, m != 0u)) continue;
+        expand_kind<true>(d, m & 0x3Fu, vid, d.pair_vf_off[base]);
+        expand_kind<false>(d, m >> 6, vid, d.pair_ee_off[base]);
     }
 }
 
-// Stage 3 with the secant solves spread over the warp.  Each warp takes 32
-// candidates at a time: (1) every lane sets up its candidate's cubic, finds
-// the interval ends and evaluates f there, and queues the intervals whose
-// ends differ in sign; (2) the warp runs the queued secant solves, one per
-// lane; (3) every lane tests its roots in interval order with the cumulative
-// advance and stops at the first hit.  Each piece is the arithmetic of
-// ccd_scan on the same operands, so the decisions are the same bits; only
-// the assignment of work to lanes differs (and secants after a hit are
-// computed and not used).
+// Stage 3: CCD of every candidate of one kind on x_prev and v
+// (Collision/CudaPrimitiveTests.cu:109-238, Physics/CudaCubicSolver.cu:5-153).
+// VF: vertex x4 against the face x1 x2 x3; EE: edges x1 x2 and x3 x4.  The
+// reference collects every coplanarity time of [0,1] (the ends of the
+// intervals cut at the derivative's roots where |f| < eps, and the secant
+// root of every interval whose ends differ in sign), then advances the four
+// positions by v t dt for each time in turn and tests after each advance
+// until one test hits.  Here each warp takes 32 candidates at a time:
+// (1) every lane sets up its candidate's cubic, evaluates f at the interval
+// ends and queues the intervals that need a secant solve; (2) the warp runs
+// the queued solves, one per lane; (3) every lane tests its times in the
+// reference's order with the cumulative advance and stops at the first hit.
+// The operands and operations of every piece are the reference's, so the
+// decisions are the same bits; only the assignment of work to lanes differs.
 constexpr int kCcdWarps = 8;
 struct CcdJob { float a, b, fa, fb; };
 
@@ -921,31 +873,38 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
                 }
             }
             hitout[q] = found ? 1u : 0u;
+            if (found) {
+                // the contact's weights, placed at its final index by k_ccd_emit
+                const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
+                const uint32_t slot = atomicAdd(&d.hit_n[VF ? 0 : 1], 1u);
+                if (slot < cap) {
+                    d.hit_q[VF ? 0 : 1][slot] = q;
+                    d.hit_w[VF ? 0 : 1][slot] = make_float4(wt.w0, wt.w1, wt.w2, wt.w3);
+                } else {
+                    atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
+                }
+            }
         }
         __syncwarp();
     }
 }
 
-// Stage 4: contacts written in candidate order; the CCD of the few hits is
-// evaluated again for their weights.
+// Stage 4 after k_ccd_warp: every hit written at its index in candidate order
+// (the exclusive scan of the hit flags), ids from the candidate list.
 template <bool VF>
-__global__ void k_ccd_write(DevPtrs d, const uint32_t *__restrict__ ncand) {
-    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
-    const int4 *list = VF ? d.cand : d.cand_e;
-    const uint32_t *hit = VF ? d.cand_vf : d.cand_ee;
+__global__ void k_ccd_emit(DevPtrs d) {
+    const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
+    const uint32_t n = (uint32_t)min((uint64_t)d.hit_n[VF ? 0 : 1], cap);
     const uint32_t *off = VF ? d.cand_vf_off : d.cand_ee_off;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        if (!hit[q]) continue;
-        const int4 ids = list[q];
-        Wts w;
-        candidate_ccd<VF>(d, ids, w);
+    const int4 *list = VF ? d.cand : d.cand_e;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t q = d.hit_q[VF ? 0 : 1][k];
         const uint32_t o = off[q];
-        if (VF) {
-            if (o < d.vf_cap) { d.vf_v[o] = ids; d.vf_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
-            else atomicOr(d.err, ERR_VF_OVERFLOW);
+        if (o < cap) {
+            if (VF) { d.vf_v[o] = list[q]; d.vf_w[o] = d.hit_w[0][k]; }
+            else { d.ee_v[o] = list[q]; d.ee_w[o] = d.hit_w[1][k]; }
         } else {
-            if (o < d.ee_cap) { d.ee_v[o] = ids; d.ee_w[o] = make_float4(w.w0, w.w1, w.w2, w.w3); }
-            else atomicOr(d.err, ERR_EE_OVERFLOW);
+            atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
         }
     }
 }
@@ -1017,11 +976,12 @@ void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv
     if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 1) k_narrow_expand<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 2) {
+        cudaMemsetAsync(d.hit_n, 0, 2 * sizeof(uint32_t), st);
         k_ccd_warp<true><<<grid, kCcdWarps * 32, 0, st>>>(d, ncv);
         k_ccd_warp<false><<<grid, kCcdWarps * 32, 0, st>>>(d, nce);
     } else if (stage == 3) {
-        k_ccd_write<true><<<grid, kThreads, 0, st>>>(d, ncv);
-        k_ccd_write<false><<<grid, kThreads, 0, st>>>(d, nce);
+        k_ccd_emit<true><<<grid, kThreads, 0, st>>>(d);
+        k_ccd_emit<false><<<grid, kThreads, 0, st>>>(d);
     } else {
         k_contact_ranges<<<nblk(d.C, 128), 128, 0, st>>>(d, ncv, nce);
     }
