@@ -433,6 +433,91 @@ __global__ void k_traverse_wide(DevPtrs d) {
     if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
 }
 
+// The traversal as a packet: a left-first depth-first walk of a Karras tree
+// meets the leaves in increasing index order, so leaf i's result is the
+// increasing list of leaves j > i whose boxes overlap its own, cut at the
+// chunk size.  A warp walks the tree once for its 32 consecutive leaves
+// (spatially close in Morton order): every node record is read once for the
+// warp, each lane tests its own box (and rightmost-leaf bound) against the
+// two children, and the warp descends into a child when any lane needs it.
+// Each lane keeps exactly the leaves it overlaps, in the walk's order, so
+// every chunk is the single-leaf traversal's.  A warp whose leaves span two
+// cloths walks each cloth's tree for its own lanes.
+constexpr int kPacketWarps = 32;  // stack slots for up to 1024 threads per block
+__global__ void k_traverse_packet(DevPtrs d) {
+    __shared__ int wstack[kPacketWarps][kTraverseStack];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 + lane;
+    const bool valid = s < d.Ttot;
+    int c = -1, me = 0, got = 0, chunk = 0;
+    uint32_t dropped = 0;
+    uint32_t *out = nullptr;
+    float3 amin = f3(0.f, 0.f, 0.f), amax = amin;
+    bool has_tree = false;
+    if (valid) {
+        c = d.tcloth[s];
+        const ClothDev &cd = d.cloth[c];
+        const int id = s - cd.t_off, In = cd.T - 1;
+        has_tree = In > 0;
+        me = In + id;
+        chunk = cd.chunk;
+        out = d.pair_chunk + cd.pc_off + (int64_t)id * chunk;
+        if (has_tree) {
+            amin = xyz(d.nmin[cd.n_off + me]);
+            amax = xyz(d.nmax[cd.n_off + me]);
+        }
+    }
+    unsigned pending = __ballot_sync(full, has_tree);
+    bool overflow = false;
+    while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const int cc = __shfl_sync(full, c, leader);
+        const bool mine = ((pending >> lane) & 1u) && c == cc;
+        pending &= ~__ballot_sync(full, mine);
+        const ClothDev &cd = d.cloth[cc];
+        const int In = cd.T - 1;
+        const float4 *W = d.wnode + 4 * (size_t)cd.i_off;
+        int top = 1, node = 0;
+        if (lane == 0) wstack[w][0] = -1;
+        __syncwarp();
+        const int guard_max = 4 * cd.T + 64;
+        for (int guard = 0; guard < guard_max; ++guard) {
+            const float4 *r = W + 4 * (size_t)node;
+            const float4 l0 = __ldg(r), l1 = __ldg(r + 1), r0 = __ldg(r + 2), r1 = __ldg(r + 3);
+            const int chx = __float_as_int(l0.w), rmx = __float_as_int(l1.w);
+            const int chy = __float_as_int(r0.w), rmy = __float_as_int(r1.w);
+            const bool ol = mine && rmx > me && overlap(amin, amax, xyz(l0), xyz(l1));
+            const bool orr = mine && rmy > me && overlap(amin, amax, xyz(r0), xyz(r1));
+            if (ol && chx >= In) {
+                if (got < chunk) out[got++] = (uint32_t)(chx - In);
+                else ++dropped;
+            }
+            if (orr && chy >= In) {
+                if (got < chunk) out[got++] = (uint32_t)(chy - In);
+                else ++dropped;
+            }
+            const bool tl = chx < In && __any_sync(full, ol), tr = chy < In && __any_sync(full, orr);
+            if (!tl && !tr) {
+                node = wstack[w][--top];
+            } else {
+                node = tl ? chx : chy;
+                if (tl && tr) {
+                    if (top >= kTraverseStack) { overflow = true; break; }
+                    if (lane == 0) wstack[w][top] = chy;
+                    ++top;
+                }
+            }
+            __syncwarp();
+            if (top == 0) break;
+        }
+        __syncwarp();
+    }
+    if (overflow && lane == 0) atomicOr(d.err, ERR_STACK);
+    if (valid) d.pair_cnt[s] = (uint32_t)got;
+    if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
+}
+
 // Order-preserving compaction of the per-leaf chunks into the pair list:
 // each warp takes 32 consecutive leaves and copies them one leaf at a time
 // with all 32 lanes, so reads and writes are coalesced.
@@ -963,7 +1048,7 @@ void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
     if (!d.Ttot) return;
     if (d.wnode) {
         k_pack_nodes<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
-        k_traverse_wide<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+        k_traverse_packet<<<nblk(d.Ttot, block), block, 0, st>>>(d);
     } else {
         k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
     }
