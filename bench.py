@@ -353,7 +353,8 @@ def run_ours(args, world, rank, local):
         with torch.cuda.stream(stream):
             tuned = autotune.autotune(batch, steps=2, warmup=1, cache=None,
                                       space={"traverse_block": (64, 128, 256), "jacobi_block": (256,),
-                                             "narrow_blocks_per_sm": (4, 8, 16), "solver_variant": (1, 3)})
+                                             "narrow_blocks_per_sm": (8, 16), "solver_variant": (1, 3),
+                                             "cluster_size": (8, 16)})
         tuning = {"config": tuned["config"], "candidates": len(tuned["tried"])}
 
     # ---- device-timed region ------------------------------------------------

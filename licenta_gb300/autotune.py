@@ -1,14 +1,15 @@
 """Autotuner of a batch's launch shapes.
 
 For a given batch it times a small grid of launch shapes (traversal block,
-global-memory Jacobi block, narrowphase grid, Jacobi solver variant) on the
-batch's current state and keeps the fastest.  Every candidate starts from the
+global-memory Jacobi block, narrowphase grid, Jacobi solver variant and the
+on-chip solver's cluster size) on the batch's current state and keeps the
+fastest.  Every candidate starts from the
 same saved state (lc_batch_save_state / lc_batch_load_state) and is timed
 with CUDA events over a few steps after a warm-up; the batch is left in the
 state it was given, with the winning shapes applied.
 
-Block and grid sizes never change results.  The solver variant does (the
-on-chip variants sum the Jacobi corrections in another order, all within the
+Block, grid and cluster sizes never change results.  The solver variant does
+(the variants sum the Jacobi corrections in different orders, all within the
 FP64 tolerance), so it is only searched when ``allow_variants`` is set.
 
 Results are cached per workload signature (cloth count, vertex / triangle
@@ -31,6 +32,7 @@ DEFAULT_SPACE = {
     "jacobi_block": (128, 256, 512),
     "narrow_blocks_per_sm": (4, 8, 16),
     "solver_variant": (1, 2, 3),
+    "cluster_size": (8, 16),
 }
 DEFAULT_CACHE = Path.home() / ".cache" / "licenta_gb300" / "autotune.json"
 
@@ -105,9 +107,15 @@ def autotune(batch, *, steps: int = 3, warmup: int = 1, space: dict | None = Non
     tried = []
     for values in itertools.product(*(space[k] for k in names)):
         cfg = dict(zip(names, values))
-        # the Jacobi block only matters for the global-memory solver
+        cfg.setdefault("cluster_size", 0)
+        # the Jacobi block only matters for the global-memory solver, the
+        # cluster size only for the on-chip ones
         if cfg["solver_variant"] != 1 and cfg["jacobi_block"] != space["jacobi_block"][0]:
             continue
+        if cfg["solver_variant"] == 1 and cfg["cluster_size"] not in (0, space.get("cluster_size", (0,))[0]):
+            continue
+        if cfg["solver_variant"] == 1:
+            cfg["cluster_size"] = 0
         if not set_tuning(batch, cfg):
             continue
         tried.append({"config": cfg, "ms_per_step": _time(batch, state, steps, warmup, stream)})

@@ -304,6 +304,7 @@ struct lc_batch {
     // cluster-resident solver (lc_cluster.cu)
     bool use_cluster = false;
     int cluster_cs = 8;
+    int want_cs = 0;  // 0: pick; 8 or 16: requested through lc_batch_set_tuning
     bool cluster_scatter = false;
     ClusterArgs ca{};
     // adjoint (lc_batch_adjoint_step): the tape of one recorded step
@@ -470,10 +471,19 @@ lc_status lc_batch::setup_cluster() {
         vmax = std::max(vmax, hosts[c].V);
         if (cds[c].F > 8) ok = false;
     }
+    // cluster size: the requested one (lc_tuning.cluster_size) if it fits,
+    // else the one that keeps the most CTAs resident (more warps per SM to
+    // hide the distributed-shared-memory latency), 8 on a tie
     int cs = 0;
     if (ok) {
-        if ((vmax + 7) / 8 <= dev_cap && cluster_max_active(8, (vmax + 7) / 8, scatter) > 0) cs = 8;
-        else if ((vmax + 15) / 16 <= dev_cap && cluster_max_active(16, (vmax + 15) / 16, scatter) > 0) cs = 16;
+        long best = 0;
+        for (int cand : {8, 16}) {
+            if (want_cs && cand != want_cs) continue;
+            const int cap = (vmax + cand - 1) / cand;
+            if (cap > dev_cap) continue;
+            const long act = (long)cluster_max_active(cand, cap, scatter) * cand;
+            if (act > best) { best = act; cs = cand; }
+        }
     }
     if (!cs) {
         if (opt.solver_variant >= 2) return fail(LC_ERR_NOT_SUPPORTED, "cluster solver: a cloth does not fit on chip");
@@ -1013,6 +1023,7 @@ lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t) {
     t->jacobi_block = b->jacobi_block;
     t->narrow_blocks_per_sm = b->narrow_grid / sm_count();
     t->solver_variant = b->use_cluster ? (b->cluster_scatter ? 3 : 2) : 1;
+    t->cluster_size = b->use_cluster ? b->cluster_cs : 0;
     return LC_OK;
 }
 
@@ -1020,7 +1031,8 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     if (!b || !t) return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: bad arguments");
     auto ok_block = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
     if (!ok_block(t->traverse_block) || !ok_block(t->jacobi_block) || t->narrow_blocks_per_sm < 1 ||
-        t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3)
+        t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3 ||
+        (t->cluster_size != 0 && t->cluster_size != 8 && t->cluster_size != 16))
         return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: value out of range");
     if (b->opt.adjoint && t->solver_variant != 1)
         return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_tuning: an adjoint batch keeps solver variant 1");
@@ -1028,11 +1040,15 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     b->traverse_block = t->traverse_block;
     b->jacobi_block = t->jacobi_block;
     b->narrow_grid = sm_count() * t->narrow_blocks_per_sm;
-    const int prev = b->opt.solver_variant;
+    const int prev = b->opt.solver_variant, prev_cs = b->want_cs;
     b->opt.solver_variant = t->solver_variant;
-    const lc_status s = b->setup_cluster();
+    b->want_cs = t->cluster_size;
+    lc_status s = b->setup_cluster();
+    if (s == LC_OK && t->solver_variant >= 2 && t->cluster_size && b->cluster_cs != t->cluster_size)
+        s = fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_tuning: cluster size does not fit");
     if (s != LC_OK) {
         b->opt.solver_variant = prev;
+        b->want_cs = prev_cs;
         b->setup_cluster();
         return s;
     }

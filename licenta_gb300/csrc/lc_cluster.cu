@@ -269,7 +269,7 @@ constexpr float kFix = 33554432.f;           // 2^25
 constexpr float kFixInv = 1.f / 33554432.f;  // exact power of two
 
 template <int CS>
-__global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster_scatter(DevPtrs d, ClusterArgs a) {
+__global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevPtrs d, ClusterArgs a) {
     cg::cluster_group cluster = cg::this_cluster();
     const int r = (int)cluster.block_rank();
     const int c = a.cl_cloth[blockIdx.x / CS];
