@@ -44,7 +44,7 @@ NCLOTH = 256
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
@@ -459,8 +459,9 @@ def run_ours(args, world, rank, local):
         "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "e2e": e2e,
         "gpu_launches": int(prof["kernels_per_step"]) * args.steps,
         "profile": {"phases_ms": prof["phases"], "jacobi_ms": prof["jacobi_ms"], "traverse_ms": prof["traverse_ms"],
-                    "narrow_ms": prof["narrow_ms"], "sort_ms": prof["sort_ms"], "kernels_per_step": prof["kernels_per_step"],
-                    "sizes": alg["_sizes"]},
+                    "narrow_ms": prof["narrow_ms"], "ccd_vf_ms": prof["ccd_vf_ms"], "ccd_ee_ms": prof["ccd_ee_ms"],
+                    "solver_ms": prof["solver_ms"], "sort_ms": prof["sort_ms"],
+                    "kernels_per_step": prof["kernels_per_step"], "sizes": alg["_sizes"]},
         "plain": plain,
         "adjoint": adj,
         "lbvh": lbvh,

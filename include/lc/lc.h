@@ -187,13 +187,15 @@ typedef struct lc_profile {
                                  5 Perform Triangle Tests, 6 PBD Solver, 7 PBD Integration */
     float jacobi_ms;          /* one Jacobi iteration launch */
     float traverse_ms;        /* one traversal launch */
-    float narrow_ms;          /* candidate + CCD count launch */
+    float narrow_ms;          /* one narrowphase filter launch (per-pair candidate counts) */
     float sort_ms;            /* whole segmented sort */
     float step_ms;            /* sum of the phases */
     uint32_t kernels_per_step;
     float solver_ms;          /* whole solver (set-up + iterations + integration on the cluster path) */
     int32_t solver_variant;   /* 1 = per-vertex gather, 2 = cluster on-chip */
     int32_t cluster_size;     /* CTAs per cloth on the cluster path */
+    float ccd_vf_ms;          /* one vertex-face CCD launch */
+    float ccd_ee_ms;          /* one edge-edge CCD launch */
 } lc_profile;
 lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile *out);
 

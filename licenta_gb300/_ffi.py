@@ -69,7 +69,7 @@ class Profile(C.Structure):
     _fields_ = [("phase_ms", C.c_float * 7), ("jacobi_ms", C.c_float), ("traverse_ms", C.c_float),
                 ("narrow_ms", C.c_float), ("sort_ms", C.c_float), ("step_ms", C.c_float),
                 ("kernels_per_step", C.c_uint32), ("solver_ms", C.c_float), ("solver_variant", C.c_int32),
-                ("cluster_size", C.c_int32)]
+                ("cluster_size", C.c_int32), ("ccd_vf_ms", C.c_float), ("ccd_ee_ms", C.c_float)]
 
 
 PHASES = ("1. PBD External", "2. Update Triangles", "3. Build BVH", "4. Create Triangle Tests",

@@ -146,7 +146,7 @@ class ClothBatch:
         return dict(phases=dict(zip(_ffi.PHASES, list(p.phase_ms))), jacobi_ms=p.jacobi_ms,
                     traverse_ms=p.traverse_ms, narrow_ms=p.narrow_ms, sort_ms=p.sort_ms, step_ms=p.step_ms,
                     kernels_per_step=p.kernels_per_step, solver_ms=p.solver_ms, solver_variant=p.solver_variant,
-                    cluster_size=p.cluster_size)
+                    cluster_size=p.cluster_size, ccd_vf_ms=p.ccd_vf_ms, ccd_ee_ms=p.ccd_ee_ms)
 
     def set_sphere(self, cloth: int, pos, radius: float) -> None:
         p = (C.c_float * 3)(*[float(v) for v in pos])

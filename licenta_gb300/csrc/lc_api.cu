@@ -337,7 +337,8 @@ struct lc_batch {
 
     // profiling: when non-null, events are recorded at phase boundaries
     cudaEvent_t *prof_ev = nullptr;    // 8 events per step
-    cudaEvent_t *kern_ev = nullptr;    // pairs around single kernels: [0,1] jacobi, [2,3] traverse, [4,5] narrow, [6,7] sort
+    cudaEvent_t *kern_ev = nullptr;    // pairs around single kernels: [0,1] jacobi, [2,3] traverse, [4,5] narrow
+                                       // filter, [6,7] sort, [8,9] VF CCD, [10,11] EE CCD
     uint32_t launches = 0;
 };
 
@@ -392,11 +393,15 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     // 5. Perform Triangle Tests
     LC_KEV(4);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 0, st);  // filter
+    LC_KEV(5);
     scan_u32(d.pair_vf_cnt, d.pair_vf_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand, nullptr, st);
     scan_u32(d.pair_ee_cnt, d.pair_ee_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand_e, nullptr, st);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 1, st);  // expand
-    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 2, st);  // CCD
-    LC_KEV(5);
+    LC_KEV(8);
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 2, st);  // VF CCD
+    LC_KEV(9);
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 5, st);  // EE CCD
+    LC_KEV(10);
     scan_u32(d.cand_vf, d.cand_vf_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nvf, &d.counters[1], st);
     scan_u32(d.cand_ee, d.cand_ee_off, ncand_e, 0, (uint32_t)d.cand_cap, d.scan_tmp, nee, &d.counters[2], st);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 3, st);  // write contacts
@@ -1458,13 +1463,13 @@ lc_status lc_batch_read_state(lc_batch *b, float *x, float *xp, float *v, int32_
 lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile *out) {
     if (!b || !out || nsteps < 1) return fail(LC_ERR_INVALID_ARG, "lc_batch_profile: bad arguments");
     cudaStream_t st = (cudaStream_t)stream;
-    std::vector<cudaEvent_t> pev(8 * (size_t)nsteps), kev(8 * (size_t)nsteps);
+    std::vector<cudaEvent_t> pev(8 * (size_t)nsteps), kev(12 * (size_t)nsteps);
     for (auto &e : pev) LC_CUDA(cudaEventCreate(&e));
     for (auto &e : kev) LC_CUDA(cudaEventCreate(&e));
     lc_status s = LC_OK;
     for (int k = 0; k < nsteps && s == LC_OK; ++k) {
         b->prof_ev = &pev[8 * (size_t)k];
-        b->kern_ev = &kev[8 * (size_t)k];
+        b->kern_ev = &kev[12 * (size_t)k];
         s = b->enqueue_step(st);
     }
     b->prof_ev = nullptr;
@@ -1478,12 +1483,15 @@ lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile
                 cudaEventElapsedTime(&ms, pev[8 * k + p], pev[8 * k + p + 1]);
                 out->phase_ms[p] += ms / nsteps;
             }
-            cudaEventElapsedTime(&ms, kev[8 * k + 0], kev[8 * k + 1]);
+            const cudaEvent_t *e = &kev[12 * (size_t)k];
+            cudaEventElapsedTime(&ms, e[0], e[1]);
             out->solver_ms += ms / nsteps;
             out->jacobi_ms += (b->use_cluster ? ms / b->max_iters : ms) / nsteps;
-            cudaEventElapsedTime(&ms, kev[8 * k + 2], kev[8 * k + 3]); out->traverse_ms += ms / nsteps;
-            cudaEventElapsedTime(&ms, kev[8 * k + 4], kev[8 * k + 5]); out->narrow_ms += ms / nsteps;
-            cudaEventElapsedTime(&ms, kev[8 * k + 6], kev[8 * k + 7]); out->sort_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, e[2], e[3]); out->traverse_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, e[4], e[5]); out->narrow_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, e[6], e[7]); out->sort_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, e[8], e[9]); out->ccd_vf_ms += ms / nsteps;
+            cudaEventElapsedTime(&ms, e[9], e[10]); out->ccd_ee_ms += ms / nsteps;
         }
         for (int p = 0; p < 7; ++p) out->step_ms += out->phase_ms[p];
         out->solver_variant = b->use_cluster ? (b->cluster_scatter ? 3 : 2) : 1;

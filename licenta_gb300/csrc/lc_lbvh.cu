@@ -1063,6 +1063,7 @@ void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv
     else if (stage == 2) {
         cudaMemsetAsync(d.hit_n, 0, 2 * sizeof(uint32_t), st);
         k_ccd_warp<true><<<grid, kCcdWarps * 32, 0, st>>>(d, ncv);
+    } else if (stage == 5) {
         k_ccd_warp<false><<<grid, kCcdWarps * 32, 0, st>>>(d, nce);
     } else if (stage == 3) {
         k_ccd_emit<true><<<grid, kThreads, 0, st>>>(d);

@@ -357,6 +357,7 @@ template <class R> class Cloth {
         std::vector<u32> ground_it;  // V
         std::vector<u8> lra;         // V*F
         std::vector<u8> dyn;         // iterations x 4*(vf+ee)
+        std::vector<int8_t> sphere;  // V: ray-sphere outcome -1 / 0 / 1
         std::vector<V> x_in, v_b;    // damping inputs: state x, velocity after the global damping
         std::vector<std::vector<V>> xk;  // solver iterates x^0 .. x^K
         double M = 0, xcm[3] = {0, 0, 0}, vcm[3] = {0, 0, 0}, om[3] = {0, 0, 0}, I[3][3] = {};
@@ -1074,6 +1075,7 @@ template <class R> class Cloth {
     void sphere_create(R th) {
         V sc = mk<R>(prm.spherePos[0], prm.spherePos[1], prm.spherePos[2]);
         R rad = R(prm.sphereRadius) + th;
+        if (recording) rec.sphere.assign(tp.V, 0);
         for (int i = 0; i < tp.V; ++i) {
             V pos = x[i], prev = xp[i];
             V q;
@@ -1090,6 +1092,7 @@ template <class R> class Cloth {
                     q = prev + dir * (-b - std::sqrt(disc));
                 }
             }
+            if (recording) rec.sphere[i] = (int8_t)ret;
             if (ret == -1) {
                 V qs = sc + normalize(q - sc) * rad;
                 V ns = normalize(qs - sc);

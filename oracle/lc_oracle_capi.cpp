@@ -347,3 +347,105 @@ extern "C" int lco_set_stiffness_d(lco_world *w, int c, const double *ks, const 
         return (int)LC_OK;
     });
 }
+
+// ---- solver pin -------------------------------------------------------------
+// The static topology of cloth c in the layouts the reference's solver kernels
+// take (Physics/CudaPBD.cu:942-962, :1571-1592, :1656-1688): stretch ends s12
+// (2E), rest lengths sl0 (E), bend vertices b (4B), the per-vertex slot CSR
+// soff (V+1) with its entries sent (S, kind<<30 | role<<28 | constraint),
+// pinned ids fixed (F), attachment lengths lra_l0 (V*F), inverse masses invm
+// (V) and pinned flags (V).  counts receives {F, S}; any output may be null.
+extern "C" int lco_topology(lco_world *w, int c, int *s12, double *sl0, int *b, int *soff, int *sent, int *fixed,
+                            double *lra_l0, float *invm, uint8_t *pinned, int counts[2]) {
+    return with_cloth(w, c, [&](auto &cl) {
+        const auto &tp = cl.tp;
+        const size_t E = tp.s1.size(), B = tp.b1.size();
+        if (counts) { counts[0] = (int)tp.fixed.size(); counts[1] = (int)tp.sent.size(); }
+        if (s12) for (size_t i = 0; i < E; ++i) { s12[2 * i] = tp.s1[i]; s12[2 * i + 1] = tp.s2[i]; }
+        if (sl0) std::copy(tp.sl0.begin(), tp.sl0.end(), sl0);
+        if (b)
+            for (size_t i = 0; i < B; ++i) {
+                b[4 * i] = tp.b1[i]; b[4 * i + 1] = tp.b2[i]; b[4 * i + 2] = tp.b3[i]; b[4 * i + 3] = tp.b4[i];
+            }
+        if (soff) std::copy(tp.soff.begin(), tp.soff.end(), soff);
+        if (sent) std::copy(tp.sent.begin(), tp.sent.end(), sent);
+        if (fixed) std::copy(tp.fixed.begin(), tp.fixed.end(), fixed);
+        if (lra_l0) std::copy(tp.lra_l0.begin(), tp.lra_l0.end(), lra_l0);
+        if (invm) for (int i = 0; i < tp.V; ++i) invm[i] = (float)cl.invm[i];
+        if (pinned) std::copy(tp.pinned.begin(), tp.pinned.end(), pinned);
+        return (int)LC_OK;
+    });
+}
+
+// PBDStepSolver and the velocity update of _FinalUpdate (Physics/CudaPBD.cu:
+// 632-660, :1916-1932) on a given state: x (predicted positions) and xp
+// (previous positions), 3V floats each, with the given contacts.  x_out
+// receives the positions after the solver iterations, v_out and xp_out the
+// velocities and previous positions after the update (no world clamp).
+// Decisions set by lco_set_forced beforehand are imposed; the decisions the
+// solve took are kept for lco_solve_decisions.
+extern "C" int lco_solve_on(lco_world *w, int c, const float *x, const float *xp, const lc_contact *vf,
+                            uint64_t nvf, const lc_contact *ee, uint64_t nee, float *x_out, float *v_out,
+                            float *xp_out) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        const int Vn = cl.tp.V;
+        for (int i = 0; i < Vn; ++i) {
+            cl.x[i] = mk<R>(R(x[3 * i]), R(x[3 * i + 1]), R(x[3 * i + 2]));
+            cl.xp[i] = mk<R>(R(xp[3 * i]), R(xp[3 * i + 1]), R(xp[3 * i + 2]));
+        }
+        std::vector<Contact> cvf(nvf), cee(nee);
+        for (uint64_t i = 0; i < nvf; ++i) std::memcpy(&cvf[i], &vf[i], sizeof(Contact));
+        for (uint64_t i = 0; i < nee; ++i) std::memcpy(&cee[i], &ee[i], sizeof(Contact));
+        if (cl.forced.on && cl.forced.dyn.size() != (size_t)cl.prm.solverIterations * 4 * (nvf + nee)) {
+            cl.forced.on = false;
+            return (int)LC_ERR_INVALID_ARG;
+        }
+        cl.recording = true;
+        cl.solve(cvf, cee);
+        cl.recording = false;
+        cl.forced.on = false;
+        if (!cl.prm.sphereOn) cl.rec.sphere.assign(Vn, 0);
+        const R dt = R(cl.prm.timestep);
+        for (int i = 0; i < Vn; ++i) {
+            const auto p = cl.x[i];
+            x_out[3 * i] = (float)p.x; x_out[3 * i + 1] = (float)p.y; x_out[3 * i + 2] = (float)p.z;
+            auto vel = cl.tp.pinned[i] ? mk<R>(0, 0, 0) : (p - cl.xp[i]) / dt;
+            auto q = cl.tp.pinned[i] ? cl.xp[i] : p;
+            v_out[3 * i] = (float)vel.x; v_out[3 * i + 1] = (float)vel.y; v_out[3 * i + 2] = (float)vel.z;
+            xp_out[3 * i] = (float)q.x; xp_out[3 * i + 1] = (float)q.y; xp_out[3 * i + 2] = (float)q.z;
+        }
+        return (int)LC_OK;
+    });
+}
+
+// The discrete decisions of the last lco_solve_on, in the layouts of
+// lco_set_forced: ground (V), ground_it (V), lra (V*F), dyn (iterations x
+// 4 x (VF + EE contacts); dyn_cap bytes at most, *dyn_len receives the full
+// length), sphere (V).  Any output may be null.
+extern "C" int lco_solve_decisions(lco_world *w, int c, uint8_t *ground, uint32_t *ground_it, uint8_t *lra,
+                                   uint8_t *dyn, uint64_t dyn_cap, uint64_t *dyn_len, int8_t *sphere) {
+    return with_cloth(w, c, [&](auto &cl) {
+        const auto &r = cl.rec;
+        if (dyn_len) *dyn_len = r.dyn.size();
+        if (ground) std::copy(r.ground.begin(), r.ground.end(), ground);
+        if (ground_it) std::copy(r.ground_it.begin(), r.ground_it.end(), ground_it);
+        if (lra) std::copy(r.lra.begin(), r.lra.end(), lra);
+        if (dyn) std::memcpy(dyn, r.dyn.data(), std::min<uint64_t>(dyn_cap, r.dyn.size()));
+        if (sphere) std::copy(r.sphere.begin(), r.sphere.end(), sphere);
+        return (int)LC_OK;
+    });
+}
+
+// The positions after iteration k (0 = before the first) of the last
+// lco_solve_on, 3V floats.
+extern "C" int lco_solve_iterate(lco_world *w, int c, int k, float *x) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (k < 0 || k >= (int)cl.rec.xk.size()) return (int)LC_ERR_INVALID_ARG;
+        const auto &xs = cl.rec.xk[k];
+        for (size_t i = 0; i < xs.size(); ++i) {
+            x[3 * i] = (float)xs[i].x; x[3 * i + 1] = (float)xs[i].y; x[3 * i + 2] = (float)xs[i].z;
+        }
+        return (int)LC_OK;
+    });
+}

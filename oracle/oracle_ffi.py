@@ -54,6 +54,10 @@ def lib() -> C.CDLL:
             "lco_adj_backward": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, VP]),
             "lco_adj_clear": (C.c_int, [VP, C.c_int]),
             "lco_set_stiffness_d": (C.c_int, [VP, C.c_int, VP, VP]),
+            "lco_topology": (C.c_int, [VP, C.c_int] + [VP] * 10),
+            "lco_solve_on": (C.c_int, [VP, C.c_int, VP, VP, VP, C.c_uint64, VP, C.c_uint64, VP, VP, VP]),
+            "lco_solve_iterate": (C.c_int, [VP, C.c_int, C.c_int, VP]),
+            "lco_solve_decisions": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -211,6 +215,72 @@ class Oracle:
         ks = None if k_stretch is None else np.ascontiguousarray(k_stretch, np.float64)
         kb = None if k_bend is None else np.ascontiguousarray(k_bend, np.float64)
         _chk(lib().lco_set_stiffness_d(self._h, c, _p(ks), _p(kb)), "set_stiffness_d")
+
+    # ---- solver pin -------------------------------------------------------
+    def topology(self, c: int) -> dict:
+        """The static topology of cloth c: stretch ends s12 (E, 2), rest
+        lengths sl0 (E), bend vertices b (B, 4), the per-vertex slot CSR soff
+        (V+1) and its entries sent (kind << 30 | role << 28 | constraint),
+        pinned ids fixed (F), attachment lengths lra_l0 (V, F), inverse masses
+        invm (V) and pinned flags (V)."""
+        nv, nt, ne, nb = self.sizes(c)
+        counts = np.zeros(2, np.int32)
+        _chk(lib().lco_topology(self._h, c, *([None] * 9), _p(counts)), "topology")
+        F, S = int(counts[0]), int(counts[1])
+        t = dict(s12=np.empty((ne, 2), np.int32), sl0=np.empty(ne), b=np.empty((nb, 4), np.int32),
+                 soff=np.empty(nv + 1, np.int32), sent=np.empty(S, np.int32), fixed=np.empty(F, np.int32),
+                 lra_l0=np.empty((nv, F)), invm=np.empty(nv, np.float32), pinned=np.empty(nv, np.uint8))
+        _chk(lib().lco_topology(self._h, c, *[_p(t[k]) for k in ("s12", "sl0", "b", "soff", "sent", "fixed",
+                                                                    "lra_l0", "invm", "pinned")], None), "topology")
+        return t
+
+    def solve_on(self, c: int, x, x_prev, vf: tuple, ee: tuple, forced: dict | None = None):
+        """The solver iterations and the velocity update on a given predicted
+        state with given contacts (vf, ee: (vertex ids (N, 4), weights (N, 4))).
+        ``forced`` (the keys of ``solve_decisions``) imposes another solve's
+        discrete decisions.  Returns (x after the iterations, v, x_prev after
+        the update)."""
+        nv = self.sizes(c)[0]
+        if forced is not None:
+            self.force_decisions(c, forced["ground"], forced["ground_it"], forced["lra"], forced["dyn"],
+                                 forced.get("sphere"))
+        xs = np.ascontiguousarray(x, np.float32).reshape(nv, 3)
+        xps = np.ascontiguousarray(x_prev, np.float32).reshape(nv, 3)
+
+        def pack(t):
+            v, w = t
+            v = np.asarray(v, np.int32).reshape(-1, 4)
+            w = np.asarray(w, np.float32).reshape(-1, 4)
+            if len(v) and (v.min() < 0 or v.max() >= nv):
+                raise ValueError("contact vertex id out of range")
+            return np.ascontiguousarray(np.concatenate([v, w.view(np.int32)], axis=1)), len(v)
+        a, na = pack(vf)
+        b, nb_ = pack(ee)
+        out = [np.empty((nv, 3), np.float32) for _ in range(3)]
+        _chk(lib().lco_solve_on(self._h, c, _p(xs), _p(xps), _p(a), na, _p(b), nb_, *[_p(o) for o in out]),
+             "solve_on")
+        return tuple(out)
+
+    def solve_iterate(self, c: int, k: int) -> np.ndarray:
+        """Positions after iteration k (0 = before the first) of the last solve_on."""
+        out = np.empty((self.sizes(c)[0], 3), np.float32)
+        _chk(lib().lco_solve_iterate(self._h, c, k, _p(out)), "solve_iterate")
+        return out
+
+    def solve_decisions(self, c: int) -> dict:
+        """The discrete decisions of the last solve_on: ground constraints
+        created (V), ground terms counted per iteration (V bit masks),
+        attachments active (V x F), contact corrections counted (iterations x
+        4 x (VF + EE)) and ray-sphere outcomes (V)."""
+        nv = self.sizes(c)[0]
+        F = self.topology(c)["fixed"].size
+        n = C.c_uint64()
+        _chk(lib().lco_solve_decisions(self._h, c, None, None, None, None, 0, C.byref(n), None), "solve_decisions")
+        out = dict(ground=np.empty(nv, np.uint8), ground_it=np.empty(nv, np.uint32), lra=np.empty(nv * F, np.uint8),
+                   dyn=np.empty(n.value, np.uint8), sphere=np.empty(nv, np.int8))
+        _chk(lib().lco_solve_decisions(self._h, c, _p(out["ground"]), _p(out["ground_it"]), _p(out["lra"]),
+                                       _p(out["dyn"]), n.value, C.byref(n), _p(out["sphere"])), "solve_decisions")
+        return out
 
     def thickness(self, c: int) -> float:
         h = C.c_float()

@@ -25,7 +25,11 @@ edits its sources) make its kernels compile with nvcc 13:
 * ``-include oracle/ref_pin/ref_shim.h`` — routes norm3df to the length the
   restatement uses (the one deliberate substitution);
 * ``-rdc=true`` (the project's GenerateRelocatableDeviceCode, LicentaV2.vcxproj
-  :107,156) and ``-fmad=false`` (separate roundings, as the restatement).
+  :107,156) and ``-fmad=false`` (separate roundings, as the restatement);
+* ``-DNDEBUG`` — compiles out the device-side ``assert`` calls (Core/CudaUtils.cu
+  :74,207,415,424, Physics/CudaPBD.cu:1540,1626); they check values and
+  change none, and a failed device assert would stop the GPU context instead
+  of reporting a difference.
 
 Usage: python -m oracle.ref_pin.build_ref [reference-root]
 """
@@ -87,7 +91,7 @@ def build(root: Path | None = None, force: bool = False) -> Path | None:
             return CUBIN
     obj = OUT / "obj"
     obj.mkdir(parents=True, exist_ok=True)
-    flags = [ARCH, "-std=c++17", "-rdc=true", "-fmad=false", "-w",
+    flags = [ARCH, "-std=c++17", "-rdc=true", "-fmad=false", "-w", "-DNDEBUG",
              "-DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP",
              "-Xcudafe", "--no_alternative_tokens", "-Xcompiler", "-fno-operator-names",
              "-I", str(HERE / "stub"), "-include", str(HERE / "ref_shim.h"),

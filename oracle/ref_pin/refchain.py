@@ -58,7 +58,27 @@ KERNELS = {
     "tri_tests": "CreateTriangleTests",
     "feature_aabb": "FeatureAABBTests",
     "ccd": "CCDTriangleTests",
+    # PBDStepSolver and _FinalUpdate (Physics/CudaPBD.cu:632-660, :929-940)
+    "ground_create": "_CreateGroundConstraints",
+    "lra_create": "_CreateLRAConstraints",
+    "sphere_create": "_CreateSphereConstraints",
+    "ground_apply": "_ApplyGroundCorrections",
+    "lra_apply": "_ApplyLRACorrections",
+    "static_project": "_ProjectStaticConstraints",
+    "static_apply": "_ApplyStaticCorrections",
+    "dyn_project": "_ProjectDynamicConstraints",
+    "dyn_apply": "_ApplyDynamicCorrections",
+    "sphere_apply": "_ApplySphereCorrections",
+    "final_correction": "FinalCorrectionStep",
+    "final_update": "_FinalUpdate",
+    # FixedUpdate's world clamp (Physics/CudaDeformableBody.cpp:616)
+    "world_clamp": "_WorldConstraints",
 }
+
+
+class Float3(C.Structure):
+    """CUDA float3 passed by value."""
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
 
 
 class _Driver:
@@ -132,7 +152,7 @@ class RefKernels:
             return
         vals = []
         for a in args:
-            if isinstance(a, C._SimpleCData):
+            if isinstance(a, (C._SimpleCData, C.Structure)):
                 vals.append(a)
             elif hasattr(a, "data_ptr"):
                 vals.append(C.c_void_p(a.data_ptr()))
@@ -141,6 +161,8 @@ class RefKernels:
             else:
                 raise TypeError(f"argument {a!r}: pass a ctypes scalar, a tensor or None")
         params = (C.c_void_p * len(vals))(*[C.cast(C.pointer(v), C.c_void_p) for v in vals])
+        if n_threads >= 1 << 31:
+            raise ValueError("launch too large")
         stream = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
         blocks = (n_threads + THREADS - 1) // THREADS
         self.drv("cuLaunchKernel", self.fn[key], blocks, 1, 1, THREADS, 1, 1, 0, stream, params, None)
@@ -290,6 +312,143 @@ class RefKernels:
         out["vf"] = vf[vff[:nvf].bool()].cpu().numpy()
         out["ee"] = ee[eef[:nee].bool()].cpu().numpy()
         return out
+
+    # ------------------------------------------------------------------
+    def solve(self, x, x_prev, topo: dict, vf, ee, *, iterations: int, k_stretch: float, k_bend: float,
+              thickness: float, ground_y: float, dt: float, sphere: tuple | None = None,
+              world: tuple | None = None) -> dict:
+        """PBDStepSolver followed by PBDStepIntegration (Physics/CudaPBD.cu:
+        632-667), run with the reference's own solver kernels.
+
+        x, x_prev: (V, 3) float32 predicted and previous positions; topo: the
+        static topology in the oracle's layout (oracle_ffi.Oracle.topology:
+        stretch ends, rest lengths, bend vertices, the per-vertex slot CSR,
+        pinned ids, attachment lengths, inverse masses, pinned flags); vf, ee:
+        (N, 12) int32 PrimitiveContact records (Physics/Structs.h:106-129);
+        sphere: (centre, radius) or None; world: (min corner, max corner).
+        Returns the positions after the solver iterations (``x``), the
+        velocities and previous positions after _FinalUpdate (``v``,
+        ``x_prev``), the positions after the world clamp of
+        Physics/CudaDeformableUtils.cu:251-267 (``x_end``), and how many
+        ground constraints and attachments the step activated.
+
+        The host work between launches restates the reference's host code:
+        the per-iteration clears of the accumulators, and for the contact
+        corrections the stable key sort, run-length encoding and exclusive
+        sum of Physics/CudaPBD.cu:711-721 (CUB there, numpy here; a stable
+        sort's result is unique).
+        """
+        torch = self.torch
+        f32, i32 = np.float32, np.int32
+        x = np.ascontiguousarray(x, f32)
+        xp = np.ascontiguousarray(x_prev, f32)
+        V = x.shape[0]
+        s12 = np.asarray(topo["s12"], i32).reshape(-1, 2)
+        bq = np.asarray(topo["b"], i32).reshape(-1, 4)
+        soff = np.asarray(topo["soff"], i32)
+        sent = np.asarray(topo["sent"], i32)
+        fixed = np.asarray(topo["fixed"], i32)
+        E, B, S, F = len(s12), len(bq), len(sent), len(fixed)
+        if x.shape != (V, 3) or xp.shape != (V, 3) or len(soff) != V + 1 or soff[0] != 0 or soff[-1] != S \
+                or np.any(np.diff(soff) < 0):
+            raise ValueError("state and slot offsets do not match")
+        for a in (s12, bq, fixed):
+            if a.size and (a.min() < 0 or a.max() >= V):
+                raise ValueError("vertex id out of range")
+        # Slot of each (constraint, role): the inverse of the CSR entries.
+        kind, role, cid = (sent >> 30) & 1, (sent >> 28) & 3, sent & 0x0FFFFFFF
+        so = np.full((E, 2), -1, i32)
+        bo = np.full((B, 4), -1, i32)
+        slots = np.arange(S, dtype=i32)
+        st, bd = kind == 0, kind == 1
+        if np.any(cid[st] >= E) or np.any(role[st] > 1) or np.any(cid[bd] >= B):
+            raise ValueError("slot entry out of range")
+        so[cid[st], role[st]] = slots[st]
+        bo[cid[bd], role[bd]] = slots[bd]
+        if (so < 0).any() or (bo < 0).any():
+            raise ValueError("a constraint end has no slot")
+        vf = np.ascontiguousarray(vf, i32).reshape(-1, 12)
+        ee = np.ascontiguousarray(ee, i32).reshape(-1, 12)
+        for c in (vf, ee):
+            if len(c) and (c[:, :4].min() < 0 or c[:, :4].max() >= V):
+                raise ValueError("contact vertex out of range")
+        nvf, nee = len(vf), len(ee)
+        N = nvf + nee
+
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        d_x, d_xp = dev(x), dev(xp)
+        d_invm = dev(np.asarray(topo["invm"], f32))
+        d_fixedv = dev(np.asarray(topo["pinned"], np.uint8) != 0)
+        d_s1, d_s2 = dev(s12[:, 0]), dev(s12[:, 1])
+        d_s1o, d_s2o = dev(so[:, 0]), dev(so[:, 1])
+        d_sl0 = dev(np.asarray(topo["sl0"], np.float64).astype(f32))
+        d_b = [dev(bq[:, j]) for j in range(4)]
+        d_bo = [dev(bo[:, j]) for j in range(4)]
+        d_phi0 = dev(np.full(max(B, 1), np.float32(3.14159265359), f32))  # Physics/CudaPBD.cu:35,368
+        d_soff = dev(soff)
+        cor = torch.zeros((max(S, 1), 3), dtype=torch.float32, device="cuda")
+        d_fixed = dev(fixed if F else np.zeros(1, i32))
+        d_l0 = dev(np.asarray(topo["lra_l0"], np.float64).reshape(V, F).astype(f32) if F else np.zeros(1, f32))
+        lflag = torch.zeros(max(V * F, 1), dtype=torch.bool, device="cuda")
+        gq = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        gn = torch.zeros_like(gq)
+        gflag = torch.zeros(V, dtype=torch.bool, device="cuda")
+        acc = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        cnt = torch.zeros(V, dtype=torch.int32, device="cuda")
+        h, it = C.c_float(thickness), C.c_int(iterations)
+
+        self.launch("ground_create", V, C.c_int(V), d_x, d_xp, d_invm, C.c_float(ground_y), h, gq, gn, gflag)
+        if F:
+            self.launch("lra_create", V * F, C.c_int(V), C.c_int(F), d_x, d_fixedv, d_fixed, d_l0, lflag)
+        if sphere is not None:
+            sq, sn = torch.zeros_like(gq), torch.zeros_like(gq)
+            sflag = torch.zeros(V, dtype=torch.bool, device="cuda")
+            centre, radius = sphere
+            self.launch("sphere_create", V, C.c_int(V), d_x, d_xp, d_invm, Float3(*[float(q) for q in centre]),
+                        C.c_float(radius), h, sq, sn, sflag)
+        if N:
+            d_vf = dev(vf if nvf else np.zeros((1, 12), i32))
+            d_ee = dev(ee if nee else np.zeros((1, 12), i32))
+            raw_ids = torch.zeros(4 * N, dtype=torch.int32, device="cuda")
+            raw_vals = torch.zeros((4 * N, 3), dtype=torch.float32, device="cuda")
+        for _ in range(iterations):
+            acc.zero_()
+            cnt.zero_()
+            self.launch("ground_apply", V, C.c_int(V), d_x, d_invm, gflag, gq, gn, acc, cnt)
+            if F:
+                self.launch("lra_apply", V, C.c_int(V), C.c_int(F), d_x, d_invm, d_fixed, d_l0, lflag, acc, cnt)
+            self.launch("static_project", E + B, C.c_int(E), C.c_int(B), it, d_x, d_invm, d_s1, d_s2, d_s1o, d_s2o,
+                        C.c_float(k_stretch), d_sl0, *d_b, *d_bo, C.c_float(k_bend), d_phi0, cor)
+            self.launch("static_apply", V, C.c_int(V), cor, d_soff, acc, cnt)
+            if N:
+                self.launch("dyn_project", N, d_x, d_xp, d_invm, h, d_vf, C.c_uint64(nvf), d_ee, C.c_uint64(nee),
+                            raw_ids, raw_vals)
+                torch.cuda.synchronize()
+                ids = raw_ids.cpu().numpy().view(np.uint32)
+                if ids.max() >= V:
+                    raise RuntimeError("correction id out of range")
+                order = np.argsort(ids, kind="stable")
+                sids = ids[order]
+                starts = np.flatnonzero(np.r_[True, sids[1:] != sids[:-1]]).astype(i32)
+                runs = len(starts)
+                d_uniq = dev(sids[starts].astype(np.uint32).view(i32))
+                d_pref = dev(starts)
+                d_vals = dev(raw_vals.cpu().numpy()[order])
+                self.launch("dyn_apply", runs, C.c_int(runs), d_uniq, d_pref, d_vals, C.c_uint64(4 * N), acc, cnt)
+            if sphere is not None:
+                self.launch("sphere_apply", V, C.c_int(V), d_x, h, sflag, sq, sn, acc, cnt)
+            self.launch("final_correction", V, C.c_int(V), acc, cnt, d_x)
+        torch.cuda.synchronize()
+        x_solved = d_x.cpu().numpy().copy()
+        d_v = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        self.launch("final_update", V, C.c_int(V), d_x, d_xp, d_v, d_fixedv, C.c_float(dt))
+        if world is not None:
+            lo, hi = world
+            self.launch("world_clamp", V, C.c_int(V), d_x, Float3(*[float(q) for q in lo]),
+                        Float3(*[float(q) for q in hi]))
+        torch.cuda.synchronize()
+        return dict(x=x_solved, v=d_v.cpu().numpy(), x_prev=d_xp.cpu().numpy(), x_end=d_x.cpu().numpy(),
+                    ground_flags=int(gflag.sum()), lra_flags=int(lflag[:V * F].sum()) if F else 0)
 
 
 def _check_tree(L, R, Pa, T) -> int:

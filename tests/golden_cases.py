@@ -28,6 +28,12 @@ CASES = [
          wind=(1.5, 0.0, -1.0), mesh_thickness=True),
     dict(name="cloth48_k06_step45", scene="small_cloth", kw=dict(seed=9, n=48, stiffness=0.6), steps=45,
          wind=(-1.2, 0.0, 0.8)),
+    # an unpinned cloth that has landed on the ground (ground constraints)
+    dict(name="ground24_step16", scene="small_cloth", kw=dict(seed=3, n=24), steps=16, unpin=True,
+         world_min_y=0.9),
+    # an unpinned cloth draped over the analytic sphere
+    dict(name="sphere24_step22", scene="small_cloth", kw=dict(seed=4, n=24), steps=22, unpin=True,
+         sphere=((0.5, 0.7, 0.5), 0.2)),
 ]
 
 
@@ -37,6 +43,15 @@ def make_spec(case: dict):
         scenes.set_constant_wind(spec.params, tuple(case["wind"]))
     if case.get("mesh_thickness"):
         spec.params.thicknessFromMesh = 1
+    if case.get("unpin"):
+        spec.pinned[:] = 0
+    if case.get("world_min_y") is not None:
+        spec.params.worldMin[1] = case["world_min_y"]
+    if case.get("sphere"):
+        centre, radius = case["sphere"]
+        spec.params.sphereOn = 1
+        spec.params.spherePos[:] = centre
+        spec.params.sphereRadius = radius
     return spec
 
 
@@ -49,6 +64,16 @@ def load(path: Path) -> dict:
 
 def golden_files():
     return sorted(GOLDEN.glob("*.npz"))
+
+
+def solver_inputs(spec, d: dict, oracle) -> dict:
+    """Arguments of the reference's solver chain (refchain.RefKernels.solve)
+    for the golden's state: the oracle's topology and the cloth's parameters."""
+    p = spec.params
+    sphere = ((tuple(p.spherePos), float(p.sphereRadius)) if p.sphereOn else None)
+    return dict(topo=oracle.topology(0), iterations=int(p.solverIterations), k_stretch=float(p.kStretch),
+                k_bend=float(p.kBend), thickness=float(d["thickness"]), ground_y=float(p.worldMin[1]),
+                dt=float(p.timestep), sphere=sphere, world=(tuple(p.worldMin), tuple(p.worldMax)))
 
 
 def expected(d: dict) -> dict:
@@ -145,3 +170,106 @@ def compare_oracle(spec, d: dict) -> list[str]:
         return diff(lambda name: o.debug(0, name), d)
     finally:
         o.close()
+
+
+# Tolerance of the solver comparisons: 1e-5 m on positions (the parity bar of
+# the solver against the FP64 restatement); velocities are position
+# differences over one timestep, so theirs is 1e-5 m / dt.
+SOLVER_ATOL_X = 1e-5
+
+
+def oracle_solve(spec, d: dict, fp64: bool, forced: dict | None = None):
+    """The oracle's solver iterations and velocity update on the golden's
+    predicted state with the reference's contacts, optionally with imposed
+    decisions: (x, v, x_prev, the decisions taken)."""
+    from oracle.oracle_ffi import Oracle
+    o = Oracle([spec], fp64=fp64)
+    try:
+        vf = (d["ref_vf"][:, :4], d["ref_vf"][:, 4:8].view(np.float32))
+        ee = (d["ref_ee"][:, :4], d["ref_ee"][:, 4:8].view(np.float32))
+        x, v, xp = o.solve_on(0, d["x"], d["x_prev"], vf, ee, forced=forced)
+        return x, v, xp, o.solve_decisions(0)
+    finally:
+        o.close()
+
+
+DECISIONS = ("ground", "ground_it", "lra", "dyn", "sphere")
+
+
+def decision_diff(a: dict, b: dict) -> int:
+    """How many discrete decisions differ between two solves of one state."""
+    n = 0
+    for k in DECISIONS:
+        x, y = np.asarray(a[k]).ravel(), np.asarray(b[k]).ravel()
+        if x.shape != y.shape:
+            return -1
+        if k == "ground_it":
+            n += int(np.unpackbits((x ^ y).view(np.uint8)).sum())
+        else:
+            n += int(np.count_nonzero(x != y))
+    return n
+
+
+def bend_conditioning(spec, d: dict) -> tuple[float, float]:
+    """(smallest 1 - d over every bend and solver iterate, the smallest value
+    at which positions are still comparable within SOLVER_ATOL_X).
+
+    d = n1 . n2 is the cosine of the reference's bend angle on the raw
+    positions (Physics/CudaPBD.cu:1035-1058).  As d -> 1 its correction is
+    0 * inf: sqrt(1 - d^2) (phi - phi0) over a scale factor that vanishes like
+    1 - d, applied along vectors of size sqrt(1 - d).  A float rounding of the
+    unit normals (eps = 2^-24) then moves the correction by about
+    L eps / sqrt(1 - d) for edges of length L, so two correct FP32
+    implementations, or FP32 and FP64, agree within the tolerance only while
+    1 - d >= (L eps / tol)^2.  The iterates are the FP32 oracle's, which
+    follow the reference's formulas."""
+    from oracle.oracle_ffi import Oracle
+    o = Oracle([spec], fp64=False)
+    try:
+        vf = (d["ref_vf"][:, :4], d["ref_vf"][:, 4:8].view(np.float32))
+        ee = (d["ref_ee"][:, :4], d["ref_ee"][:, 4:8].view(np.float32))
+        o.solve_on(0, d["x"], d["x_prev"], vf, ee)
+        t = o.topology(0)
+        b = t["b"]
+        worst = np.inf
+        for k in range(int(spec.params.solverIterations)):
+            x = o.solve_iterate(0, k).astype(np.float64)
+            c23 = np.cross(x[b[:, 1]], x[b[:, 2]])
+            c24 = np.cross(x[b[:, 1]], x[b[:, 3]])
+            n1 = c23 / np.linalg.norm(c23, axis=1, keepdims=True)
+            n2 = c24 / np.linalg.norm(c24, axis=1, keepdims=True)
+            worst = min(worst, float((1.0 - (n1 * n2).sum(axis=1)).min()))
+        edge = float(np.max(t["sl0"]))
+        return worst, (edge * 2.0 ** -24 / SOLVER_ATOL_X) ** 2
+    finally:
+        o.close()
+
+
+def well_conditioned(spec, d: dict) -> bool:
+    worst, bound = bend_conditioning(spec, d)
+    return worst >= bound
+
+
+def compare_oracle_solver(spec, d: dict) -> dict:
+    """Largest differences between the oracle's solver and the reference's,
+    on positions after the iterations and on velocities.
+
+    The FP32 oracle runs on its own decisions; the share of vertices on which
+    it agrees with the reference bit for bit is reported.  The FP64 oracle
+    runs with the FP32 oracle's decisions imposed: the Jacobi update divides
+    by the number of non-zero corrections, so a threshold that FP32 and FP64
+    decide differently (a contact or a ground plane the previous step left at
+    exactly the thickness) moves a vertex by a finite amount."""
+    out = {}
+    x, v, xp, dec32 = oracle_solve(spec, d, False)
+    for fp64 in (False, True):
+        if fp64:
+            x, v, xp, _ = oracle_solve(spec, d, True, forced=dec32)
+        tag = "fp64" if fp64 else "fp32"
+        out[f"{tag}_dx"] = float(np.abs(x - d["ref_solve_x"]).max())
+        out[f"{tag}_dv"] = float(np.abs(v - d["ref_solve_v"]).max())
+        out[f"{tag}_dxp"] = float(np.abs(xp - d["ref_solve_x_prev"]).max())
+        if not fp64:
+            same = np.all(x.view(np.uint32) == d["ref_solve_x"].view(np.uint32), axis=1)
+            out["fp32_bitexact"] = float(same.mean())
+    return out

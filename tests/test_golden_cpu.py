@@ -5,7 +5,17 @@ reference's collision kernels, compiled from its sources and run on a GPU
 (tests/golden/make_golden.py, oracle/ref_pin/).  The FP32 oracle must
 reproduce every stage bit for bit: Morton codes, the stable sort, the Karras
 hierarchy, the refit boxes and rightmost leaves, the broadphase pairs and the
-VF / EE contacts (vertex ids and weights).
+VF / EE contacts (vertex ids and weights).  The golden files also hold what
+the reference's solver kernels (PBDStepSolver, _FinalUpdate) computed from
+the same state with those contacts.  The FP32 oracle's solver, which
+evaluates the reference's formulas in the reference's order, must agree with
+it within golden_cases.SOLVER_ATOL_X on every state.  (Bit equality is not
+asked of the solver: the reference's kernels call CUDA's powf and acosf,
+whose last-place rounding differs from the host library's.)  The FP64 oracle,
+run with the FP32 oracle's discrete decisions, must agree within the same
+tolerance on every state whose bends stay away from the reference's d -> 1
+singularity (golden_cases.bend_conditioning); windy20_mesh_h_step40 passes
+within 1.7e-8 of it and is the case that shows the singularity.
 """
 from __future__ import annotations
 
@@ -36,3 +46,32 @@ def test_golden_inputs_are_in_reference_layout(path):
     assert d["ref_lefts"].shape == (T - 1,)
     assert np.all(np.diff(d["ref_morton"].astype(np.uint64).astype(object)) >= 0)
     assert sorted(d["ref_order"].tolist()) == list(range(T))
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_oracle_solver_matches_reference_kernels(path):
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    dt = float(d["dt"])
+    r = golden_cases.compare_oracle_solver(spec, d)
+    tags = ("fp32", "fp64") if golden_cases.well_conditioned(spec, d) else ("fp32",)
+    for tag in tags:
+        assert r[f"{tag}_dx"] <= golden_cases.SOLVER_ATOL_X, r
+        assert r[f"{tag}_dxp"] <= golden_cases.SOLVER_ATOL_X, r
+        assert r[f"{tag}_dv"] <= golden_cases.SOLVER_ATOL_X / dt, r
+    # most vertices come out bit-identical to the reference's kernels
+    assert r["fp32_bitexact"] >= 0.8, r
+
+
+def test_bend_singularity_is_the_only_excluded_case():
+    """Exactly one golden state is excluded from the FP64 comparison, and it
+    is excluded because a bend passes within the bound of d = 1."""
+    excluded = []
+    for path in FILES:
+        d = golden_cases.load(path)
+        spec = golden_cases.make_spec(d["case"])
+        worst, bound = golden_cases.bend_conditioning(spec, d)
+        if worst < bound:
+            excluded.append((path.stem, worst, bound))
+    assert [e[0] for e in excluded] == ["windy20_mesh_h_step40"], excluded
+    assert excluded[0][1] < 0.2 * excluded[0][2]

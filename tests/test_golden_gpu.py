@@ -5,7 +5,12 @@ damping and wind are switched off so that its prediction x = x_prev + dt v
 reproduces the golden's predicted positions bit for bit, and the triangle
 order is set to the golden's pre-sort order.  One step later its Morton
 codes, sorted order, hierarchy, refit boxes, rightmost leaves, pairs and
-VF / EE contacts must equal the reference's bit for bit.
+VF / EE contacts must equal the reference's bit for bit, and its positions
+and velocities after the solver, the velocity update and the world clamp
+must agree with what the reference's solver kernels computed from the same
+state within golden_cases.SOLVER_ATOL_X (1e-5 m; 1e-5 m / dt on velocities)
+on every state whose bends stay away from the reference's d -> 1
+singularity (golden_cases.bend_conditioning).
 """
 from __future__ import annotations
 
@@ -39,5 +44,14 @@ def test_engine_matches_reference_kernels(path):
         assert np.array_equal(b.debug(0, "PRED_X").view(np.uint32), d["x"].view(np.uint32))
         assert np.array_equal(b.debug(0, "PERM_BEFORE"), d["perm_before"].astype(np.uint32))
         assert golden_cases.diff(lambda name: b.debug(0, name), d) == []
+        st = b.get_state(0)
+        assert np.isfinite(st["x"]).all() and np.isfinite(st["v"]).all()
+        if not golden_cases.well_conditioned(spec, d):
+            return
+        dt = float(d["dt"])
+        dx = np.abs(st["x"] - d["ref_solve_x_end"]).max()
+        dv = np.abs(st["v"] - d["ref_solve_v"]).max()
+        assert dx <= golden_cases.SOLVER_ATOL_X, dx
+        assert dv <= golden_cases.SOLVER_ATOL_X / dt, dv
     finally:
         b.close()
