@@ -418,9 +418,11 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             const int li[4] = {v.x - vo, v.y - vo, v.z - vo, v.w - vo};
             const float4 P[4] = {X(li[0]), X(li[1]), X(li[2]), X(li[3])};
             const uint32_t ent = 4u * (isvf ? gi : nvf_all + gi);
+            float3 cs[4];
+            contact_all_pos(P[0], P[1], P[2], P[3], w, isvf, h, cs);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const float3 corr = contact_corr_pos(P[0], P[1], P[2], P[3], w, isvf, h, j);
+                const float3 corr = cs[j];
                 const bool nz = !is_zero(corr);
                 if (nz) add_corr(li[j], corr, true);
                 if (d.dbg_dyn_nz) d.dbg_dyn_nz[(size_t)it * d.dyn_cap + ent + j] = nz ? 1 : 0;

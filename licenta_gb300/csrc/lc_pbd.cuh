@@ -123,4 +123,46 @@ __device__ __forceinline__ float3 contact_corr_pos(float4 A, float4 B, float4 C,
     return mul(mul(neg(n), b3), -s * D.w);
 }
 
+// The same contact evaluated once for its four slots: out[j] equals
+// contact_corr_pos(..., j) (the same expressions on the same operands).
+__device__ __forceinline__ void contact_all_pos(float4 A, float4 B, float4 C, float4 D, float4 w, bool isvf, float h,
+                                                float3 out[4]) {
+    float3 n;
+    float s;
+    float b[4];
+    if (isvf) {
+        b[0] = 1.f;
+        b[1] = clampf(-w.y, 0.f, 1.f), b[2] = clampf(-w.z, 0.f, 1.f), b[3] = clampf(-w.w, 0.f, 1.f);
+        const float3 q = add(add(mul(xyz(B), b[1]), mul(xyz(C), b[2])), mul(xyz(D), b[3]));
+        n = sub(xyz(A), q);
+        const float l = len(n);
+        n = dvs(n, l);
+        const float cc = l - h;
+        s = A.w + B.w * b[1] * b[1] + C.w * b[2] * b[2] + D.w * b[3] * b[3];
+        if (s == 0.f) { out[0] = out[1] = out[2] = out[3] = f3(0.f, 0.f, 0.f); return; }
+        s = cc / s;
+        s = cc < 0.f ? s : 0.f;
+        out[0] = mul(n, -s * A.w);
+        out[1] = mul(mul(neg(n), b[1]), -s * B.w);
+        out[2] = mul(mul(neg(n), b[2]), -s * C.w);
+        out[3] = mul(mul(neg(n), b[3]), -s * D.w);
+        return;
+    }
+    b[0] = w.x, b[1] = w.y, b[2] = -w.z, b[3] = -w.w;
+    const float3 q0 = add(mul(xyz(A), b[0]), mul(xyz(B), b[1]));
+    const float3 q1 = add(mul(xyz(C), b[2]), mul(xyz(D), b[3]));
+    n = sub(q0, q1);
+    const float l = len(n);
+    n = dvs(n, l);
+    const float cc = l - h;
+    s = A.w * b[0] * b[0] + B.w * b[1] * b[1] + C.w * b[2] * b[2] + D.w * b[3] * b[3];
+    if (s == 0.f) { out[0] = out[1] = out[2] = out[3] = f3(0.f, 0.f, 0.f); return; }
+    s = cc / s;
+    s = cc < 0.f ? s : 0.f;
+    out[0] = mul(mul(n, b[0]), -s * A.w);
+    out[1] = mul(mul(n, b[1]), -s * B.w);
+    out[2] = mul(mul(neg(n), b[2]), -s * C.w);
+    out[3] = mul(mul(neg(n), b[3]), -s * D.w);
+}
+
 }  // namespace lc
