@@ -256,14 +256,20 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
 // ---------------------------------------------------------------------------
 // Scatter variant: every constraint is evaluated once per iteration by one
 // thread of the cluster, which adds its corrections to the owners'
-// accumulators (local or distributed shared memory).  Accumulators are 64-bit
-// fixed point (2^-32 m), so the sums are exact and independent of the order
+// accumulators (local or distributed shared memory).  Accumulators are
+// fixed-point integers, so the sums are exact and independent of the order
 // the atomics land in, and results stay deterministic.
-// Shared memory per vertex: x (16) + 3 x s64 (24) + count (4) + ground (4) +
-// LRA flags (1).
+// Shared memory per vertex: x (16) + two packed sums (16) + ground (4) + LRA
+// flags (1).
 // ---------------------------------------------------------------------------
 // Correction sums in 32-bit fixed point: 2^25 per metre, i.e. 3e-8 m steps
-// (finer than a float's spacing at 1 m) and +-64 m of range.
+// (finer than a float's spacing at 1 m) and +-64 m of range.  Two 64-bit
+// words per vertex hold the four sums, so one correction costs two atomics:
+//   xc = X * 2^32 + count  (the count never reaches 2^32, so it never carries
+//                           into X, and X wraps like a 32-bit sum)
+//   yz = Y * 2^32 + Z      (an exact 64-bit integer sum: Z is the low word
+//                           read as signed, Y = (yz - Z) / 2^32)
+// The decoded sums are the same integers as four separate 32-bit sums.
 constexpr int kScatterBytesPerVertex = 37;
 constexpr float kFix = 33554432.f;           // 2^25
 constexpr float kFixInv = 1.f / 33554432.f;  // exact power of two
@@ -282,11 +288,9 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
     const int cap = a.chunk_cap;
     extern __shared__ float4 smem4[];
     float4 *xs = smem4;
-    int *ax = reinterpret_cast<int *>(xs + cap);
-    int *ay = ax + cap;
-    int *az = ay + cap;
-    uint32_t *cnt = reinterpret_cast<uint32_t *>(az + cap);
-    float *gq = reinterpret_cast<float *>(cnt + cap);
+    unsigned long long *axc = reinterpret_cast<unsigned long long *>(xs + cap);
+    unsigned long long *ayz = axc + cap;
+    float *gq = reinterpret_cast<float *>(ayz + cap);
     uint8_t *lra = reinterpret_cast<uint8_t *>(gq + cap);
     const uint32_t magic = (uint32_t)((0x100000000ull + chunk - 1) / chunk);
     auto owner = [&](int li) { return (int)__umulhi((uint32_t)li, magic); };
@@ -298,21 +302,18 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
     auto add_corr = [&](int li, float3 v, bool count) {
         const int o = owner(li);
         const int k = li - o * chunk;
-        int *px = o == r ? ax : cluster.map_shared_rank(ax, o);
-        int *py = o == r ? ay : cluster.map_shared_rank(ay, o);
-        int *pz = o == r ? az : cluster.map_shared_rank(az, o);
-        atomicAdd(px + k, __float2int_rn(v.x * kFix));
-        atomicAdd(py + k, __float2int_rn(v.y * kFix));
-        atomicAdd(pz + k, __float2int_rn(v.z * kFix));
-        if (count) atomicAdd(o == r ? cnt + k : cluster.map_shared_rank(cnt, o) + k, 1u);
+        unsigned long long *pxc = o == r ? axc : cluster.map_shared_rank(axc, o);
+        unsigned long long *pyz = o == r ? ayz : cluster.map_shared_rank(ayz, o);
+        const int ix = __float2int_rn(v.x * kFix), iy = __float2int_rn(v.y * kFix), iz = __float2int_rn(v.z * kFix);
+        atomicAdd(pxc + k, ((unsigned long long)(uint32_t)ix << 32) + (count ? 1ull : 0ull));
+        atomicAdd(pyz + k, ((unsigned long long)(uint32_t)iy << 32) + (unsigned long long)(long long)iz);
     };
     const float qnan = __int_as_float(0x7fc00000);
     for (int i = tid; i < n_own; i += bs) {
         const int g = vo + lo + i;
         const float4 x4 = d.x[g];
         xs[i] = x4;
-        ax[i] = ay[i] = az[i] = 0;
-        cnt[i] = 0;
+        axc[i] = ayz[i] = 0ull;
         lra[i] = 0;
         float q = qnan;
         float4 qdbg = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -433,8 +434,8 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             const float cv = x4.y - gq[i];
             const bool ground = cv < 0.f;
             if (ground) {
-                atomicAdd(ay + i, __float2int_rn(-cv * kFix));
-                atomicAdd(cnt + i, 1u);
+                atomicAdd(ayz + i, (unsigned long long)(uint32_t)__float2int_rn(-cv * kFix) << 32);
+                atomicAdd(axc + i, 1ull);
             }
             if (d.dbg_ground_it) {
                 const uint32_t bit = ground ? (1u << it) : 0u;
@@ -455,14 +456,16 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
         cluster.sync();
         for (int i = tid; i < n_own; i += bs) {
             const int g = vo + lo + i;
-            const float n = (float)(__ldg(&d.soff[g + 1]) - __ldg(&d.soff[g]) + (int)cnt[i]);
+            const unsigned long long xc = axc[i], yz = ayz[i];
+            const int sx = (int)(uint32_t)(xc >> 32), sz = (int)(uint32_t)yz;
+            const int sy = (int)(uint32_t)((yz - (unsigned long long)(long long)sz) >> 32);
+            const float n = (float)(__ldg(&d.soff[g + 1]) - __ldg(&d.soff[g]) + (int)(uint32_t)xc);
             float4 x4 = xs[i];
-            x4.x += (__int2float_rn(ax[i]) * kFixInv) / n;
-            x4.y += (__int2float_rn(ay[i]) * kFixInv) / n;
-            x4.z += (__int2float_rn(az[i]) * kFixInv) / n;
+            x4.x += (__int2float_rn(sx) * kFixInv) / n;
+            x4.y += (__int2float_rn(sy) * kFixInv) / n;
+            x4.z += (__int2float_rn(sz) * kFixInv) / n;
             xs[i] = x4;
-            ax[i] = ay[i] = az[i] = 0;
-            cnt[i] = 0;
+            axc[i] = ayz[i] = 0ull;
         }
         cluster.sync();
     }
