@@ -658,6 +658,19 @@ __device__ bool test_ee(float3 x1, float3 x2, float3 x3, float3 x4, float th, Wt
     return false;
 }
 
+// A test_ee hit places both closest points on their segments (the parallel
+// case uses the midpoints, the others clamp the parameters to [0,1]), up to
+// a few float roundings of the coordinates, and needs their distance <= th.
+// So edges whose boxes are apart by more than th plus a margin far above
+// those roundings (1e-5 m + th/1000) cannot hit, and the test is skipped:
+// the decision and the weights are the reference's bits either way.
+__device__ __forceinline__ bool ee_far(float3 a, float3 b, float3 c, float3 d, float th) {
+    const float m = th + 1e-5f + 1e-3f * th;
+    return fminf(a.x, b.x) - fmaxf(c.x, d.x) > m || fminf(c.x, d.x) - fmaxf(a.x, b.x) > m ||
+           fminf(a.y, b.y) - fmaxf(c.y, d.y) > m || fminf(c.y, d.y) - fmaxf(a.y, b.y) > m ||
+           fminf(a.z, b.z) - fmaxf(c.z, d.z) > m || fminf(c.z, d.z) - fmaxf(a.z, b.z) > m;
+}
+
 // Particle swept box of Collision/FeatureList.cu:134-148, recomputed from
 // x and x_prev (min/max are exact, so this equals the stored boxes).
 struct Box { float3 lo, hi; };
@@ -947,6 +960,7 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
                 x2 = add(x2, mul(v2, tt));
                 x3 = add(x3, mul(v3, tt));
                 x4 = add(x4, mul(v4, tt));
+                if (!VF && ee_far(x1, x2, x3, x4, h)) return false;
                 return VF ? test_vf(x4, x1, x2, x3, h, wt) : test_ee(x1, x2, x3, x4, h, wt);
             };
             for (int i = 0; i <= ncp && !found; ++i) {

@@ -4,12 +4,23 @@
 // read-backs of Core/CubWrappers.cuh:26-50, 77-89.
 //
 // Reduce-then-scan over a fixed grid of kScanBlocks blocks: block b owns the
-// contiguous range [b*chunk, (b+1)*chunk) of the n inputs.  Deterministic.
+// contiguous range [b*chunk, (b+1)*chunk) of the n inputs, chunk a whole
+// number of 2048-element tiles.  A thread's 8 values of a tile are then 32
+// contiguous bytes on a 32-byte boundary (when the arrays start on 16-byte
+// boundaries, as cudaMalloc's do), read and written as two 16-byte vectors.
+// Deterministic.
 #include "lc_internal.cuh"
 
 namespace lc {
 
 constexpr int kScanItems = 8;  // per thread per tile
+constexpr uint32_t kScanTile = kThreads * kScanItems;
+
+// Elements per block: ceil(n / kScanBlocks) rounded up to whole tiles.
+__device__ __forceinline__ uint64_t scan_chunk(uint32_t n) {
+    const uint64_t c = ((uint64_t)n + kScanBlocks - 1) / kScanBlocks;
+    return (c + kScanTile - 1) / kScanTile * kScanTile;
+}
 
 __device__ __forceinline__ uint32_t scan_len(const uint32_t *n_dev, uint32_t n_static, uint32_t n_cap) {
     uint32_t n = n_dev ? *n_dev : n_static;
@@ -51,11 +62,11 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t &total)
 __global__ void k_scan_reduce(const uint32_t *__restrict__ in, const uint32_t *n_dev, uint32_t n_static,
                               uint32_t n_cap, uint32_t *__restrict__ partial) {
     const uint32_t n = scan_len(n_dev, n_static, n_cap);
-    const uint32_t chunk = (n + kScanBlocks - 1) / kScanBlocks;
-    const uint32_t b0 = blockIdx.x * chunk;
-    const uint32_t b1 = min(n, b0 + chunk);
+    const uint64_t chunk = scan_chunk(n);
+    const uint64_t b0 = blockIdx.x * chunk;
+    const uint64_t b1 = min((uint64_t)n, b0 + chunk);
     uint32_t s = 0;
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += kThreads) s += in[i];
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += kThreads) s += in[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     __shared__ uint32_t ws[kThreads / 32];
@@ -89,27 +100,42 @@ __global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restric
                             uint32_t n_static, uint32_t n_cap, const uint32_t *__restrict__ partial,
                             uint32_t *total_out, unsigned long long *total_out64) {
     const uint32_t n = scan_len(n_dev, n_static, n_cap);
-    const uint32_t chunk = (n + kScanBlocks - 1) / kScanBlocks;
-    const uint32_t b0 = blockIdx.x * chunk;
-    const uint32_t b1 = min(n, b0 + chunk);
+    const uint64_t chunk = scan_chunk(n);
+    const uint64_t b0 = blockIdx.x * chunk;
+    const uint64_t b1 = min((uint64_t)n, b0 + chunk);
+    const bool vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
     uint32_t carry = partial[blockIdx.x];
-    for (uint32_t base = b0; base < b1; base += kThreads * kScanItems) {
+    for (uint64_t base = b0; base < b1; base += kScanTile) {
         uint32_t vals[kScanItems];
         uint32_t local = 0;
-        const uint32_t mine = base + threadIdx.x * kScanItems;
+        const uint64_t mine = base + (uint64_t)threadIdx.x * kScanItems;
+        const bool full = vec && mine + kScanItems <= b1;
+        if (full) {
+            const uint4 a0 = *reinterpret_cast<const uint4 *>(in + mine);
+            const uint4 a1 = *reinterpret_cast<const uint4 *>(in + mine + 4);
+            vals[0] = a0.x; vals[1] = a0.y; vals[2] = a0.z; vals[3] = a0.w;
+            vals[4] = a1.x; vals[5] = a1.y; vals[6] = a1.z; vals[7] = a1.w;
+        } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            uint32_t i = mine + k;
-            vals[k] = i < b1 ? in[i] : 0u;
-            local += vals[k];
+            for (int k = 0; k < kScanItems; ++k) vals[k] = mine + k < b1 ? in[mine + k] : 0u;
         }
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) local += vals[k];
         uint32_t tot;
         uint32_t ex = block_excl_scan(local, tot) + carry;
+        uint32_t o[kScanItems];
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
-            uint32_t i = mine + k;
-            if (i < b1) out[i] = ex;
+            o[k] = ex;
             ex += vals[k];
+        }
+        if (full) {
+            *reinterpret_cast<uint4 *>(out + mine) = make_uint4(o[0], o[1], o[2], o[3]);
+            *reinterpret_cast<uint4 *>(out + mine + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k)
+                if (mine + k < b1) out[mine + k] = o[k];
         }
         carry += tot;
     }
