@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-lbvh", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--lanes", type=int, default=2,
+                    help="concurrent batches the workload is cut into (lc_group_step)")
     ap.add_argument("--cloths", type=int, default=NCLOTH,
                     help="cloths per GPU (the workload has 256; fewer only for small profiling cases)")
     return ap.parse_args()
@@ -196,6 +198,23 @@ def sampled_profile(batch, state, steps: int, stream, samples: int = 5) -> dict:
     return acc
 
 
+def combined_profile(profs: list) -> dict:
+    """The member batches' profiles (each measured alone) as one: per-kernel
+    times and pair / contact counts add up, since together they do the
+    whole workload's work."""
+    out = {k: (dict(v) if isinstance(v, dict) else v) for k, v in profs[0].items()}
+    for p in profs[1:]:
+        for k, v in p.items():
+            if isinstance(v, dict):
+                for q in v:
+                    out[k][q] += v[q]
+            elif isinstance(v, float) and k != "samples":
+                out[k] += v
+    out["kernels_per_step"] = sum(int(p["kernels_per_step"]) for p in profs)
+    out["lanes"] = len(profs)
+    return out
+
+
 def algorithmic_bytes(batch, specs, prof) -> dict:
     """Compulsory DRAM bytes per launch of the hot kernels (the model is
     written out in the design doc).  Pair and contact counts are the profile's
@@ -326,9 +345,10 @@ def lbvh_timing(seed: int, count: int = 1_000_000) -> dict:
             "l2": "flushed by a 256 MB write before each timed build"}
 
 
-def cpu_baseline(specs, seed: int, cloths: int = 64, steps: int = 2) -> dict:
+def cpu_baseline(specs, seed: int, cloths: int = 256, steps: int = 5) -> dict:
     """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
-    cloths on every host core, on a seeded sample of the workload."""
+    cloths on every host core, on a bounded sample of the workload (every
+    cloth by default, for a few steps: about 10 s of host work)."""
     from oracle.oracle_ffi import Oracle, max_threads
     rng = np.random.default_rng(seed + 7)
     pick = sorted(rng.choice(len(specs), size=min(cloths, len(specs)), replace=False).tolist())
@@ -377,7 +397,7 @@ def run_ours(args, world, rank, local):
     import torch
     import torch.distributed as dist
 
-    from licenta_gb300 import ClothBatch, scenes
+    from licenta_gb300 import ClothBatch, ClothBatchGroup, scenes
 
     torch.cuda.set_device(local)
     if world > 1 and not dist.is_initialized():
@@ -395,23 +415,30 @@ def run_ours(args, world, rank, local):
         return float(t.item())
 
     specs = scenes.batched_cloths(seed=args.seed + rank, count=args.cloths)
-    batch = ClothBatch(specs)
+    # the workload as `lanes` concurrent batches of contiguous cloth ranges
+    batch = ClothBatchGroup(specs, lanes=args.lanes) if args.lanes > 1 else ClothBatch(specs)
+    members = batch.batches if args.lanes > 1 else [batch]
     stream = torch.cuda.Stream()
     batch.step(args.warmup, stream)
     batch.sync()
     tuning = None
     if not args.no_autotune:
-        # launch shapes picked by the project's autotuner on this state (each
-        # candidate timed from the same saved state; the state is restored)
+        # launch shapes picked by the project's autotuner on this state, for
+        # each member batch (each candidate timed from the same saved state;
+        # the state is restored)
         from licenta_gb300 import autotune
+        tuning = {"config": [], "candidates": 0}
         with torch.cuda.stream(stream):
-            tuned = autotune.autotune(batch, steps=2, warmup=1, cache=None,
-                                      space={"traverse_block": (64, 128, 256), "jacobi_block": (256,),
-                                             "narrow_blocks_per_sm": (8, 16), "solver_variant": (1, 3),
-                                             "cluster_size": (8, 16)})
-        tuning = {"config": tuned["config"], "candidates": len(tuned["tried"])}
+            for m in members:
+                tuned = autotune.autotune(m, steps=2, warmup=1, cache=None,
+                                          space={"traverse_block": (64, 128, 256), "jacobi_block": (256,),
+                                                 "narrow_blocks_per_sm": (8, 16), "solver_variant": (1, 3),
+                                                 "cluster_size": (8, 16)})
+                tuning["config"].append(tuned["config"])
+                tuning["candidates"] += len(tuned["tried"])
 
-    state0 = save_state(batch, stream)  # start of the timed rollout, for the sampled profile
+    # start of the timed rollout, for the sampled profile
+    state0 = [save_state(m, stream) for m in members]
 
     # ---- device-timed region ------------------------------------------------
     clocks = ClockSampler(local)
@@ -451,7 +478,7 @@ def run_ours(args, world, rank, local):
            "what": "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state"}
 
     # ---- profile + roofline: steps sampled over the timed rollout ------------
-    prof = sampled_profile(batch, state0, args.steps, stream)
+    prof = combined_profile([sampled_profile(m, st, args.steps, stream) for m, st in zip(members, state0)])
     alg = algorithmic_bytes(batch, specs, prof)
     iters = 10
     if prof["solver_variant"] >= 2:  # cluster-resident solver: one launch per step
@@ -511,6 +538,7 @@ def run_ours(args, world, rank, local):
                    "global_batch": world * args.cloths, "cloths_per_gpu": args.cloths,
                    "vertices_per_gpu": V, "triangles_per_gpu": T, "iterations": 10, "dt": 1.0 / 60.0,
                    "parallelism": f"shard-by-cloth x{world}",
+                   "concurrent_batches": args.lanes,
                    "l2": f"inputs larger than L2 (vertex state {state_mb:.0f} MB + constraints + pair buffers)"},
         "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "e2e": e2e,
         "gpu_launches": int(prof["kernels_per_step"]) * args.steps,
@@ -519,7 +547,8 @@ def run_ours(args, world, rank, local):
                     "solver_ms": prof["solver_ms"], "sort_ms": prof["sort_ms"],
                     "kernels_per_step": prof["kernels_per_step"], "sizes": alg["_sizes"],
                     "sampled_steps": prof["samples"],
-                    "what": "per-launch times averaged over steps sampled evenly across the timed rollout"},
+                    "what": "per-launch times averaged over steps sampled evenly across the timed rollout; with "
+                            "concurrent batches, each kernel's launches of the member batches, timed alone, summed"},
         "plain": plain,
         "adjoint": adj,
         "lbvh": lbvh,

@@ -144,6 +144,22 @@ lc_status lc_batch_step(lc_batch *b, int32_t nsteps, void *stream);
 /* Waits for the stream work of the batch and reports latched device errors. */
 lc_status lc_batch_sync(lc_batch *b);
 
+/* Concurrent batches.  A group steps several batches (for example the two
+ * halves of one workload) at the same time, each on a stream of the group's
+ * own, forked from and joined back into the caller's stream: one batch's
+ * latency-bound kernels (hierarchy build, on-chip solver) then overlap with
+ * the other's.  The batches stay owned by the caller and usable on their own;
+ * each must be in at most one group and be destroyed after it.  An extension
+ * of lc_batch_step (Physics/CudaDeformableBody.cpp:550-627 for each cloth)
+ * with no counterpart in the reference. */
+typedef struct lc_group lc_group;
+lc_status lc_group_create(lc_batch *const *batches, int32_t count, lc_group **out);
+/* nsteps x lc_batch_step of every batch, interleaved step by step across the
+ * group's streams; stream waits for all of them.  lc_batch_sync of a member
+ * then waits on stream. */
+lc_status lc_group_step(lc_group *g, int32_t nsteps, void *stream);
+lc_status lc_group_destroy(lc_group *g);
+
 lc_status lc_batch_num_cloths(const lc_batch *b, int32_t *out);
 lc_status lc_batch_cloth_sizes(const lc_batch *b, int32_t cloth, int32_t *num_vertices,
                                int32_t *num_triangles);

@@ -89,6 +89,9 @@ SIGNATURES = {
     "lc_batch_set_constraint_stiffness": (C.c_int, [VP, VP, VP, C.c_int32]),
     "lc_batch_get_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
     "lc_batch_set_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
+    "lc_group_create": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
+    "lc_group_step": (C.c_int, [VP, C.c_int32, VP]),
+    "lc_group_destroy": (C.c_int, [VP]),
     "lc_batch_state_size": (C.c_int, [VP, C.POINTER(C.c_uint64)]),
     "lc_batch_save_state": (C.c_int, [VP, VP, VP]),
     "lc_batch_load_state": (C.c_int, [VP, VP, VP]),

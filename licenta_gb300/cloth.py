@@ -190,6 +190,94 @@ class ClothBatch:
         return out
 
 
+class ClothBatchGroup:
+    """One workload stepped as several concurrent batches (lc_group_*).
+
+    The cloths are cut into ``lanes`` contiguous ranges of about equal vertex
+    count; each range is its own ClothBatch and the group steps them on
+    streams of its own, so one batch's latency-bound kernels overlap with the
+    others'.  Whole-state copies take the same packed arrays as ClothBatch
+    (cloth order), each lane reading or writing its slice.
+    """
+
+    def __init__(self, specs: Sequence[ClothSpec], lanes: int = 2, **kw):
+        specs = list(specs)
+        if lanes < 1 or lanes > len(specs):
+            raise ValueError("lanes must lie in 1..number of cloths")
+        cum = np.cumsum([s.num_vertices for s in specs])
+        cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / lanes)) + 1 for k in range(1, lanes)] + [len(specs)]
+        cuts = sorted(set(min(max(c, 1), len(specs)) for c in cuts[1:-1]) | {0, len(specs)})
+        self.ranges = list(zip(cuts[:-1], cuts[1:]))
+        self.batches = [ClothBatch(specs[a:b], **kw) for a, b in self.ranges]
+        self.specs = specs
+        self.num_vertices = [s.num_vertices for s in specs]
+        self._voff = [int(sum(self.num_vertices[:a])) for a, _ in self.ranges]
+        arr = (C.c_void_p * len(self.batches))(*[b._h.value for b in self.batches])
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().lc_group_create(arr, len(self.batches), C.byref(h)), "lc_group_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _ffi.lib().lc_group_destroy(self._h)
+            self._h = None
+        for b in getattr(self, "batches", []):
+            b.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, nsteps: int = 1, stream=None) -> None:
+        _ffi.check(_ffi.lib().lc_group_step(self._h, nsteps, _stream_handle(stream)), "lc_group_step")
+
+    def sync(self) -> None:
+        for b in self.batches:
+            b.sync()
+
+    def locate(self, cloth: int) -> tuple[ClothBatch, int]:
+        """The member batch holding a cloth and the cloth's index there."""
+        for (a, e), b in zip(self.ranges, self.batches):
+            if a <= cloth < e:
+                return b, cloth - a
+        raise IndexError(cloth)
+
+    def get_state(self, cloth: int) -> dict:
+        b, k = self.locate(cloth)
+        return b.get_state(k)
+
+    def _slices(self, ptrs, stride: int):
+        for off, b in zip(self._voff, self.batches):
+            yield b, [None if p is None else p + off * stride for p in ptrs]
+
+    def write_state(self, x, x_prev, v, is_host: bool, stream=None) -> None:
+        for b, (px, pp, pv) in self._slices((x, x_prev, v), 12):
+            b.write_state(px, pp, pv, is_host, stream)
+
+    def read_state(self, x, x_prev, v, is_host: bool, stream=None) -> None:
+        for b, (px, pp, pv) in self._slices((x, x_prev, v), 12):
+            b.read_state(px, pp, pv, is_host, stream)
+
+    def counters(self) -> dict:
+        out = dict(pairs=0, vf=0, ee=0, dropped=0)
+        for b in self.batches:
+            for k, v in b.counters().items():
+                out[k] += v
+        return out
+
+    def constraint_counts(self, cloth: int) -> tuple[int, int]:
+        b, k = self.locate(cloth)
+        return b.constraint_counts(k)
+
+
 class CudaDeformableBody:
     """Physics::CudaDeformableBody on the GB300 engine (one-cloth batch).
 

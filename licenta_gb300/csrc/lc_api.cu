@@ -988,6 +988,72 @@ lc_status lc_batch_step(lc_batch *b, int32_t nsteps, void *stream) {
     return LC_OK;
 }
 
+// ----- concurrent batches ----------------------------------------------------
+struct lc_group {
+    std::vector<lc_batch *> b;
+    std::vector<cudaStream_t> lane;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+};
+
+lc_status lc_group_destroy(lc_group *g) {
+    if (!g) return LC_OK;
+    for (size_t i = 0; i < g->lane.size(); ++i) {
+        if (g->lane[i]) cudaStreamSynchronize(g->lane[i]);
+        for (lc_batch *b : g->b)
+            if (b->last_stream == g->lane[i]) b->last_stream = nullptr;
+        if (g->lane[i]) cudaStreamDestroy(g->lane[i]);
+    }
+    for (cudaEvent_t e : g->join)
+        if (e) cudaEventDestroy(e);
+    if (g->fork) cudaEventDestroy(g->fork);
+    delete g;
+    return LC_OK;
+}
+
+lc_status lc_group_create(lc_batch *const *batches, int32_t count, lc_group **out) {
+    if (!batches || count < 1 || !out) return fail(LC_ERR_INVALID_ARG, "lc_group_create: bad arguments");
+    *out = nullptr;
+    for (int i = 0; i < count; ++i) {
+        if (!batches[i]) return fail(LC_ERR_INVALID_ARG, "lc_group_create: null batch");
+        for (int j = 0; j < i; ++j)
+            if (batches[j] == batches[i]) return fail(LC_ERR_INVALID_ARG, "lc_group_create: a batch appears twice");
+    }
+    lc_group *g = new lc_group();
+    g->b.assign(batches, batches + count);
+    g->lane.assign(count, nullptr);
+    g->join.assign(count, nullptr);
+    cudaError_t e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+    for (int i = 0; i < count && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&g->lane[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        lc_group_destroy(g);
+        return fail(LC_ERR_CUDA, std::string("lc_group_create: ") + cudaGetErrorString(e));
+    }
+    *out = g;
+    return LC_OK;
+}
+
+lc_status lc_group_step(lc_group *g, int32_t nsteps, void *stream) {
+    if (!g || nsteps < 0) return fail(LC_ERR_INVALID_ARG, "lc_group_step: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    LC_CUDA(cudaEventRecord(g->fork, st));
+    const size_t n = g->b.size();
+    for (size_t i = 0; i < n; ++i) LC_CUDA(cudaStreamWaitEvent(g->lane[i], g->fork, 0));
+    lc_status s = LC_OK;
+    for (int k = 0; k < nsteps && s == LC_OK; ++k)
+        for (size_t i = 0; i < n && s == LC_OK; ++i) s = lc_batch_step(g->b[i], 1, g->lane[i]);
+    // join what was enqueued, also after a failure
+    for (size_t i = 0; i < n; ++i) {
+        LC_CUDA(cudaEventRecord(g->join[i], g->lane[i]));
+        LC_CUDA(cudaStreamWaitEvent(st, g->join[i], 0));
+        g->b[i]->last_stream = st;
+    }
+    return s;
+}
+
 lc_status lc_batch_sync(lc_batch *b) {
     if (!b) return fail(LC_ERR_INVALID_ARG, "lc_batch_sync: null batch");
     LC_CUDA(cudaStreamSynchronize(b->last_stream));

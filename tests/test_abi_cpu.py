@@ -64,6 +64,12 @@ def test_invalid_arguments_are_rejected_before_any_device_work():
     assert L.lc_lbvh_create(0, 64, 0, C.byref(h)) == 1
     assert b"bad" in L.lc_last_error_string()
     assert L.lc_status_string(3) == b"contact capacity overflow"
+    # a group needs distinct, non-null batches (checked before any device call)
+    fake = (C.c_void_p * 2)(0x1000, 0x1000)
+    assert L.lc_group_create(fake, 2, C.byref(h)) == 1
+    assert b"twice" in L.lc_last_error_string()
+    assert L.lc_group_create(None, 1, C.byref(h)) == 1
+    assert L.lc_group_step(None, 1, None) == 1
 
 
 def test_grid_generator_matches_reference_topology_and_oracle():
