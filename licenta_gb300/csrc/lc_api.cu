@@ -616,6 +616,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.v, V, "v")); LC_TRY(A.alloc(d.vn, V, "vn"));
     int4 *tri; LC_TRY(A.alloc(tri, T, "tri")); d.tri = tri;
     LC_TRY(A.alloc(d.perm, T, "perm")); LC_TRY(A.alloc(d.perm_alt, T, "perm_alt"));
+    LC_TRY(A.alloc(d.tri_slot, T, "tri_slot"));
     LC_TRY(A.alloc(d.keys, T, "keys")); LC_TRY(A.alloc(d.keys_alt, T, "keys_alt"));
     LC_TRY(A.alloc(d.payload, T, "payload")); LC_TRY(A.alloc(d.payload_alt, T, "payload_alt"));
     LC_TRY(A.alloc(d.fn, T, "fn"));

@@ -77,6 +77,7 @@ struct DevPtrs {
     const int4 *tri;       // original triangle -> (v1, v2, v3 global ids, features)
     uint32_t *perm;        // slot -> original triangle (global)
     uint32_t *perm_alt;
+    int4 *tri_slot;        // slot -> its triangle record (tri[perm[slot]]), written after each sort
     unsigned long long *keys, *keys_alt;
     uint32_t *payload, *payload_alt;  // pre-sort slot carried through the sort
     float4 *fn;            // face normal per original triangle

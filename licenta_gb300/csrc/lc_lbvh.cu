@@ -207,7 +207,9 @@ __global__ void k_post_sort(DevPtrs d) {
     const int c = d.tcloth[s];
     const ClothDev &cd = d.cloth[c];
     const int src = cd.t_off + (int)d.payload[s];
-    d.perm_alt[s] = d.perm[src];
+    const uint32_t orig = d.perm[src];
+    d.perm_alt[s] = orig;
+    if (d.tri_slot) d.tri_slot[s] = d.tri[orig];  // one gather per slot instead of two per pair
     if (!cd.leaf_quirk) {
         const int node = cd.n_off + (cd.T - 1) + (s - cd.t_off);
         d.nmin[node] = d.leaf_tmp_min[src];
@@ -710,7 +712,7 @@ __device__ uint16_t pair_filter(const DevPtrs &d, uint32_t p) {
     const uint2 pr = d.pairs[p];
     const int c = d.tcloth[pr.x];
     const float h = d.cloth[c].h;
-    const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+    const int4 A = d.tri_slot[pr.x], B = d.tri_slot[pr.y];
     const int fa = A.w, fb = B.w;
     const int vid[6] = {A.x, A.y, A.z, B.x, B.y, B.z};
     uint32_t want = 0;
@@ -830,7 +832,7 @@ __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) 
         int vid[6] = {0, 0, 0, 0, 0, 0};
         if (m) {
             const uint2 pr = d.pairs[p];
-            const int4 A = d.tri[d.perm[pr.x]], B = d.tri[d.perm[pr.y]];
+            const int4 A = d.tri_slot[pr.x], B = d.tri_slot[pr.y];
             vid[0] = A.x; vid[1] = A.y; vid[2] = A.z; vid[3] = B.x; vid[4] = B.y; vid[5] = B.z;
         }
         if (!__any_sync(0xffffffffu, m != 0u)) continue;
