@@ -250,7 +250,9 @@ enum {
     LC_DBG_LRA = 18,          /* u8 per vertex x pinned vertex: attachment active (:1588) */
     LC_DBG_DYN_ACTIVE = 19,   /* u8 per iteration x (VF contacts, then EE contacts) x 4 slots:
                                  correction non-zero, i.e. counted (:1466) */
-    LC_DBG_SPHERE = 20        /* i8 per vertex: ray-sphere outcome -1/0/1 (:1523) */
+    LC_DBG_SPHERE = 20,       /* i8 per vertex: ray-sphere outcome -1/0/1 (:1523) */
+    LC_DBG_VF_NORMAL = 21     /* float3 per vertex-face contact: face normal at the hit, which friction
+                                 uses (Collision/CudaPrimitiveTests.cu:393); batches with friction only */
 };
 
 /* A contact as the solver consumes it: the ids/weights of

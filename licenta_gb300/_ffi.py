@@ -22,7 +22,7 @@ LC_MORTON_K30 = 1
 
 DBG = dict(PRED_X=1, PRED_XPREV=2, PRED_V=3, PERM_BEFORE=4, MORTON=5, PERM=6, LEFTS=7, RIGHTS=8,
            PARENTS=9, RML=10, NODE_AABB=11, PAIRS=12, VF=13, EE=14, FEATURES=15, GROUND=16,
-           GROUND_ACTIVE=17, LRA=18, DYN_ACTIVE=19, SPHERE=20)
+           GROUND_ACTIVE=17, LRA=18, DYN_ACTIVE=19, SPHERE=20, VF_NORMAL=21)
 
 F3 = C.c_float * 3
 

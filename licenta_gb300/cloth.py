@@ -171,7 +171,7 @@ class ClothBatch:
     _DT = {1: (np.float32, 3), 2: (np.float32, 3), 3: (np.float32, 3), 4: (np.uint32, 1), 5: (np.uint64, 1),
            6: (np.uint32, 1), 7: (np.int32, 1), 8: (np.int32, 1), 9: (np.int32, 1), 10: (np.int32, 2),
            11: (np.float32, 6), 12: (np.uint32, 2), 15: (np.uint8, 1), 16: (np.uint8, 1), 17: (np.uint32, 1),
-           18: (np.uint8, 1), 19: (np.uint8, 1), 20: (np.int8, 1)}
+           18: (np.uint8, 1), 19: (np.uint8, 1), 20: (np.int8, 1), 21: (np.float32, 3)}
 
     def debug(self, cloth: int, what: str) -> np.ndarray:
         sel = _ffi.DBG[what]

@@ -42,6 +42,7 @@ void launch_solver_setup(const DevPtrs &d, bool sphere, cudaStream_t st);
 void launch_jacobi(const DevPtrs &d, const float4 *xa, float4 *xb, int it, const uint32_t *nvf, int block,
                    cudaStream_t st);
 void launch_integrate(const DevPtrs &d, const float4 *xs, cudaStream_t st);
+void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st);
 void scan_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, uint32_t n_static, uint32_t n_cap,
               uint32_t *partial, uint32_t *total_out, unsigned long long *total_out64, cudaStream_t st);
 unsigned long long morton3_host(float x, float y, float z, int mode);
@@ -410,7 +411,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
     // per-vertex contact CSR feeds the gather solvers; the scatter solver
     // walks the cloth's contact ranges instead.
-    if (!(use_cluster && cluster_scatter)) {
+    if (!(use_cluster && cluster_scatter) || d.friction_any) {  // friction sums per vertex too
         LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         launch_dyn(d, nvf, nee, narrow_grid, 0, st);
@@ -423,6 +424,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
         LC_TRY(enqueue_cluster_solver(this, st));
         LC_KEV(1);
         LC_PHASE(6);
+        if (d.friction_any) launch_friction(d, nvf, st);
         LC_PHASE(7);
         LC_CUDA(cudaGetLastError());
         return LC_OK;
@@ -444,6 +446,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     LC_PHASE(6);
     // 7. PBD Integration + WorldConstraints
     launch_integrate(d, a, st);
+    if (d.friction_any) launch_friction(d, nvf, st);
     LC_PHASE(7);
     LC_CUDA(cudaGetLastError());
     return LC_OK;
@@ -516,6 +519,8 @@ static void fill_cloth_dev(const HostCloth &hc, ClothDev &cd) {
     cd.wind_on = p.windOn ? 1 : 0;
     cd.ground_on = p.groundOn ? 1 : 0;
     cd.sphere_on = p.sphereOn ? 1 : 0;
+    cd.friction = p.useFriction ? 1 : 0;
+    cd.kfriction = p.kFriction;
     cd.morton_mode = p.mortonMode;
     cd.leaf_quirk = p.refLeafAabbQuirk ? 1 : 0;
     cd.dt = p.timestep;
@@ -587,6 +592,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
         b->max_iters = std::max(b->max_iters, cd.iters);
         b->any_wind |= cd.wind_on != 0;
         b->any_sphere |= cd.sphere_on != 0;
+        b->d.friction_any |= cd.friction;
         if (hc.p.mortonMode != b->hosts[0].p.mortonMode)
             return fail(LC_ERR_INVALID_ARG, "all cloths of a batch must use the same Morton mode");
     }
@@ -595,6 +601,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     if (V > (1ll << 31) - 2 || T > (1ll << 31) - 2 || E + B >= (1ll << 29) || PC > 0xFFFFFFF0ll)
         return fail(LC_ERR_INVALID_ARG, "batch too large for 32-bit indices");
     b->sort_passes = b->hosts[0].p.mortonMode == LC_MORTON_K30 ? 4 : 8;
+    if (opt.adjoint && b->d.friction_any)
+        return fail(LC_ERR_NOT_SUPPORTED, "adjoint: friction is not differentiated; create the batch without useFriction");
 
     DevPtrs &d = b->d;
     DeviceArena &A = b->arena;
@@ -645,6 +653,10 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.hit_q[0], vf_cap, "hit_q_vf")); LC_TRY(A.alloc(d.hit_w[0], vf_cap, "hit_w_vf"));
     LC_TRY(A.alloc(d.hit_q[1], ee_cap, "hit_q_ee")); LC_TRY(A.alloc(d.hit_w[1], ee_cap, "hit_w_ee"));
     LC_TRY(A.alloc(d.hit_n, 2, "hit_n"));
+    if (d.friction_any) {
+        LC_TRY(A.alloc(d.vf_n, vf_cap, "vf_n"));
+        LC_TRY(A.alloc(d.hit_nrm, vf_cap, "hit_nrm_vf"));
+    }
     LC_TRY(A.alloc(d.dyn_cnt, V, "dyn_cnt")); LC_TRY(A.alloc(d.dyn_off, V + 1, "dyn_off"));
     LC_TRY(A.alloc(d.dyn_cur, V, "dyn_cur")); LC_TRY(A.alloc(d.dyn_ent, d.dyn_cap, "dyn_ent"));
     int *soff; uint32_t *sent; int2 *sids; float2 *spar; int4 *bids; float *bkp;
@@ -1450,6 +1462,24 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, ui
             }
             if (count) *count = outv.size();
             if (dst && !outv.empty()) std::memcpy(dst, outv.data(), sizeof(lc_contact) * std::min<uint64_t>(outv.size(), cap));
+            return LC_OK;
+        }
+        case LC_DBG_VF_NORMAL: {
+            if (!d.vf_n) return fail(LC_ERR_INVALID_ARG, "VF normals are kept only in batches with friction");
+            std::vector<uint64_t> gi;
+            std::vector<int4> iv;
+            std::vector<float4> wv;
+            LC_TRY(b->cloth_contacts(c, true, gi, iv, wv));
+            std::vector<float4> all(gi.empty() ? 0 : gi.back() + 1);
+            if (!all.empty())
+                LC_CUDA(cudaMemcpy(all.data(), d.vf_n, sizeof(float4) * all.size(), cudaMemcpyDeviceToHost));
+            if (count) *count = gi.size();
+            if (dst)
+                for (uint64_t i = 0; i < std::min<uint64_t>(gi.size(), cap); ++i) {
+                    ((float *)dst)[3 * i] = all[gi[i]].x;
+                    ((float *)dst)[3 * i + 1] = all[gi[i]].y;
+                    ((float *)dst)[3 * i + 2] = all[gi[i]].z;
+                }
             return LC_OK;
         }
         case LC_DBG_GROUND: {

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
             qdbg = f4(qc, 1.f);
         }
         gq[i] = q;
-        if (d.dbg_ground_it) d.ground_qc[g] = qdbg;
+        if (d.dbg_ground_it || d.friction_any) d.ground_qc[g] = qdbg;
     }
     cluster.sync();
     // ---- LRA flags (Physics/CudaPBD.cu:1571-1592) --------------------------
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             qdbg = f4(qc, 1.f);
         }
         gq[i] = q;
-        if (d.dbg_ground_it) d.ground_qc[g] = qdbg;
+        if (d.dbg_ground_it || d.friction_any) d.ground_qc[g] = qdbg;
     }
     cluster.sync();
     if (cd.F) {

@@ -41,6 +41,8 @@ struct ClothDev {
     int iters;             // solver iterations
     int wind_on;
     int ground_on, sphere_on;
+    int friction;          // CudaPBD::ApplyFriction after the integration (useFriction)
+    float kfriction;
     int morton_mode, leaf_quirk;
     float dt, h, kdamp, kglobal;
     float g[3];
@@ -103,10 +105,13 @@ struct DevPtrs {
     uint32_t *cand_vf, *cand_ee;          // per candidate: CCD hit flags
     uint32_t *hit_q[2];                   // VF / EE hits in any order: candidate index ...
     float4 *hit_w[2];                     // ... and contact weights (capacity vf_cap / ee_cap)
+    float4 *hit_nrm;                      // VF hits: unit face normal at the hit (friction; may be null)
     uint32_t *hit_n;                      // [2] hit counts of the step
     uint32_t *cand_vf_off, *cand_ee_off;  // per candidate: output slot (exclusive scans)
     uint4 *crange;         // per cloth: [vf0, vf1) and [ee0, ee1) contact ranges
     int4 *vf_v; float4 *vf_w;   // VF contacts (ids, weights)
+    float4 *vf_n;               // VF contacts: face normal at the hit (friction; may be null)
+    int friction_any;           // some cloth of the batch uses friction
     int4 *ee_v; float4 *ee_w;   // EE contacts
     uint64_t vf_cap, ee_cap;
     uint32_t *dyn_cnt, *dyn_off, *dyn_cur;  // per vertex dynamic-correction entries

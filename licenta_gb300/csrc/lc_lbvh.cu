@@ -560,7 +560,7 @@ __global__ void k_pair_compact(DevPtrs d) {
 // feature AABB cull of Collision/CudaPrimitiveTests.cu:427-490, CCD of
 // :109-238 with Physics/CudaCubicSolver.cu:5-153 and the tests at :252-425.
 // ---------------------------------------------------------------------------
-struct Wts { float w0, w1, w2, w3; };
+struct Wts { float w0, w1, w2, w3; float3 n; };
 
 __device__ __forceinline__ float triple(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41,
                                         float t) {
@@ -610,6 +610,7 @@ __device__ bool test_vf(float3 x4, float3 x1, float3 x2, float3 x3, float th, Wt
         const float lo = 0.f, hi = 1.f + del;
         if (between(w1, lo, hi) && between(w2, lo, hi) && between(w3, lo, hi)) {
             w.w0 = 1.f; w.w1 = -w1; w.w2 = -w2; w.w3 = -w3;
+            w.n = n;
             return true;
         }
     }
@@ -981,6 +982,7 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
                 if (slot < cap) {
                     d.hit_q[VF ? 0 : 1][slot] = q;
                     d.hit_w[VF ? 0 : 1][slot] = make_float4(wt.w0, wt.w1, wt.w2, wt.w3);
+                    if (VF && d.hit_nrm) d.hit_nrm[slot] = make_float4(wt.n.x, wt.n.y, wt.n.z, 0.f);
                 } else {
                     atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
                 }
@@ -1002,7 +1004,11 @@ __global__ void k_ccd_emit(DevPtrs d) {
         const uint32_t q = d.hit_q[VF ? 0 : 1][k];
         const uint32_t o = off[q];
         if (o < cap) {
-            if (VF) { d.vf_v[o] = list[q]; d.vf_w[o] = d.hit_w[0][k]; }
+            if (VF) {
+                d.vf_v[o] = list[q];
+                d.vf_w[o] = d.hit_w[0][k];
+                if (d.vf_n) d.vf_n[o] = d.hit_nrm[k];
+            }
             else { d.ee_v[o] = list[q]; d.ee_w[o] = d.hit_w[1][k]; }
         } else {
             atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);

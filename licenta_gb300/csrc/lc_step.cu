@@ -474,4 +474,61 @@ void launch_integrate(const DevPtrs &d, const float4 *xs, cudaStream_t st) {
     if (d.Vtot) k_integrate<<<nblk(d.Vtot), kThreads, 0, st>>>(d, xs);
 }
 
+// CudaPBD::ApplyFriction (Physics/CudaPBD.cu:770-833) for the cloths with
+// useFriction, after the integration; velocities only.  Per vertex:
+//  * _DampVelRigid (:1879-1912): the reference launches it with 255 threads
+//    per block over ceil(V/256) blocks (:777), so it reaches only the first
+//    255*ceil(V/256) vertices of a cloth; those with a ground constraint this
+//    step have their normal velocity scaled by 1 - kFriction and the sum
+//    reflected about the ground normal (0, 1, 0).
+//  * _ApplyFrictionVF / _AccumulateFriction (:1745-1794, :1846-1877): the
+//    face normals of the vertex's VF contacts summed in contact order (the
+//    per-vertex contact lists are sorted by entry, as the reference's stable
+//    key sort leaves them).  _ApplyFrictionEE (:1796-1845) never writes its
+//    entries' vertex ids, so EE entries take no part (what the reference
+//    computes for a step without EE contacts).
+//  * FinalFrictionStep (:1700-1723): with a non-zero sum, the normal velocity
+//    along the summed direction is scaled by (1 - kFriction)^count and the
+//    sum reflected about it.
+__global__ void k_friction(DevPtrs d, const uint32_t *__restrict__ nvf_dev) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.Vtot) return;
+    const ClothDev &cd = d.cloth[d.vcloth[i]];
+    if (!cd.friction) return;
+    const float kf = cd.kfriction;
+    float3 v = xyz(d.v[i]);
+    const int li = i - cd.v_off;
+    const int reach = (cd.V + 255) / 256 * 255;
+    if (li < reach && d.ground_qc[i].w != 0.f) {
+        const float3 n = f3(0.f, 1.f, 0.f);
+        float3 vn = mul(n, dot(v, n));
+        const float3 vt = sub(v, vn);
+        vn = mul(vn, 1.f - kf);
+        const float3 r = add(vt, vn);
+        v = sub(r, mul(n, 2.f * dot(r, n)));
+    }
+    const uint32_t nvf4 = 4u * (uint32_t)min((uint64_t)*nvf_dev, d.vf_cap);
+    float3 acc = f3(0.f, 0.f, 0.f);
+    int cnt = 0;
+    for (uint32_t e = d.dyn_off[i]; e < d.dyn_off[i + 1]; ++e) {
+        const uint32_t ent = d.dyn_ent[e];
+        if (ent >= nvf4) continue;
+        acc = add(acc, xyz(d.vf_n[ent >> 2]));
+        ++cnt;
+    }
+    if (cnt != 0 && !is_zero(acc)) {
+        const float3 fn = normalize(acc);
+        float3 vn = mul(fn, dot(v, fn));
+        const float3 vt = sub(v, vn);
+        vn = mul(vn, powf(1.f - kf, (float)cnt));
+        const float3 r = add(vn, vt);
+        v = sub(r, mul(fn, 2.f * dot(r, fn)));
+    }
+    d.v[i] = f4(v, d.v[i].w);
+}
+
+void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st) {
+    if (d.Vtot) k_friction<<<nblk(d.Vtot), kThreads, 0, st>>>(d, nvf);
+}
+
 }  // namespace lc

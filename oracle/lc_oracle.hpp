@@ -330,12 +330,15 @@ template <class R> class Cloth {
     std::vector<V> nmin, nmax;  // node AABBs (2T-1)
     std::vector<u32> pairs;     // (i, j) flattened
     std::vector<Contact> vf, ee;
+    std::vector<V> vf_n;          // unit face normal of each VF contact at its hit (friction)
+    std::vector<u8> ground_flag;  // ground constraints of the last solve (friction)
     std::vector<V> pmin, pmax;  // particle swept AABBs
     u64 dropped = 0;
     int stack_overflow = 0;
 
     bool have_frozen = false;
     std::vector<Contact> frozen_vf, frozen_ee;
+    std::vector<V> frozen_vf_n;  // their face normals, for friction (empty: no friction on frozen contacts)
 
     // Discrete decisions replayed from another implementation for one step
     // (ground / LRA / sphere activation, per-iteration counted terms), so that
@@ -364,6 +367,12 @@ template <class R> class Cloth {
     };
     bool recording = false;
     Record rec;
+    // Smallest 1 - n1.n2 over the bends and the solver iterates of the last
+    // solve (when track_bend): how close a bend came to the d -> 1
+    // singularity of the reference's formula, where the correction is 0 * inf
+    // and rounding alone moves it by a finite amount.
+    bool track_bend = false;
+    double bend_min = 1e300;
     std::vector<Record> records;  // one per recorded step of a rollout
 
     void init(const lc_cloth_desc &d) {
@@ -725,10 +734,11 @@ template <class R> class Cloth {
         return d1 < d2 ? e1 : e2;
     }
     // Collision/CudaPrimitiveTests.cu:348-406
-    static bool test_vf(V x4, V x1, V x2, V x3, Contact &c, R th) {
+    static bool test_vf(V x4, V x1, V x2, V x3, Contact &c, R th, V *nout = nullptr) {
         V x13 = x1 - x3, x23 = x2 - x3, x43 = x4 - x3;
         V crs = cross(x2 - x1, x3 - x1);
         V n = normalize(crs);
+        if (nout) *nout = n;
         if (std::fabs(dot(x43, n)) <= th) {
             R dt = dot(x13, x23);
             R m11 = dot(x13, x13), m12 = dt, m21 = dt, m22 = dot(x23, x23);
@@ -799,6 +809,7 @@ template <class R> class Cloth {
     void narrowphase() {
         vf.clear();
         ee.clear();
+        vf_n.clear();
         R th = R(h), dt = R(prm.timestep);
         size_t P = pairs.size() / 2;
         for (size_t p = 0; p < P; ++p) {
@@ -813,7 +824,8 @@ template <class R> class Cloth {
                 Contact c;
                 c.v[0] = P1[s % 3]; c.v[1] = F1[0]; c.v[2] = F1[1]; c.v[3] = F1[2];
                 c.w[0] = c.w[1] = c.w[2] = c.w[3] = -1.f;
-                if (vf_candidate(c, th, dt)) vf.push_back(c);
+                V nrm = mk<R>(0, 0, 0);
+                if (vf_candidate(c, th, dt, &nrm)) { vf.push_back(c); vf_n.push_back(nrm); }
             }
             // EE slot k: edge ea of A x edge eb of B.
             static const int ea_v[3][2] = {{0, 1}, {0, 2}, {1, 2}};
@@ -830,7 +842,7 @@ template <class R> class Cloth {
         }
     }
 
-    bool vf_candidate(Contact &c, R th, R dt) {
+    bool vf_candidate(Contact &c, R th, R dt, V *nout = nullptr) {
         V tmin = min3(pmin[c.v[1]], pmin[c.v[2]], pmin[c.v[3]]);
         V tmax = max3(pmax[c.v[1]], pmax[c.v[2]], pmax[c.v[3]]);
         if (!overlap(pmin[c.v[0]], pmax[c.v[0]], tmin, tmax)) return false;
@@ -842,7 +854,7 @@ template <class R> class Cloth {
         for (int i = 0; i < n; ++i) {
             R t = times[i] * dt;
             x4 = x4 + v4 * t; x1 = x1 + v1 * t; x2 = x2 + v2 * t; x3 = x3 + v3 * t;
-            if (test_vf(x4, x1, x2, x3, c, th)) return true;
+            if (test_vf(x4, x1, x2, x3, c, th, nout)) return true;
         }
         return false;
     }
@@ -869,7 +881,8 @@ template <class R> class Cloth {
         R th = R(h);
         R gh = R(prm.worldMin[1]);
         // Physics/CudaPBD.cu:1477-1507 — ground constraints.
-        std::vector<u8> gflag(Vn, 0);
+        std::vector<u8> &gflag = ground_flag;
+        gflag.assign(Vn, 0);
         std::vector<V> qc(Vn), nc(Vn);
         if (prm.groundOn) {
             for (int i = 0; i < Vn; ++i) {
@@ -923,7 +936,9 @@ template <class R> class Cloth {
             rec.dyn.assign((size_t)prm.solverIterations * corr_dyn.size(), 0);
             rec.xk.assign(1, x);
         }
+        bend_min = 1e300;
         for (int it = 0; it < prm.solverIterations; ++it) {
+            if (track_bend) track_bend_conditioning();
             for (int i = 0; i < Vn; ++i) { acc[i] = mk<R>(0, 0, 0); cnt[i] = 0; }
             // ground, Physics/CudaPBD.cu:1594-1629
             for (int i = 0; i < Vn; ++i)
@@ -982,6 +997,21 @@ template <class R> class Cloth {
             // Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
             for (int i = 0; i < Vn; ++i) x[i] = x[i] + acc[i] / R(cnt[i]);
             if (recording) rec.xk.push_back(x);
+        }
+    }
+
+    void track_bend_conditioning() {
+        for (size_t k = 0; k < tp.b1.size(); ++k) {
+            const V &p2 = x[tp.b2[k]], &p3 = x[tp.b3[k]], &p4 = x[tp.b4[k]];
+            const double a[3] = {(double)p2.x, (double)p2.y, (double)p2.z};
+            const double b[3] = {(double)p3.x, (double)p3.y, (double)p3.z};
+            const double c[3] = {(double)p4.x, (double)p4.y, (double)p4.z};
+            const double u[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            const double w[3] = {a[1] * c[2] - a[2] * c[1], a[2] * c[0] - a[0] * c[2], a[0] * c[1] - a[1] * c[0]};
+            const double lu = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+            const double lw = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            if (lu <= 0 || lw <= 0) continue;
+            bend_min = std::min(bend_min, 1.0 - (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) / (lu * lw));
         }
     }
 
@@ -1381,6 +1411,54 @@ template <class R> class Cloth {
         gxp.swap(gxp0);
     }
 
+    // ---- friction, CudaPBD::ApplyFriction (Physics/CudaPBD.cu:770-833) -------
+    // Runs after the integration when useFriction is set (Physics/
+    // CudaDeformableBody.cpp:596-602) and changes velocities only.
+    //  * _DampVelRigid (:1879-1912), launched with 255 threads per block over
+    //    ceil(V/256) blocks (:777), so only the first 255*ceil(V/256)
+    //    vertices are reached: their normal velocity against the ground
+    //    plane is scaled by 1 - kFriction and the sum reflected.  (The
+    //    sphere flags it also reads are never set.)
+    //  * _ApplyFrictionVF (:1745-1794) gives each of a VF contact's four
+    //    vertices the contact's face normal; the stable sort + run-length
+    //    sums of :813-824 add them per vertex in contact order.
+    //    _ApplyFrictionEE (:1796-1845) leaves its entries' vertex ids
+    //    unwritten (the lines are commented out), so those entries land on
+    //    whatever ids the buffer held; here they are left out, which is what
+    //    the reference computes when a step has no EE contacts.
+    //  * FinalFrictionStep (:1700-1723): a vertex with a non-zero sum has its
+    //    normal velocity along the summed direction scaled by
+    //    (1 - kFriction)^count and the sum reflected.
+    void friction(const std::vector<Contact> &cvf, const std::vector<V> &nrm) {
+        const int Vn = tp.V;
+        const R kf = R(prm.kFriction);
+        const V up = mk<R>(0, 1, 0);
+        auto reflect = [](V a, V n) { return a - R(2) * dot(a, n) * n; };
+        const int reach = std::min(Vn, ((Vn + 255) / 256) * 255);
+        for (int i = 0; i < reach; ++i) {
+            if (!ground_flag[i]) continue;
+            V vn = dot(v[i], up) * up;
+            V vt = v[i] - vn;
+            vn = vn * (R(1) - kf);
+            v[i] = reflect(vt + vn, up);
+        }
+        std::vector<V> acc(Vn, mk<R>(0, 0, 0));
+        std::vector<int> cnt(Vn, 0);
+        for (size_t c = 0; c < cvf.size() && c < nrm.size(); ++c)
+            for (int s = 0; s < 4; ++s) {
+                acc[cvf[c].v[s]] = acc[cvf[c].v[s]] + nrm[c];
+                cnt[cvf[c].v[s]] += 1;
+            }
+        for (int i = 0; i < Vn; ++i) {
+            if (cnt[i] == 0 || is_zero(acc[i])) continue;
+            V fn = normalize(acc[i]);
+            V vn = dot(v[i], fn) * fn;
+            V vt = v[i] - vn;
+            vn = vn * R(std::pow(R(1) - kf, R(cnt[i])));
+            v[i] = reflect(vn + vt, fn);
+        }
+    }
+
     void step() {
         external();
         pred_x = x; pred_xp = xp; pred_v = v;
@@ -1389,9 +1467,15 @@ template <class R> class Cloth {
             solve(frozen_vf, frozen_ee);
         else
             solve(vf, ee);
+        const bool frozen = have_frozen;
         have_frozen = false;
         forced.on = false;
         integrate();
+        if (prm.useFriction) {
+            if (!frozen) friction(vf, vf_n);
+            else if (frozen_vf_n.size() == frozen_vf.size()) friction(frozen_vf, frozen_vf_n);
+        }
+        frozen_vf_n.clear();
     }
 };
 

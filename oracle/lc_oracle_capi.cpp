@@ -449,3 +449,50 @@ extern "C" int lco_solve_iterate(lco_world *w, int c, int k, float *x) {
         return (int)LC_OK;
     });
 }
+
+// CudaPBD::ApplyFriction (Cloth::friction) on given velocities v (3V floats),
+// ground-constraint flags (V bytes), VF contacts and their face normals
+// (3 floats each); v_out receives the velocities after it.
+extern "C" int lco_friction_on(lco_world *w, int c, const float *v, const uint8_t *ground, const lc_contact *vf,
+                               const float *normals, uint64_t nvf, float *v_out) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        using Vt = typename std::remove_reference_t<decltype(cl)>::V;
+        const int Vn = cl.tp.V;
+        for (int i = 0; i < Vn; ++i) cl.v[i] = mk<R>(R(v[3 * i]), R(v[3 * i + 1]), R(v[3 * i + 2]));
+        cl.ground_flag.assign(ground, ground + Vn);
+        std::vector<Contact> cvf(nvf);
+        std::vector<Vt> nrm(nvf);
+        for (uint64_t k = 0; k < nvf; ++k) {
+            std::memcpy(&cvf[k], &vf[k], sizeof(Contact));
+            for (int s = 0; s < 4; ++s)
+                if (cvf[k].v[s] < 0 || cvf[k].v[s] >= Vn) return (int)LC_ERR_INVALID_ARG;
+            nrm[k] = mk<R>(R(normals[3 * k]), R(normals[3 * k + 1]), R(normals[3 * k + 2]));
+        }
+        cl.friction(cvf, nrm);
+        for (int i = 0; i < Vn; ++i) {
+            v_out[3 * i] = (float)cl.v[i].x; v_out[3 * i + 1] = (float)cl.v[i].y; v_out[3 * i + 2] = (float)cl.v[i].z;
+        }
+        return (int)LC_OK;
+    });
+}
+
+// Face normals (3 floats each) of the contacts given to lco_set_frozen_contacts,
+// so that the next step's friction runs on them.
+extern "C" int lco_set_frozen_normals(lco_world *w, int c, const float *n, uint64_t count) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        cl.frozen_vf_n.resize(count);
+        for (uint64_t k = 0; k < count; ++k) cl.frozen_vf_n[k] = mk<R>(R(n[3 * k]), R(n[3 * k + 1]), R(n[3 * k + 2]));
+        return (int)LC_OK;
+    });
+}
+
+// Bend conditioning of the next solves of cloth c (on != 0 to track it) and
+// its value for the last one: min over bends and iterates of 1 - n1.n2.
+extern "C" int lco_track_bend(lco_world *w, int c, int on) {
+    return with_cloth(w, c, [&](auto &cl) { cl.track_bend = on != 0; return (int)LC_OK; });
+}
+extern "C" int lco_bend_conditioning(lco_world *w, int c, double *out) {
+    return with_cloth(w, c, [&](auto &cl) { *out = cl.bend_min; return (int)LC_OK; });
+}

@@ -57,6 +57,10 @@ def lib() -> C.CDLL:
             "lco_topology": (C.c_int, [VP, C.c_int] + [VP] * 10),
             "lco_solve_on": (C.c_int, [VP, C.c_int, VP, VP, VP, C.c_uint64, VP, C.c_uint64, VP, VP, VP]),
             "lco_solve_iterate": (C.c_int, [VP, C.c_int, C.c_int, VP]),
+            "lco_set_frozen_normals": (C.c_int, [VP, C.c_int, VP, C.c_uint64]),
+            "lco_track_bend": (C.c_int, [VP, C.c_int, C.c_int]),
+            "lco_bend_conditioning": (C.c_int, [VP, C.c_int, C.POINTER(C.c_double)]),
+            "lco_friction_on": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
             "lco_solve_decisions": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
         }
         for name, (res, args) in sig.items():
@@ -157,7 +161,7 @@ class Oracle:
         w = np.ascontiguousarray(wind, dtype=np.float64)
         _chk(lib().lco_set_wind(self._h, c, _p(w), rng), "set_wind")
 
-    def freeze_contacts(self, c: int, vf: tuple, ee: tuple) -> None:
+    def freeze_contacts(self, c: int, vf: tuple, ee: tuple, vf_normals=None) -> None:
         def pack(t):
             v, w = t
             arr = (_ffi.Contact * max(len(v), 1))()
@@ -168,6 +172,9 @@ class Oracle:
         a, na = pack(vf)
         b, nb = pack(ee)
         _chk(lib().lco_set_frozen_contacts(self._h, c, a, na, b, nb), "set_frozen_contacts")
+        if vf_normals is not None:
+            nr = np.ascontiguousarray(vf_normals, np.float32).reshape(-1, 3)
+            _chk(lib().lco_set_frozen_normals(self._h, c, _p(nr), len(nr)), "set_frozen_normals")
 
     def force_decisions(self, c: int, ground, ground_it, lra, dyn, sphere=None) -> None:
         """Replay another implementation's discrete decisions in the next step."""
@@ -260,6 +267,31 @@ class Oracle:
         _chk(lib().lco_solve_on(self._h, c, _p(xs), _p(xps), _p(a), na, _p(b), nb_, *[_p(o) for o in out]),
              "solve_on")
         return tuple(out)
+
+    def track_bend(self, c: int, on: bool = True) -> None:
+        _chk(lib().lco_track_bend(self._h, c, 1 if on else 0), "track_bend")
+
+    def bend_conditioning(self, c: int) -> float:
+        """min over bends and solver iterates of 1 - n1.n2 in the last solve
+        (tracked after track_bend)."""
+        out = C.c_double()
+        _chk(lib().lco_bend_conditioning(self._h, c, C.byref(out)), "bend_conditioning")
+        return out.value
+
+    def friction_on(self, c: int, v, ground, vf: tuple, normals) -> np.ndarray:
+        """Friction (CudaPBD::ApplyFriction) on given velocities with the given
+        ground flags, VF contacts (ids (N, 4), weights (N, 4)) and their face
+        normals (N, 3); returns the velocities after it."""
+        nv = self.sizes(c)[0]
+        vs = np.ascontiguousarray(v, np.float32).reshape(nv, 3)
+        g = np.ascontiguousarray(ground, np.uint8).reshape(nv)
+        ids = np.asarray(vf[0], np.int32).reshape(-1, 4)
+        w = np.asarray(vf[1], np.float32).reshape(-1, 4)
+        recs = np.ascontiguousarray(np.concatenate([ids, w.view(np.int32)], axis=1))
+        nr = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        out = np.empty((nv, 3), np.float32)
+        _chk(lib().lco_friction_on(self._h, c, _p(vs), _p(g), _p(recs), _p(nr), len(ids), _p(out)), "friction_on")
+        return out
 
     def solve_iterate(self, c: int, k: int) -> np.ndarray:
         """Positions after iteration k (0 = before the first) of the last solve_on."""

@@ -46,12 +46,12 @@ def check_collision(batch, c, o32, pre_vn, tag=""):
     return n
 
 
-def fp64_step_error(batch, c, o64, pre, perm, sphere: bool):
+def fp64_step_error(batch, c, o64, pre, perm, sphere: bool, friction: bool = False):
     """Max |x_gpu - x_fp64| (metres) after the step the batch just took."""
     o64.set_state(0, **{k: v.astype(np.float64) for k, v in pre.items()})
     o64.set_perm(0, perm)
     vf, ee = batch.debug(c, "VF"), batch.debug(c, "EE")
-    o64.freeze_contacts(0, vf, ee)
+    o64.freeze_contacts(0, vf, ee, batch.debug(c, "VF_NORMAL") if friction else None)
     o64.force_decisions(0, batch.debug(c, "GROUND"), batch.debug(c, "GROUND_ACTIVE"), batch.debug(c, "LRA"),
                         batch.debug(c, "DYN_ACTIVE"), batch.debug(c, "SPHERE") if sphere else None)
     o64.step_one(0)
@@ -61,3 +61,14 @@ def fp64_step_error(batch, c, o64, pre, perm, sphere: bool):
         if not np.isfinite(g[k]).all():
             raise AssertionError(f"non-finite {k}")
     return float(np.abs(g["x"] - r["x"]).max()), float(np.abs(g["v"] - r["v"]).max())
+
+
+def conditioning_bound(spec, tol: float) -> float:
+    """The smallest 1 - n1.n2 of a bend at which the reference's bend
+    correction is still determined within `tol` by FP32 arithmetic: near
+    d = 1 it is 0 * inf, and one rounding of the unit normals moves it by
+    about L 2^-24 / sqrt(1 - d) for edges of length L."""
+    p = np.asarray(spec.positions, np.float64)
+    idx = np.asarray(spec.indices, np.int64).reshape(-1, 3)
+    L = max(float(np.linalg.norm(p[idx[:, a]] - p[idx[:, b]], axis=1).max()) for a, b in ((0, 1), (1, 2), (2, 0)))
+    return (L * 2.0 ** -24 / tol) ** 2

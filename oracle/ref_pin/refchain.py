@@ -73,6 +73,11 @@ KERNELS = {
     "final_update": "_FinalUpdate",
     # FixedUpdate's world clamp (Physics/CudaDeformableBody.cpp:616)
     "world_clamp": "_WorldConstraints",
+    # CudaPBD::ApplyFriction (Physics/CudaPBD.cu:770-833)
+    "damp_rigid": "_DampVelRigid",
+    "apply_friction": "_ApplyFriction",
+    "accumulate_friction": "_AccumulateFriction",
+    "final_friction": "FinalFrictionStep",
 }
 
 
@@ -147,7 +152,10 @@ class RefKernels:
                 raise RuntimeError(f"kernel {ident}: {len(hits)} matches in the cubin: {hits}")
             self.fn[key] = names[hits[0]]
 
-    def launch(self, key: str, n_threads: int, *args) -> None:
+    def launch(self, key: str, n_threads: int, *args, block: int = THREADS, blocks: int | None = None) -> None:
+        """Launches a reference kernel with `block` threads per block over
+        ceil(n_threads / THREADS) blocks (the reference's own grid size),
+        or `blocks` when given."""
         if n_threads <= 0:
             return
         vals = []
@@ -164,8 +172,9 @@ class RefKernels:
         if n_threads >= 1 << 31:
             raise ValueError("launch too large")
         stream = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
-        blocks = (n_threads + THREADS - 1) // THREADS
-        self.drv("cuLaunchKernel", self.fn[key], blocks, 1, 1, THREADS, 1, 1, 0, stream, params, None)
+        if blocks is None:
+            blocks = (n_threads + THREADS - 1) // THREADS
+        self.drv("cuLaunchKernel", self.fn[key], blocks, 1, 1, block, 1, 1, 0, stream, params, None)
 
     # ------------------------------------------------------------------
     def collide(self, x, x_prev, v, triangles, features, thickness: float, dt: float, chunk: int = 64,
@@ -448,7 +457,57 @@ class RefKernels:
                         Float3(*[float(q) for q in hi]))
         torch.cuda.synchronize()
         return dict(x=x_solved, v=d_v.cpu().numpy(), x_prev=d_xp.cpu().numpy(), x_end=d_x.cpu().numpy(),
+                    ground=gflag.cpu().numpy().astype(np.uint8),
                     ground_flags=int(gflag.sum()), lra_flags=int(lflag[:V * F].sum()) if F else 0)
+
+    # ------------------------------------------------------------------
+    def friction(self, v, ground, vf, k_friction: float) -> np.ndarray:
+        """CudaPBD::ApplyFriction (Physics/CudaPBD.cu:770-833) with the
+        reference's kernels on velocities v (V, 3) after _FinalUpdate, the
+        step's ground-constraint flags and its VF contacts (N, 12) int32
+        PrimitiveContact records, whose normals the kernels read.
+
+        _DampVelRigid runs with the reference's launch shape, 255 threads per
+        block over ceil(V/256) blocks (:777).  _ApplyFriction gets no EE
+        contacts: its EE half leaves the vertex ids of its entries unwritten
+        (:1796-1845), which with EE contacts present would sort and
+        accumulate whatever ids the buffer held.  The CUB sort, run-length
+        encoding and exclusive sum (:813-818) run on the host.  Returns the
+        velocities after FinalFrictionStep."""
+        torch = self.torch
+        f32, i32 = np.float32, np.int32
+        vel = np.ascontiguousarray(v, f32)
+        V = vel.shape[0]
+        ground = np.ascontiguousarray(ground, np.uint8).reshape(V)
+        vf = np.ascontiguousarray(vf, i32).reshape(-1, 12)
+        if len(vf) and (vf[:, :4].min() < 0 or vf[:, :4].max() >= V):
+            raise ValueError("contact vertex out of range")
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        d_v = dev(vel)
+        d_g = dev(ground != 0)
+        d_gn = dev(np.tile(np.array([0, 1, 0], f32), (V, 1)))  # ground normals (Physics/CudaPBD.cu:1492)
+        kf = C.c_float(k_friction)
+        blocks = (V + THREADS - 1) // THREADS
+        self.launch("damp_rigid", V, C.c_int(V), d_v, kf, d_g, d_gn, None, None, block=THREADS - 1, blocks=blocks)
+        acc = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        cnt = torch.zeros(V, dtype=torch.int32, device="cuda")
+        N = len(vf)
+        if N:
+            d_vf = dev(vf)
+            ids = torch.zeros(4 * N, dtype=torch.int32, device="cuda")
+            vals = torch.zeros((4 * N, 3), dtype=torch.float32, device="cuda")
+            self.launch("apply_friction", N, d_v, kf, d_vf, C.c_uint64(N), None, C.c_uint64(0), ids, vals)
+            torch.cuda.synchronize()
+            h_ids = ids.cpu().numpy().view(np.uint32)
+            order = np.argsort(h_ids, kind="stable")
+            sids = h_ids[order]
+            starts = np.flatnonzero(np.r_[True, sids[1:] != sids[:-1]]).astype(i32)
+            runs = len(starts)
+            self.launch("accumulate_friction", runs, C.c_int(runs), kf, dev(sids[starts].view(i32)), dev(starts),
+                        dev(vals.cpu().numpy()[order]), C.c_uint64(4 * N), acc, cnt)
+        self.launch("final_friction", V, C.c_int(V), kf, acc, cnt, d_v)
+        torch.cuda.synchronize()
+        return d_v.cpu().numpy()
 
 
 def _check_tree(L, R, Pa, T) -> int:

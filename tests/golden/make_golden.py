@@ -12,7 +12,9 @@ the state the collision stages see at the next step (predicted positions,
 previous positions, velocities, the triangle order before the Morton sort)
 and runs the reference's collision chain on it (oracle/ref_pin/refchain.py),
 then the reference's solver chain (PBDStepSolver, _FinalUpdate and the world
-clamp) on the same state with the contacts its collision chain found.
+clamp) on the same state with the contacts its collision chain found, and
+the reference's friction kernels (CudaPBD::ApplyFriction) on the solver's
+velocities.
 The inputs and the reference's outputs go to OUTDIR/<case>.npz; the tests
 hold the oracle (tests/test_golden_cpu.py) and the engine
 (tests/test_golden_gpu.py) to them bit for bit.  The script also prints how
@@ -67,6 +69,10 @@ def main(outdir: str) -> int:
             raise ValueError("the reference always projects ground constraints: keep groundOn")
         sol = ref.solve(x, xp, vf=r["vf"], ee=r["ee"], **golden_cases.solver_inputs(spec, data, o))
         data.update({"ref_solve_" + k: sol[k] for k in ("x", "v", "x_prev", "x_end")})
+        # friction (CudaPBD::ApplyFriction) on the solver's velocities with the
+        # step's ground flags and VF contacts
+        data["ref_ground"] = sol["ground"]
+        data["ref_friction_v"] = ref.friction(sol["v"], sol["ground"], r["vf"], float(spec.params.kFriction))
         raced = int(np.sum(np.any(raw["node_min"] != r["node_min"], axis=1) | np.any(raw["node_max"] != r["node_max"],
                                                                                         axis=1)))
         np.savez_compressed(out / f"{case['name']}.npz", **data)
@@ -74,8 +80,9 @@ def main(outdir: str) -> int:
         # how the FP32 oracle compares on the same inputs
         diffs = golden_cases.compare_oracle(spec, data)
         sdiff = golden_cases.compare_oracle_solver(spec, data)
+        fdiff = golden_cases.compare_oracle_friction(spec, data)
         print(f"{case['name']}: T={len(perm)} pairs={len(r['pairs'])} vf={len(r['vf'])} ee={len(r['ee'])} "
-              f"ground={sol['ground_flags']} lra={sol['lra_flags']} solver vs FP32 oracle {sdiff} "
+              f"ground={sol['ground_flags']} lra={sol['lra_flags']} solver vs FP32 oracle {sdiff} friction {fdiff} "
               f"nodes raced in the unseeded refit={raced} "
               f"oracle {'agrees' if not diffs else 'DIFFERS: ' + ', '.join(diffs)}")
         bad += bool(diffs)

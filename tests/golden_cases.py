@@ -273,3 +273,28 @@ def compare_oracle_solver(spec, d: dict) -> dict:
             same = np.all(x.view(np.uint32) == d["ref_solve_x"].view(np.uint32), axis=1)
             out["fp32_bitexact"] = float(same.mean())
     return out
+
+
+# Friction changes velocities only; from the same inputs the oracle and the
+# reference's kernels differ by roundings (CUDA's powf against the host's).
+FRICTION_ATOL_V = 1e-5
+
+
+def compare_oracle_friction(spec, d: dict) -> dict:
+    """Largest velocity differences between the oracle's friction (FP32, FP64)
+    and the reference's friction kernels, on the reference solver's
+    velocities, ground flags and VF contacts (with their normals)."""
+    from oracle.oracle_ffi import Oracle
+    vf = d["ref_vf"]
+    ids, w = vf[:, :4], vf[:, 4:8].view(np.float32)
+    normals = np.ascontiguousarray(vf[:, 9:12]).view(np.float32)
+    out = {}
+    for fp64 in (False, True):
+        o = Oracle([spec], fp64=fp64)
+        try:
+            v = o.friction_on(0, d["ref_solve_v"], d["ref_ground"], (ids, w), normals)
+        finally:
+            o.close()
+        out["fp64_dv" if fp64 else "fp32_dv"] = float(np.abs(v - d["ref_friction_v"]).max())
+    out["changed"] = float(np.abs(d["ref_friction_v"] - d["ref_solve_v"]).max())
+    return out

@@ -75,3 +75,15 @@ def test_bend_singularity_is_the_only_excluded_case():
             excluded.append((path.stem, worst, bound))
     assert [e[0] for e in excluded] == ["windy20_mesh_h_step40"], excluded
     assert excluded[0][1] < 0.2 * excluded[0][2]
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_oracle_friction_matches_reference_kernels(path):
+    """CudaPBD::ApplyFriction: the oracle's restatement (FP32 and FP64) against
+    the reference's friction kernels on the same velocities, ground flags and
+    VF contacts."""
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    r = golden_cases.compare_oracle_friction(spec, d)
+    assert r["fp32_dv"] <= golden_cases.FRICTION_ATOL_V, r
+    assert r["fp64_dv"] <= golden_cases.FRICTION_ATOL_V, r

@@ -10,7 +10,8 @@ and velocities after the solver, the velocity update and the world clamp
 must agree with what the reference's solver kernels computed from the same
 state within golden_cases.SOLVER_ATOL_X (1e-5 m; 1e-5 m / dt on velocities)
 on every state whose bends stay away from the reference's d -> 1
-singularity (golden_cases.bend_conditioning).
+singularity (golden_cases.bend_conditioning).  With useFriction the
+velocities are compared with the reference's friction kernels' output.
 """
 from __future__ import annotations
 
@@ -25,11 +26,13 @@ pytestmark = pytest.mark.gpu
 FILES = golden_cases.golden_files()
 
 
+@pytest.mark.parametrize("friction", [False, True], ids=["plain", "friction"])
 @pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
-def test_engine_matches_reference_kernels(path):
+def test_engine_matches_reference_kernels(path, friction):
     d = golden_cases.load(path)
     spec = golden_cases.make_spec(d["case"])
     p = spec.params
+    p.useFriction = 1 if friction else 0
     p.gravity[:] = (0.0, 0.0, 0.0)
     p.kDamp = 0.0
     p.globalVelDamp = 0.0
@@ -50,7 +53,7 @@ def test_engine_matches_reference_kernels(path):
             return
         dt = float(d["dt"])
         dx = np.abs(st["x"] - d["ref_solve_x_end"]).max()
-        dv = np.abs(st["v"] - d["ref_solve_v"]).max()
+        dv = np.abs(st["v"] - d["ref_friction_v" if friction else "ref_solve_v"]).max()
         assert dx <= golden_cases.SOLVER_ATOL_X, dx
         assert dv <= golden_cases.SOLVER_ATOL_X / dt, dv
     finally:
