@@ -74,7 +74,8 @@ typedef struct lc_cloth_params {
     int32_t windOn;
     float worldMin[3];
     float worldMax[3];
-    int32_t dims[2];         /* informational; vertex count comes from the mesh */
+    int32_t dims[2];         /* grid rows x columns; triangle bending (useTriangleBending) walks the grid
+                                with them, otherwise informational */
     int32_t solverIterations;
     int32_t ccdIterations;   /* stored, unused by the live step */
     int32_t BVHChunkSize;

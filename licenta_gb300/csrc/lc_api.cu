@@ -171,14 +171,47 @@ static lc_status build_host_cloth(const lc_cloth_desc &d, HostCloth &hc) {
             }
         }
     }
-    const int E = (int)hc.s_ids.size(), B = (int)hc.b_ids.size();
     for (const int4 &b : hc.b_ids)
         if (b.x < 0 || b.y < 0 || b.z < 0 || b.w < 0)
             return fail(LC_ERR_INVALID_ARG, "degenerate triangle pair (repeated vertex) in the mesh");
+    if (d.params.useTriangleBending) {
+        // Physics/CudaPBD.cu:474-509 — triangle bends instead of the dihedral
+        // ones: every three consecutive vertices of a grid row, then of a grid
+        // column, (b0, v, b1), with h0 = |v - centroid|.  w holds h0's bits.
+        const int nx = d.params.dims[0], ny = d.params.dims[1];
+        if (nx < 1 || ny < 1 || (int64_t)nx * ny != hc.V)
+            return fail(LC_ERR_INVALID_ARG, "useTriangleBending needs a grid cloth: dims[0] * dims[1] == vertex count");
+        auto lin = [&](int i, int j) { return i * nx + j; };
+        auto add_tri = [&](int v1, int v3, int v2) -> bool {
+            if (v1 < 0 || v2 < 0 || v3 < 0 || v1 >= hc.V || v2 >= hc.V || v3 >= hc.V) return false;
+            double c[3], h2 = 0;
+            for (int k = 0; k < 3; ++k) c[k] = ((double)hc.pos[3 * v1 + k] + hc.pos[3 * v2 + k] + hc.pos[3 * v3 + k]) / 3.0;
+            for (int k = 0; k < 3; ++k) h2 += ((double)hc.pos[3 * v3 + k] - c[k]) * ((double)hc.pos[3 * v3 + k] - c[k]);
+            const float h0 = (float)std::sqrt(h2);
+            int bits;
+            std::memcpy(&bits, &h0, sizeof(bits));
+            hc.b_ids.push_back(make_int4(v1, v2, v3, bits));
+            return true;
+        };
+        hc.b_ids.clear();
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j + 2 < ny; ++j)
+                if (!add_tri(lin(i, j), lin(i, j + 1), lin(i, j + 2)))
+                    return fail(LC_ERR_INVALID_ARG, "triangle bend outside the grid");
+        for (int i = 0; i + 2 < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                if (!add_tri(lin(i, j), lin(i + 1, j), lin(i + 2, j)))
+                    return fail(LC_ERR_INVALID_ARG, "triangle bend outside the grid");
+    }
+    const int E = (int)hc.s_ids.size(), B = (int)hc.b_ids.size();
+    const int roles = d.params.useTriangleBending ? 3 : 4;
     // Physics/CudaPBD.cu:146-233 — per-vertex slots, stretch first then bend.
     std::vector<int> cnt(hc.V, 0);
     for (const int2 &s : hc.s_ids) { cnt[s.x]++; cnt[s.y]++; }
-    for (const int4 &b : hc.b_ids) { cnt[b.x]++; cnt[b.y]++; cnt[b.z]++; cnt[b.w]++; }
+    for (const int4 &b : hc.b_ids) {
+        cnt[b.x]++; cnt[b.y]++; cnt[b.z]++;
+        if (roles == 4) cnt[b.w]++;
+    }
     hc.soff.assign(hc.V + 1, 0);
     for (int i = 0; i < hc.V; ++i) hc.soff[i + 1] = hc.soff[i] + cnt[i];
     hc.sent.assign(hc.soff[hc.V], 0);
@@ -189,7 +222,8 @@ static lc_status build_host_cloth(const lc_cloth_desc &d, HostCloth &hc) {
     for (int i = 0; i < E; ++i) { put(hc.s_ids[i].x, 0, 0, i); put(hc.s_ids[i].y, 0, 1, i); }
     for (int i = 0; i < B; ++i) {
         put(hc.b_ids[i].x, 1, 0, i); put(hc.b_ids[i].y, 1, 1, i);
-        put(hc.b_ids[i].z, 1, 2, i); put(hc.b_ids[i].w, 1, 3, i);
+        put(hc.b_ids[i].z, 1, 2, i);
+        if (roles == 4) put(hc.b_ids[i].w, 1, 3, i);
     }
     // Physics/CudaPBD.cu:48-81 — LRA to every pinned vertex.
     for (int i = 0; i < hc.V; ++i)
@@ -519,6 +553,7 @@ static void fill_cloth_dev(const HostCloth &hc, ClothDev &cd) {
     cd.wind_on = p.windOn ? 1 : 0;
     cd.ground_on = p.groundOn ? 1 : 0;
     cd.sphere_on = p.sphereOn ? 1 : 0;
+    cd.tri_bend = p.useTriangleBending ? 1 : 0;
     cd.friction = p.useFriction ? 1 : 0;
     cd.kfriction = p.kFriction;
     cd.morton_mode = p.mortonMode;
@@ -601,6 +636,9 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     if (V > (1ll << 31) - 2 || T > (1ll << 31) - 2 || E + B >= (1ll << 29) || PC > 0xFFFFFFF0ll)
         return fail(LC_ERR_INVALID_ARG, "batch too large for 32-bit indices");
     b->sort_passes = b->hosts[0].p.mortonMode == LC_MORTON_K30 ? 4 : 8;
+    for (int c = 0; c < n && opt.adjoint; ++c)
+        if (b->cds[c].tri_bend)
+            return fail(LC_ERR_NOT_SUPPORTED, "adjoint: triangle bending is not differentiated");
     if (opt.adjoint && b->d.friction_any)
         return fail(LC_ERR_NOT_SUPPORTED, "adjoint: friction is not differentiated; create the batch without useFriction");
 

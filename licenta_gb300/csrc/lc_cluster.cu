@@ -187,7 +187,11 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
                     const uint32_t k = ent & 0x1FFFFFFFu;
                     const int role = (int)((ent >> 29) & 3u);
                     float3 corr;
-                    if (ent >> 31) {
+                    if ((ent >> 31) && cd.tri_bend) {
+                        const int4 id = __ldg(&d.b_ids[k]);
+                        corr = tri_bend_corr_pos(X(xa, id.x - vo), X(xa, id.y - vo), X(xa, id.z - vo),
+                                                 __ldg(&d.b_kp[k]), __int_as_float(id.w), role);
+                    } else if (ent >> 31) {
                         const int4 id = __ldg(&d.b_ids[k]);
                         corr = bend_corr_pos(X(xa, id.x - vo), X(xa, id.y - vo), X(xa, id.z - vo), X(xa, id.w - vo),
                                              __ldg(&d.b_kp[k]), d.kpi_gap, role);
@@ -398,7 +402,7 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             add_corr(i1, stretch_corr_pos(p1, p2, par.x, par.y, 0), false);
             add_corr(i2, stretch_corr_pos(p1, p2, par.x, par.y, 1), false);
         }
-        for (int k = bb + tid; k < be; k += bs) {
+        for (int k = bb + tid; k < (cd.tri_bend ? bb : be); k += bs) {
             const int4 id = __ldg(&d.b_ids[k]);
             const float kp = __ldg(&d.b_kp[k]);
             const int li[4] = {id.x - vo, id.y - vo, id.z - vo, id.w - vo};
@@ -409,6 +413,15 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
 #pragma unroll
                 for (int j = 0; j < 4; ++j) add_corr(li[j], mul(q[j], -(p[j].w * s)), false);
             }
+        }
+        // triangle bends (Physics/CudaPBD.cu:1149-1187), when the cloth uses them
+        for (int k = bb + tid; k < (cd.tri_bend ? be : bb); k += bs) {
+            const int4 id = __ldg(&d.b_ids[k]);
+            const float kp = __ldg(&d.b_kp[k]), h0 = __int_as_float(id.w);
+            const int li[3] = {id.x - vo, id.y - vo, id.z - vo};
+            const float4 p[3] = {X(li[0]), X(li[1]), X(li[2])};
+#pragma unroll
+            for (int j = 0; j < 3; ++j) add_corr(li[j], tri_bend_corr_pos(p[0], p[1], p[2], kp, h0, j), false);
         }
         const uint32_t nv = cr.y - cr.x, ncont = nv + (cr.w - cr.z);
         for (uint32_t k = r * bs + tid; k < ncont; k += CS * bs) {

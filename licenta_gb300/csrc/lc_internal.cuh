@@ -41,6 +41,7 @@ struct ClothDev {
     int iters;             // solver iterations
     int wind_on;
     int ground_on, sphere_on;
+    int tri_bend;          // bends are triangle bends (useTriangleBending): b_ids = (b0, b1, v, h0 bits)
     int friction;          // CudaPBD::ApplyFriction after the integration (useFriction)
     float kfriction;
     int morton_mode, leaf_quirk;

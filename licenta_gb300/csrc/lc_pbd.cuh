@@ -58,6 +58,19 @@ __device__ __forceinline__ float3 bend_corr_pos(float4 a1, float4 a2, float4 a3,
     return mul(q, -(wr * ts));
 }
 
+// Physics/CudaPBD.cu:1149-1187 — triangle bending (useTriangleBending): the
+// middle vertex v of three collinear grid vertices (b0, v, b1) is kept at the
+// rest distance h0 from their centroid.  Slot roles: 0 = b0, 1 = b1, 2 = v.
+__device__ __forceinline__ float3 tri_bend_corr_pos(float4 b0, float4 b1, float4 v, float kp, float h0, int role) {
+    const float W = b0.w + b1.w + 2.f * v.w;
+    const float3 c = dvs(add(add(xyz(b0), xyz(b1)), xyz(v)), 3.f);
+    const float3 hv = sub(xyz(v), c);
+    const float l = len(hv);
+    if (l <= kEpsPbd) return f3(0.f, 0.f, 0.f);
+    const float3 term = mul(mul(dvs(hv, W), kp), 1.f - h0 / l);
+    return role == 0 ? mul(term, 2.f * b0.w) : role == 1 ? mul(term, 2.f * b1.w) : mul(term, -4.f * v.w);
+}
+
 // The same bend constraint evaluated once for all four vertices: q[j] and the
 // scale s such that vertex j's correction is -(w_j s) q[j].  Returns false
 // when the reference returns zero corrections.

@@ -326,6 +326,12 @@ __device__ __forceinline__ float3 stretch_corr(const DevPtrs &d, const float4 *_
     return stretch_corr_pos(xa[id.x], xa[id.y], par.x, par.y, role);
 }
 
+__device__ __forceinline__ float3 tri_bend_corr(const DevPtrs &d, const float4 *__restrict__ xa, uint32_t k,
+                                                int role) {
+    const int4 id = __ldg(&d.b_ids[k]);
+    return tri_bend_corr_pos(xa[id.x], xa[id.y], xa[id.z], __ldg(&d.b_kp[k]), __int_as_float(id.w), role);
+}
+
 __device__ __forceinline__ float3 bend_corr(const DevPtrs &d, const float4 *__restrict__ xa, uint32_t k, int role) {
     const int4 id = __ldg(&d.b_ids[k]);
     return bend_corr_pos(xa[id.x], xa[id.y], xa[id.z], xa[id.w], __ldg(&d.b_kp[k]), d.kpi_gap, role);
@@ -389,7 +395,8 @@ __global__ void k_jacobi(DevPtrs d, const float4 *__restrict__ xa, float4 *__res
             const uint32_t ent = __ldg(&d.sent[e]);
             const uint32_t k = ent & 0x1FFFFFFFu;
             const int role = (int)((ent >> 29) & 3u);
-            sa = add(sa, (ent >> 31) ? bend_corr(d, xa, k, role) : stretch_corr(d, xa, k, role));
+            sa = add(sa, (ent >> 31) ? (cd.tri_bend ? tri_bend_corr(d, xa, k, role) : bend_corr(d, xa, k, role))
+                                     : stretch_corr(d, xa, k, role));
         }
         acc = add(acc, sa);
         cnt += s1 - s0;

@@ -168,6 +168,8 @@ struct Topology {
     std::vector<int> fixed;      // pinned ids (Physics/CudaPBD.cu:48-58)
     std::vector<double> lra_l0;  // V*F
     std::vector<double> kst, kbd;  // per-constraint stiffness
+    bool tri_bend = false;       // bends are triangle bends (b1, b2, b3 = b0, b1, v; th0 rest heights)
+    std::vector<double> th0;
     double vmass = 0;
 };
 
@@ -247,13 +249,38 @@ inline void build_topology(const lc_cloth_desc &d, Topology &tp) {
             }
         }
     }
+    if (d.params.useTriangleBending) {
+        // Physics/CudaPBD.cu:474-509 — triangle bends replace the dihedral
+        // ones (:159-178): every three consecutive vertices of a grid row,
+        // then of a grid column; h0 = |v - centroid|.
+        tp.tri_bend = true;
+        tp.b1.clear(); tp.b2.clear(); tp.b3.clear(); tp.b4.clear();
+        const int nx = d.params.dims[0], ny = d.params.dims[1];
+        auto lin = [&](int i, int j) { return i * nx + j; };
+        auto add = [&](int v1, int v3, int v2) {
+            double c[3], h2 = 0;
+            for (int k = 0; k < 3; ++k) c[k] = ((double)P[3 * v1 + k] + P[3 * v2 + k] + P[3 * v3 + k]) / 3.0;
+            for (int k = 0; k < 3; ++k) h2 += ((double)P[3 * v3 + k] - c[k]) * ((double)P[3 * v3 + k] - c[k]);
+            tp.b1.push_back(v1); tp.b2.push_back(v2); tp.b3.push_back(v3); tp.b4.push_back(-1);
+            tp.th0.push_back((double)(float)std::sqrt(h2));
+        };
+        if ((long)nx * ny == tp.V) {
+            for (int i = 0; i < nx; ++i)
+                for (int j = 0; j + 2 < ny; ++j) add(lin(i, j), lin(i, j + 1), lin(i, j + 2));
+            for (int i = 0; i + 2 < nx; ++i)
+                for (int j = 0; j < ny; ++j) add(lin(i, j), lin(i + 1, j), lin(i + 2, j));
+        }
+    }
     int E = (int)tp.s1.size(), B = (int)tp.b1.size();
     tp.kst.assign(E, d.params.kStretch);
     tp.kbd.assign(B, d.params.kBend);
     // Physics/CudaPBD.cu:146-233 — per-vertex slots, stretch first then bend.
     std::vector<int> cnt(tp.V, 0);
     for (int i = 0; i < E; ++i) { cnt[tp.s1[i]]++; cnt[tp.s2[i]]++; }
-    for (int i = 0; i < B; ++i) { cnt[tp.b1[i]]++; cnt[tp.b2[i]]++; cnt[tp.b3[i]]++; cnt[tp.b4[i]]++; }
+    for (int i = 0; i < B; ++i) {
+        cnt[tp.b1[i]]++; cnt[tp.b2[i]]++; cnt[tp.b3[i]]++;
+        if (!tp.tri_bend) cnt[tp.b4[i]]++;
+    }
     tp.soff.assign(tp.V + 1, 0);
     for (int i = 0; i < tp.V; ++i) tp.soff[i + 1] = tp.soff[i] + cnt[i];
     tp.sent.assign(tp.soff[tp.V], 0);
@@ -264,7 +291,8 @@ inline void build_topology(const lc_cloth_desc &d, Topology &tp) {
     for (int i = 0; i < E; ++i) { put(tp.s1[i], ENT_STRETCH, 0, i); put(tp.s2[i], ENT_STRETCH, 1, i); }
     for (int i = 0; i < B; ++i) {
         put(tp.b1[i], ENT_BEND, 0, i); put(tp.b2[i], ENT_BEND, 1, i);
-        put(tp.b3[i], ENT_BEND, 2, i); put(tp.b4[i], ENT_BEND, 3, i);
+        put(tp.b3[i], ENT_BEND, 2, i);
+        if (!tp.tri_bend) put(tp.b4[i], ENT_BEND, 3, i);
     }
     // Physics/CudaPBD.cu:48-81 — long-range attachments to every pinned vertex.
     tp.fixed.clear();
@@ -1001,6 +1029,7 @@ template <class R> class Cloth {
     }
 
     void track_bend_conditioning() {
+        if (tp.tri_bend) return;  // triangle bends have no dihedral angle
         for (size_t k = 0; k < tp.b1.size(); ++k) {
             const V &p2 = x[tp.b2[k]], &p3 = x[tp.b3[k]], &p4 = x[tp.b4[k]];
             const double a[3] = {(double)p2.x, (double)p2.y, (double)p2.z};
@@ -1029,6 +1058,21 @@ template <class R> class Cloth {
             V n = diff / l;
             V tt = (l - R(tp.sl0[c])) * n * kp / ws;
             return role == 0 ? (-w1) * tt : w2 * tt;
+        }
+        if (tp.tri_bend) {
+            // Physics/CudaPBD.cu:1149-1187 — triangle bend (b0, b1, v)
+            R kp = kpb[c];
+            const int i0 = tp.b1[c], i1 = tp.b2[c], iv = tp.b3[c];
+            R wb0 = invm[i0], wb1 = invm[i1], wv = invm[iv];
+            R W = wb0 + wb1 + R(2) * wv;
+            V cc = (x[i0] + x[i1] + x[iv]) / R(3);
+            V hv = x[iv] - cc;
+            R l = len(hv);
+            if (l <= R(kEpsPbd)) return mk<R>(0, 0, 0);
+            V term = kp * (hv / W) * (R(1) - R(tp.th0[c]) / l);
+            if (role == 0) return (R(2) * wb0) * term;
+            if (role == 1) return (R(2) * wb1) * term;
+            return (R(-4) * wv) * term;
         }
         // Physics/CudaPBD.cu:1024-1147 (raw positions, phi0 = PI)
         R kp = kpb[c];

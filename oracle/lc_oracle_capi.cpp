@@ -322,6 +322,7 @@ extern "C" int lco_adj_backward(lco_world *w, int c, double *gx, double *gxp, do
             axp[i] = mk<R>(R(gxp[3 * i]), R(gxp[3 * i + 1]), R(gxp[3 * i + 2]));
             av[i] = mk<R>(R(gv[3 * i]), R(gv[3 * i + 1]), R(gv[3 * i + 2]));
         }
+        if (cl.tp.tri_bend) return (int)LC_ERR_NOT_SUPPORTED;  // triangle bending is not differentiated
         std::vector<double> ks(cl.tp.s1.size(), 0.0), kb(cl.tp.b1.size(), 0.0);
         for (int s = (int)cl.records.size() - 1; s >= 0; --s) cl.backward(cl.records[s], ax, axp, av, ks, kb);
         for (int i = 0; i < Vn; ++i) {
@@ -495,4 +496,15 @@ extern "C" int lco_track_bend(lco_world *w, int c, int on) {
 }
 extern "C" int lco_bend_conditioning(lco_world *w, int c, double *out) {
     return with_cloth(w, c, [&](auto &cl) { *out = cl.bend_min; return (int)LC_OK; });
+}
+
+// Triangle bending: *is_tri = 1 when the cloth's bends are triangle bends
+// (then lco_topology's b rows are (b0, b1, v, -1)) and h0 receives their rest
+// heights (one per bend).
+extern "C" int lco_tri_bends(lco_world *w, int c, int *is_tri, double *h0) {
+    return with_cloth(w, c, [&](auto &cl) {
+        if (is_tri) *is_tri = cl.tp.tri_bend ? 1 : 0;
+        if (h0) std::copy(cl.tp.th0.begin(), cl.tp.th0.end(), h0);
+        return (int)LC_OK;
+    });
 }

@@ -58,6 +58,7 @@ def lib() -> C.CDLL:
             "lco_solve_on": (C.c_int, [VP, C.c_int, VP, VP, VP, C.c_uint64, VP, C.c_uint64, VP, VP, VP]),
             "lco_solve_iterate": (C.c_int, [VP, C.c_int, C.c_int, VP]),
             "lco_set_frozen_normals": (C.c_int, [VP, C.c_int, VP, C.c_uint64]),
+            "lco_tri_bends": (C.c_int, [VP, C.c_int, VP, VP]),
             "lco_track_bend": (C.c_int, [VP, C.c_int, C.c_int]),
             "lco_bend_conditioning": (C.c_int, [VP, C.c_int, C.POINTER(C.c_double)]),
             "lco_friction_on": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
@@ -229,7 +230,8 @@ class Oracle:
         lengths sl0 (E), bend vertices b (B, 4), the per-vertex slot CSR soff
         (V+1) and its entries sent (kind << 30 | role << 28 | constraint),
         pinned ids fixed (F), attachment lengths lra_l0 (V, F), inverse masses
-        invm (V) and pinned flags (V)."""
+        invm (V) and pinned flags (V); with triangle bending (tri_bend), b
+        rows are (b0, b1, v, -1) and h0 their rest heights."""
         nv, nt, ne, nb = self.sizes(c)
         counts = np.zeros(2, np.int32)
         _chk(lib().lco_topology(self._h, c, *([None] * 9), _p(counts)), "topology")
@@ -239,6 +241,12 @@ class Oracle:
                  lra_l0=np.empty((nv, F)), invm=np.empty(nv, np.float32), pinned=np.empty(nv, np.uint8))
         _chk(lib().lco_topology(self._h, c, *[_p(t[k]) for k in ("s12", "sl0", "b", "soff", "sent", "fixed",
                                                                     "lra_l0", "invm", "pinned")], None), "topology")
+        tri = C.c_int()
+        _chk(lib().lco_tri_bends(self._h, c, C.byref(tri), None), "tri_bends")
+        t["tri_bend"] = bool(tri.value)
+        t["h0"] = np.zeros(nb)
+        if t["tri_bend"]:
+            _chk(lib().lco_tri_bends(self._h, c, None, _p(t["h0"])), "tri_bends")
         return t
 
     def solve_on(self, c: int, x, x_prev, vf: tuple, ee: tuple, forced: dict | None = None):

@@ -65,6 +65,7 @@ KERNELS = {
     "ground_apply": "_ApplyGroundCorrections",
     "lra_apply": "_ApplyLRACorrections",
     "static_project": "_ProjectStaticConstraints",
+    "static_project_tri": "_ProjectStaticConstraintsTriBend",
     "static_apply": "_ApplyStaticCorrections",
     "dyn_project": "_ProjectDynamicConstraints",
     "dyn_apply": "_ApplyDynamicCorrections",
@@ -358,10 +359,12 @@ class RefKernels:
         sent = np.asarray(topo["sent"], i32)
         fixed = np.asarray(topo["fixed"], i32)
         E, B, S, F = len(s12), len(bq), len(sent), len(fixed)
+        tri = bool(topo.get("tri_bend", False))
+        nb_roles = 3 if tri else 4
         if x.shape != (V, 3) or xp.shape != (V, 3) or len(soff) != V + 1 or soff[0] != 0 or soff[-1] != S \
                 or np.any(np.diff(soff) < 0):
             raise ValueError("state and slot offsets do not match")
-        for a in (s12, bq, fixed):
+        for a in (s12, bq[:, :nb_roles], fixed):
             if a.size and (a.min() < 0 or a.max() >= V):
                 raise ValueError("vertex id out of range")
         # Slot of each (constraint, role): the inverse of the CSR entries.
@@ -374,7 +377,9 @@ class RefKernels:
             raise ValueError("slot entry out of range")
         so[cid[st], role[st]] = slots[st]
         bo[cid[bd], role[bd]] = slots[bd]
-        if (so < 0).any() or (bo < 0).any():
+        if np.any(role[bd] >= nb_roles):
+            raise ValueError("slot entry out of range")
+        if (so < 0).any() or (bo[:, :nb_roles] < 0).any():
             raise ValueError("a constraint end has no slot")
         vf = np.ascontiguousarray(vf, i32).reshape(-1, 12)
         ee = np.ascontiguousarray(ee, i32).reshape(-1, 12)
@@ -394,6 +399,7 @@ class RefKernels:
         d_b = [dev(bq[:, j]) for j in range(4)]
         d_bo = [dev(bo[:, j]) for j in range(4)]
         d_phi0 = dev(np.full(max(B, 1), np.float32(3.14159265359), f32))  # Physics/CudaPBD.cu:35,368
+        d_h0 = dev(np.asarray(topo.get("h0", np.zeros(max(B, 1))), np.float64).astype(f32) if B else np.zeros(1, f32))
         d_soff = dev(soff)
         cor = torch.zeros((max(S, 1), 3), dtype=torch.float32, device="cuda")
         d_fixed = dev(fixed if F else np.zeros(1, i32))
@@ -426,8 +432,12 @@ class RefKernels:
             self.launch("ground_apply", V, C.c_int(V), d_x, d_invm, gflag, gq, gn, acc, cnt)
             if F:
                 self.launch("lra_apply", V, C.c_int(V), C.c_int(F), d_x, d_invm, d_fixed, d_l0, lflag, acc, cnt)
-            self.launch("static_project", E + B, C.c_int(E), C.c_int(B), it, d_x, d_invm, d_s1, d_s2, d_s1o, d_s2o,
-                        C.c_float(k_stretch), d_sl0, *d_b, *d_bo, C.c_float(k_bend), d_phi0, cor)
+            if tri:  # Physics/CudaPBD.cu:840-851
+                self.launch("static_project_tri", E + B, C.c_int(E), C.c_int(B), it, d_x, d_invm, d_s1, d_s2, d_s1o,
+                            d_s2o, C.c_float(k_stretch), d_sl0, *d_b[:3], *d_bo[:3], C.c_float(k_bend), d_h0, cor)
+            else:
+                self.launch("static_project", E + B, C.c_int(E), C.c_int(B), it, d_x, d_invm, d_s1, d_s2, d_s1o, d_s2o,
+                            C.c_float(k_stretch), d_sl0, *d_b, *d_bo, C.c_float(k_bend), d_phi0, cor)
             self.launch("static_apply", V, C.c_int(V), cor, d_soff, acc, cnt)
             if N:
                 self.launch("dyn_project", N, d_x, d_xp, d_invm, h, d_vf, C.c_uint64(nvf), d_ee, C.c_uint64(nee),

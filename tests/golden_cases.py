@@ -34,6 +34,8 @@ CASES = [
     # an unpinned cloth draped over the analytic sphere
     dict(name="sphere24_step22", scene="small_cloth", kw=dict(seed=4, n=24), steps=22, unpin=True,
          sphere=((0.5, 0.7, 0.5), 0.2)),
+    # triangle bending instead of the dihedral bends, folded onto itself
+    dict(name="tribend28_step139", scene="small_cloth", kw=dict(seed=12, n=28), steps=139, tri_bend=True),
 ]
 
 
@@ -43,6 +45,8 @@ def make_spec(case: dict):
         scenes.set_constant_wind(spec.params, tuple(case["wind"]))
     if case.get("mesh_thickness"):
         spec.params.thicknessFromMesh = 1
+    if case.get("tri_bend"):
+        spec.params.useTriangleBending = 1
     if case.get("unpin"):
         spec.pinned[:] = 0
     if case.get("world_min_y") is not None:
@@ -232,7 +236,8 @@ def bend_conditioning(spec, d: dict) -> tuple[float, float]:
         t = o.topology(0)
         b = t["b"]
         worst = np.inf
-        for k in range(int(spec.params.solverIterations)):
+        # triangle bends have no dihedral angle, hence no such singularity
+        for k in range(0 if t["tri_bend"] else int(spec.params.solverIterations)):
             x = o.solve_iterate(0, k).astype(np.float64)
             c23 = np.cross(x[b[:, 1]], x[b[:, 2]])
             c24 = np.cross(x[b[:, 1]], x[b[:, 3]])

@@ -102,6 +102,15 @@ def test_friction_parity(variant):
     assert contacts > 0
 
 
+@pytest.mark.parametrize("variant", [1, 2, 3], ids=["gather", "cluster", "scatter"])
+def test_triangle_bending_parity(variant):
+    """useTriangleBending: triangle bends (Physics/CudaPBD.cu:474-509,
+    1149-1187) in place of the dihedral ones, next to a dihedral cloth."""
+    tri = scenes.small_cloth(seed=12, n=28)
+    tri.params.useTriangleBending = 1
+    run_parity([tri, scenes.small_cloth(seed=13, n=16)], steps=150, check_every=10, variant=variant)
+
+
 def test_uneven_batch_parity():
     specs = scenes.batched_cloths(seed=11, count=5, n_min=5, n_max=40)
     run_parity(specs, steps=15, check_every=2)
