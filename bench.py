@@ -300,6 +300,47 @@ def adjoint_timing(seed: int) -> dict:
             "what": "backward = segment re-run from checkpoints + recorded step + reverse pass, per step"}
 
 
+def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20) -> dict:
+    """The batched differentiable rollout: 128 cloths (sides U{32..128}), each
+    dropped onto its own analytic sphere, 100 steps, 10 iterations,
+    checkpoints every 20 steps; loss = summed squared distance of the final
+    positions to a target.  One forward rollout and its backward pass after
+    one warm-up pair, CUDA events; the sphere projection is held fixed in the
+    reverse pass."""
+    import torch
+    from licenta_gb300 import scenes
+    from licenta_gb300.adjoint import ClothRollout, DiffCloth
+
+    specs = scenes.batched_sphere_cloths(seed=seed)
+    cloth = DiffCloth(specs, checkpoint_every=every)
+    ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
+    kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
+    x0 = torch.tensor(np.concatenate([s.positions for s in specs]), device="cuda", requires_grad=True)
+    v0 = torch.zeros_like(x0, requires_grad=True)
+    target = x0.detach() - torch.tensor([0.0, 0.5, 0.0], device="cuda")
+
+    def once():
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        out = ClothRollout.apply(cloth, steps, ks, kb, x0, v0)
+        loss = ((out - target) ** 2).sum()
+        e[1].record()
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), float(ks.grad.abs().max())
+
+    once()
+    fwd, bwd, gmax = once()
+    V = cloth.V
+    cloth.close()
+    return {"workload": f"batched differentiable rollout: {len(specs)} cloths (sides 32..128, {V} vertices) onto "
+                        f"their own spheres, {steps} steps, 10 iterations, checkpoints every {every}",
+            "forward_ms_per_step": fwd / steps, "backward_ms_per_step": bwd / steps,
+            "adjoint_over_forward": bwd / fwd, "cloth_steps_per_s_forward": len(specs) * steps / (fwd / 1000.0),
+            "max_abs_dL_dk_stretch": gmax}
+
+
 def large_cloth_timing(seed: int, steps: int = 30, warmup: int = 5) -> dict:
     """The plain large workload: one 512x512 cloth (262,144 vertices) dropped
     from y = 1 m onto the analytic sphere of radius 0.3 m, 20 iterations,
@@ -574,6 +615,9 @@ def run_ours(args, world, rank, local):
     large = None
     if rank == 0 and not args.no_large:
         large = large_cloth_timing(args.seed)
+    adj_batched = None
+    if rank == 0 and not args.no_adjoint:
+        adj_batched = adjoint_batched_timing(args.seed)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -604,6 +648,7 @@ def run_ours(args, world, rank, local):
         "adjoint": adj,
         "lbvh": lbvh,
         "large_cloth": large,
+        "adjoint_batched": adj_batched,
         "tuning": tuning,
     }
     if rank == 0:

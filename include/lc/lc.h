@@ -185,6 +185,19 @@ lc_status lc_batch_set_triangle_order(lc_batch *b, int32_t cloth, const uint32_t
  * m_dPrevPositions.  Asynchronous on stream when dst is pinned or device memory. */
 lc_status lc_batch_read_positions(lc_batch *b, float *dst, int32_t is_host, void *stream);
 
+/* DeformableUtils::FinalVerticesUpdate (Physics/CudaDeformableUtils.cu:319-344,
+ * called by CudaDeformableBody::FinalVertUpdate, Physics/CudaDeformableBody.cpp:473-495)
+ * into a caller-owned DEVICE buffer of interleaved vertex records, for a
+ * renderer or a wire format to map without a host round trip: record i of the
+ * batch (cloths packed in order) starts at dst + i * stride bytes; its three
+ * position floats (the published positions, x_prev) go at pos_offset and its
+ * three normal floats (the running vertex normals) at normal_offset, and no
+ * other byte is written.  Rendering::VertexFormat is stride 48, position 0,
+ * normal 28 (Rendering/VertexFormat.h:24-30).  Offsets must be 4-byte
+ * aligned, the stride a multiple of 4 and at least 12 past both offsets. */
+lc_status lc_batch_write_vertex_records(lc_batch *b, void *dst, int64_t stride, int32_t pos_offset,
+                                        int32_t normal_offset, void *stream);
+
 /* Whole-batch state in one call each way, packed in cloth order (3 floats
  * per vertex per array; NULL arrays are skipped).  Asynchronous on stream;
  * host memory should be pinned.  Used by callers that keep the cloth state on

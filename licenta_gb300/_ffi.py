@@ -89,6 +89,7 @@ SIGNATURES = {
     "lc_batch_set_constraint_stiffness": (C.c_int, [VP, VP, VP, C.c_int32]),
     "lc_batch_get_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
     "lc_batch_set_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
+    "lc_batch_write_vertex_records": (C.c_int, [VP, VP, C.c_int64, C.c_int32, C.c_int32, VP]),
     "lc_group_create": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
     "lc_group_step": (C.c_int, [VP, C.c_int32, VP]),
     "lc_group_destroy": (C.c_int, [VP]),

@@ -128,6 +128,15 @@ class ClothBatch:
         _ffi.check(_ffi.lib().lc_batch_read_positions(self._h, C.c_void_p(dst_ptr), 1 if is_host else 0,
                                                       _stream_handle(stream)), "lc_batch_read_positions")
 
+    def write_vertex_records(self, dst_ptr: int, stride: int = 48, pos_offset: int = 0, normal_offset: int = 28,
+                             stream=None) -> None:
+        """Positions (x_prev) and running normals into interleaved device
+        records, Rendering::VertexFormat by default (48 B: position at 0,
+        normal at 28); other bytes of the records are left as they are."""
+        _ffi.check(_ffi.lib().lc_batch_write_vertex_records(self._h, C.c_void_p(dst_ptr), stride, pos_offset,
+                                                            normal_offset, _stream_handle(stream)),
+                   "lc_batch_write_vertex_records")
+
     def write_state(self, x: int | None, x_prev: int | None, v: int | None, is_host: bool, stream=None) -> None:
         """Upload the whole batch state from packed float3 arrays (raw pointers)."""
         vp = lambda a: None if a is None else C.c_void_p(a)

@@ -43,6 +43,7 @@ void launch_jacobi(const DevPtrs &d, const float4 *xa, float4 *xb, int it, const
                    cudaStream_t st);
 void launch_integrate(const DevPtrs &d, const float4 *xs, cudaStream_t st);
 void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st);
+void launch_vertex_records(const DevPtrs &d, void *dst, int64_t stride, int pos_off, int nrm_off, cudaStream_t st);
 void scan_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, uint32_t n_static, uint32_t n_cap,
               uint32_t *partial, uint32_t *total_out, unsigned long long *total_out64, cudaStream_t st);
 unsigned long long morton3_host(float x, float y, float z, int mode);
@@ -1251,6 +1252,25 @@ lc_status lc_batch_read_positions(lc_batch *b, float *dst, int32_t is_host, void
     cudaStream_t st = (cudaStream_t)stream;
     LC_CUDA(cudaMemcpy2DAsync(dst, 3 * sizeof(float), b->d.xp, sizeof(float4), 3 * sizeof(float), b->d.Vtot,
                               is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    return LC_OK;
+}
+
+lc_status lc_batch_write_vertex_records(lc_batch *b, void *dst, int64_t stride, int32_t pos_offset,
+                                        int32_t normal_offset, void *stream) {
+    if (!b || !dst) return fail(LC_ERR_INVALID_ARG, "lc_batch_write_vertex_records: bad arguments");
+    if (stride < 12 || stride % 4 || pos_offset < 0 || normal_offset < 0 || pos_offset % 4 || normal_offset % 4 ||
+        pos_offset + 12 > stride || normal_offset + 12 > stride ||
+        (pos_offset < normal_offset + 12 && normal_offset < pos_offset + 12) ||
+        reinterpret_cast<uintptr_t>(dst) % 4)
+        return fail(LC_ERR_INVALID_ARG, "lc_batch_write_vertex_records: stride / offsets / alignment");
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, dst) != cudaSuccess ||
+        (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)) {
+        cudaGetLastError();
+        return fail(LC_ERR_INVALID_ARG, "lc_batch_write_vertex_records: dst must be device memory");
+    }
+    launch_vertex_records(b->d, dst, stride, pos_offset, normal_offset, (cudaStream_t)stream);
+    LC_CUDA(cudaGetLastError());
     return LC_OK;
 }
 

@@ -534,6 +534,25 @@ __global__ void k_friction(DevPtrs d, const uint32_t *__restrict__ nvf_dev) {
     d.v[i] = f4(v, d.v[i].w);
 }
 
+// Physics/CudaDeformableUtils.cu:327-344: position (x_prev) and running
+// normal into interleaved records; nothing else of a record is touched.
+__global__ void k_vertex_records(DevPtrs d, unsigned char *__restrict__ dst, int64_t stride, int pos_off,
+                                 int nrm_off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.Vtot) return;
+    const float4 p = d.xp[i], n = d.vn[i];
+    float *pp = reinterpret_cast<float *>(dst + (int64_t)i * stride + pos_off);
+    float *pn = reinterpret_cast<float *>(dst + (int64_t)i * stride + nrm_off);
+    pp[0] = p.x; pp[1] = p.y; pp[2] = p.z;
+    pn[0] = n.x; pn[1] = n.y; pn[2] = n.z;
+}
+
+void launch_vertex_records(const DevPtrs &d, void *dst, int64_t stride, int pos_off, int nrm_off, cudaStream_t st) {
+    if (d.Vtot)
+        k_vertex_records<<<nblk(d.Vtot), kThreads, 0, st>>>(d, static_cast<unsigned char *>(dst), stride, pos_off,
+                                                            nrm_off);
+}
+
 void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st) {
     if (d.Vtot) k_friction<<<nblk(d.Vtot), kThreads, 0, st>>>(d, nvf);
 }

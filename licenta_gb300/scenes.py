@@ -139,6 +139,34 @@ def batched_cloths(seed: int = 0, count: int = 256, n_min: int = 16, n_max: int 
     return out
 
 
+def batched_sphere_cloths(seed: int = 0, count: int = 128, n_min: int = 32, n_max: int = 128,
+                          iterations: int = 10) -> list[ClothSpec]:
+    """The batched differentiable workload: 128 unpinned cloths, side drawn
+    from U{32..128}, 1 m square centred over the origin at y = 1 m, each
+    dropped onto its own sphere at the origin with radius U[0.2, 0.4] m (the
+    reference's analytic sphere collider, CudaPBD::SetSpherePos), stiffness
+    0.9, 10 iterations."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(n_min, n_max + 1, size=count)
+    radii = rng.uniform(0.2, 0.4, size=count)
+    out = []
+    for c in range(count):
+        n = int(sides[c])
+        p = base_params(iterations, 0.9)
+        p.dims[:] = (n, n)
+        p.worldMin[:] = (-1.0, -1.0, -1.0)
+        p.worldMax[:] = (1.0, 1.0, 1.0)
+        p.mortonOrigin[:] = (-1.0, -1.0, -1.0)
+        p.mortonScale = 0.5
+        p.sphereOn = 1
+        p.spherePos[:] = (0.0, 0.0, 0.0)
+        p.sphereRadius = float(radii[c])
+        out.append(ClothSpec(grid_positions(n, rng, origin=(-0.5, -0.5)), grid_indices(n),
+                             np.zeros(n * n, dtype=np.uint8), p, dict(workload="batched-sphere", n=n,
+                                                                      r=float(radii[c]))))
+    return out
+
+
 def adjoint_cloth(seed: int = 0, n: int = 64, stiffness: float = 0.9, wind=(0.0, 0.0, 0.0)) -> ClothSpec:
     """64x64 grid, 10 iterations (differentiable rollout workload)."""
     rng = np.random.default_rng(seed)

@@ -12,6 +12,8 @@ in twenty may be.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -109,6 +111,35 @@ def test_triangle_bending_parity(variant):
     tri = scenes.small_cloth(seed=12, n=28)
     tri.params.useTriangleBending = 1
     run_parity([tri, scenes.small_cloth(seed=13, n=16)], steps=150, check_every=10, variant=variant)
+
+
+def test_vertex_records(cuda):
+    """lc_batch_write_vertex_records into Rendering::VertexFormat records
+    (48 B): position = published x_prev, normal = running vertex normal, and
+    the color and uv bytes of every record untouched."""
+    torch = cuda
+    specs = [scenes.small_cloth(seed=1, n=12), scenes.small_cloth(seed=2, n=9)]
+    b = ClothBatch(specs)
+    b.step(5)
+    V = sum(sp.num_vertices for sp in specs)
+    buf = torch.full((V * 48,), 0xAB, dtype=torch.uint8, device="cuda")
+    b.write_vertex_records(buf.data_ptr())
+    b.sync()
+    rec = buf.cpu().numpy().view(np.float32).reshape(V, 12)
+    raw = buf.cpu().numpy().reshape(V, 48)
+    off = 0
+    for c, sp in enumerate(specs):
+        st = b.get_state(c)
+        n = sp.num_vertices
+        assert np.array_equal(rec[off:off + n, 0:3], st["x_prev"])
+        assert np.array_equal(rec[off:off + n, 7:10], st["vn"])
+        off += n
+    assert np.all(raw[:, 12:28] == 0xAB) and np.all(raw[:, 40:48] == 0xAB)
+    L = _ffi.lib()
+    assert L.lc_batch_write_vertex_records(b._h, C.c_void_p(buf.data_ptr()), 48, 0, 8, None) == 1  # overlap
+    host = np.zeros(V * 12, np.float32)
+    assert L.lc_batch_write_vertex_records(b._h, host.ctypes.data_as(C.c_void_p), 48, 0, 28, None) == 1
+    b.close()
 
 
 def test_uneven_batch_parity():
