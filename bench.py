@@ -328,17 +328,22 @@ def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20) -> dict
         loss.backward()
         e[2].record()
         torch.cuda.synchronize()
-        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), float(ks.grad.abs().max())
+        g = ks.grad.abs()
+        fin = torch.isfinite(g)
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), float(fin.float().mean()), \
+            float(g[fin].max()) if bool(fin.any()) else 0.0
 
     once()
-    fwd, bwd, gmax = once()
+    fwd, bwd, finite, gmax = once()
     V = cloth.V
     cloth.close()
     return {"workload": f"batched differentiable rollout: {len(specs)} cloths (sides 32..128, {V} vertices) onto "
                         f"their own spheres, {steps} steps, 10 iterations, checkpoints every {every}",
             "forward_ms_per_step": fwd / steps, "backward_ms_per_step": bwd / steps,
             "adjoint_over_forward": bwd / fwd, "cloth_steps_per_s_forward": len(specs) * steps / (fwd / 1000.0),
-            "max_abs_dL_dk_stretch": gmax}
+            "dL_dk_stretch_finite_share": finite, "max_finite_abs_dL_dk_stretch": gmax,
+            "note": "the exact reverse pass grows ~1e14 per 20 steps in these contact-rich drapes; gradients "
+                    "beyond float range come out as inf (never NaN)"}
 
 
 def large_cloth_timing(seed: int, steps: int = 30, warmup: int = 5) -> dict:

@@ -127,6 +127,13 @@ class ClothRollout(torch.autograd.Function):
         gv = torch.zeros_like(gx)
         gks = torch.zeros(cloth.E, dtype=torch.float32, device="cuda")
         gkb = torch.zeros(cloth.B, dtype=torch.float32, device="cuda")
+        ncl = len(cloth.batch.num_vertices)
+        vcl = torch.repeat_interleave(torch.arange(ncl, device="cuda"),
+                                      torch.tensor(cloth.batch.num_vertices, device="cuda"))
+        counts = [cloth.batch.constraint_counts(c) for c in range(ncl)]
+        ecl = torch.repeat_interleave(torch.arange(ncl, device="cuda"), torch.tensor([e for e, _ in counts], device="cuda"))
+        bcl = torch.repeat_interleave(torch.arange(ncl, device="cuda"), torch.tensor([b for _, b in counts], device="cuda"))
+        exp60 = torch.zeros(ncl, dtype=torch.float32, device="cuda")
         for seg in range(len(ctx.ckpts) - 1, -1, -1):
             first = seg * cloth.every
             last = min(steps, first + cloth.every)
@@ -140,4 +147,29 @@ class ClothRollout(torch.autograd.Function):
             for n in range(last - 1, first - 1, -1):
                 cloth.load(states[n - first])
                 cloth.adjoint_step(gx, gxp, gv, gks, gkb)
-        return None, None, gks, gkb, gx + gxp, gv
+                # Each cloth's reverse pass is linear in its seed: when a
+                # cloth's grows past 2^60 (contact-rich rollouts amplify it by
+                # up to ~1e14 per 20 steps) its accumulators are scaled by
+                # 2^-60, exactly, and its exponent kept on the device, so no
+                # intermediate product overflows in float; the results are
+                # rescaled once at the end (to inf where the true gradient is
+                # beyond float range).
+                m = torch.zeros(ncl, dtype=torch.float32, device="cuda")
+                rows = torch.maximum(torch.maximum(gx.abs().amax(1), gxp.abs().amax(1)), gv.abs().amax(1))
+                m.scatter_reduce_(0, vcl, rows, reduce="amax")
+                big = m > 2.0 ** 60
+                f = torch.where(big, torch.tensor(2.0 ** -60, device="cuda"), torch.tensor(1.0, device="cuda"))
+                fv = f[vcl].unsqueeze(1)
+                gx.mul_(fv)
+                gxp.mul_(fv)
+                gv.mul_(fv)
+                gks.mul_(f[ecl])
+                gkb.mul_(f[bcl])
+                exp60 += big.to(torch.float32)
+
+        def unscale(t, idx):
+            sc = torch.pow(torch.tensor(2.0 ** 60, device="cuda"), exp60)[idx]
+            if t.dim() == 2:
+                sc = sc.unsqueeze(1)
+            return torch.where(t == 0, t, t * sc)
+        return (None, None, unscale(gks, ecl), unscale(gkb, bcl), unscale(gx + gxp, vcl), unscale(gv, vcl))

@@ -114,3 +114,41 @@ def test_stiffness_recovered_by_gradient_descent():
                 p.clamp_(0.05, 0.99)
     cloth.close()
     assert losses[-1] < losses[0], losses
+
+
+def test_rescaled_reverse_pass_is_exact():
+    """Contact-rich rollouts amplify the reverse pass by up to ~1e14 per 20
+    steps; ClothRollout.backward scales a cloth's accumulators by 2^-60 when
+    they pass 2^60 and rescales at the end.  The reverse pass is linear in its
+    seed and a power-of-two scaling is exact in floating point, so a seed
+    2^70 times larger on one cloth (which triggers its scaling) must give that
+    cloth's gradients 2^70 times larger and leave the other cloth's alone."""
+    specs = [scenes.small_cloth(seed=21, n=12), scenes.small_cloth(seed=22, n=10)]
+    cloth = DiffCloth(specs, checkpoint_every=4)
+    x0 = torch.tensor(np.concatenate([s.positions for s in specs]), device="cuda")
+    n0 = specs[0].num_vertices
+    grads = []
+    for big in (False, True):
+        ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
+        kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
+        xi = x0.clone().requires_grad_(True)
+        v0 = torch.zeros_like(x0, requires_grad=True)
+        out = ClothRollout.apply(cloth, 10, ks, kb, xi, v0)
+        seed = torch.ones_like(out)
+        if big:
+            seed[:n0] *= 2.0 ** 70  # only the first cloth's seed is large
+        out.backward(seed)
+        grads.append([t.grad.clone() for t in (ks, kb, xi, v0)])
+    cloth.close()
+    small, large = grads
+    from licenta_gb300 import ClothBatch
+    b = ClothBatch(specs)
+    ce, cb = b.constraint_counts(0)
+    b.close()
+    s = 2.0 ** 70
+    for g_s, g_l, k in zip(small, large, (ce, cb, n0, n0)):
+        # first cloth: scaled by 2^70 (exact up to subnormals of the small run)
+        a, b_ = g_s[:k] * s, g_l[:k]
+        assert torch.allclose(a, b_, rtol=1e-6, atol=float(b_.abs().max()) * 1e-9)
+        assert torch.equal(g_s[k:], g_l[k:])  # second cloth: untouched
+    assert torch.isfinite(large[0]).all()
