@@ -295,6 +295,9 @@ typedef struct lc_tuning {
     int32_t narrow_blocks_per_sm;  /* grid of the narrowphase and contact kernels, in blocks per SM */
     int32_t solver_variant;        /* 1, 2 or 3 as lc_batch_options.solver_variant (2, 3 need every cloth on chip) */
     int32_t cluster_size;          /* CTAs per cloth of the on-chip solvers: 8, 16, or 0 to pick */
+    int32_t contact_gather;        /* variant 3: 0 = each contact scatters its four corrections (atomics into
+                                      the owners' shared memory), 1 = each owned vertex gathers its contact
+                                      slots (local atomics only; every contact evaluated per slot) */
 } lc_tuning;
 lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t);
 lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t);

@@ -62,7 +62,7 @@ class BatchOptions(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("traverse_block", C.c_int32), ("jacobi_block", C.c_int32), ("narrow_blocks_per_sm", C.c_int32),
-                ("solver_variant", C.c_int32), ("cluster_size", C.c_int32)]
+                ("solver_variant", C.c_int32), ("cluster_size", C.c_int32), ("contact_gather", C.c_int32)]
 
 
 class Profile(C.Structure):

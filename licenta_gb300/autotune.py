@@ -33,6 +33,7 @@ DEFAULT_SPACE = {
     "narrow_blocks_per_sm": (4, 8, 16),
     "solver_variant": (1, 2, 3),
     "cluster_size": (8, 16),
+    "contact_gather": (0, 1),
 }
 DEFAULT_CACHE = Path.home() / ".cache" / "licenta_gb300" / "autotune.json"
 
@@ -46,7 +47,7 @@ def get_tuning(batch) -> dict:
 def set_tuning(batch, cfg: dict) -> bool:
     """Applies cfg; False when the batch cannot take it (e.g. a solver
     variant that needs every cloth on chip)."""
-    t = _ffi.Tuning(**{k: int(cfg[k]) for k, _ in _ffi.Tuning._fields_})
+    t = _ffi.Tuning(**{k: int(cfg.get(k, 0)) for k, _ in _ffi.Tuning._fields_})
     rc = _ffi.lib().lc_batch_set_tuning(batch._h, C.byref(t))
     if rc == 0:
         return True
@@ -116,6 +117,12 @@ def autotune(batch, *, steps: int = 3, warmup: int = 1, space: dict | None = Non
             continue
         if cfg["solver_variant"] == 1:
             cfg["cluster_size"] = 0
+        # the contact mode only matters for the scatter solver
+        cfg.setdefault("contact_gather", 0)
+        if cfg["solver_variant"] != 3 and cfg["contact_gather"] != space.get("contact_gather", (0,))[0]:
+            continue
+        if cfg["solver_variant"] != 3:
+            cfg["contact_gather"] = 0
         if not set_tuning(batch, cfg):
             continue
         tried.append({"config": cfg, "ms_per_step": _time(batch, state, steps, warmup, stream)})

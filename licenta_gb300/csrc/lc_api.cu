@@ -51,6 +51,7 @@ struct ClusterArgs {
     const int *cl_cloth;
     const uint32_t *nvf;
     int chunk_cap;
+    int contact_gather;      // scatter solver: contacts gathered per owned vertex (no remote atomics)
 };
 cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, bool scatter, int nclusters,
                                  cudaStream_t st);
@@ -446,13 +447,14 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
     // per-vertex contact CSR feeds the gather solvers; the scatter solver
     // walks the cloth's contact ranges instead.
-    if (!(use_cluster && cluster_scatter) || d.friction_any) {  // friction sums per vertex too
+    const bool ordered = !(use_cluster && cluster_scatter) || d.friction_any;  // float sums in entry order
+    if (ordered || (use_cluster && cluster_scatter && ca.contact_gather)) {
         LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         launch_dyn(d, nvf, nee, narrow_grid, 0, st);
         scan_u32(d.dyn_cnt, d.dyn_off, nullptr, (uint32_t)d.Vtot, (uint32_t)d.Vtot, d.scan_tmp, nullptr, nullptr, st);
         launch_dyn(d, nvf, nee, narrow_grid, 1, st);
-        launch_dyn(d, nvf, nee, narrow_grid, 2, st);
+        if (ordered) launch_dyn(d, nvf, nee, narrow_grid, 2, st);
     }
     if (use_cluster) {
         LC_KEV(0);
@@ -1147,6 +1149,7 @@ lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t) {
     t->narrow_blocks_per_sm = b->narrow_grid / sm_count();
     t->solver_variant = b->use_cluster ? (b->cluster_scatter ? 3 : 2) : 1;
     t->cluster_size = b->use_cluster ? b->cluster_cs : 0;
+    t->contact_gather = b->ca.contact_gather;
     return LC_OK;
 }
 
@@ -1155,13 +1158,16 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     auto ok_block = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
     if (!ok_block(t->traverse_block) || !ok_block(t->jacobi_block) || t->narrow_blocks_per_sm < 1 ||
         t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3 ||
-        (t->cluster_size != 0 && t->cluster_size != 8 && t->cluster_size != 16))
+        (t->cluster_size != 0 && t->cluster_size != 8 && t->cluster_size != 16) ||
+        t->contact_gather < 0 || t->contact_gather > 1)
         return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: value out of range");
     if (b->opt.adjoint && t->solver_variant != 1)
         return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_tuning: an adjoint batch keeps solver variant 1");
     LC_CUDA(cudaDeviceSynchronize());
     b->traverse_block = t->traverse_block;
     b->jacobi_block = t->jacobi_block;
+    if (b->ca.contact_gather != t->contact_gather) b->invalidate_graph();
+    b->ca.contact_gather = t->contact_gather;
     b->narrow_grid = sm_count() * t->narrow_blocks_per_sm;
     const int prev = b->opt.solver_variant, prev_cs = b->want_cs;
     b->opt.solver_variant = t->solver_variant;

@@ -34,6 +34,7 @@ struct ClusterArgs {
     const int *cl_cloth;     // cluster -> cloth (largest first)
     const uint32_t *nvf;     // VF contacts this step (device count)
     int chunk_cap;
+    int contact_gather;      // scatter solver: contacts gathered per owned vertex (no remote atomics)
 };
 
 template <int CS>
@@ -423,7 +424,28 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
 #pragma unroll
             for (int j = 0; j < 3; ++j) add_corr(li[j], tri_bend_corr_pos(p[0], p[1], p[2], kp, h0, j), false);
         }
-        const uint32_t nv = cr.y - cr.x, ncont = nv + (cr.w - cr.z);
+        if (a.contact_gather) {
+            // Contacts by owned vertex: each entry of the per-vertex contact
+            // lists (one contact slot) is evaluated by the CTA that owns the
+            // slot's vertex, whose accumulators are then local; every
+            // contact is evaluated once per slot instead of once.
+            const uint32_t e0 = d.dyn_off[vo + lo], e1 = d.dyn_off[vo + lo + n_own];
+            for (uint32_t e = e0 + tid; e < e1; e += bs) {
+                const uint32_t ent = d.dyn_ent[e];
+                const uint32_t ci = ent >> 2;
+                const int slot = (int)(ent & 3u);
+                const bool isvf = ci < nvf_all;
+                const int4 v = isvf ? d.vf_v[ci] : d.ee_v[ci - nvf_all];
+                const float4 w = isvf ? d.vf_w[ci] : d.ee_w[ci - nvf_all];
+                const int li[4] = {v.x - vo, v.y - vo, v.z - vo, v.w - vo};
+                const float4 P[4] = {X(li[0]), X(li[1]), X(li[2]), X(li[3])};
+                const float3 corr = contact_corr_pos(P[0], P[1], P[2], P[3], w, isvf, h, slot);
+                const bool nz = !is_zero(corr);
+                if (nz) add_corr(li[slot], corr, true);
+                if (d.dbg_dyn_nz) d.dbg_dyn_nz[(size_t)it * d.dyn_cap + ent] = nz ? 1 : 0;
+            }
+        }
+        const uint32_t nv = cr.y - cr.x, ncont = a.contact_gather ? 0u : nv + (cr.w - cr.z);
         for (uint32_t k = r * bs + tid; k < ncont; k += CS * bs) {
             const bool isvf = k < nv;
             const uint32_t gi = isvf ? cr.x + k : cr.z + (k - nv);

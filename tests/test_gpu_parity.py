@@ -26,8 +26,13 @@ pytestmark = pytest.mark.gpu
 POS_TOL = 1e-5  # metres, on a 1 m cloth: the 1e-5 relative bound
 
 
-def run_parity(specs, steps, check_every=1, variant=0, friction=False):
+def run_parity(specs, steps, check_every=1, variant=0, friction=False, contact_gather=0):
     batch = ClothBatch(specs, debug_capture=True, solver_variant=variant)
+    if contact_gather:
+        from licenta_gb300 import autotune
+        cfg = autotune.get_tuning(batch)
+        cfg["contact_gather"] = contact_gather
+        assert autotune.set_tuning(batch, cfg)
     o32 = [Oracle([s], fp64=False) for s in specs]
     o64 = [Oracle([s], fp64=True) for s in specs]
     for o in o64:
@@ -59,9 +64,10 @@ def run_parity(specs, steps, check_every=1, variant=0, friction=False):
     return worst, contacts
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3], ids=["gather", "cluster", "scatter"])
-def test_small_cloth_parity_through_contacts(variant):
-    worst, contacts = run_parity([scenes.small_cloth(seed=0)], steps=60, variant=variant)
+@pytest.mark.parametrize("variant,gather", [(1, 0), (2, 0), (3, 0), (3, 1)],
+                         ids=["gather", "cluster", "scatter", "scatter-contact-gather"])
+def test_small_cloth_parity_through_contacts(variant, gather):
+    worst, contacts = run_parity([scenes.small_cloth(seed=0)], steps=60, variant=variant, contact_gather=gather)
     assert contacts > 0, "the run should reach self-contact"
 
 
