@@ -6,6 +6,8 @@
 // roundings of the reference kernels, so Morton codes, tree topology, pair
 // lists and contact lists are bit-exact against the FP32 oracle for the
 // same input positions.
+#include <cuda/atomic>
+
 #include "lc_internal.cuh"
 
 namespace lc {
@@ -295,9 +297,11 @@ __global__ void k_refit(DevPtrs d) {
             if (pid != 0) atomicOr(d.err, ERR_TREE);
             return;
         }
-        __threadfence();
-        if (atomicAdd(&d.visit[cd.i_off + pid], 1) == 0) return;
-        __threadfence();
+        // acq_rel at device scope: releases this thread's writes of the child
+        // it came from, and the second arrival acquires the first one's
+        // (the reference's arrival counter has no ordering at all)
+        cuda::atomic_ref<int, cuda::thread_scope_device> visit(d.visit[cd.i_off + pid]);
+        if (visit.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
         const int2 ch = __ldcg(&d.child[cd.i_off + pid]);
         const float4 lmn = __ldcg(&d.nmin[cd.n_off + ch.x]), lmx = __ldcg(&d.nmax[cd.n_off + ch.x]);
         const float4 rmn = __ldcg(&d.nmin[cd.n_off + ch.y]), rmx = __ldcg(&d.nmax[cd.n_off + ch.y]);
