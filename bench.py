@@ -240,8 +240,9 @@ def algorithmic_bytes(batch, specs, prof) -> dict:
         "solver": 16 * V + 16 * V + 48 * V + 16 * E + 20 * B + 32 * C,
         # leaf box + pair writes + count, every node record once
         "traverse": 32 * T + 4 * P + 4 * T + 48 * (2 * T - 1),
-        # pair read, counts + mask written, triangle records, per-vertex state once
-        "narrow": 18 * P + 20 * T + 48 * V,
+        # pair read, mask written (candidate counts per 32 pairs), triangle
+        # records, per-vertex state once
+        "narrow": 10 * P + 20 * T + 48 * V,
         "_sizes": dict(V=V, T=T, E=E, B=B, P=P, C=C),
     }
 

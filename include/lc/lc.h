@@ -118,7 +118,8 @@ typedef struct lc_batch_options {
                                  3 = cluster on-chip scatter with fixed-point accumulators */
     int32_t block_size;       /* block size of the global-memory Jacobi kernel (0 = default) */
     uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull, per kind (VF, EE);
-                                 default min(15 * pair capacity, max(32 * total triangles, 4 Mi)) */
+                                 default min(15 * pair capacity, max(32 * total triangles, 4 Mi)); at most
+                                 2^31 - 16 */
     int32_t adjoint;          /* 1: keep the tape lc_batch_adjoint_step needs (implies solver_variant 1) */
 } lc_batch_options;
 
@@ -217,7 +218,7 @@ typedef struct lc_profile {
                                  5 Perform Triangle Tests, 6 PBD Solver, 7 PBD Integration */
     float jacobi_ms;          /* one Jacobi iteration launch */
     float traverse_ms;        /* one traversal launch */
-    float narrow_ms;          /* one narrowphase filter launch (per-pair candidate counts) */
+    float narrow_ms;          /* one narrowphase filter launch (candidate masks, counts per group of pairs) */
     float sort_ms;            /* whole segmented sort */
     float step_ms;            /* sum of the phases */
     uint32_t kernels_per_step;
@@ -328,6 +329,18 @@ lc_status lc_batch_load_state(lc_batch *b, const void *src, void *stream);
  * accumulate dL/dk. */
 lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gx_prev, float *gv, float *gk_stretch,
                                 float *gk_bend, void *stream);
+
+/* lc_batch_adjoint_step for long rollouts whose gradient outgrows float
+ * (contact-rich drapes amplify it by up to ~1e14 per 20 steps).  After the
+ * reverse pass, every cloth c whose gx / gx_prev / gv has an entry above 2^60
+ * in magnitude has all five accumulators (its vertices' entries of gx,
+ * gx_prev, gv and its constraints' entries of gk_stretch, gk_bend) multiplied
+ * by 2^-60, and exponent[c] (device, one int32 per cloth, zeroed by the
+ * caller before the first step) is incremented; the true gradient is the
+ * stored value times 2^(60 * exponent[c]).  The reverse pass is linear in
+ * its seed, so the scaling is exact while values stay normal. */
+lc_status lc_batch_adjoint_step_rescaled(lc_batch *b, float *gx, float *gx_prev, float *gv, float *gk_stretch,
+                                         float *gk_bend, int32_t *exponent, void *stream);
 
 /* ----- standalone LBVH (the GenerateBVH2 / ComputeTreeAABBs /
  * GetAABBCollisions chain of Collision/CudaBVH.cu over caller triangles) --- */

@@ -97,6 +97,7 @@ SIGNATURES = {
     "lc_batch_save_state": (C.c_int, [VP, VP, VP]),
     "lc_batch_load_state": (C.c_int, [VP, VP, VP]),
     "lc_batch_adjoint_step": (C.c_int, [VP, VP, VP, VP, VP, VP, VP]),
+    "lc_batch_adjoint_step_rescaled": (C.c_int, [VP, VP, VP, VP, VP, VP, VP, VP]),
     "lc_batch_destroy": (C.c_int, [VP]),
     "lc_batch_step": (C.c_int, [VP, C.c_int32, VP]),
     "lc_batch_sync": (C.c_int, [VP]),

@@ -91,9 +91,17 @@ class DiffCloth:
         self.batch.read_state(None, out.data_ptr(), None, False, self._stream())
         return out
 
-    def adjoint_step(self, gx, gxp, gv, gks, gkb) -> None:
-        _ffi.check(_ffi.lib().lc_batch_adjoint_step(self.h, _p(gx), _p(gxp), _p(gv), _p(gks), _p(gkb),
-                                                    self._sp()), "lc_batch_adjoint_step")
+    def adjoint_step(self, gx, gxp, gv, gks, gkb, exponent: torch.Tensor | None = None) -> None:
+        """Reverse pass of one step; with exponent (int32, one per cloth) the
+        rescaled form: a cloth's accumulators are scaled by 2^-60 whenever
+        its state gradient passes 2^60, and exponent[c] counts the scalings."""
+        if exponent is None:
+            _ffi.check(_ffi.lib().lc_batch_adjoint_step(self.h, _p(gx), _p(gxp), _p(gv), _p(gks), _p(gkb),
+                                                        self._sp()), "lc_batch_adjoint_step")
+        else:
+            _ffi.check(_ffi.lib().lc_batch_adjoint_step_rescaled(self.h, _p(gx), _p(gxp), _p(gv), _p(gks), _p(gkb),
+                                                                 _p(exponent), self._sp()),
+                       "lc_batch_adjoint_step_rescaled")
 
     def close(self) -> None:
         self.batch.close()
@@ -133,7 +141,7 @@ class ClothRollout(torch.autograd.Function):
         counts = [cloth.batch.constraint_counts(c) for c in range(ncl)]
         ecl = torch.repeat_interleave(torch.arange(ncl, device="cuda"), torch.tensor([e for e, _ in counts], device="cuda"))
         bcl = torch.repeat_interleave(torch.arange(ncl, device="cuda"), torch.tensor([b for _, b in counts], device="cuda"))
-        exp60 = torch.zeros(ncl, dtype=torch.float32, device="cuda")
+        exp60 = torch.zeros(ncl, dtype=torch.int32, device="cuda")
         for seg in range(len(ctx.ckpts) - 1, -1, -1):
             first = seg * cloth.every
             last = min(steps, first + cloth.every)
@@ -146,29 +154,16 @@ class ClothRollout(torch.autograd.Function):
                 states.append(buf)
             for n in range(last - 1, first - 1, -1):
                 cloth.load(states[n - first])
-                cloth.adjoint_step(gx, gxp, gv, gks, gkb)
                 # Each cloth's reverse pass is linear in its seed: when a
-                # cloth's grows past 2^60 (contact-rich rollouts amplify it by
-                # up to ~1e14 per 20 steps) its accumulators are scaled by
-                # 2^-60, exactly, and its exponent kept on the device, so no
-                # intermediate product overflows in float; the results are
+                # cloth's state gradient passes 2^60 its accumulators are
+                # scaled by 2^-60 on the device and its exponent counted, so
+                # no intermediate product overflows in float; the results are
                 # rescaled once at the end (to inf where the true gradient is
                 # beyond float range).
-                m = torch.zeros(ncl, dtype=torch.float32, device="cuda")
-                rows = torch.maximum(torch.maximum(gx.abs().amax(1), gxp.abs().amax(1)), gv.abs().amax(1))
-                m.scatter_reduce_(0, vcl, rows, reduce="amax")
-                big = m > 2.0 ** 60
-                f = torch.where(big, torch.tensor(2.0 ** -60, device="cuda"), torch.tensor(1.0, device="cuda"))
-                fv = f[vcl].unsqueeze(1)
-                gx.mul_(fv)
-                gxp.mul_(fv)
-                gv.mul_(fv)
-                gks.mul_(f[ecl])
-                gkb.mul_(f[bcl])
-                exp60 += big.to(torch.float32)
+                cloth.adjoint_step(gx, gxp, gv, gks, gkb, exp60)
 
         def unscale(t, idx):
-            sc = torch.pow(torch.tensor(2.0 ** 60, device="cuda"), exp60)[idx]
+            sc = torch.pow(torch.tensor(2.0 ** 60, device="cuda"), exp60.to(torch.float32))[idx]
             if t.dim() == 2:
                 sc = sc.unsqueeze(1)
             return torch.where(t == 0, t, t * sc)

@@ -16,6 +16,11 @@ namespace lc {
 namespace {
 
 constexpr int kAdjFixedMax = 8;  // pinned vertices per cloth reduced in shared memory
+// The rescaled reverse pass: a cloth whose state gradients exceed 2^60 has all
+// its accumulators multiplied by 2^-60 (contact-rich rollouts amplify the
+// gradient by up to ~1e14 per 20 steps, and the float range ends near 2^128).
+constexpr float kRescaleAbove = 0x1p60f;
+constexpr float kRescaleBy = 0x1p-60f;
 
 // f(d) = (|d| - l0) d/|d| (stretch, LRA and contact corrections); its
 // Jacobian I - (l0/|d|)(I - n n^T) is symmetric, applied here to g.
@@ -349,14 +354,17 @@ __global__ void k_adj_damp1(DevPtrs d, AdjPtrs A, const float4 *a) {
     const ClothDev &cd = d.cloth[c];
     const double *t = d.damp + (size_t)c * 16;
     const int i = d.vblk_start[blockIdx.x] + threadIdx.x;
+    // the mass centre once per block: FP64 division is slow on this part
+    __shared__ float cm[3];
+    if (threadIdx.x < 3) cm[threadIdx.x] = (float)(t[1 + threadIdx.x] / t[0]);
+    __syncthreads();
     float s[6] = {0, 0, 0, 0, 0, 0};
     if (i < cd.v_off + cd.V) {
         const float3 ai = xyz(a[i]);
         A.gxp[i] = f4(add(xyz(A.gxp[i]), ai), 0.f);
         const float3 gvc = mul(ai, cd.dt);
         A.u[i] = f4(gvc, 0.f);
-        const double ms = t[0];
-        const float3 xcm = f3((float)(t[1] / ms), (float)(t[2] / ms), (float)(t[3] / ms));
+        const float3 xcm = f3(cm[0], cm[1], cm[2]);
         const float3 r = sub(xyz(A.tape_xin[i]), xcm);
         const float3 cr = cross(r, gvc);
         s[0] = gvc.x; s[1] = gvc.y; s[2] = gvc.z;
@@ -442,23 +450,72 @@ __global__ void k_adj_damp2(DevPtrs d, AdjPtrs A) {
 }
 
 // float3-packed (3 floats per vertex) <-> float4 gradient buffers.
-__global__ void k_adj_unpack(const float *__restrict__ src, float4 *__restrict__ dst, int n) {
+// The caller's state gradients (3 packed floats per vertex) to and from the
+// float4 work copies, all three arrays in one launch.
+__global__ void k_adj_unpack(AdjPtrs A, const float *__restrict__ gx, const float *__restrict__ gxp,
+                             const float *__restrict__ gv, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f);
+    if (i >= n) return;
+    A.gx[i] = make_float4(gx[3 * i], gx[3 * i + 1], gx[3 * i + 2], 0.f);
+    A.gxp[i] = make_float4(gxp[3 * i], gxp[3 * i + 1], gxp[3 * i + 2], 0.f);
+    A.gv[i] = make_float4(gv[3 * i], gv[3 * i + 1], gv[3 * i + 2], 0.f);
 }
-__global__ void k_adj_pack(const float4 *__restrict__ src, float *__restrict__ dst, int n) {
+
+__device__ __forceinline__ float put3(float *dst, int i, float4 v) {
+    dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z;
+    return fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fabsf(v.z));
+}
+
+// flag (may be null): flag[c] = 1 when a state gradient of cloth c is above
+// kRescaleAbove in magnitude after the step.
+__global__ void k_adj_pack(DevPtrs d, AdjPtrs A, float *__restrict__ gx, float *__restrict__ gxp,
+                           float *__restrict__ gv, uint32_t *__restrict__ flag, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) { const float4 v = src[i]; dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z; }
+    if (i >= n) return;
+    const float m = fmaxf(fmaxf(put3(gx, i, A.gx[i]), put3(gxp, i, A.gxp[i])), put3(gv, i, A.gv[i]));
+    if (flag && m > kRescaleAbove) flag[d.vcloth[i]] = 1u;
+}
+
+// Scales every accumulator of a flagged cloth by kRescaleBy (a power of two,
+// so the product is exact while it stays normal), counts the scaling in
+// exponent[c] and clears the flags the next call sets.  Threads [0, V) take
+// vertices, [V, V+E) stretch and [V+E, V+E+B) bend constraints.
+__global__ void k_adj_rescale(DevPtrs d, float *__restrict__ gx, float *__restrict__ gxp, float *__restrict__ gv,
+                              float *__restrict__ gks, float *__restrict__ gkb, const uint32_t *__restrict__ flag,
+                              uint32_t *__restrict__ flag_next, int32_t *__restrict__ exponent, int E, int B) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int V = d.Vtot;
+    if (i < d.C) flag_next[i] = 0u;
+    if (i < V) {
+        const int c = d.vcloth[i];
+        if (!flag[c]) return;
+        if (i == d.cloth[c].v_off) exponent[c] += 1;
+        for (int k = 0; k < 3; ++k) {
+            gx[3 * i + k] *= kRescaleBy; gxp[3 * i + k] *= kRescaleBy; gv[3 * i + k] *= kRescaleBy;
+        }
+    } else if (i < (int64_t)V + E) {
+        const int e = (int)(i - V);
+        if (gks && flag[d.vcloth[d.s_ids[e].x]]) gks[e] *= kRescaleBy;
+    } else if (i < (int64_t)V + E + B) {
+        const int b = (int)(i - V - E);
+        if (gkb && flag[d.vcloth[d.b_ids[b].x]]) gkb[b] *= kRescaleBy;
+    }
 }
 
 // ---------------------------------------------------------------------------
 static inline int nb(int64_t n, int b = kThreads) { return (int)((n + b - 1) / b); }
 
-void launch_adj_unpack(const float *src, float4 *dst, int n, cudaStream_t st) {
-    if (n) k_adj_unpack<<<nb(n), kThreads, 0, st>>>(src, dst, n);
+void launch_adj_unpack(const AdjPtrs &A, const float *gx, const float *gxp, const float *gv, int n, cudaStream_t st) {
+    if (n) k_adj_unpack<<<nb(n), kThreads, 0, st>>>(A, gx, gxp, gv, n);
 }
-void launch_adj_pack(const float4 *src, float *dst, int n, cudaStream_t st) {
-    if (n) k_adj_pack<<<nb(n), kThreads, 0, st>>>(src, dst, n);
+void launch_adj_pack(const DevPtrs &d, const AdjPtrs &A, float *gx, float *gxp, float *gv, uint32_t *flag, int n,
+                     cudaStream_t st) {
+    if (n) k_adj_pack<<<nb(n), kThreads, 0, st>>>(d, A, gx, gxp, gv, flag, n);
+}
+void launch_adj_rescale(const DevPtrs &d, float *gx, float *gxp, float *gv, float *gks, float *gkb,
+                        const uint32_t *flag, uint32_t *flag_next, int32_t *exponent, int E, int B, cudaStream_t st) {
+    const int64_t n = (int64_t)d.Vtot + E + B;
+    if (n) k_adj_rescale<<<nb(n), kThreads, 0, st>>>(d, gx, gxp, gv, gks, gkb, flag, flag_next, exponent, E, B);
 }
 
 // The reverse sweep.  a, g: two float4 work buffers of Vtot entries.

@@ -32,8 +32,11 @@ void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv
                    int stage, cudaStream_t st);
 void launch_wind(const DevPtrs &d, cudaStream_t st);
 void launch_external(const DevPtrs &d, cudaStream_t st, float4 *save_x = nullptr, float4 *save_v = nullptr);
-void launch_adj_unpack(const float *src, float4 *dst, int n, cudaStream_t st);
-void launch_adj_pack(const float4 *src, float *dst, int n, cudaStream_t st);
+void launch_adj_unpack(const AdjPtrs &A, const float *gx, const float *gxp, const float *gv, int n, cudaStream_t st);
+void launch_adj_pack(const DevPtrs &d, const AdjPtrs &A, float *gx, float *gxp, float *gv, uint32_t *flag, int n,
+                     cudaStream_t st);
+void launch_adj_rescale(const DevPtrs &d, float *gx, float *gxp, float *gv, float *gks, float *gkb,
+                        const uint32_t *flag, uint32_t *flag_next, int32_t *exponent, int E, int B, cudaStream_t st);
 void launch_adjoint(const DevPtrs &d, const AdjPtrs &A, float4 *a, float4 *g, const uint32_t *nvf, const uint32_t *nee,
                     int grid, int nfixed, float *gk_stretch, float *gk_bend, cudaStream_t st);
 void launch_vertex_normals(const DevPtrs &d, cudaStream_t st);
@@ -349,6 +352,8 @@ struct lc_batch {
     AdjPtrs adj{};
     float4 *tape_x = nullptr, *tape_xin = nullptr, *tape_vb = nullptr;
     float4 *adj_a = nullptr, *adj_g = nullptr;
+    uint32_t *adj_flag = nullptr;  // 2 x C rescale flags, used alternately (lc_batch_adjoint_step_rescaled)
+    int adj_flip = 0;
     int nfixed = 0;
     // debug copies
     float4 *dbg_x = nullptr, *dbg_xp = nullptr, *dbg_v = nullptr;
@@ -429,18 +434,20 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     LC_PHASE(4);
     // 5. Perform Triangle Tests
     LC_KEV(4);
-    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 0, st);  // filter
+    launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 0, st);  // filter: masks + counts per group of pairs
     LC_KEV(5);
-    scan_u32(d.pair_vf_cnt, d.pair_vf_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand, nullptr, st);
-    scan_u32(d.pair_ee_cnt, d.pair_ee_off, npairs, 0, (uint32_t)d.pair_cap, d.scan_tmp, ncand_e, nullptr, st);
+    const uint32_t gcap = (uint32_t)(d.pair_cap / kPairGroup + 1);
+    scan_u32(d.grp_vf_cnt, d.grp_vf_off, d.ngroups, 0, gcap, d.scan_tmp, ncand, nullptr, st);
+    scan_u32(d.grp_ee_cnt, d.grp_ee_off, d.ngroups, 0, gcap, d.scan_tmp, ncand_e, nullptr, st);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 1, st);  // expand
     LC_KEV(8);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 2, st);  // VF CCD
     LC_KEV(9);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 5, st);  // EE CCD
     LC_KEV(10);
-    scan_u32(d.cand_vf, d.cand_vf_off, ncand, 0, (uint32_t)d.cand_cap, d.scan_tmp, nvf, &d.counters[1], st);
-    scan_u32(d.cand_ee, d.cand_ee_off, ncand_e, 0, (uint32_t)d.cand_cap, d.scan_tmp, nee, &d.counters[2], st);
+    const uint32_t hcap = (uint32_t)(d.cand_cap / 32 + 1);
+    scan_u32(d.hitg_cnt[0], d.hitg_off[0], d.hitg_n, 0, hcap, d.scan_tmp, nvf, &d.counters[1], st);
+    scan_u32(d.hitg_cnt[1], d.hitg_off[1], d.hitg_n + 1, 0, hcap, d.scan_tmp, nee, &d.counters[2], st);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 3, st);  // write contacts
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 4, st);  // per-cloth ranges
     LC_PHASE(5);
@@ -636,7 +643,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     }
     tile_first[n] = (int)stile_cloth.size();
     vb_first[n] = (int)vblk_cloth.size();
-    if (V > (1ll << 31) - 2 || T > (1ll << 31) - 2 || E + B >= (1ll << 29) || PC > 0xFFFFFFF0ll)
+    // pair slots below 2^31: the narrowphase loops stride 32-bit pair indices
+    if (V > (1ll << 31) - 2 || T > (1ll << 31) - 2 || E + B >= (1ll << 29) || PC > 0x7FFFFFFFll)
         return fail(LC_ERR_INVALID_ARG, "batch too large for 32-bit indices");
     b->sort_passes = b->hosts[0].p.mortonMode == LC_MORTON_K30 ? 4 : 8;
     for (int c = 0; c < n && opt.adjoint; ++c)
@@ -679,15 +687,23 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));
-    LC_TRY(A.alloc(d.pair_vf_cnt, PC, "pair_vf_cnt")); LC_TRY(A.alloc(d.pair_ee_cnt, PC, "pair_ee_cnt"));
-    LC_TRY(A.alloc(d.pair_vf_off, PC + 1, "pair_vf_off")); LC_TRY(A.alloc(d.pair_ee_off, PC + 1, "pair_ee_off"));
+    const int64_t GC = PC / kPairGroup + 1;  // groups of kPairGroup pairs
+    LC_TRY(A.alloc(d.grp_vf_cnt, GC, "grp_vf_cnt")); LC_TRY(A.alloc(d.grp_ee_cnt, GC, "grp_ee_cnt"));
+    LC_TRY(A.alloc(d.grp_vf_off, GC + 1, "grp_vf_off")); LC_TRY(A.alloc(d.grp_ee_off, GC + 1, "grp_ee_off"));
+    LC_TRY(A.alloc(d.ngroups, 1, "ngroups"));
+    LC_CUDA(cudaMemset(d.ngroups, 0, sizeof(uint32_t)));
     // at most 15 candidates per pair; by default room for 32 per triangle
     d.cand_cap = opt.cand_capacity ? opt.cand_capacity
                                    : std::min<uint64_t>(15 * (uint64_t)PC, std::max<uint64_t>(32 * (uint64_t)T, 1u << 22));
-    d.cand_cap = std::min<uint64_t>(d.cand_cap, 0xFFFFFFF0ull);
+    d.cand_cap = std::min<uint64_t>(d.cand_cap, 0x7FFFFFF0ull);  // strided 32-bit candidate loops stay below 2^32
     LC_TRY(A.alloc(d.cand, d.cand_cap, "vf candidates")); LC_TRY(A.alloc(d.cand_e, d.cand_cap, "ee candidates"));
-    LC_TRY(A.alloc(d.cand_vf, d.cand_cap, "cand_vf")); LC_TRY(A.alloc(d.cand_ee, d.cand_cap, "cand_ee"));
-    LC_TRY(A.alloc(d.cand_vf_off, d.cand_cap + 1, "cand_vf_off")); LC_TRY(A.alloc(d.cand_ee_off, d.cand_cap + 1, "cand_ee_off"));
+    const uint64_t HG = d.cand_cap / 32 + 1;  // groups of 32 candidates
+    for (int k = 0; k < 2; ++k) {
+        LC_TRY(A.alloc(d.hitg_mask[k], HG, "hit masks")); LC_TRY(A.alloc(d.hitg_cnt[k], HG, "hit counts"));
+        LC_TRY(A.alloc(d.hitg_off[k], HG + 1, "hit offsets"));
+    }
+    LC_TRY(A.alloc(d.hitg_n, 2, "hit groups"));
+    LC_CUDA(cudaMemset(d.hitg_n, 0, 2 * sizeof(uint32_t)));
     LC_TRY(A.alloc(d.crange, n, "contact ranges"));
     LC_TRY(A.alloc(d.vf_v, vf_cap, "vf_v")); LC_TRY(A.alloc(d.vf_w, vf_cap, "vf_w"));
     LC_TRY(A.alloc(d.ee_v, ee_cap, "ee_v")); LC_TRY(A.alloc(d.ee_w, ee_cap, "ee_w"));
@@ -829,6 +845,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
         LC_TRY(A.alloc(J.fixed, 3 * std::max<int64_t>(F, 1), "adj_fixed"));
         LC_CUDA(cudaMemset(J.fixed, 0, sizeof(float) * 3 * std::max<int64_t>(F, 1)));
         LC_TRY(A.alloc(J.red, 8 * (vblk_cloth.size() + (size_t)n), "adj_red"));
+        LC_TRY(A.alloc(b->adj_flag, 2 * (size_t)n, "adj_flag"));
+        LC_CUDA(cudaMemset(b->adj_flag, 0, sizeof(uint32_t) * 2 * (size_t)n));
         // static CSR entry of every (constraint, role): where a constraint's
         // reverse contribution to each of its vertices goes
         std::vector<int> sslot(std::max<int64_t>(2 * E, 1), 0), bslot(std::max<int64_t>(4 * B, 1), 0);
@@ -1394,11 +1412,12 @@ lc_status lc_batch_load_state(lc_batch *b, const void *src, void *stream) {
     return LC_OK;
 }
 
-// One step forward (recorded) and its reverse pass; see lc.h.
-lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, float *gk_stretch, float *gk_bend,
-                                void *stream) {
-    if (!b || !gx || !gxp || !gv) return fail(LC_ERR_INVALID_ARG, "lc_batch_adjoint_step: bad arguments");
-    if (!b->opt.adjoint) return fail(LC_ERR_INVALID_ARG, "lc_batch_adjoint_step: batch created without the adjoint option");
+// One step forward (recorded) and its reverse pass; exponent (may be null)
+// selects the rescaled form.  See lc.h.
+static lc_status adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, float *gk_stretch, float *gk_bend,
+                              int32_t *exponent, void *stream, const char *who) {
+    if (!b || !gx || !gxp || !gv) return fail(LC_ERR_INVALID_ARG, std::string(who) + ": bad arguments");
+    if (!b->opt.adjoint) return fail(LC_ERR_INVALID_ARG, std::string(who) + ": batch created without the adjoint option");
     cudaStream_t st = (cudaStream_t)stream;
     b->last_stream = st;
     b->recording = true;
@@ -1406,15 +1425,28 @@ lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, f
     b->recording = false;
     if (s != LC_OK) return s;
     const int V = b->d.Vtot;
-    launch_adj_unpack(gx, b->adj.gx, V, st);
-    launch_adj_unpack(gxp, b->adj.gxp, V, st);
-    launch_adj_unpack(gv, b->adj.gv, V, st);
+    uint32_t *flag = exponent ? b->adj_flag + (size_t)b->adj_flip * b->C : nullptr;
+    launch_adj_unpack(b->adj, gx, gxp, gv, V, st);
     launch_adjoint(b->d, b->adj, b->adj_a, b->adj_g, b->nvf, b->nee, b->narrow_grid, b->nfixed, gk_stretch, gk_bend, st);
-    launch_adj_pack(b->adj.gx, gx, V, st);
-    launch_adj_pack(b->adj.gxp, gxp, V, st);
-    launch_adj_pack(b->adj.gv, gv, V, st);
+    launch_adj_pack(b->d, b->adj, gx, gxp, gv, flag, V, st);
+    if (exponent) {
+        uint32_t *next = b->adj_flag + (size_t)(1 - b->adj_flip) * b->C;
+        launch_adj_rescale(b->d, gx, gxp, gv, gk_stretch, gk_bend, flag, next, exponent, b->adj.E, b->adj.B, st);
+        b->adj_flip = 1 - b->adj_flip;
+    }
     LC_CUDA(cudaGetLastError());
     return LC_OK;
+}
+
+lc_status lc_batch_adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, float *gk_stretch, float *gk_bend,
+                                void *stream) {
+    return adjoint_step(b, gx, gxp, gv, gk_stretch, gk_bend, nullptr, stream, "lc_batch_adjoint_step");
+}
+
+lc_status lc_batch_adjoint_step_rescaled(lc_batch *b, float *gx, float *gxp, float *gv, float *gk_stretch,
+                                         float *gk_bend, int32_t *exponent, void *stream) {
+    if (!exponent) return fail(LC_ERR_INVALID_ARG, "lc_batch_adjoint_step_rescaled: exponent is null");
+    return adjoint_step(b, gx, gxp, gv, gk_stretch, gk_bend, exponent, stream, "lc_batch_adjoint_step_rescaled");
 }
 
 lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]) {

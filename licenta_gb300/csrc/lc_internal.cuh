@@ -17,6 +17,7 @@ constexpr int kSortBuckets = 1 << kSortBits;
 constexpr int kSortTile = 2048;          // keys per sort tile (256 threads x 8)
 constexpr int kTraverseStack = 64;       // Collision/CudaBVH.cu:38
 constexpr int kScanBlocks = 1024;        // fixed grid of the device-count scans
+constexpr int kPairGroup = 32;           // consecutive pairs per narrowphase expansion warp (one per lane)
 
 // Device error word bits (latched, reported by lc_batch_sync).
 enum : uint32_t {
@@ -99,16 +100,19 @@ struct DevPtrs {
     uint2 *pairs;          // compacted (global slot i, global slot j)
     uint64_t pair_cap;
     uint16_t *pair_mask;   // per pair: bits 0..5 VF, 6..14 EE candidates past the AABB cull
-    uint32_t *pair_vf_cnt, *pair_ee_cnt;  // per pair: VF / EE candidate counts
-    uint32_t *pair_vf_off, *pair_ee_off;  // per pair: first candidate (exclusive scans), totals at [npairs]
+    uint32_t *grp_vf_cnt, *grp_ee_cnt;    // per group of 32 consecutive pairs: VF / EE candidate counts
+    uint32_t *grp_vf_off, *grp_ee_off;    // per group: first candidate (exclusive scans)
+    uint32_t *ngroups;                    // groups of the step (device)
     int4 *cand, *cand_e;                  // VF / EE candidates: their four vertex ids, in candidate order
     uint64_t cand_cap;                    // per list
-    uint32_t *cand_vf, *cand_ee;          // per candidate: CCD hit flags
+    uint32_t *hitg_mask[2];               // per group of 32 candidates (VF, EE): CCD hit bits
+    uint32_t *hitg_cnt[2];                // per group: hits
+    uint32_t *hitg_off[2];                // per group: first contact (exclusive scans), total at [groups]
+    uint32_t *hitg_n;                     // [2] groups of the step (device)
     uint32_t *hit_q[2];                   // VF / EE hits in any order: candidate index ...
     float4 *hit_w[2];                     // ... and contact weights (capacity vf_cap / ee_cap)
     float4 *hit_nrm;                      // VF hits: unit face normal at the hit (friction; may be null)
     uint32_t *hit_n;                      // [2] hit counts of the step
-    uint32_t *cand_vf_off, *cand_ee_off;  // per candidate: output slot (exclusive scans)
     uint4 *crange;         // per cloth: [vf0, vf1) and [ee0, ee1) contact ranges
     int4 *vf_v; float4 *vf_w;   // VF contacts (ids, weights)
     float4 *vf_n;               // VF contacts: face normal at the hit (friction; may be null)

@@ -150,54 +150,94 @@ __global__ void k_sort_offsets(DevPtrs d, const int *__restrict__ tile_first) {
     }
 }
 
-__global__ void k_sort_scatter(DevPtrs d, const unsigned long long *__restrict__ kin,
-                               const uint32_t *__restrict__ pin, unsigned long long *__restrict__ kout,
-                               uint32_t *__restrict__ pout, int shift) {
+// One tile per block, ranked without block-wide rounds: warp w takes the
+// tile's keys [256 w, 256 w + 256) in 8 steps of 32 and ranks each key among
+// the warp's earlier keys of its digit (warp-private counts, no block
+// barrier); one scan per digit over the warps then gives every key its slot
+// in the tile sorted by digit, stable because index order is (warp, step,
+// lane).  The sorted tile is staged in shared memory and written out with
+// consecutive threads on consecutive slots of each digit's run.
+__global__ void __launch_bounds__(kThreads) k_sort_scatter(DevPtrs d, const unsigned long long *__restrict__ kin,
+                                                           const uint32_t *__restrict__ pin,
+                                                           unsigned long long *__restrict__ kout,
+                                                           uint32_t *__restrict__ pout, int shift) {
     constexpr int W = kThreads / 32;
-    __shared__ uint32_t base[kSortBuckets];
-    __shared__ uint32_t wcnt[W][kSortBuckets];
+    constexpr int R = kSortTile / kThreads;  // keys per lane
+    static_assert(kThreads == kSortBuckets && kSortTile == W * 32 * R, "one thread per digit, 32 R keys per warp");
+    __shared__ uint32_t wcnt[W][kSortBuckets];  // per warp: keys of each digit (then: first tile slot)
+    __shared__ uint32_t lbase[kSortBuckets];    // first tile slot per digit
+    __shared__ uint32_t gbase[kSortBuckets];    // first global slot per digit (from k_sort_offsets)
+    __shared__ uint32_t wsum[W];
+    __shared__ unsigned long long skey[kSortTile];
+    __shared__ uint32_t spay[kSortTile];
     const int tile = blockIdx.x;
     const int c = d.stile_cloth[tile];
     const int start = d.stile_start[tile];
     const ClothDev &cd = d.cloth[c];
-    const int end = min(start + kSortTile, cd.t_off + cd.T);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    base[threadIdx.x] = d.shist[(size_t)tile * kSortBuckets + threadIdx.x];
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    for (int r = 0; r < kSortTile / kThreads; ++r) {
-        const int i = start + r * kThreads + threadIdx.x;
-        const bool valid = i < end;
-        unsigned long long key = 0;
-        uint32_t pl = 0;
-        uint32_t dig = kSortBuckets;  // sentinel for empty lanes
-        if (valid) {
-            key = kin[i];
-            pl = pin[i];
-            dig = (uint32_t)(key >> shift) & (kSortBuckets - 1);
-        }
-        for (int k = threadIdx.x; k < W * kSortBuckets; k += kThreads) (&wcnt[0][0])[k] = 0;
-        __syncthreads();
-        const uint32_t peers = __match_any_sync(0xffffffffu, dig);
-        const uint32_t rank = __popc(peers & lt_mask);
-        if (valid && rank == 0) wcnt[wid][dig] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t o = base[threadIdx.x];
+    const int n = min(kSortTile, cd.t_off + cd.T - start);
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    gbase[t] = d.shist[(size_t)tile * kSortBuckets + t];
 #pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const uint32_t t = wcnt[w][threadIdx.x];
-                wcnt[w][threadIdx.x] = o;
-                o += t;
-            }
-            base[threadIdx.x] = o;
+    for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
+    __syncthreads();
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    unsigned long long kr[R];
+    uint32_t pr[R], rk[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int li = wid * 32 * R + r * 32 + lane;
+        const bool valid = li < n;
+        kr[r] = valid ? kin[start + li] : 0ull;
+        pr[r] = valid ? pin[start + li] : 0u;
+        const uint32_t dig = valid ? (uint32_t)(kr[r] >> shift) & (kSortBuckets - 1) : kSortBuckets;
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig);
+        const uint32_t before = valid ? wcnt[wid][dig] : 0u;
+        rk[r] = before + __popc(peers & lt_mask);
+        __syncwarp();
+        if (valid && (peers & lt_mask) == 0) wcnt[wid][dig] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // thread t owns digit t: its tile total, then the exclusive scan of the
+    // totals over the digits (first slot of the digit) and over the warps
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) tot += wcnt[w][t];
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    uint32_t run = incl - tot;
+    for (int w = 0; w < wid; ++w) run += wsum[w];
+    lbase[t] = run;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const uint32_t v = wcnt[w][t];
+        wcnt[w][t] = run;
+        run += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int li = wid * 32 * R + r * 32 + lane;
+        if (li < n) {
+            const uint32_t dig = (uint32_t)(kr[r] >> shift) & (kSortBuckets - 1);
+            const uint32_t pos = wcnt[wid][dig] + rk[r];
+            skey[pos] = kr[r];
+            spay[pos] = pr[r];
         }
-        __syncthreads();
-        if (valid) {
-            const uint32_t pos = wcnt[wid][dig] + rank;
-            kout[pos] = key;
-            pout[pos] = pl;
-        }
-        __syncthreads();
+    }
+    __syncthreads();
+    for (int i = t; i < n; i += kThreads) {
+        const unsigned long long key = skey[i];
+        const uint32_t dig = (uint32_t)(key >> shift) & (kSortBuckets - 1);
+        const uint32_t g = gbase[dig] + (uint32_t)i - lbase[dig];
+        kout[g] = key;
+        pout[g] = spay[i];
     }
 }
 
@@ -281,8 +321,8 @@ __global__ void k_karras(DevPtrs d) {
 }
 
 // Bottom-up refit: Collision/CudaBVH.cu:128-149.  The second arrival at a
-// node unions its children; a fence orders the child writes before the
-// arrival counter, and the children are re-read from L2.
+// node unions its children; the arrival counter is an acq_rel atomic, which
+// orders the child writes before it, and the children are re-read from L2.
 __global__ void k_refit(DevPtrs d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.Ttot) return;
@@ -297,12 +337,16 @@ __global__ void k_refit(DevPtrs d) {
             if (pid != 0) atomicOr(d.err, ERR_TREE);
             return;
         }
+        // child ids and parent links come from k_karras (an earlier launch):
+        // they are read ahead of the counter, so their round trip overlaps
+        // the release below instead of following the acquire
+        const int2 ch = __ldg(&d.child[cd.i_off + pid]);
+        const int up = pid ? __ldg(&d.parent[cd.n_off + pid]) : 0;
         // acq_rel at device scope: releases this thread's writes of the child
         // it came from, and the second arrival acquires the first one's
         // (the reference's arrival counter has no ordering at all)
         cuda::atomic_ref<int, cuda::thread_scope_device> visit(d.visit[cd.i_off + pid]);
         if (visit.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
-        const int2 ch = __ldcg(&d.child[cd.i_off + pid]);
         const float4 lmn = __ldcg(&d.nmin[cd.n_off + ch.x]), lmx = __ldcg(&d.nmax[cd.n_off + ch.x]);
         const float4 rmn = __ldcg(&d.nmin[cd.n_off + ch.y]), rmx = __ldcg(&d.nmax[cd.n_off + ch.y]);
         d.nmin[cd.n_off + pid] = f4(vmin(xyz(lmn), xyz(rmn)), 0.f);
@@ -314,9 +358,31 @@ __global__ void k_refit(DevPtrs d) {
         else { const int2 q = __ldcg(&d.rml[cd.i_off + ch.y]); rr = max(q.x, q.y); }
         d.rml[cd.i_off + pid] = make_int2(rl, rr);
         if (pid == 0) return;
-        pid = __ldcg(&d.parent[cd.n_off + pid]);
+        pid = up;
     }
     atomicOr(d.err, ERR_TREE);
+}
+
+// Wide node records for the traversal: per internal node both children's
+// boxes, with the child ids and rightmost leaves in the w lanes, so that one
+// node visit is one contiguous 64-byte read instead of six dependent ones.
+// A separate pass after the refit, not part of it: a node the refit never
+// reaches (a run of >= 3 equal codes, see k_karras) still gets its record
+// from its children's boxes, as the per-node reads of the traversal see them.
+__global__ void k_pack_nodes(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const ClothDev &cd = d.cloth[d.tcloth[s]];
+    const int k = s - cd.t_off;
+    if (k >= cd.T - 1) return;
+    const int2 ch = d.child[cd.i_off + k], rm = d.rml[cd.i_off + k];
+    const float4 *nmin = d.nmin + cd.n_off, *nmax = d.nmax + cd.n_off;
+    const float4 a = nmin[ch.x], b = nmax[ch.x], c = nmin[ch.y], e = nmax[ch.y];
+    float4 *w = d.wnode + 4 * (size_t)(cd.i_off + k);
+    w[0] = make_float4(a.x, a.y, a.z, __int_as_float(ch.x));
+    w[1] = make_float4(b.x, b.y, b.z, __int_as_float(rm.x));
+    w[2] = make_float4(c.x, c.y, c.z, __int_as_float(ch.y));
+    w[3] = make_float4(e.x, e.y, e.z, __int_as_float(rm.y));
 }
 
 // Leaf-vs-tree traversal: Collision/CudaBVH.cu:23-113.  Pairs (i, j>i) in
@@ -370,74 +436,7 @@ __global__ void k_traverse(DevPtrs d) {
     if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
 }
 
-// Wide node records for the traversal: per internal node both children's
-// boxes, with the child ids and rightmost leaves in the w lanes, so that one
-// node visit is one contiguous 64-byte read instead of six dependent ones.
-__global__ void k_pack_nodes(DevPtrs d) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.Ttot) return;
-    const ClothDev &cd = d.cloth[d.tcloth[s]];
-    const int k = s - cd.t_off;
-    if (k >= cd.T - 1) return;
-    const int2 ch = d.child[cd.i_off + k], rm = d.rml[cd.i_off + k];
-    const float4 *nmin = d.nmin + cd.n_off, *nmax = d.nmax + cd.n_off;
-    const float4 a = nmin[ch.x], b = nmax[ch.x], c = nmin[ch.y], e = nmax[ch.y];
-    float4 *w = d.wnode + 4 * (size_t)(cd.i_off + k);
-    w[0] = make_float4(a.x, a.y, a.z, __int_as_float(ch.x));
-    w[1] = make_float4(b.x, b.y, b.z, __int_as_float(rm.x));
-    w[2] = make_float4(c.x, c.y, c.z, __int_as_float(ch.y));
-    w[3] = make_float4(e.x, e.y, e.z, __int_as_float(rm.y));
-}
 
-// k_traverse on the wide node records: the same tests in the same order.
-__global__ void k_traverse_wide(DevPtrs d) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.Ttot) return;
-    const int c = d.tcloth[s];
-    const ClothDev &cd = d.cloth[c];
-    const int id = s - cd.t_off;
-    const int In = cd.T - 1;
-    if (In <= 0) { d.pair_cnt[s] = 0; return; }
-    const int me = In + id;
-    const int chunk = cd.chunk;
-    uint32_t *out = d.pair_chunk + cd.pc_off + (int64_t)id * chunk;
-    const float4 *W = d.wnode + 4 * (size_t)cd.i_off;
-    const float3 amin = xyz(d.nmin[cd.n_off + me]), amax = xyz(d.nmax[cd.n_off + me]);
-    int stack[kTraverseStack];
-    stack[0] = -1;
-    int top = 1, node = 0, got = 0;
-    uint32_t dropped = 0;
-    const int guard_max = 4 * cd.T + 64;
-    for (int guard = 0; guard < guard_max; ++guard) {
-        const float4 *r = W + 4 * (size_t)node;
-        const float4 l0 = __ldg(r), l1 = __ldg(r + 1), r0 = __ldg(r + 2), r1 = __ldg(r + 3);
-        const int chx = __float_as_int(l0.w), rmx = __float_as_int(l1.w);
-        const int chy = __float_as_int(r0.w), rmy = __float_as_int(r1.w);
-        const bool ol = rmx > me && overlap(amin, amax, xyz(l0), xyz(l1));
-        const bool orr = rmy > me && overlap(amin, amax, xyz(r0), xyz(r1));
-        if (ol && chx >= In) {
-            if (got < chunk) out[got++] = (uint32_t)(chx - In);
-            else ++dropped;
-        }
-        if (orr && chy >= In) {
-            if (got < chunk) out[got++] = (uint32_t)(chy - In);
-            else ++dropped;
-        }
-        const bool tl = ol && chx < In, tr = orr && chy < In;
-        if (!tl && !tr) {
-            node = stack[--top];
-        } else {
-            node = tl ? chx : chy;
-            if (tl && tr) {
-                if (top >= kTraverseStack) { atomicOr(d.err, ERR_STACK); break; }
-                stack[top++] = chy;
-            }
-        }
-        if (top == 0) break;
-    }
-    d.pair_cnt[s] = (uint32_t)got;
-    if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
-}
 
 // The traversal as a packet: a left-first depth-first walk of a Karras tree
 // meets the leaves in increasing index order, so leaf i's result is the
@@ -449,11 +448,11 @@ __global__ void k_traverse_wide(DevPtrs d) {
 // Each lane keeps exactly the leaves it overlaps, in the walk's order, so
 // every chunk is the single-leaf traversal's.  A warp whose leaves span two
 // cloths walks each cloth's tree for its own lanes.
-constexpr int kPacketWarps = 32;  // stack slots for up to 1024 threads per block
 __global__ void k_traverse_packet(DevPtrs d) {
-    __shared__ int wstack[kPacketWarps][kTraverseStack];
+    extern __shared__ int wstack_all[];  // kTraverseStack slots per warp of the block (sized at launch)
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int *wstack = wstack_all + w * kTraverseStack;
     const int s = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 + lane;
     const bool valid = s < d.Ttot;
     int c = -1, me = 0, got = 0, chunk = 0;
@@ -485,7 +484,7 @@ __global__ void k_traverse_packet(DevPtrs d) {
         const int In = cd.T - 1;
         const float4 *W = d.wnode + 4 * (size_t)cd.i_off;
         int top = 1, node = 0;
-        if (lane == 0) wstack[w][0] = -1;
+        if (lane == 0) wstack[0] = -1;
         __syncwarp();
         const int guard_max = 4 * cd.T + 64;
         for (int guard = 0; guard < guard_max; ++guard) {
@@ -505,12 +504,12 @@ __global__ void k_traverse_packet(DevPtrs d) {
             }
             const bool tl = chx < In && __any_sync(full, ol), tr = chy < In && __any_sync(full, orr);
             if (!tl && !tr) {
-                node = wstack[w][--top];
+                node = wstack[--top];
             } else {
                 node = tl ? chx : chy;
                 if (tl && tr) {
                     if (top >= kTraverseStack) { overflow = true; break; }
-                    if (lane == 0) wstack[w][top] = chy;
+                    if (lane == 0) wstack[top] = chy;
                     ++top;
                 }
             }
@@ -523,6 +522,7 @@ __global__ void k_traverse_packet(DevPtrs d) {
     if (valid) d.pair_cnt[s] = (uint32_t)got;
     if (dropped) atomicAdd(&d.counters[3], (unsigned long long)dropped);
 }
+
 
 // Order-preserving compaction of the per-leaf chunks into the pair list:
 // each warp takes 32 consecutive leaves and copies them one leaf at a time
@@ -558,7 +558,6 @@ __global__ void k_pair_compact(DevPtrs d) {
         }
     }
 }
-
 // ---------------------------------------------------------------------------
 // Narrowphase.  Candidate slots of Collision/CudaCollisionDetection.cu:53-189,
 // feature AABB cull of Collision/CudaPrimitiveTests.cu:427-490, CCD of
@@ -713,8 +712,7 @@ __device__ __forceinline__ int4 candidate_ids(const int vid[6], int s) {
 // AABB cull (Collision/CudaPrimitiveTests.cu:240-248, 427-490).  The checks
 // commute, so the surviving set is the reference's; the six vertex boxes are
 // built once per pair.
-__device__ uint16_t pair_filter(const DevPtrs &d, uint32_t p) {
-    const uint2 pr = d.pairs[p];
+__device__ __forceinline__ uint16_t pair_filter(const DevPtrs &d, uint2 pr) {
     const int c = d.tcloth[pr.x];
     const float h = d.cloth[c].h;
     const int4 A = d.tri_slot[pr.x], B = d.tri_slot[pr.y];
@@ -772,14 +770,39 @@ __device__ uint16_t pair_filter(const DevPtrs &d, uint32_t p) {
     return (uint16_t)mask;
 }
 
-__global__ void k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) {
-    const uint32_t n = *npairs;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint16_t m = pair_filter(d, p);
-        d.pair_mask[p] = m;
-        d.pair_vf_cnt[p] = (uint32_t)__popc((unsigned)(m & 0x3Fu));
-        d.pair_ee_cnt[p] = (uint32_t)__popc((unsigned)(m >> 6));
+
+// Stage 1 for every pair, one thread per pair: its candidate mask, and per
+// group of kPairGroup consecutive pairs (one warp iteration: the stride is a
+// whole number of warps) the group's VF and EE candidate counts, whose scans
+// give every group its first candidate; the number of groups at ngroups.
+__global__ void __launch_bounds__(kThreads, 4) k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) {
+    static_assert(kPairGroup == 32, "a group is one warp iteration");
+    const uint32_t n = *npairs, G = (n + kPairGroup - 1) / kPairGroup;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d.ngroups = G;
+    const int lane = threadIdx.x & 31;
+    const uint32_t end = G * kPairGroup;  // whole warps stay in the loop together (pair counts stay below 2^31)
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < end; p += gridDim.x * blockDim.x) {
+        const uint16_t m = p < n ? pair_filter(d, d.pairs[p]) : (uint16_t)0;
+        if (p < n) d.pair_mask[p] = m;
+        const uint32_t vf = __reduce_add_sync(0xffffffffu, (unsigned)__popc((unsigned)(m & 0x3Fu)));
+        const uint32_t ee = __reduce_add_sync(0xffffffffu, (unsigned)__popc((unsigned)(m >> 6)));
+        if (lane == 0) { d.grp_vf_cnt[p / kPairGroup] = vf; d.grp_ee_cnt[p / kPairGroup] = ee; }
     }
+}
+
+// First VF (or EE) candidate of pair p <= npairs: its group's offset plus the
+// candidates of the pairs before it in the group; total when p starts a
+// group past the last.
+template <bool VF>
+__device__ __forceinline__ uint32_t pair_cand_off(const DevPtrs &d, uint32_t p, uint32_t total) {
+    const uint32_t g = p / kPairGroup;
+    if (g >= *d.ngroups) return total;
+    uint32_t o = VF ? d.grp_vf_off[g] : d.grp_ee_off[g];
+    for (uint32_t q = g * kPairGroup; q < p; ++q) {
+        const unsigned m = d.pair_mask[q];
+        o += (uint32_t)__popc(VF ? (m & 0x3Fu) : (m >> 6));
+    }
+    return o;
 }
 
 // Stage 2: the surviving candidates written in the reference's order (pair,
@@ -841,8 +864,8 @@ __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) 
             vid[0] = A.x; vid[1] = A.y; vid[2] = A.z; vid[3] = B.x; vid[4] = B.y; vid[5] = B.z;
         }
         if (!__any_sync(0xffffffffu, m != 0u)) continue;
-        expand_kind<true>(d, m & 0x3Fu, vid, d.pair_vf_off[base]);
-        expand_kind<false>(d, m >> 6, vid, d.pair_ee_off[base]);
+        expand_kind<true>(d, m & 0x3Fu, vid, d.grp_vf_off[base / kPairGroup]);
+        expand_kind<false>(d, m >> 6, vid, d.grp_ee_off[base / kPairGroup]);
     }
 }
 
@@ -871,7 +894,10 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
     __shared__ float roots[kCcdWarps][3][32];
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
     const int4 *list = VF ? d.cand : d.cand_e;
-    uint32_t *hitout = VF ? d.cand_vf : d.cand_ee;
+    // hit bits per group of 32 candidates (one warp iteration: base is a
+    // multiple of 32); the scan of their counts orders the contacts
+    uint32_t *hmask = d.hitg_mask[VF ? 0 : 1], *hcnt = d.hitg_cnt[VF ? 0 : 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.hitg_n[VF ? 0 : 1] = (n + 31) / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned full = 0xffffffffu;
     const uint32_t nwarps = gridDim.x * kCcdWarps;
@@ -953,6 +979,7 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
             roots[w][iv][own] = secant(x21, x31, x41, v21, v31, v41, jb.a, jb.b, jb.fa, jb.fb);
         }
         __syncwarp();
+        bool found = false;
         if (valid) {
             const ClothDev &cd = d.cloth[d.vcloth[ids.x]];
             const int i1 = VF ? ids.y : ids.x, i2 = VF ? ids.z : ids.y, i3 = VF ? ids.w : ids.z, i4 = VF ? ids.x : ids.w;
@@ -960,7 +987,6 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
             const float3 v1 = xyz(d.v[i1]), v2 = xyz(d.v[i2]), v3 = xyz(d.v[i3]), v4 = xyz(d.v[i4]);
             const float h = cd.h, dt = cd.dt;
             Wts wt;
-            bool found = false;
             auto hit = [&](float t) {
                 const float tt = t * dt;
                 x1 = add(x1, mul(v1, tt));
@@ -978,7 +1004,6 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
                     if (t != -15.f && hit(t)) { found = true; break; }
                 }
             }
-            hitout[q] = found ? 1u : 0u;
             if (found) {
                 // the contact's weights, placed at its final index by k_ccd_emit
                 const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
@@ -992,8 +1017,24 @@ __global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const ui
                 }
             }
         }
+        const unsigned hb = __ballot_sync(full, found);
+        if (lane == 0) {
+            hmask[base / 32] = hb;
+            hcnt[base / 32] = (uint32_t)__popc(hb);
+        }
         __syncwarp();
     }
+}
+
+// Contacts of the candidates before candidate q <= n (n the kind's
+// candidate count): its group's first contact plus the hits before it in
+// the group.
+template <bool VF>
+__device__ __forceinline__ uint32_t hit_index(const DevPtrs &d, uint32_t q) {
+    const int k = VF ? 0 : 1;
+    const uint32_t g = q / 32, r = q % 32;
+    if (g >= d.hitg_n[k]) return d.hitg_off[k][d.hitg_n[k]];
+    return d.hitg_off[k][g] + (uint32_t)__popc(d.hitg_mask[k][g] & ((1u << r) - 1u));
 }
 
 // Stage 4 after k_ccd_warp: every hit written at its index in candidate order
@@ -1002,11 +1043,10 @@ template <bool VF>
 __global__ void k_ccd_emit(DevPtrs d) {
     const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
     const uint32_t n = (uint32_t)min((uint64_t)d.hit_n[VF ? 0 : 1], cap);
-    const uint32_t *off = VF ? d.cand_vf_off : d.cand_ee_off;
     const int4 *list = VF ? d.cand : d.cand_e;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const uint32_t q = d.hit_q[VF ? 0 : 1][k];
-        const uint32_t o = off[q];
+        const uint32_t o = hit_index<VF>(d, q);
         if (o < cap) {
             if (VF) {
                 d.vf_v[o] = list[q];
@@ -1028,12 +1068,12 @@ __global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncv, co
     const ClothDev &cd = d.cloth[c];
     const uint32_t nv = (uint32_t)min((uint64_t)*ncv, d.cand_cap), ne = (uint32_t)min((uint64_t)*nce, d.cand_cap);
     const uint32_t p0 = d.pair_off[cd.t_off], p1 = d.pair_off[cd.t_off + cd.T];
-    const uint32_t v0 = min(d.pair_vf_off[p0], nv), v1 = min(d.pair_vf_off[p1], nv);
-    const uint32_t e0 = min(d.pair_ee_off[p0], ne), e1 = min(d.pair_ee_off[p1], ne);
-    d.crange[c] = make_uint4((uint32_t)min((uint64_t)d.cand_vf_off[v0], d.vf_cap),
-                             (uint32_t)min((uint64_t)d.cand_vf_off[v1], d.vf_cap),
-                             (uint32_t)min((uint64_t)d.cand_ee_off[e0], d.ee_cap),
-                             (uint32_t)min((uint64_t)d.cand_ee_off[e1], d.ee_cap));
+    const uint32_t v0 = min(pair_cand_off<true>(d, p0, nv), nv), v1 = min(pair_cand_off<true>(d, p1, nv), nv);
+    const uint32_t e0 = min(pair_cand_off<false>(d, p0, ne), ne), e1 = min(pair_cand_off<false>(d, p1, ne), ne);
+    d.crange[c] = make_uint4((uint32_t)min((uint64_t)hit_index<true>(d, v0), d.vf_cap),
+                             (uint32_t)min((uint64_t)hit_index<true>(d, v1), d.vf_cap),
+                             (uint32_t)min((uint64_t)hit_index<false>(d, e0), d.ee_cap),
+                             (uint32_t)min((uint64_t)hit_index<false>(d, e1), d.ee_cap));
 }
 
 // ---------------------------------------------------------------------------
@@ -1074,7 +1114,7 @@ void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
     if (!d.Ttot) return;
     if (d.wnode) {
         k_pack_nodes<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
-        k_traverse_packet<<<nblk(d.Ttot, block), block, 0, st>>>(d);
+        k_traverse_packet<<<nblk(d.Ttot, block), block, (size_t)(block / 32) * kTraverseStack * sizeof(int), st>>>(d);
     } else {
         k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
     }

@@ -114,10 +114,13 @@ __global__ void k_damp_moments(DevPtrs d) {
     const double *t = d.damp + (size_t)c * 16;
     const int i = d.vblk_start[blockIdx.x] + threadIdx.x;
     const bool valid = i < cd.v_off + cd.V;
+    // the mass centre once per block: FP64 division is slow on this part
+    __shared__ float cm[3];
+    if (threadIdx.x < 3) cm[threadIdx.x] = (float)(t[1 + threadIdx.x] / t[0]);
+    __syncthreads();
     float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (valid) {
-        const double ms = t[0];
-        const float3 xcm = f3((float)(t[1] / ms), (float)(t[2] / ms), (float)(t[3] / ms));
+        const float3 xcm = f3(cm[0], cm[1], cm[2]);
         const float m = d.xp[i].w;
         const float3 r = sub(xyz(d.x[i]), xcm);
         const float3 l = cross(r, mul(xyz(d.v[i]), m));

@@ -178,6 +178,31 @@ def adjoint_cloth(seed: int = 0, n: int = 64, stiffness: float = 0.9, wind=(0.0,
                      dict(workload="adjoint", n=n, steps=60))
 
 
+def equal_code_cloth(seed: int = 26, copies: int = 4, n: int = 10,
+                     offset=(0.0009218, 0.0, -0.0031407)) -> ClothSpec:
+    """A 10x10 grid 0.1 m wide around the world origin plus `copies`
+    near-coincident loose triangles (2e-8 m apart, shifted by `offset`) beside
+    its centre.  Their Morton codes are equal, and a run of >= 3 equal codes
+    makes two internal nodes of the Karras hierarchy claim one child, so the
+    refit never reaches some nodes, the root among them (their boxes stay
+    zero, where the reference's would stay stale).  World box and Morton
+    frame [-1, 1]^3, 10 iterations, stiffness 0.9."""
+    rng = np.random.default_rng(seed)
+    p = base_params(10, 0.9)
+    p.worldMin[:] = (-1.0, -1.0, -1.0)
+    p.worldMax[:] = (1.0, 1.0, 1.0)
+    p.mortonOrigin[:] = (-1.0, -1.0, -1.0)
+    p.mortonScale = 0.5
+    pos = grid_positions(n, rng, y=0.0, span=0.1, origin=(-0.05, -0.05))
+    tri = np.array([[0.002, 0.0005, 0.001], [0.004, 0.0005, 0.003], [0.001, 0.0005, 0.004]], np.float32)
+    extra = np.concatenate([tri + np.float32(2e-8 * k) for k in range(copies)]).astype(np.float32)
+    extra += np.asarray(offset, dtype=np.float32)
+    idx = np.concatenate([grid_indices(n), (pos.shape[0] + np.arange(3 * copies, dtype=np.uint32)).reshape(-1, 3)])
+    return ClothSpec(np.concatenate([pos, extra]).astype(np.float32), idx.astype(np.uint32),
+                     np.zeros(pos.shape[0] + 3 * copies, dtype=np.uint8), p,
+                     dict(workload="equal-codes", copies=copies))
+
+
 def random_triangle_boxes(count: int, seed: int = 0):
     """LBVH microbenchmark input: first vertex uniform in the unit cube, two
     edges of length U[1e-3, 5e-3] in uniformly random directions; returns the

@@ -152,3 +152,46 @@ def test_rescaled_reverse_pass_is_exact():
         assert torch.allclose(a, b_, rtol=1e-6, atol=float(b_.abs().max()) * 1e-9)
         assert torch.equal(g_s[k:], g_l[k:])  # second cloth: untouched
     assert torch.isfinite(large[0]).all()
+
+
+def test_rescaled_entry_matches_plain_entry():
+    """lc_batch_adjoint_step_rescaled against lc_batch_adjoint_step on the same
+    state and seeds: a cloth whose state gradient passes 2^60 comes back
+    scaled by exactly 2^-60 with its exponent counted, the other comes back
+    bit-identical with exponent 0.  The calls alternate two flag buffers, so
+    the sequence (plain, large, plain, plain) checks that a raised flag is
+    cleared before either buffer is used again."""
+    specs = [scenes.small_cloth(seed=31, n=12), scenes.small_cloth(seed=32, n=10)]
+    cloth = DiffCloth(specs, checkpoint_every=4)
+    x0 = torch.tensor(np.concatenate([s.positions for s in specs]), device="cuda")
+    cloth.set_stiffness(torch.full((cloth.E,), 0.9, device="cuda"), torch.full((cloth.B,), 0.9, device="cuda"))
+    cloth.set_initial(x0, torch.zeros_like(x0))
+    cloth.step(3)
+    state = cloth.new_state()
+    cloth.save(state)
+    n0, V = specs[0].num_vertices, cloth.V
+    ce, cb = cloth.batch.constraint_counts(0)
+    gen = torch.Generator(device="cuda")
+    for k, scale in enumerate((1.0, 2.0 ** 70, 1.0, 1.0)):
+        gen.manual_seed(5 + k)
+        seeds = [torch.randn((V, 3), device="cuda", generator=gen) for _ in range(3)]
+        for t in seeds:
+            t[:n0] *= scale
+        runs = []
+        for rescaled in (False, True):
+            g = [t.clone() for t in seeds] + [torch.zeros(cloth.E, device="cuda"), torch.zeros(cloth.B, device="cuda")]
+            exponent = torch.zeros(2, dtype=torch.int32, device="cuda")
+            cloth.load(state)
+            cloth.adjoint_step(*g, exponent if rescaled else None)
+            runs.append((g, exponent))
+        torch.cuda.synchronize()
+        (plain, _), (scaled, exponent) = runs
+        assert exponent.tolist() == ([1, 0] if scale > 1.0 else [0, 0])
+        f = 2.0 ** (60 * int(exponent[0]))
+        for a, b, n in zip(plain, scaled, (n0, n0, n0, ce, cb)):
+            want, got = a[:n], b[:n] * f
+            normal = want.abs() >= 2.0 ** -60  # normal after the 2^-60 scaling: exact
+            assert torch.equal(got[normal], want[normal])
+            assert float((got - want).abs().max()) <= 2.0 ** -80
+            assert torch.equal(a[n:], b[n:])
+    cloth.close()

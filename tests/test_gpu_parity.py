@@ -257,6 +257,34 @@ def test_standalone_lbvh_pairs_equal_brute_force(cuda):
     h.close()
 
 
+def test_malformed_hierarchy_reads_current_boxes():
+    """Runs of >= 3 equal Morton codes leave internal nodes, the root among
+    them, unreached by the refit (scenes.equal_code_cloth).  The traversal's
+    node records must then hold the boxes the reference's per-node reads see
+    in this step, not records left from an earlier step: the cloth steps twice
+    with its loose triangles spread apart (a well-formed hierarchy), then takes
+    the near-coincident state and one more step, checked bit-exact (codes,
+    hierarchy, boxes, pairs, contacts) against the oracle."""
+    bad = scenes.equal_code_cloth()
+    good = scenes.equal_code_cloth(offset=(0.0, 0.0, 0.0))
+    n0 = good.num_vertices - 12
+    good.positions[n0:] += np.repeat(np.arange(4, dtype=np.float32) * 0.01, 3)[:, None] * np.float32([1, 0, 0])
+    batch = ClothBatch([good], debug_capture=True)
+    batch.step(2)
+    batch.sync()
+    assert np.any(batch.debug(0, "NODE_AABB")[0] != 0), "the spread-out state builds a well-formed hierarchy"
+    vn = batch.get_state(0)["vn"]
+    batch.set_state(0, x=bad.positions, x_prev=bad.positions, v=np.zeros_like(bad.positions), vn=vn)
+    o32 = Oracle([bad], fp64=False)
+    pre = parity.capture_pre(batch, 0)
+    batch.step(1)
+    batch.sync()
+    parity.check_collision(batch, 0, o32, pre[0]["vn"], tag="malformed hierarchy")
+    assert np.all(batch.debug(0, "NODE_AABB")[0] == 0), "the root stays unreached in the near-coincident state"
+    o32.close()
+    batch.close()
+
+
 def test_body_interface_fixed_update_and_update():
     from licenta_gb300 import CudaDeformableBody
     s = scenes.small_cloth(seed=2, n=16)

@@ -181,3 +181,23 @@ def test_k30_mode_runs_and_sorts():
     o = stepped(s, 3)
     m = o.debug(0, "MORTON")
     assert m.max() < (1 << 30) and np.all(m[1:] >= m[:-1])
+
+
+def test_equal_code_scene_leaves_nodes_unreached():
+    """The scene of the malformed-hierarchy GPU test: runs of equal Morton
+    codes leave internal nodes, the root among them, unreached by the refit
+    (zero boxes, zero rightmost leaves), while the same mesh with its loose
+    triangles spread apart builds a well-formed hierarchy."""
+    bad = scenes.equal_code_cloth()
+    good = scenes.equal_code_cloth(offset=(0.0, 0.0, 0.0))
+    n0 = good.num_vertices - 12
+    good.positions[n0:] += np.repeat(np.arange(4, dtype=np.float32) * 0.01, 3)[:, None] * np.float32([1, 0, 0])
+    for spec, broken in ((bad, True), (good, False)):
+        o = Oracle([spec], fp64=False)
+        o.external(0)
+        o.collide(0)
+        T = o.T[0]
+        box, rml = o.debug(0, "NODE_AABB")[:T - 1], o.debug(0, "RML")
+        unreached = np.flatnonzero(np.all(box == 0, axis=1) & np.all(rml == 0, axis=1))
+        o.close()
+        assert (0 in unreached) == broken and (len(unreached) > 0) == broken
