@@ -504,8 +504,9 @@ def run_ours(args, world, rank, local):
         return float(t.item())
 
     specs = scenes.batched_cloths(seed=args.seed + rank, count=args.cloths)
-    # the workload as `lanes` concurrent batches of contiguous cloth ranges
-    batch = ClothBatchGroup(specs, lanes=args.lanes) if args.lanes > 1 else ClothBatch(specs)
+    # the workload as `lanes` concurrent batches: ranges of the cloths ordered
+    # by size, so each lane holds cloths of like size and is tuned on its own
+    batch = ClothBatchGroup(specs, lanes=args.lanes, order="size") if args.lanes > 1 else ClothBatch(specs)
     members = batch.batches if args.lanes > 1 else [batch]
     stream = torch.cuda.Stream()
     batch.step(args.warmup, stream)
@@ -640,6 +641,7 @@ def run_ours(args, world, rank, local):
                    "vertices_per_gpu": V, "triangles_per_gpu": T, "iterations": 10, "dt": 1.0 / 60.0,
                    "parallelism": f"shard-by-cloth x{world}",
                    "concurrent_batches": args.lanes,
+                   "lane_order": "cloths by vertex count, largest first" if args.lanes > 1 else None,
                    "l2": f"inputs larger than L2 (vertex state {state_mb:.0f} MB + constraints + pair buffers)"},
         "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "clocks": clk, "e2e": e2e,
         "gpu_launches": int(prof["kernels_per_step"]) * args.steps,

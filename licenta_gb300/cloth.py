@@ -202,17 +202,34 @@ class ClothBatch:
 class ClothBatchGroup:
     """One workload stepped as several concurrent batches (lc_group_*).
 
-    The cloths are cut into ``lanes`` contiguous ranges of about equal vertex
-    count; each range is its own ClothBatch and the group steps them on
+    The group's cloths are cut into ``lanes`` contiguous ranges of about equal
+    vertex count; each range is its own ClothBatch and the group steps them on
     streams of its own, so one batch's latency-bound kernels overlap with the
     others'.  Whole-state copies take the same packed arrays as ClothBatch
-    (cloth order), each lane reading or writing its slice.
+    (group order), each lane reading or writing its slice.
+
+    ``order="given"`` keeps the caller's cloth order.  ``order="size"`` orders
+    the cloths by vertex count, largest first, so each lane holds cloths of
+    like size and can take its own launch shapes (the small cloths' lane
+    picks smaller solver clusters); group cloth c is then specs[order[c]],
+    and every per-cloth call and packed array of the group is in that order.
     """
 
-    def __init__(self, specs: Sequence[ClothSpec], lanes: int = 2, **kw):
+    @staticmethod
+    def group_order(specs: Sequence[ClothSpec], order: str = "given") -> list[int]:
+        """Indices into specs, in the group's cloth order."""
+        if order == "given":
+            return list(range(len(specs)))
+        if order == "size":
+            return sorted(range(len(specs)), key=lambda i: (-specs[i].num_vertices, i))
+        raise ValueError("order must be 'given' or 'size'")
+
+    def __init__(self, specs: Sequence[ClothSpec], lanes: int = 2, order: str = "given", **kw):
         specs = list(specs)
         if lanes < 1 or lanes > len(specs):
             raise ValueError("lanes must lie in 1..number of cloths")
+        self.order = self.group_order(specs, order)
+        specs = [specs[i] for i in self.order]
         cum = np.cumsum([s.num_vertices for s in specs])
         cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / lanes)) + 1 for k in range(1, lanes)] + [len(specs)]
         cuts = sorted(set(min(max(c, 1), len(specs)) for c in cuts[1:-1]) | {0, len(specs)})

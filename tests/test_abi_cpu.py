@@ -112,3 +112,20 @@ def test_morton_encoder_matches_oracle(mode):
         assert L.lc_morton3d(0.5, 0.0, 0.0, mode) == 1 << 62
     else:
         assert L.lc_morton3d(1.0, 1.0, 1.0, mode) == (1 << 30) - 1
+
+
+def test_group_orders():
+    """ClothBatchGroup's cloth orders: the caller's, or by vertex count
+    (largest first, ties in the caller's order), always a permutation."""
+    from licenta_gb300 import ClothBatchGroup
+    specs = scenes.batched_cloths(seed=3, count=12, n_min=8, n_max=20)
+    assert ClothBatchGroup.group_order(specs) == list(range(12))
+    o = ClothBatchGroup.group_order(specs, "size")
+    assert sorted(o) == list(range(12))
+    v = [specs[i].num_vertices for i in o]
+    assert v == sorted(v, reverse=True)
+    for a, b in zip(o, o[1:]):
+        if specs[a].num_vertices == specs[b].num_vertices:
+            assert a < b
+    with pytest.raises(ValueError):
+        ClothBatchGroup.group_order(specs, "random")

@@ -44,3 +44,34 @@ def test_group_matches_single_batch(cuda):
     finally:
         grp.close()
         one.close()
+
+
+def test_size_ordered_group_matches_single_batch(cuda):
+    """order="size": the group holds the cloths largest first, its lanes are
+    ranges of that order (each tuned on its own), and group cloth c evolves
+    exactly as cloth order[c] of the caller's list stepped in one batch."""
+    torch = cuda
+    from licenta_gb300 import autotune
+    specs = scenes.batched_cloths(seed=8, count=10, n_min=10, n_max=44)
+    one = ClothBatch(specs)
+    grp = ClothBatchGroup(specs, lanes=2, order="size")
+    try:
+        assert sorted(grp.order) == list(range(len(specs)))
+        sizes = [specs[i].num_vertices for i in grp.order]
+        assert sizes == sorted(sizes, reverse=True)
+        # a smaller cluster on the small cloths' lane changes launch shapes only
+        cfg = autotune.get_tuning(grp.batches[1])
+        cfg["cluster_size"] = 8
+        assert autotune.set_tuning(grp.batches[1], cfg)
+        s = torch.cuda.Stream()
+        one.step(25, s)
+        grp.step(25, s)
+        one.sync()
+        grp.sync()
+        for c, i in enumerate(grp.order):
+            a, b = one.get_state(i), grp.get_state(c)
+            for k in ("x", "x_prev", "v"):
+                assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), (c, i, k)
+    finally:
+        grp.close()
+        one.close()
