@@ -523,7 +523,7 @@ def run_ours(args, world, rank, local):
                 tuned = autotune.autotune(m, steps=2, warmup=1, cache=None,
                                           space={"traverse_block": (64, 128, 256), "jacobi_block": (256,),
                                                  "narrow_blocks_per_sm": (8, 16), "solver_variant": (1, 3),
-                                                 "cluster_size": (8, 16), "contact_gather": (0,)})
+                                                 "cluster_size": (4, 8, 16), "contact_gather": (0,)})
                 tuning["config"].append(tuned["config"])
                 tuning["candidates"] += len(tuned["tried"])
 

@@ -202,7 +202,9 @@ lc_status lc_batch_write_vertex_records(lc_batch *b, void *dst, int64_t stride, 
 /* Whole-batch state in one call each way, packed in cloth order (3 floats
  * per vertex per array; NULL arrays are skipped).  Asynchronous on stream;
  * host memory should be pinned.  Used by callers that keep the cloth state on
- * the host between steps. */
+ * the host between steps.  A host array moves as one contiguous copy through
+ * a staging buffer of the batch, so copies of one batch must stay ordered on
+ * one stream at a time. */
 lc_status lc_batch_write_state(lc_batch *b, const float *x, const float *x_prev, const float *v,
                                int32_t is_host, void *stream);
 lc_status lc_batch_read_state(lc_batch *b, float *x, float *x_prev, float *v, int32_t is_host,
@@ -295,7 +297,7 @@ typedef struct lc_tuning {
     int32_t jacobi_block;          /* threads per block of the global-memory Jacobi kernel */
     int32_t narrow_blocks_per_sm;  /* grid of the narrowphase and contact kernels, in blocks per SM */
     int32_t solver_variant;        /* 1, 2 or 3 as lc_batch_options.solver_variant (2, 3 need every cloth on chip) */
-    int32_t cluster_size;          /* CTAs per cloth of the on-chip solvers: 8, 16, or 0 to pick */
+    int32_t cluster_size;          /* CTAs per cloth of the on-chip solvers: 4, 8, 16, or 0 to pick */
     int32_t contact_gather;        /* variant 3: 0 = each contact scatters its four corrections (atomics into
                                       the owners' shared memory), 1 = each owned vertex gathers its contact
                                       slots (local atomics only; every contact evaluated per slot) */

@@ -32,7 +32,7 @@ DEFAULT_SPACE = {
     "jacobi_block": (128, 256, 512),
     "narrow_blocks_per_sm": (4, 8, 16),
     "solver_variant": (1, 2, 3),
-    "cluster_size": (8, 16),
+    "cluster_size": (4, 8, 16),
     "contact_gather": (0, 1),
 }
 DEFAULT_CACHE = Path.home() / ".cache" / "licenta_gb300" / "autotune.json"

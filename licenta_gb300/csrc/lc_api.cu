@@ -47,6 +47,8 @@ void launch_jacobi(const DevPtrs &d, const float4 *xa, float4 *xb, int it, const
 void launch_integrate(const DevPtrs &d, const float4 *xs, cudaStream_t st);
 void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st);
 void launch_vertex_records(const DevPtrs &d, void *dst, int64_t stride, int pos_off, int nrm_off, cudaStream_t st);
+void launch_xyz_unpack(const float *src, float4 *dst, int n, cudaStream_t st);
+void launch_xyz_pack(const float4 *src, float *dst, int n, cudaStream_t st);
 void scan_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, uint32_t n_static, uint32_t n_cap,
               uint32_t *partial, uint32_t *total_out, unsigned long long *total_out64, cudaStream_t st);
 unsigned long long morton3_host(float x, float y, float z, int mode);
@@ -344,7 +346,7 @@ struct lc_batch {
     // cluster-resident solver (lc_cluster.cu)
     bool use_cluster = false;
     int cluster_cs = 8;
-    int want_cs = 0;  // 0: pick; 8 or 16: requested through lc_batch_set_tuning
+    int want_cs = 0;  // 0: pick; 4, 8 or 16: requested through lc_batch_set_tuning
     bool cluster_scatter = false;
     ClusterArgs ca{};
     // adjoint (lc_batch_adjoint_step): the tape of one recorded step
@@ -353,6 +355,7 @@ struct lc_batch {
     float4 *tape_x = nullptr, *tape_xin = nullptr, *tape_vb = nullptr;
     float4 *adj_a = nullptr, *adj_g = nullptr;
     uint32_t *adj_flag = nullptr;  // 2 x C rescale flags, used alternately (lc_batch_adjoint_step_rescaled)
+    float *io = nullptr;           // 3 floats per vertex: staging of host <-> device state copies
     int adj_flip = 0;
     int nfixed = 0;
     // debug copies
@@ -529,7 +532,7 @@ lc_status lc_batch::setup_cluster() {
     int cs = 0;
     if (ok) {
         long best = 0;
-        for (int cand : {8, 16}) {
+        for (int cand : {8, 16, 4}) {
             if (want_cs && cand != want_cs) continue;
             const int cap = (vmax + cand - 1) / cand;
             if (cap > dev_cap) continue;
@@ -687,6 +690,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));
+    LC_TRY(A.alloc(b->io, 3 * std::max<int64_t>(V, 1), "state staging"));
     const int64_t GC = PC / kPairGroup + 1;  // groups of kPairGroup pairs
     LC_TRY(A.alloc(d.grp_vf_cnt, GC, "grp_vf_cnt")); LC_TRY(A.alloc(d.grp_ee_cnt, GC, "grp_ee_cnt"));
     LC_TRY(A.alloc(d.grp_vf_off, GC + 1, "grp_vf_off")); LC_TRY(A.alloc(d.grp_ee_off, GC + 1, "grp_ee_off"));
@@ -1176,7 +1180,7 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     auto ok_block = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
     if (!ok_block(t->traverse_block) || !ok_block(t->jacobi_block) || t->narrow_blocks_per_sm < 1 ||
         t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3 ||
-        (t->cluster_size != 0 && t->cluster_size != 8 && t->cluster_size != 16) ||
+        (t->cluster_size != 0 && t->cluster_size != 4 && t->cluster_size != 8 && t->cluster_size != 16) ||
         t->contact_gather < 0 || t->contact_gather > 1)
         return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: value out of range");
     if (b->opt.adjoint && t->solver_variant != 1)
@@ -1210,16 +1214,31 @@ lc_status lc_batch_constraint_counts(const lc_batch *b, int32_t c, int32_t *ns, 
     return LC_OK;
 }
 
-static lc_status get3(const float4 *src, int n, float *dst, int is_host) {
+// Packed xyz (12 B per vertex) from / to n float4 state entries, on stream
+// st.  A host transfer is one contiguous copy through the batch's staging
+// buffer plus a (un)packing kernel: a strided copy of 12 of every 16 bytes
+// moves only a few GB/s through the copy engines.  The staging buffer is the
+// batch's own, so copies of one batch are ordered on one stream at a time.
+static lc_status take_xyz(lc_batch *b, float *dst, const float4 *src, int n, int is_host, cudaStream_t st) {
     if (!dst) return LC_OK;
-    LC_CUDA(cudaMemcpy2D(dst, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float), n,
-                         is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice));
+    launch_xyz_pack(src, is_host ? b->io : dst, n, st);
+    if (is_host) LC_CUDA(cudaMemcpyAsync(dst, b->io, 3 * sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, st));
     return LC_OK;
 }
-static lc_status set3(float4 *dst, int n, const float *src, int is_host) {
+static lc_status put_xyz(lc_batch *b, float4 *dst, const float *src, int n, int is_host, cudaStream_t st) {
     if (!src) return LC_OK;
-    LC_CUDA(cudaMemcpy2D(dst, sizeof(float4), src, 3 * sizeof(float), 3 * sizeof(float), n,
-                         is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice));
+    if (is_host) LC_CUDA(cudaMemcpyAsync(b->io, src, 3 * sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, st));
+    launch_xyz_unpack(is_host ? b->io : src, dst, n, st);
+    return LC_OK;
+}
+static lc_status get3(lc_batch *b, const float4 *src, int n, float *dst, int is_host) {
+    LC_TRY(take_xyz(b, dst, src, n, is_host, 0));
+    LC_CUDA(cudaStreamSynchronize(0));
+    return LC_OK;
+}
+static lc_status set3(lc_batch *b, float4 *dst, int n, const float *src, int is_host) {
+    LC_TRY(put_xyz(b, dst, src, n, is_host, 0));
+    LC_CUDA(cudaStreamSynchronize(0));
     return LC_OK;
 }
 
@@ -1227,10 +1246,10 @@ lc_status lc_batch_get_state(lc_batch *b, int32_t c, float *x, float *xp, float 
     if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
     LC_TRY(lc_batch_sync(b));
     const ClothDev &cd = b->cds[c];
-    LC_TRY(get3(b->d.x + cd.v_off, cd.V, x, is_host));
-    LC_TRY(get3(b->d.xp + cd.v_off, cd.V, xp, is_host));
-    LC_TRY(get3(b->d.v + cd.v_off, cd.V, v, is_host));
-    LC_TRY(get3(b->d.vn + cd.v_off, cd.V, vn, is_host));
+    LC_TRY(get3(b, b->d.x + cd.v_off, cd.V, x, is_host));
+    LC_TRY(get3(b, b->d.xp + cd.v_off, cd.V, xp, is_host));
+    LC_TRY(get3(b, b->d.v + cd.v_off, cd.V, v, is_host));
+    LC_TRY(get3(b, b->d.vn + cd.v_off, cd.V, vn, is_host));
     return LC_OK;
 }
 
@@ -1239,10 +1258,10 @@ lc_status lc_batch_set_state(lc_batch *b, int32_t c, const float *x, const float
     if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
     LC_CUDA(cudaDeviceSynchronize());
     const ClothDev &cd = b->cds[c];
-    LC_TRY(set3(b->d.x + cd.v_off, cd.V, x, is_host));
-    LC_TRY(set3(b->d.xp + cd.v_off, cd.V, xp, is_host));
-    LC_TRY(set3(b->d.v + cd.v_off, cd.V, v, is_host));
-    LC_TRY(set3(b->d.vn + cd.v_off, cd.V, vn, is_host));
+    LC_TRY(set3(b, b->d.x + cd.v_off, cd.V, x, is_host));
+    LC_TRY(set3(b, b->d.xp + cd.v_off, cd.V, xp, is_host));
+    LC_TRY(set3(b, b->d.v + cd.v_off, cd.V, v, is_host));
+    LC_TRY(set3(b, b->d.vn + cd.v_off, cd.V, vn, is_host));
     return LC_OK;
 }
 
@@ -1274,8 +1293,8 @@ lc_status lc_batch_set_triangle_order(lc_batch *b, int32_t c, const uint32_t *pe
 lc_status lc_batch_read_positions(lc_batch *b, float *dst, int32_t is_host, void *stream) {
     if (!b || !dst) return fail(LC_ERR_INVALID_ARG, "bad arguments");
     cudaStream_t st = (cudaStream_t)stream;
-    LC_CUDA(cudaMemcpy2DAsync(dst, 3 * sizeof(float), b->d.xp, sizeof(float4), 3 * sizeof(float), b->d.Vtot,
-                              is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    LC_TRY(take_xyz(b, dst, b->d.xp, b->d.Vtot, is_host, st));
+    LC_CUDA(cudaGetLastError());
     return LC_OK;
 }
 
@@ -1489,9 +1508,9 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, ui
                           what == LC_DBG_PERM_BEFORE;
     if (need_dbg && !b->opt.debug_capture) return fail(LC_ERR_INVALID_ARG, "batch created without debug_capture");
     switch (what) {
-        case LC_DBG_PRED_X: if (count) *count = cd.V; return get3(b->dbg_x + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
-        case LC_DBG_PRED_XPREV: if (count) *count = cd.V; return get3(b->dbg_xp + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
-        case LC_DBG_PRED_V: if (count) *count = cd.V; return get3(b->dbg_v + cd.v_off, std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PRED_X: if (count) *count = cd.V; return get3(b, b->dbg_x + cd.v_off, (int)std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PRED_XPREV: if (count) *count = cd.V; return get3(b, b->dbg_xp + cd.v_off, (int)std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
+        case LC_DBG_PRED_V: if (count) *count = cd.V; return get3(b, b->dbg_v + cd.v_off, (int)std::min<uint64_t>(cd.V, cap), (float *)dst, 1);
         case LC_DBG_PERM_BEFORE:
         case LC_DBG_PERM: {
             std::vector<uint32_t> t(cd.T);
@@ -1634,22 +1653,22 @@ lc_status lc_batch_write_state(lc_batch *b, const float *x, const float *xp, con
                                void *stream) {
     if (!b) return fail(LC_ERR_INVALID_ARG, "null batch");
     cudaStream_t st = (cudaStream_t)stream;
-    const cudaMemcpyKind k = is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     const int n = b->d.Vtot;
-    if (x) LC_CUDA(cudaMemcpy2DAsync(b->d.x, sizeof(float4), x, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
-    if (xp) LC_CUDA(cudaMemcpy2DAsync(b->d.xp, sizeof(float4), xp, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
-    if (v) LC_CUDA(cudaMemcpy2DAsync(b->d.v, sizeof(float4), v, 3 * sizeof(float), 3 * sizeof(float), n, k, st));
+    LC_TRY(put_xyz(b, b->d.x, x, n, is_host, st));
+    LC_TRY(put_xyz(b, b->d.xp, xp, n, is_host, st));
+    LC_TRY(put_xyz(b, b->d.v, v, n, is_host, st));
+    LC_CUDA(cudaGetLastError());
     return LC_OK;
 }
 
 lc_status lc_batch_read_state(lc_batch *b, float *x, float *xp, float *v, int32_t is_host, void *stream) {
     if (!b) return fail(LC_ERR_INVALID_ARG, "null batch");
     cudaStream_t st = (cudaStream_t)stream;
-    const cudaMemcpyKind k = is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     const int n = b->d.Vtot;
-    if (x) LC_CUDA(cudaMemcpy2DAsync(x, 3 * sizeof(float), b->d.x, sizeof(float4), 3 * sizeof(float), n, k, st));
-    if (xp) LC_CUDA(cudaMemcpy2DAsync(xp, 3 * sizeof(float), b->d.xp, sizeof(float4), 3 * sizeof(float), n, k, st));
-    if (v) LC_CUDA(cudaMemcpy2DAsync(v, 3 * sizeof(float), b->d.v, sizeof(float4), 3 * sizeof(float), n, k, st));
+    LC_TRY(take_xyz(b, x, b->d.x, n, is_host, st));
+    LC_TRY(take_xyz(b, xp, b->d.xp, n, is_host, st));
+    LC_TRY(take_xyz(b, v, b->d.v, n, is_host, st));
+    LC_CUDA(cudaGetLastError());
     return LC_OK;
 }
 

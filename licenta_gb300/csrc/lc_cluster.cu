@@ -571,6 +571,7 @@ static cudaError_t launch_cs(const DevPtrs &d, const ClusterArgs &a, int ncluste
 cudaError_t launch_solve_cluster(const DevPtrs &d, const ClusterArgs &a, int cs, bool scatter, int nclusters,
                                  cudaStream_t st) {
     if (cs == 16) return scatter ? launch_cs<16, true>(d, a, nclusters, st) : launch_cs<16, false>(d, a, nclusters, st);
+    if (cs == 4) return scatter ? launch_cs<4, true>(d, a, nclusters, st) : launch_cs<4, false>(d, a, nclusters, st);
     return scatter ? launch_cs<8, true>(d, a, nclusters, st) : launch_cs<8, false>(d, a, nclusters, st);
 }
 
@@ -595,6 +596,7 @@ static int max_active(int chunk_cap) {
 // How many clusters of cs CTAs the device can hold at once (0: unsupported).
 int cluster_max_active(int cs, int chunk_cap, bool scatter) {
     if (cs == 16) return scatter ? max_active<16, true>(chunk_cap) : max_active<16, false>(chunk_cap);
+    if (cs == 4) return scatter ? max_active<4, true>(chunk_cap) : max_active<4, false>(chunk_cap);
     return scatter ? max_active<8, true>(chunk_cap) : max_active<8, false>(chunk_cap);
 }
 

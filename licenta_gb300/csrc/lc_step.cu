@@ -556,6 +556,28 @@ void launch_vertex_records(const DevPtrs &d, void *dst, int64_t stride, int pos_
                                                             nrm_off);
 }
 
+// Packed xyz (12 B per vertex, the caller's layout) to and from the float4
+// state arrays; the w lane (mass or inverse mass) is left as it is.
+__global__ void k_xyz_unpack(const float *__restrict__ src, float4 *__restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 o = dst[i];
+    dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], o.w);
+}
+__global__ void k_xyz_pack(const float4 *__restrict__ src, float *__restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = src[i];
+    dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z;
+}
+
+void launch_xyz_unpack(const float *src, float4 *dst, int n, cudaStream_t st) {
+    if (n > 0) k_xyz_unpack<<<nblk(n), kThreads, 0, st>>>(src, dst, n);
+}
+void launch_xyz_pack(const float4 *src, float *dst, int n, cudaStream_t st) {
+    if (n > 0) k_xyz_pack<<<nblk(n), kThreads, 0, st>>>(src, dst, n);
+}
+
 void launch_friction(const DevPtrs &d, const uint32_t *nvf, cudaStream_t st) {
     if (d.Vtot) k_friction<<<nblk(d.Vtot), kThreads, 0, st>>>(d, nvf);
 }

@@ -216,7 +216,7 @@ def test_cluster_profile_reports_variant():
     b = ClothBatch(specs)
     b.step(2)
     p = b.profile(1)
-    assert p["solver_variant"] == 3 and p["cluster_size"] in (8, 16)
+    assert p["solver_variant"] == 3 and p["cluster_size"] in (4, 8, 16)
     assert p["kernels_per_step"] > 10 and p["step_ms"] > 0
     b.close()
 
