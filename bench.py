@@ -555,9 +555,12 @@ def run_ours(args, world, rank, local):
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(args.steps):
-        batch.write_state(*(h.data_ptr() for h in host), True, stream)
-        batch.step(1, stream)
-        batch.read_state(*(h.data_ptr() for h in host), True, stream)
+        if args.lanes > 1:  # each lane's copies and step on its own stream
+            batch.step_io(*(h.data_ptr() for h in host), *(h.data_ptr() for h in host), True, stream)
+        else:
+            batch.write_state(*(h.data_ptr() for h in host), True, stream)
+            batch.step(1, stream)
+            batch.read_state(*(h.data_ptr() for h in host), True, stream)
     f1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -565,7 +568,9 @@ def run_ours(args, world, rank, local):
     batch.sync()
     e2e = {"value": world * args.cloths * args.steps / (ms_e2e / 1000.0), "unit": UNIT,
            "h2d_bytes_per_step": 3 * 12 * V, "d2h_bytes_per_step": 3 * 12 * V,
-           "what": "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state"}
+           "what": ("lc_group_step_io: per lane, lc_batch_write_state (x, x_prev, v from pinned host) + "
+                    "lc_batch_step + lc_batch_read_state on the lane's stream" if args.lanes > 1 else
+                    "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state")}
 
     # ---- profile + roofline: steps sampled over the timed rollout ------------
     prof = combined_profile([sampled_profile(m, st, args.steps, stream) for m, st in zip(members, state0)])

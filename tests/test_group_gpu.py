@@ -75,3 +75,32 @@ def test_size_ordered_group_matches_single_batch(cuda):
     finally:
         grp.close()
         one.close()
+
+
+def test_step_io_matches_write_step_read(cuda):
+    """lc_group_step_io (each member's copies and step on its own stream) gives
+    the same states, bit for bit, as lc_batch_write_state + lc_group_step +
+    lc_batch_read_state on the caller's stream, step after step."""
+    torch = cuda
+    specs = scenes.batched_cloths(seed=9, count=8, n_min=12, n_max=36)
+    a = ClothBatchGroup(specs, lanes=2, order="size")
+    b = ClothBatchGroup(specs, lanes=2, order="size")
+    try:
+        s = torch.cuda.Stream()
+        V = sum(sp.num_vertices for sp in specs)
+        ha = [torch.empty((V, 3), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+        hb = [torch.empty((V, 3), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+        a.read_state(*(h.data_ptr() for h in ha), True, s)
+        b.read_state(*(h.data_ptr() for h in hb), True, s)
+        for _ in range(6):
+            a.write_state(*(h.data_ptr() for h in ha), True, s)
+            a.step(1, s)
+            a.read_state(*(h.data_ptr() for h in ha), True, s)
+            b.step_io(*(h.data_ptr() for h in hb), *(h.data_ptr() for h in hb), True, s)
+        torch.cuda.synchronize()
+        for x, y in zip(ha, hb):
+            assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+        assert a.counters()["pairs"] == b.counters()["pairs"]
+    finally:
+        a.close()
+        b.close()
