@@ -217,9 +217,9 @@ def combined_profile(profs: list) -> dict:
 
 
 def algorithmic_bytes(batch, specs, prof) -> dict:
-    """Compulsory DRAM bytes per launch of the hot kernels (the model is
-    written out in the design doc).  Pair and contact counts are the profile's
-    (averaged over its sampled steps)."""
+    """Compulsory DRAM bytes per launch of the hot kernels: each kernel's
+    per-unit bytes (below) times the units one launch processes.  Pair and
+    contact counts are the profile's (averaged over its sampled steps)."""
     V = sum(s.num_vertices for s in specs)
     T = sum(s.num_triangles for s in specs)
     E = B = 0

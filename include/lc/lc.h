@@ -302,7 +302,7 @@ lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]);
  * results; the solver variant sums the Jacobi corrections differently (all
  * variants stay within the FP64 tolerance). */
 typedef struct lc_tuning {
-    int32_t traverse_block;        /* threads per block of the BVH traversal (32..1024, multiple of 32) */
+    int32_t traverse_block;        /* threads per block of the BVH traversal (32..256, multiple of 32) */
     int32_t jacobi_block;          /* threads per block of the global-memory Jacobi kernel */
     int32_t narrow_blocks_per_sm;  /* grid of the narrowphase and contact kernels, in blocks per SM */
     int32_t solver_variant;        /* 1, 2 or 3 as lc_batch_options.solver_variant (2, 3 need every cloth on chip) */

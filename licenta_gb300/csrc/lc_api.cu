@@ -1206,7 +1206,8 @@ lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t) {
 lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     if (!b || !t) return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: bad arguments");
     auto ok_block = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
-    if (!ok_block(t->traverse_block) || !ok_block(t->jacobi_block) || t->narrow_blocks_per_sm < 1 ||
+    if (!ok_block(t->traverse_block) || t->traverse_block > kTraverseBlockMax || !ok_block(t->jacobi_block) ||
+        t->narrow_blocks_per_sm < 1 ||
         t->narrow_blocks_per_sm > 64 || t->solver_variant < 1 || t->solver_variant > 3 ||
         (t->cluster_size != 0 && t->cluster_size != 4 && t->cluster_size != 8 && t->cluster_size != 16) ||
         t->contact_gather < 0 || t->contact_gather > 1)

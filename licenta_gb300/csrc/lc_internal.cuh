@@ -16,6 +16,7 @@ constexpr int kSortBits = 8;
 constexpr int kSortBuckets = 1 << kSortBits;
 constexpr int kSortTile = 2048;          // keys per sort tile (256 threads x 8)
 constexpr int kTraverseStack = 64;       // Collision/CudaBVH.cu:38
+constexpr int kTraverseBlockMax = 256;   // largest traversal block (the packet kernel is bounded for 6 of them per SM)
 constexpr int kScanBlocks = 1024;        // fixed grid of the device-count scans
 constexpr int kPairGroup = 32;           // consecutive pairs per narrowphase expansion warp (one per lane)
 

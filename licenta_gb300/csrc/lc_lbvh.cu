@@ -448,7 +448,10 @@ __global__ void k_traverse(DevPtrs d) {
 // Each lane keeps exactly the leaves it overlaps, in the walk's order, so
 // every chunk is the single-leaf traversal's.  A warp whose leaves span two
 // cloths walks each cloth's tree for its own lanes.
-__global__ void k_traverse_packet(DevPtrs d) {
+// At most 40 registers (6 blocks of 256, or 12 of 128, per SM): the walk
+// waits on dependent node fetches, and 12 resident 4-warp blocks hide more of
+// that latency than the 10 that 41 registers allowed.
+__global__ void __launch_bounds__(kTraverseBlockMax, 6) k_traverse_packet(DevPtrs d) {
     extern __shared__ int wstack_all[];  // kTraverseStack slots per warp of the block (sized at launch)
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -886,8 +889,10 @@ __global__ void k_narrow_expand(DevPtrs d, const uint32_t *__restrict__ npairs) 
 constexpr int kCcdWarps = 8;
 struct CcdJob { float a, b, fa, fb; };
 
+// At most 64 registers, for 4 resident blocks per SM instead of 3 (a few
+// words spill to L1): measured 0.83 -> 0.80 ms per step for VF, EE unchanged.
 template <bool VF>
-__global__ void __launch_bounds__(kCcdWarps * 32) k_ccd_warp(DevPtrs d, const uint32_t *__restrict__ ncand) {
+__global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const uint32_t *__restrict__ ncand) {
     __shared__ float geom[kCcdWarps][18][33];     // x21 x31 x41 v21 v31 v41 per lane (padded)
     __shared__ CcdJob jobs[kCcdWarps][96];
     __shared__ uint8_t job_owner[kCcdWarps][96];  // lane << 2 | interval
