@@ -124,25 +124,45 @@ __global__ void k_sort_hist(DevPtrs d, const unsigned long long *__restrict__ ke
 }
 
 // One block per cloth: turns the per-tile digit counts into global scatter
-// offsets (digit-major, tile-minor within the cloth).
-__global__ void k_sort_offsets(DevPtrs d, const int *__restrict__ tile_first) {
+// offsets (digit-major, tile-minor within the cloth).  kOffsetsSplit threads
+// per digit each take a contiguous quarter of the cloth's tiles, with their
+// loads unrolled, so a cloth of hundreds of tiles (one segment of a million
+// keys) is not one serial chain of loads per digit.
+constexpr int kOffsetsSplit = 4;
+__global__ void __launch_bounds__(kSortBuckets * kOffsetsSplit) k_sort_offsets(DevPtrs d,
+                                                                               const int *__restrict__ tile_first) {
     const int c = blockIdx.x;
-    const int d0 = threadIdx.x;  // one thread per digit (blockDim == kSortBuckets)
+    const int d0 = threadIdx.x % kSortBuckets, q = threadIdx.x / kSortBuckets;
     const int t0 = tile_first[c], t1 = tile_first[c + 1];
-    uint32_t tot = 0;
-    for (int t = t0; t < t1; ++t) tot += d.shist[(size_t)t * kSortBuckets + d0];
-    // exclusive scan of the 256 digit totals
+    const int per = (t1 - t0 + kOffsetsSplit - 1) / kOffsetsSplit;
+    const int a = min(t1, t0 + q * per), e = min(t1, a + per);
+    uint32_t part = 0;
+#pragma unroll 8
+    for (int t = a; t < e; ++t) part += d.shist[(size_t)t * kSortBuckets + d0];
+    __shared__ uint32_t qs[kOffsetsSplit][kSortBuckets];
     __shared__ uint32_t s[kSortBuckets];
-    s[d0] = tot;
+    qs[q][d0] = part;
+    __syncthreads();
+    // digit totals, then their exclusive scan (threads of quarter 0)
+    uint32_t tot = 0;
+    if (q == 0) {
+#pragma unroll
+        for (int k = 0; k < kOffsetsSplit; ++k) tot += qs[k][d0];
+        s[d0] = tot;
+    }
     __syncthreads();
     for (int o = 1; o < kSortBuckets; o <<= 1) {
-        uint32_t v = d0 >= o ? s[d0 - o] : 0u;
+        const uint32_t v = (q == 0 && d0 >= o) ? s[d0 - o] : 0u;
         __syncthreads();
-        s[d0] += v;
+        if (q == 0) s[d0] += v;
         __syncthreads();
     }
-    uint32_t run = (uint32_t)d.cloth[c].t_off + s[d0] - tot;
-    for (int t = t0; t < t1; ++t) {
+    if (q == 0) s[d0] -= tot;  // exclusive
+    __syncthreads();
+    uint32_t run = (uint32_t)d.cloth[c].t_off + s[d0];
+    for (int k = 0; k < q; ++k) run += qs[k][d0];
+#pragma unroll 8
+    for (int t = a; t < e; ++t) {
         const size_t k = (size_t)t * kSortBuckets + d0;
         const uint32_t n = d.shist[k];
         d.shist[k] = run;
@@ -1102,7 +1122,7 @@ void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream
         const uint32_t *pin = even ? d.payload : d.payload_alt;
         uint32_t *pout = even ? d.payload_alt : d.payload;
         k_sort_hist<<<d.nstiles, kThreads, 0, st>>>(d, kin, p * kSortBits);
-        k_sort_offsets<<<d.C, kSortBuckets, 0, st>>>(d, tile_first);
+        k_sort_offsets<<<d.C, kSortBuckets * kOffsetsSplit, 0, st>>>(d, tile_first);
         k_sort_scatter<<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits);
     }
 }
