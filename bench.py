@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-lbvh", action="store_true")
+    ap.add_argument("--only-lbvh", action="store_true",
+                    help="run only the LBVH microbenchmark and print its line (for profiling it alone)")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--lanes", type=int, default=2,
@@ -554,10 +556,10 @@ def run_ours(args, world, rank, local):
     barrier()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
-    for _ in range(args.steps):
-        if args.lanes > 1:  # each lane's copies and step on its own stream
-            batch.step_io(*(h.data_ptr() for h in host), *(h.data_ptr() for h in host), True, stream)
-        else:
+    if args.lanes > 1:  # every step's copies and step on each lane's own stream
+        batch.step_io(*(h.data_ptr() for h in host), *(h.data_ptr() for h in host), True, stream, nsteps=args.steps)
+    else:
+        for _ in range(args.steps):
             batch.write_state(*(h.data_ptr() for h in host), True, stream)
             batch.step(1, stream)
             batch.read_state(*(h.data_ptr() for h in host), True, stream)
@@ -568,8 +570,8 @@ def run_ours(args, world, rank, local):
     batch.sync()
     e2e = {"value": world * args.cloths * args.steps / (ms_e2e / 1000.0), "unit": UNIT,
            "h2d_bytes_per_step": 3 * 12 * V, "d2h_bytes_per_step": 3 * 12 * V,
-           "what": ("lc_group_step_io: per lane, lc_batch_write_state (x, x_prev, v from pinned host) + "
-                    "lc_batch_step + lc_batch_read_state on the lane's stream" if args.lanes > 1 else
+           "what": ("lc_group_step_io: every step, per lane, lc_batch_write_state (x, x_prev, v from pinned "
+                    "host) + lc_batch_step + lc_batch_read_state on the lane's stream" if args.lanes > 1 else
                     "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state")}
 
     # ---- profile + roofline: steps sampled over the timed rollout ------------
@@ -676,6 +678,12 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.only_lbvh:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            print(json.dumps({"metric": "LBVH builds/s", **lbvh_timing(args.seed)}), flush=True)
         return
     run_ours(args, world, rank, local)
 

@@ -160,15 +160,17 @@ lc_status lc_group_create(lc_batch *const *batches, int32_t count, lc_group **ou
  * group's streams; stream waits for all of them.  lc_batch_sync of a member
  * then waits on stream. */
 lc_status lc_group_step(lc_group *g, int32_t nsteps, void *stream);
-/* One step of every batch with its state moved in and out, for callers that
- * keep the state on the host: on each batch's stream of the group, its slice
- * of x_in, x_prev_in, v_in (packed as lc_batch_write_state takes them, the
- * batches' cloths one after the other in group order) is written, the batch
- * steps once and its state is read into the same slice of the out arrays, so
- * one batch's copies overlap the others' steps.  NULL arrays are skipped; in
- * and out may be the same arrays.  stream waits for all of it. */
-lc_status lc_group_step_io(lc_group *g, const float *x_in, const float *x_prev_in, const float *v_in, float *x_out,
-                           float *x_prev_out, float *v_out, int32_t is_host, void *stream);
+/* nsteps steps of every batch with its state moved in and out at each step,
+ * for callers that keep the state on the host: on each batch's stream of the
+ * group, step after step, its slice of x_in, x_prev_in, v_in (packed as
+ * lc_batch_write_state takes them, the batches' cloths one after the other in
+ * group order) is written, the batch steps once and its state is read into
+ * the same slice of the out arrays.  The batches are joined only at the end,
+ * so one batch's copies overlap the others' steps.  NULL arrays are skipped;
+ * in and out may be the same arrays (each step then starts from the state the
+ * previous one read back).  stream waits for all of it. */
+lc_status lc_group_step_io(lc_group *g, int32_t nsteps, const float *x_in, const float *x_prev_in, const float *v_in,
+                           float *x_out, float *x_prev_out, float *v_out, int32_t is_host, void *stream);
 lc_status lc_group_destroy(lc_group *g);
 
 lc_status lc_batch_num_cloths(const lc_batch *b, int32_t *out);

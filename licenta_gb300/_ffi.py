@@ -92,7 +92,7 @@ SIGNATURES = {
     "lc_batch_write_vertex_records": (C.c_int, [VP, VP, C.c_int64, C.c_int32, C.c_int32, VP]),
     "lc_group_create": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
     "lc_group_step": (C.c_int, [VP, C.c_int32, VP]),
-    "lc_group_step_io": (C.c_int, [VP, VP, VP, VP, VP, VP, VP, C.c_int32, VP]),
+    "lc_group_step_io": (C.c_int, [VP, C.c_int32, VP, VP, VP, VP, VP, VP, C.c_int32, VP]),
     "lc_group_destroy": (C.c_int, [VP]),
     "lc_batch_state_size": (C.c_int, [VP, C.POINTER(C.c_uint64)]),
     "lc_batch_save_state": (C.c_int, [VP, VP, VP]),

@@ -265,13 +265,15 @@ class ClothBatchGroup:
     def step(self, nsteps: int = 1, stream=None) -> None:
         _ffi.check(_ffi.lib().lc_group_step(self._h, nsteps, _stream_handle(stream)), "lc_group_step")
 
-    def step_io(self, x_in, x_prev_in, v_in, x_out, x_prev_out, v_out, is_host: bool, stream=None) -> None:
-        """One step with the whole state moved in and out (pointers to packed
-        3-float arrays in group order, None to skip): each member batch copies
-        its slice in, steps and copies it out on its own stream, so one
-        batch's copies overlap the others' steps."""
+    def step_io(self, x_in, x_prev_in, v_in, x_out, x_prev_out, v_out, is_host: bool, stream=None,
+                nsteps: int = 1) -> None:
+        """nsteps steps, the whole state moved in and out at each (pointers to
+        packed 3-float arrays in group order, None to skip): each member batch
+        copies its slice in, steps and copies it out on its own stream, and
+        the members are joined only at the end, so one batch's copies overlap
+        the others' steps."""
         p = [None if a is None else C.c_void_p(a) for a in (x_in, x_prev_in, v_in, x_out, x_prev_out, v_out)]
-        _ffi.check(_ffi.lib().lc_group_step_io(self._h, *p, 1 if is_host else 0, _stream_handle(stream)),
+        _ffi.check(_ffi.lib().lc_group_step_io(self._h, nsteps, *p, 1 if is_host else 0, _stream_handle(stream)),
                    "lc_group_step_io")
 
     def sync(self) -> None:

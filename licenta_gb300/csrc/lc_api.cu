@@ -1130,24 +1130,26 @@ lc_status lc_group_step(lc_group *g, int32_t nsteps, void *stream) {
     return s;
 }
 
-lc_status lc_group_step_io(lc_group *g, const float *x_in, const float *xp_in, const float *v_in, float *x_out,
-                           float *xp_out, float *v_out, int32_t is_host, void *stream) {
-    if (!g) return fail(LC_ERR_INVALID_ARG, "lc_group_step_io: null group");
+lc_status lc_group_step_io(lc_group *g, int32_t nsteps, const float *x_in, const float *xp_in, const float *v_in,
+                           float *x_out, float *xp_out, float *v_out, int32_t is_host, void *stream) {
+    if (!g || nsteps < 0) return fail(LC_ERR_INVALID_ARG, "lc_group_step_io: bad arguments");
     cudaStream_t st = (cudaStream_t)stream;
     LC_CUDA(cudaEventRecord(g->fork, st));
     const size_t n = g->b.size();
-    size_t off = 0;  // floats before this batch's slice
+    for (size_t i = 0; i < n; ++i) LC_CUDA(cudaStreamWaitEvent(g->lane[i], g->fork, 0));
     lc_status s = LC_OK;
-    for (size_t i = 0; i < n && s == LC_OK; ++i) {
-        lc_batch *b = g->b[i];
-        cudaStream_t ls = g->lane[i];
-        LC_CUDA(cudaStreamWaitEvent(ls, g->fork, 0));
-        auto in = [&](const float *p) { return p ? p + off : nullptr; };
-        auto out = [&](float *p) { return p ? p + off : nullptr; };
-        s = lc_batch_write_state(b, in(x_in), in(xp_in), in(v_in), is_host, ls);
-        if (s == LC_OK) s = lc_batch_step(b, 1, ls);
-        if (s == LC_OK) s = lc_batch_read_state(b, out(x_out), out(xp_out), out(v_out), is_host, ls);
-        off += 3 * (size_t)b->d.Vtot;
+    for (int k = 0; k < nsteps && s == LC_OK; ++k) {
+        size_t off = 0;  // floats before this batch's slice
+        for (size_t i = 0; i < n && s == LC_OK; ++i) {
+            lc_batch *b = g->b[i];
+            cudaStream_t ls = g->lane[i];
+            auto in = [&](const float *p) { return p ? p + off : nullptr; };
+            auto out = [&](float *p) { return p ? p + off : nullptr; };
+            s = lc_batch_write_state(b, in(x_in), in(xp_in), in(v_in), is_host, ls);
+            if (s == LC_OK) s = lc_batch_step(b, 1, ls);
+            if (s == LC_OK) s = lc_batch_read_state(b, out(x_out), out(xp_out), out(v_out), is_host, ls);
+            off += 3 * (size_t)b->d.Vtot;
+        }
     }
     // join what was enqueued, also after a failure
     for (size_t i = 0; i < n; ++i) {

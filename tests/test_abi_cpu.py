@@ -70,7 +70,7 @@ def test_invalid_arguments_are_rejected_before_any_device_work():
     assert b"twice" in L.lc_last_error_string()
     assert L.lc_group_create(None, 1, C.byref(h)) == 1
     assert L.lc_group_step(None, 1, None) == 1
-    assert L.lc_group_step_io(None, None, None, None, None, None, None, 1, None) == 1
+    assert L.lc_group_step_io(None, 1, None, None, None, None, None, None, 1, None) == 1
     assert L.lc_batch_adjoint_step_rescaled(None, None, None, None, None, None, None, None) == 1
     assert b"exponent" in L.lc_last_error_string()
 

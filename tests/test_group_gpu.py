@@ -78,9 +78,10 @@ def test_size_ordered_group_matches_single_batch(cuda):
 
 
 def test_step_io_matches_write_step_read(cuda):
-    """lc_group_step_io (each member's copies and step on its own stream) gives
-    the same states, bit for bit, as lc_batch_write_state + lc_group_step +
-    lc_batch_read_state on the caller's stream, step after step."""
+    """lc_group_step_io (each member's copies and steps on its own stream,
+    joined at the end) gives the same states, bit for bit, as
+    lc_batch_write_state + lc_group_step + lc_batch_read_state on the caller's
+    stream, step after step: one call of one step, then one of five."""
     torch = cuda
     specs = scenes.batched_cloths(seed=9, count=8, n_min=12, n_max=36)
     a = ClothBatchGroup(specs, lanes=2, order="size")
@@ -96,7 +97,8 @@ def test_step_io_matches_write_step_read(cuda):
             a.write_state(*(h.data_ptr() for h in ha), True, s)
             a.step(1, s)
             a.read_state(*(h.data_ptr() for h in ha), True, s)
-            b.step_io(*(h.data_ptr() for h in hb), *(h.data_ptr() for h in hb), True, s)
+        b.step_io(*(h.data_ptr() for h in hb), *(h.data_ptr() for h in hb), True, s)
+        b.step_io(*(h.data_ptr() for h in hb), *(h.data_ptr() for h in hb), True, s, nsteps=5)
         torch.cuda.synchronize()
         for x, y in zip(ha, hb):
             assert torch.equal(x.view(torch.int32), y.view(torch.int32))
