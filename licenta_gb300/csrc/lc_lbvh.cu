@@ -65,7 +65,7 @@ __global__ void k_triangles(DevPtrs d) {
     const float3 a = xyz(d.x[t.x]), b = xyz(d.x[t.y]), cc = xyz(d.x[t.z]);
     const float3 pa = xyz(d.xp[t.x]), pb = xyz(d.xp[t.y]), pc = xyz(d.xp[t.z]);
     const float h = cd.h;
-    if (cd.wind_on) d.fn[orig] = f4(normalize(cross(sub(b, a), sub(cc, a))), 0.f);
+    d.fn[orig] = f4(normalize(cross(sub(b, a), sub(cc, a))), 0.f);
     const float3 mn = subc(min3(a, b, cc), h), mx = addc(max3(a, b, cc), h);
     const float3 pmn = subc(min3(pa, pb, pc), h), pmx = addc(max3(pa, pb, pc), h);
     const float3 smn = vmin(mn, pmn), smx = vmax(mx, pmx);

@@ -176,11 +176,11 @@ __global__ void k_damp_apply(DevPtrs d) {
 
 // UpdateVertexNormals (Physics/CudaDeformableUtils.cu:190-249) as a gather
 // over each vertex's triangles: the running sum is kept (not zeroed) and
-// renormalised, as in the reference.
+// renormalised, as in the reference, every step for every cloth (the wind
+// term reads them and the vertex records publish them).
 __global__ void k_vertex_normals(DevPtrs d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.Vtot) return;
-    if (!d.cloth[d.vcloth[i]].wind_on) return;
     float3 a = xyz(d.vn[i]);
     for (int k = d.vt_off[i]; k < d.vt_off[i + 1]; ++k) a = add(a, xyz(d.fn[d.vt_idx[k]]));
     d.vn[i] = f4(normalize(a), 0.f);

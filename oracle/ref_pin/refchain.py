@@ -74,6 +74,18 @@ KERNELS = {
     "final_update": "_FinalUpdate",
     # FixedUpdate's world clamp (Physics/CudaDeformableBody.cpp:616)
     "world_clamp": "_WorldConstraints",
+    # PBDStepExternal (Physics/CudaPBD.cu:610-630) with DampVelocities (:411-458)
+    "external_forces": "ApplyExternalForces",
+    "global_damp": "GlobalVelDamp",
+    "xm_vm": "ComputeXMVMs",
+    "ang_mom": "ComputeL",
+    "inertia": "ComputeIs",
+    "update_vels": "UpdateVels",
+    "euler": "ExplicitEuler",
+    # DeformableUtils::UpdateVertexNormals (Physics/CudaDeformableUtils.cu:190-249)
+    "create_vns": "CreateVNs",
+    "accumulate_vns": "AccumulateVNs",
+    "normalize_vns": "NormalizeVNs",
     # CudaPBD::ApplyFriction (Physics/CudaPBD.cu:770-833)
     "damp_rigid": "_DampVelRigid",
     "apply_friction": "_ApplyFriction",
@@ -176,6 +188,111 @@ class RefKernels:
         if blocks is None:
             blocks = (n_threads + THREADS - 1) // THREADS
         self.drv("cuLaunchKernel", self.fn[key], blocks, 1, 1, block, 1, 1, 0, stream, params, None)
+
+    # ------------------------------------------------------------------
+    def predict(self, x, x_prev, v, vn, masses, *, gravity, wind, dt: float, k_global: float,
+                k_damp: float) -> dict:
+        """CudaPBD::PBDStepExternal (Physics/CudaPBD.cu:610-630) with the
+        reference's own kernels: ApplyExternalForces, then DampVelocities
+        (:411-458: GlobalVelDamp, ComputeXMVMs, ComputeL, ComputeIs,
+        UpdateVels), then ExplicitEuler.
+
+        x, x_prev, v, vn: (V, 3) float32 state before the step (positions
+        after the previous step's world clamp, previous positions, velocities,
+        running vertex normals); masses: (V,) float32 (Physics/
+        CudaDeformableBody.cpp:80-82); wind: the current wind vector
+        m_crtWindDir of this step (after the host update of :613-619, which
+        the restatement draws from a seeded generator in place of
+        std::rand()).  Returns the predicted positions ``x`` and velocities
+        ``v`` and the damping's intermediate values.
+
+        The host work between the kernels restates DampVelocities' host code:
+        the six CubWrap::ReduceSum calls (Core/CubWrappers.cuh:55-75) are
+        float sums, taken here in float64 and rounded once to float32 (CUB
+        sums in another order; any order differs from this by at most about
+        V float roundings of the total), and glm::inverse of the float 3x3
+        inertia (Dependencies/glm/detail/type_mat3x3.inl:37-56, the cofactor
+        matrix over the determinant) with the matrix-vector product of glm's
+        column-major mat3 (the same file's operator*), in float32."""
+        torch = self.torch
+        f32 = np.float32
+        x = np.ascontiguousarray(x, f32)
+        V = x.shape[0]
+        arrs = [np.ascontiguousarray(a, f32).reshape(V, 3) for a in (x_prev, v, vn)]
+        m = np.ascontiguousarray(masses, f32).reshape(V)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        d_x, d_xp, d_v, d_vn, d_m = dev(x), dev(arrs[0]), dev(arrs[1]), dev(arrs[2]), dev(m)
+        aux1 = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        aux2 = torch.zeros_like(aux1)
+        n = C.c_int(V)
+        f3 = lambda a: Float3(*[float(f32(q)) for q in a])
+
+        def rsum(t):  # CubWrap::ReduceSum of float / float3 values
+            a = t.cpu().numpy().astype(np.float64)
+            return a.sum(axis=0).astype(f32)
+
+        self.launch("external_forces", V, n, d_v, d_vn, f3(gravity), f3(wind), C.c_float(dt))
+        self.launch("global_damp", V, n, d_v, C.c_float(k_global))
+        mass_sum = f32(rsum(d_m))
+        self.launch("xm_vm", V, n, d_x, d_v, d_m, aux1, aux2)
+        torch.cuda.synchronize()
+        xcm = (rsum(aux1) / mass_sum).astype(f32)
+        vcm = (rsum(aux2) / mass_sum).astype(f32)
+        self.launch("ang_mom", V, n, d_x, f3(xcm), aux2, aux1)
+        torch.cuda.synchronize()
+        L = rsum(aux1)
+        self.launch("inertia", V, n, d_x, f3(xcm), d_m, aux1, aux2)
+        torch.cuda.synchronize()
+        i1, i2 = rsum(aux1), rsum(aux2)
+        # glm::mat3 I(col0, col1, col2) of Physics/CudaPBD.cu:447-449
+        I = np.array([[i1[1] + i1[2], i2[0], i2[1]],
+                      [i2[0], i1[0] + i1[2], i2[2]],
+                      [i2[1], i2[2], i1[0] + i1[1]]], dtype=f32)  # I[col][row]
+        omega = _glm_mat3_mul(_glm_inverse3(I), L)
+        self.launch("update_vels", V, n, d_x, f3(omega), f3(xcm), f3(vcm), C.c_float(k_damp), d_v)
+        self.launch("euler", V, n, d_xp, d_v, d_x, C.c_float(dt))
+        torch.cuda.synchronize()
+        return dict(x=d_x.cpu().numpy(), v=d_v.cpu().numpy(), mass_sum=mass_sum, xcm=xcm, vcm=vcm, L=L,
+                    inertia=I, omega=omega)
+
+    def vertex_normals(self, x, x_prev, triangles, vn, thickness: float) -> np.ndarray:
+        """DeformableUtils::UpdateVertexNormals (Physics/CudaDeformableUtils.cu:
+        190-249) as FixedUpdate runs it (Physics/CudaDeformableBody.cpp:
+        562-567): _UpdateTrianglesContinuous writes each triangle's unit face
+        normal from the predicted positions x into the triangle array (still
+        in its pre-sort slot order), CreateVNs copies it to the triangle's
+        three vertices, AccumulateVNs adds them into the running normals vn
+        (never zeroed) with float atomicAdd and NormalizeVNs renormalises.
+        x, x_prev: (V, 3) float32; triangles: (T, 3) vertex ids in slot
+        order; vn: (V, 3) running normals before the step.  Returns the
+        running normals after it.  The atomic sums' order is the GPU's, so
+        results agree with an ordered sum up to float rounding."""
+        torch = self.torch
+        f32 = np.float32
+        x = np.ascontiguousarray(x, f32)
+        V = x.shape[0]
+        tris = np.ascontiguousarray(triangles, np.int64)
+        T = tris.shape[0]
+        if T < 1 or tris.min() < 0 or tris.max() >= V:
+            raise ValueError("triangle index out of range")
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        tri = np.zeros((T, 7), dtype=np.int32)
+        tri[:, :3] = tris
+        d_tri = dev(tri)
+        nodes = 2 * T - 1
+        mort = torch.zeros(T, dtype=torch.int64, device="cuda")
+        nmin = torch.zeros((nodes, 3), dtype=torch.float32, device="cuda")
+        nmax = torch.zeros_like(nmin)
+        self.launch("tri_update", T, C.c_int(T), dev(x), dev(np.ascontiguousarray(x_prev, f32)), d_tri, mort,
+                    nmin, nmax, C.c_float(thickness))
+        raw = torch.zeros((3 * T, 3), dtype=torch.float32, device="cuda")
+        raw_ids = torch.zeros(3 * T, dtype=torch.int32, device="cuda")
+        acc = dev(np.ascontiguousarray(vn, f32).reshape(V, 3))
+        self.launch("create_vns", T, C.c_int(T), d_tri, raw, raw_ids)
+        self.launch("accumulate_vns", 3 * T, C.c_int(3 * T), raw, raw_ids, acc)
+        self.launch("normalize_vns", V, C.c_int(V), acc)
+        torch.cuda.synchronize()
+        return acc.cpu().numpy()
 
     # ------------------------------------------------------------------
     def collide(self, x, x_prev, v, triangles, features, thickness: float, dt: float, chunk: int = 64,
@@ -518,6 +635,39 @@ class RefKernels:
         self.launch("final_friction", V, C.c_int(V), kf, acc, cnt, d_v)
         torch.cuda.synchronize()
         return d_v.cpu().numpy()
+
+
+def _glm_inverse3(m: np.ndarray) -> np.ndarray:
+    """glm::inverse of a float mat3 (Dependencies/glm/detail/type_mat3x3.inl
+    :37-56): the transposed cofactor matrix times the reciprocal of the
+    determinant, every operation rounded to float32.  m and the result are
+    indexed [column][row] as glm stores them."""
+    f = np.float32
+    m = np.asarray(m, f)
+    a = lambda c, r: f(m[c, r])
+    one_over_det = f(1) / (a(0, 0) * (a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2))
+                           - a(1, 0) * (a(0, 1) * a(2, 2) - a(2, 1) * a(0, 2))
+                           + a(2, 0) * (a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2)))
+    inv = np.empty((3, 3), f)
+    inv[0, 0] = +(a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)) * one_over_det
+    inv[1, 0] = -(a(1, 0) * a(2, 2) - a(2, 0) * a(1, 2)) * one_over_det
+    inv[2, 0] = +(a(1, 0) * a(2, 1) - a(2, 0) * a(1, 1)) * one_over_det
+    inv[0, 1] = -(a(0, 1) * a(2, 2) - a(2, 1) * a(0, 2)) * one_over_det
+    inv[1, 1] = +(a(0, 0) * a(2, 2) - a(2, 0) * a(0, 2)) * one_over_det
+    inv[2, 1] = -(a(0, 0) * a(2, 1) - a(2, 0) * a(0, 1)) * one_over_det
+    inv[0, 2] = +(a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2)) * one_over_det
+    inv[1, 2] = -(a(0, 0) * a(1, 2) - a(1, 0) * a(0, 2)) * one_over_det
+    inv[2, 2] = +(a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1)) * one_over_det
+    return inv
+
+
+def _glm_mat3_mul(m: np.ndarray, v) -> np.ndarray:
+    """glm's mat3 * vec3 for a column-major m[column][row]: row r of the
+    result is m[0][r] v.x + m[1][r] v.y + m[2][r] v.z, summed left to right
+    in float32."""
+    f = np.float32
+    v = np.asarray(v, f)
+    return np.array([f(m[0, r]) * v[0] + f(m[1, r]) * v[1] + f(m[2, r]) * v[2] for r in range(3)], f)
 
 
 def _check_tree(L, R, Pa, T) -> int:

@@ -7,14 +7,16 @@ has built oracle/_ref/ref_kernels.cubin from the reference checkout and
 
     python tests/golden/make_golden.py OUTDIR
 
-Each case steps a seeded cloth with the FP32 oracle to a chosen step, takes
-the state the collision stages see at the next step (predicted positions,
-previous positions, velocities, the triangle order before the Morton sort)
-and runs the reference's collision chain on it (oracle/ref_pin/refchain.py),
-then the reference's solver chain (PBDStepSolver, _FinalUpdate and the world
-clamp) on the same state with the contacts its collision chain found, and
-the reference's friction kernels (CudaPBD::ApplyFriction) on the solver's
-velocities.
+Each case steps a seeded cloth with the FP32 oracle to a chosen step and
+takes the state before the next step (positions, previous positions,
+velocities, running vertex normals, the triangle order before the Morton
+sort).  From that state the reference's own kernels run the whole step
+(oracle/ref_pin/refchain.py): the prediction (PBDStepExternal: external
+forces with gravity and wind, the rigid-mode damping, explicit Euler), the
+running vertex normals (UpdateVertexNormals), the collision chain on the
+predicted state, the solver chain (PBDStepSolver, _FinalUpdate and the world
+clamp) with the contacts its collision chain found, and the friction kernels
+(CudaPBD::ApplyFriction) on the solver's velocities.
 The inputs and the reference's outputs go to OUTDIR/<case>.npz; the tests
 hold the oracle (tests/test_golden_cpu.py) and the engine
 (tests/test_golden_gpu.py) to them bit for bit.  The script also prints how
@@ -47,17 +49,30 @@ def main(outdir: str) -> int:
         o = Oracle([spec], fp64=False)
         if case["steps"]:
             o.step(case["steps"], threads=1)
+        pre = {k: a.astype(np.float32) for k, a in o.get_state(0).items()}
+        pre_wind, pre_rng = o.wind(0)
         o.step_one(0)
-        x, xp, v = o.debug(0, "PRED_X"), o.debug(0, "PRED_XPREV"), o.debug(0, "PRED_V")
+        wind = o.wind(0)[0].astype(np.float32)  # this step's wind, after its update
         perm = o.debug(0, "PERM_BEFORE").astype(np.int64)
         feats = o.debug(0, "FEATURES")
         h = o.thickness(0)
-        dt = float(spec.params.timestep)
-        chunk = int(spec.params.BVHChunkSize)
+        p = spec.params
+        dt = float(p.timestep)
+        chunk = int(p.BVHChunkSize)
         tris = spec.indices.astype(np.int64)[perm]
+        # the reference's prediction from the pre-step state; its output is
+        # the collision stages' input below
+        pred = ref.predict(pre["x"], pre["x_prev"], pre["v"], pre["vn"], golden_cases.masses(spec),
+                           gravity=tuple(p.gravity), wind=tuple(wind), dt=dt, k_global=float(p.globalVelDamp),
+                           k_damp=float(p.kDamp))
+        x, xp, v = pred["x"], pre["x_prev"], pred["v"]
         data = dict(x=x, x_prev=xp, v=v, perm_before=perm.astype(np.int32), features=feats,
                     thickness=np.float32(h), dt=np.float32(dt), chunk=np.int32(chunk),
-                    meta=np.array(json.dumps(case)))
+                    meta=np.array(json.dumps(case)),
+                    pre_x=pre["x"], pre_x_prev=pre["x_prev"], pre_v=pre["v"], pre_vn=pre["vn"], wind=wind,
+                    pre_wind=pre_wind.astype(np.float32), pre_rng=np.uint64(pre_rng),
+                    ref_vn=ref.vertex_normals(x, xp, tris, pre["vn"], h),
+                    oracle_pred_x=o.debug(0, "PRED_X"), oracle_pred_v=o.debug(0, "PRED_V"))
         # As the reference runs: its refit may read a child before the
         # child's box is visible (kept as evidence, not compared).
         raw = ref.collide(x, xp, v, tris, feats[perm], h, dt, chunk)
@@ -81,6 +96,8 @@ def main(outdir: str) -> int:
         diffs = golden_cases.compare_oracle(spec, data)
         sdiff = golden_cases.compare_oracle_solver(spec, data)
         fdiff = golden_cases.compare_oracle_friction(spec, data)
+        pdiff = golden_cases.compare_oracle_prediction(spec, data)
+        print(f"{case['name']}: prediction vs oracle {pdiff}")
         print(f"{case['name']}: T={len(perm)} pairs={len(r['pairs'])} vf={len(r['vf'])} ee={len(r['ee'])} "
               f"ground={sol['ground_flags']} lra={sol['lra_flags']} solver vs FP32 oracle {sdiff} friction {fdiff} "
               f"nodes raced in the unseeded refit={raced} "

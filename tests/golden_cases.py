@@ -1,8 +1,11 @@
-"""Cases of the collision-stage golden vectors (tests/golden/*.npz) and the
-comparisons the tests make against them.
+"""Cases of the golden vectors (tests/golden/*.npz) and the comparisons the
+tests make against them.
 
-Each golden holds a collision-stage input state and what the reference's own
-kernels computed from it (tests/golden/make_golden.py).  The layouts follow
+Each golden holds a state before one step and what the reference's own
+kernels computed from it (tests/golden/make_golden.py): the prediction
+(predicted positions and velocities, which are also the collision stages'
+input), the running vertex normals, the collision stages, the solver and
+friction.  The layouts follow
 the reference: node arrays of 2T-1 entries with the leaves at T-1+slot
 (Collision/CudaBVH.cu:128-149), pairs as (leaf slot, leaf slot)
 (Collision/CudaBVH.cu:71,85), contacts as PrimitiveContact {v1..v4,
@@ -68,6 +71,52 @@ def load(path: Path) -> dict:
 
 def golden_files():
     return sorted(GOLDEN.glob("*.npz"))
+
+
+def masses(spec) -> np.ndarray:
+    """Per-vertex masses as the reference's body sets them
+    (Physics/CudaDeformableBody.cpp:52,80-82): objectMass over the vertex
+    count, 1000 for a pinned vertex."""
+    p = spec.params
+    m = np.full(spec.num_vertices, np.float32(p.objectMass) / np.float32(spec.num_vertices), np.float32)
+    m[np.asarray(spec.pinned) != 0] = np.float32(1000.0)
+    return m
+
+
+# Tolerances of the prediction comparisons: 1e-5 m on positions (the parity
+# bar), 1e-5 m / dt on velocities (a position difference over one timestep)
+# and 1e-5 on the unit running vertex normals, which the reference sums with
+# float atomics in the GPU's order.
+PRED_ATOL_X = 1e-5
+VN_ATOL = 1e-5
+
+
+def compare_oracle_prediction(spec, d: dict) -> dict:
+    """Largest differences between the oracle's prediction (PBDStepExternal:
+    external forces, damping, explicit Euler; FP32 and FP64) and the
+    reference kernels' from the same pre-step state, and between the
+    oracle's running vertex normals and the reference's on the reference's
+    predicted positions."""
+    from oracle.oracle_ffi import Oracle
+    out = {}
+    for fp64 in (False, True):
+        tag = "fp64" if fp64 else "fp32"
+        o = Oracle([spec], fp64=fp64)
+        try:
+            o.set_state(0, x=d["pre_x"], x_prev=d["pre_x_prev"], v=d["pre_v"], vn=d["pre_vn"])
+            o.set_wind(0, d["pre_wind"], int(d["pre_rng"]))
+            o.external(0)
+            st = o.get_state(0)
+            out[f"{tag}_dx"] = float(np.abs(st["x"] - d["x"]).max())
+            out[f"{tag}_dv"] = float(np.abs(st["v"] - d["v"]).max())
+            o.set_state(0, x=d["x"], x_prev=d["x_prev"], v=d["v"], vn=d["pre_vn"])
+            o.set_perm(0, d["perm_before"])
+            o.collide(0)
+            out[f"{tag}_dvn"] = float(np.abs(o.get_state(0)["vn"] - d["ref_vn"]).max())
+        finally:
+            o.close()
+    out["changed_dv"] = float(np.abs(d["v"] - d["pre_v"]).max())
+    return out
 
 
 def solver_inputs(spec, d: dict, oracle) -> dict:

@@ -87,3 +87,36 @@ def test_oracle_friction_matches_reference_kernels(path):
     r = golden_cases.compare_oracle_friction(spec, d)
     assert r["fp32_dv"] <= golden_cases.FRICTION_ATOL_V, r
     assert r["fp64_dv"] <= golden_cases.FRICTION_ATOL_V, r
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_oracle_prediction_matches_reference_kernels(path):
+    """PBDStepExternal (ApplyExternalForces with gravity and wind,
+    DampVelocities' global and rigid-mode damping, ExplicitEuler) and
+    UpdateVertexNormals: the oracle (FP32 and FP64) from the golden's
+    pre-step state against what the reference's kernels computed from it."""
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    r = golden_cases.compare_oracle_prediction(spec, d)
+    dt = float(d["dt"])
+    for tag in ("fp32", "fp64"):
+        assert r[f"{tag}_dx"] <= golden_cases.PRED_ATOL_X, r
+        assert r[f"{tag}_dv"] <= golden_cases.PRED_ATOL_X / dt, r
+        assert r[f"{tag}_dvn"] <= golden_cases.VN_ATOL, r
+    # the step did change the velocities (gravity alone adds 9.81 / 60 m/s)
+    assert r["changed_dv"] > 0.1, r
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_golden_prediction_is_the_collision_input(path):
+    """The collision stages' input of every golden is the reference's own
+    prediction: x = x_prev + dt v as ExplicitEuler rounds it (no fused
+    multiply-add), from the pre-step state with gravity and damping on."""
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    p = spec.params
+    assert p.kDamp > 0 and p.globalVelDamp > 0 and p.gravity[1] < 0
+    dt = np.float32(d["dt"])
+    want = (d["x_prev"] + (dt * d["v"]).astype(np.float32)).astype(np.float32)
+    assert np.array_equal(want.view(np.uint32), d["x"].view(np.uint32))
+    assert np.array_equal(d["x_prev"], d["pre_x_prev"])

@@ -1,7 +1,16 @@
 """The CUDA engine against the reference's own kernels (tests/golden/*.npz).
 
-The engine is put in the golden's collision-stage input state: gravity,
-damping and wind are switched off so that its prediction x = x_prev + dt v
+Prediction: the engine is put in the golden's pre-step state (positions,
+previous positions, velocities, running vertex normals, triangle order) with
+the case's gravity, damping and wind, and steps once.  Its predicted
+positions and velocities must agree with the reference's PBDStepExternal
+kernels within golden_cases.PRED_ATOL_X (1e-5 m; 1e-5 m / dt on
+velocities) and its running vertex normals with the reference's
+UpdateVertexNormals within golden_cases.VN_ATOL.
+
+Collision stages and solver: the engine is put in the golden's
+collision-stage input state (the reference's prediction): gravity, damping
+and wind are switched off so that its prediction x = x_prev + dt v
 reproduces the golden's predicted positions bit for bit, and the triangle
 order is set to the golden's pre-sort order.  One step later its Morton
 codes, sorted order, hierarchy, refit boxes, rightmost leaves, pairs and
@@ -56,5 +65,31 @@ def test_engine_matches_reference_kernels(path, friction):
         dv = np.abs(st["v"] - d["ref_friction_v" if friction else "ref_solve_v"]).max()
         assert dx <= golden_cases.SOLVER_ATOL_X, dx
         assert dv <= golden_cases.SOLVER_ATOL_X / dt, dv
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_engine_prediction_matches_reference_kernels(path):
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    p = spec.params
+    # the engine's wind state starts at startWindDir: the goldens use a
+    # constant wind (zero variation) or none
+    assert not p.windOn or (p.windMinVariation == 0.0 and p.windMaxVariation == 0.0)
+    b = ClothBatch([spec], debug_capture=True)
+    try:
+        b.set_state(0, x=d["pre_x"], x_prev=d["pre_x_prev"], v=d["pre_v"], vn=d["pre_vn"])
+        b.set_triangle_order(0, d["perm_before"])
+        b.step(1)
+        b.sync()
+        dt = float(d["dt"])
+        dx = np.abs(b.debug(0, "PRED_X") - d["x"]).max()
+        dv = np.abs(b.debug(0, "PRED_V") - d["v"]).max()
+        dvn = np.abs(b.get_state(0)["vn"] - d["ref_vn"]).max()
+        assert np.array_equal(b.debug(0, "PRED_XPREV"), d["x_prev"])
+        assert dx <= golden_cases.PRED_ATOL_X, dx
+        assert dv <= golden_cases.PRED_ATOL_X / dt, dv
+        assert dvn <= golden_cases.VN_ATOL, dvn
     finally:
         b.close()
