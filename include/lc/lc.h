@@ -369,6 +369,14 @@ lc_status lc_lbvh_build(lc_lbvh *h, const float *tri_min, const float *tri_max,
 lc_status lc_lbvh_pairs(lc_lbvh *h, uint32_t *out_pairs, uint64_t cap, uint64_t *count,
                         void *stream);
 lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream);
+/* Intermediate arrays of the last build, in the reference's layouts, into
+ * host memory (at most cap elements; the element count goes to *count):
+ * LC_DBG_MORTON (sorted codes), LC_DBG_PERM (sorted order), LC_DBG_LEFTS,
+ * LC_DBG_RIGHTS, LC_DBG_PARENTS, LC_DBG_RML, LC_DBG_NODE_AABB (the arrays
+ * _GenerateBVH2 and ComputeTreeAABBs write, Collision/CudaBVH.cu:128-188) and,
+ * after lc_lbvh_pairs, LC_DBG_PAIRS.  Waits for the device; for parity
+ * checks, not for a hot loop. */
+lc_status lc_lbvh_debug_get(lc_lbvh *h, int32_t what, void *dst, uint64_t cap, uint64_t *count);
 lc_status lc_lbvh_destroy(lc_lbvh *h);
 
 /* ----- allocation-free LBVH query ---------------------------------------
@@ -386,10 +394,13 @@ lc_status lc_lbvh_destroy(lc_lbvh *h);
  * beyond cap are not written and the call returns
  * LC_ERR_CAPACITY_OVERFLOW with the full number in *count), *count (host) and
  * optionally the sorted triangle ids (device memory, n u32).  The first call
- * on a device looks up the scratch address and should come before any stream
- * capture.  All calls share the scratch array and keep nothing between calls
- * that they rely on; calls that overlap on the GPU race and must be
- * serialised by the caller.  The call waits for its stream. */
+ * on a device looks up the scratch address and keeps it for the rest of the
+ * process: after a cudaDeviceReset of that device the entry point must not be
+ * called on it again.  Every call ends by copying the pair count to the host
+ * and waiting for its stream, so it cannot be issued on a stream that is
+ * being captured.  All calls share the scratch array and keep nothing between
+ * calls that they rely on; calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 #define LC_LBVH_STATIC_MAX_TRIANGLES 2048
 #define LC_LBVH_STATIC_MAX_CHUNK 64
 lc_status lc_lbvh_pairs_static(const float *tri_min, const float *tri_max, int32_t num_triangles,

@@ -121,6 +121,7 @@ SIGNATURES = {
     "lc_lbvh_build": (C.c_int, [VP, VP, VP, C.c_int32, VP]),
     "lc_lbvh_pairs": (C.c_int, [VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
     "lc_lbvh_sorted_ids": (C.c_int, [VP, VP, VP]),
+    "lc_lbvh_debug_get": (C.c_int, [VP, C.c_int32, VP, C.c_uint64, C.POINTER(C.c_uint64)]),
     "lc_lbvh_destroy": (C.c_int, [VP]),
     "lc_lbvh_pairs_static": (C.c_int, [VP, VP, C.c_int32, C.c_int32, C.c_int32, VP, C.c_uint64,
                                        C.POINTER(C.c_uint64), VP, VP]),

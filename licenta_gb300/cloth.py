@@ -188,11 +188,11 @@ class ClothBatch:
         n = C.c_uint64()
         _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, None, 0, C.byref(n)), "lc_batch_debug_get")
         if sel in (13, 14):
-            arr = (_ffi.Contact * max(n.value, 1))()
-            _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, arr, n.value, C.byref(n)), "lc_batch_debug_get")
-            v = np.array([list(arr[i].v) for i in range(n.value)], dtype=np.int32).reshape(-1, 4)
-            w = np.array([list(arr[i].w) for i in range(n.value)], dtype=np.float32).reshape(-1, 4)
-            return v, w
+            # lc_contact records: 4 int32 ids then 4 float32 weights
+            raw = np.empty((max(n.value, 1), 8), dtype=np.int32)
+            _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, _ptr(raw), n.value, C.byref(n)), "lc_batch_debug_get")
+            raw = raw[:n.value]
+            return raw[:, :4].copy(), raw[:, 4:].copy().view(np.float32)
         dt, width = self._DT[sel]
         out = np.empty((n.value, width) if width > 1 else (n.value,), dtype=dt)
         _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, _ptr(out), n.value, C.byref(n)), "lc_batch_debug_get")
@@ -366,6 +366,20 @@ class Lbvh:
     def sorted_ids(self, out_ptr: int, stream=None) -> None:
         _ffi.check(_ffi.lib().lc_lbvh_sorted_ids(self._h, C.c_void_p(out_ptr), _stream_handle(stream)),
                    "lc_lbvh_sorted_ids")
+
+    _DT = {"MORTON": (np.uint64, 1), "PERM": (np.uint32, 1), "LEFTS": (np.int32, 1), "RIGHTS": (np.int32, 1),
+           "PARENTS": (np.int32, 1), "RML": (np.int32, 2), "NODE_AABB": (np.float32, 6), "PAIRS": (np.uint32, 2)}
+
+    def debug(self, what: str) -> np.ndarray:
+        """An array of the last build (lc_lbvh_debug_get), in host memory."""
+        dt, width = self._DT[what]
+        sel = _ffi.DBG[what]
+        n = C.c_uint64()
+        L = _ffi.lib()
+        _ffi.check(L.lc_lbvh_debug_get(self._h, sel, None, 0, C.byref(n)), "lc_lbvh_debug_get")
+        out = np.empty((n.value, width) if width > 1 else (n.value,), dtype=dt)
+        _ffi.check(L.lc_lbvh_debug_get(self._h, sel, _ptr(out), n.value, C.byref(n)), "lc_lbvh_debug_get")
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -415,7 +415,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     LC_PHASE(1);
     // 2. Update Triangles
     launch_triangles(d, st);
-    if (any_wind) launch_vertex_normals(d, st);
+    launch_vertex_normals(d, st);
     LC_PHASE(2);
     // 3. Build BVH
     LC_KEV(6);
@@ -1884,6 +1884,20 @@ lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream) {
     LC_CUDA(cudaMemcpyAsync(out_ids, h->b.d.perm, sizeof(uint32_t) * h->T, cudaMemcpyDeviceToDevice,
                             (cudaStream_t)stream));
     return LC_OK;
+}
+
+lc_status lc_lbvh_debug_get(lc_lbvh *h, int32_t what, void *dst, uint64_t cap, uint64_t *count) {
+    if (!h || h->T < 1) return fail(LC_ERR_INVALID_ARG, "lc_lbvh_debug_get: no hierarchy built");
+    switch (what) {
+        case LC_DBG_MORTON: case LC_DBG_PERM: case LC_DBG_LEFTS: case LC_DBG_RIGHTS: case LC_DBG_PARENTS:
+        case LC_DBG_RML: case LC_DBG_NODE_AABB: case LC_DBG_PAIRS:
+            break;
+        default:
+            return fail(LC_ERR_NOT_SUPPORTED, "lc_lbvh_debug_get: selector not held by a standalone LBVH");
+    }
+    // the build and the query run on the caller's streams
+    LC_CUDA(cudaDeviceSynchronize());
+    return lc_batch_debug_get(&h->b, 0, what, dst, cap, count);
 }
 
 lc_status lc_lbvh_destroy(lc_lbvh *h) {

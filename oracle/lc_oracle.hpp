@@ -1503,10 +1503,14 @@ template <class R> class Cloth {
         }
     }
 
+    // One FixedUpdate.  With frozen contacts and skip_collide, the collision
+    // stages are not run (a teacher-forced step takes its contacts, and its
+    // running normals, from elsewhere).
+    bool skip_collide = false;
     void step() {
         external();
         pred_x = x; pred_xp = xp; pred_v = v;
-        collide();
+        if (!(have_frozen && skip_collide)) collide();
         if (have_frozen)
             solve(frozen_vf, frozen_ee);
         else

@@ -84,6 +84,46 @@ int lco_step(lco_world *w, int nsteps, int nthreads) {
 
 int lco_max_threads(void) { return omp_get_max_threads(); }
 
+// The collision stages of every cloth on its current state (x, x_prev, v,
+// triangle order), cloths in parallel on nthreads host threads (0 = all).
+int lco_collide_all(lco_world *w, int nthreads) {
+    if (!w) return LC_ERR_INVALID_ARG;
+    int n = w->n();
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int c = 0; c < n; ++c) {
+        if (w->fp64)
+            w->f64[c]->collide();
+        else
+            w->f32[c]->collide();
+    }
+    return LC_OK;
+}
+
+// One teacher-forced step of every cloth, in parallel: each cloth must have
+// its contacts frozen (lco_set_frozen_contacts); its collision stages are
+// skipped, so its running normals and triangle order stay as set.
+int lco_step_frozen_all(lco_world *w, int nthreads) {
+    if (!w) return LC_ERR_INVALID_ARG;
+    int n = w->n();
+    for (int c = 0; c < n; ++c)
+        if (!(w->fp64 ? w->f64[c]->have_frozen : w->f32[c]->have_frozen)) return LC_ERR_INVALID_ARG;
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int c = 0; c < n; ++c) {
+        if (w->fp64) {
+            w->f64[c]->skip_collide = true;
+            w->f64[c]->step();
+            w->f64[c]->skip_collide = false;
+        } else {
+            w->f32[c]->skip_collide = true;
+            w->f32[c]->step();
+            w->f32[c]->skip_collide = false;
+        }
+    }
+    return LC_OK;
+}
+
 int lco_sizes(lco_world *w, int c, int *nv, int *nt, int *ne, int *nb) {
     return with_cloth(w, c, [&](auto &cl) {
         if (nv) *nv = cl.tp.V;
@@ -264,6 +304,66 @@ int lco_grid_indices(int rows, int cols, uint32_t *out) {
 
 // Morton code of one point, for golden-vector checks of the encoder.
 uint64_t lco_morton(float x, float y, float z, int mode) { return morton3d(x, y, z, mode); }
+
+// The LBVH chain over caller boxes that the engine's standalone entry points
+// (lc_lbvh_build + lc_lbvh_pairs) run: Morton code of each box's midpoint
+// min + (max - min) / 2 (identity frame, Core/CudaUtils.cu:278-325), a stable
+// sort by code, the leaves' boxes gathered in the sorted order, the Karras
+// hierarchy, the refit and the traversal with at most `chunk` pairs per leaf
+// (Collision/CudaBVH.cu:23-188), through the restatement's FP32 code.
+// Outputs (any may be NULL): sorted codes and order (T), lefts / rights
+// (T-1), parents (2T-1; the root's entry -1), rightmost leaves (2 per
+// internal node), node boxes (6 floats per node), pairs (2 u32 each, at most
+// pair_cap) with their count.
+int lco_lbvh_boxes(const float *bmin, const float *bmax, int T, int chunk, int mode, uint64_t *morton_out,
+                   uint32_t *perm_out, int *lefts_out, int *rights_out, int *parents_out, int *rml_out,
+                   float *node_out, uint32_t *pairs_out, uint64_t pair_cap, uint64_t *npairs) {
+    if (!bmin || !bmax || T < 2 || chunk < 1 || (mode != LC_MORTON_REF63 && mode != LC_MORTON_K30))
+        return LC_ERR_INVALID_ARG;
+    Cloth<float> cl;
+    cl.tp.T = T;
+    cl.prm.BVHChunkSize = chunk;
+    std::vector<u64> keys(T);
+    for (int s = 0; s < T; ++s) {
+        V3<float> mn = mk<float>(bmin[3 * s], bmin[3 * s + 1], bmin[3 * s + 2]);
+        V3<float> mx = mk<float>(bmax[3 * s], bmax[3 * s + 1], bmax[3 * s + 2]);
+        V3<float> mid = mn + (mx - mn) / 2.f;
+        keys[s] = morton3d(mid.x, mid.y, mid.z, mode);
+    }
+    std::vector<u32> order(T);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](u32 a, u32 b) { return keys[a] < keys[b]; });
+    const int nodes = 2 * T - 1;
+    cl.nmin.assign(nodes, mk<float>(0, 0, 0));
+    cl.nmax.assign(nodes, mk<float>(0, 0, 0));
+    cl.morton.resize(T);
+    for (int s = 0; s < T; ++s) {
+        const u32 o = order[s];
+        cl.morton[s] = keys[o];
+        cl.nmin[T - 1 + s] = mk<float>(bmin[3 * o], bmin[3 * o + 1], bmin[3 * o + 2]);
+        cl.nmax[T - 1 + s] = mk<float>(bmax[3 * o], bmax[3 * o + 1], bmax[3 * o + 2]);
+    }
+    cl.build_tree();
+    cl.refit();
+    cl.traverse();
+    if (morton_out) std::memcpy(morton_out, cl.morton.data(), sizeof(u64) * T);
+    if (perm_out) std::memcpy(perm_out, order.data(), sizeof(u32) * T);
+    if (lefts_out) std::memcpy(lefts_out, cl.lefts.data(), sizeof(int) * (T - 1));
+    if (rights_out) std::memcpy(rights_out, cl.rights.data(), sizeof(int) * (T - 1));
+    if (parents_out) std::memcpy(parents_out, cl.parents.data(), sizeof(int) * nodes);
+    if (rml_out)
+        for (int i = 0; i < T - 1; ++i) { rml_out[2 * i] = cl.rmll[i]; rml_out[2 * i + 1] = cl.rmlr[i]; }
+    if (node_out)
+        for (int i = 0; i < nodes; ++i) {
+            float *o = node_out + 6 * i;
+            o[0] = cl.nmin[i].x; o[1] = cl.nmin[i].y; o[2] = cl.nmin[i].z;
+            o[3] = cl.nmax[i].x; o[4] = cl.nmax[i].y; o[5] = cl.nmax[i].z;
+        }
+    const uint64_t np = cl.pairs.size() / 2;
+    if (npairs) *npairs = np;
+    if (pairs_out) std::memcpy(pairs_out, cl.pairs.data(), sizeof(u32) * 2 * std::min(np, pair_cap));
+    return cl.stack_overflow ? LC_ERR_STACK_OVERFLOW : LC_OK;
+}
 
 }  // extern "C"
 

@@ -63,6 +63,10 @@ def lib() -> C.CDLL:
             "lco_bend_conditioning": (C.c_int, [VP, C.c_int, C.POINTER(C.c_double)]),
             "lco_friction_on": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
             "lco_solve_decisions": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
+            "lco_collide_all": (C.c_int, [VP, C.c_int]),
+            "lco_step_frozen_all": (C.c_int, [VP, C.c_int]),
+            "lco_lbvh_boxes": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int] + [VP] * 8 +
+                               [C.c_uint64, C.POINTER(C.c_uint64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -133,6 +137,15 @@ class Oracle:
     def collide(self, c: int) -> None:
         _chk(lib().lco_collide(self._h, c), "collide")
 
+    def collide_all(self, threads: int = 0) -> None:
+        """The collision stages of every cloth, in parallel over cloths."""
+        _chk(lib().lco_collide_all(self._h, threads), "collide_all")
+
+    def step_frozen_all(self, threads: int = 0) -> None:
+        """One step of every cloth with its frozen contacts (and any forced
+        decisions), the collision stages skipped; in parallel over cloths."""
+        _chk(lib().lco_step_frozen_all(self._h, threads), "step_frozen_all")
+
     def get_state(self, c: int) -> dict:
         V = self.V[c]
         out = {k: np.empty((V, 3), dtype=np.float64) for k in ("x", "x_prev", "v", "vn")}
@@ -163,16 +176,17 @@ class Oracle:
         _chk(lib().lco_set_wind(self._h, c, _p(w), rng), "set_wind")
 
     def freeze_contacts(self, c: int, vf: tuple, ee: tuple, vf_normals=None) -> None:
-        def pack(t):
+        def pack(t):  # lc_contact records: 4 int32 ids then 4 float32 weights
             v, w = t
-            arr = (_ffi.Contact * max(len(v), 1))()
-            for i in range(len(v)):
-                arr[i].v[:] = [int(q) for q in v[i]]
-                arr[i].w[:] = [float(q) for q in w[i]]
-            return arr, len(v)
+            v = np.asarray(v, np.int32).reshape(-1, 4)
+            w = np.asarray(w, np.float32).reshape(-1, 4)
+            rec = np.zeros((max(len(v), 1), 8), np.int32)
+            rec[:len(v), :4] = v
+            rec[:len(v), 4:] = w.view(np.int32)
+            return rec, len(v)
         a, na = pack(vf)
         b, nb = pack(ee)
-        _chk(lib().lco_set_frozen_contacts(self._h, c, a, na, b, nb), "set_frozen_contacts")
+        _chk(lib().lco_set_frozen_contacts(self._h, c, _p(a), na, _p(b), nb), "set_frozen_contacts")
         if vf_normals is not None:
             nr = np.ascontiguousarray(vf_normals, np.float32).reshape(-1, 3)
             _chk(lib().lco_set_frozen_normals(self._h, c, _p(nr), len(nr)), "set_frozen_normals")
@@ -337,15 +351,35 @@ class Oracle:
         n = C.c_uint64()
         _chk(lib().lco_debug_get(self._h, c, sel, None, 0, C.byref(n)), "debug_get")
         if sel in (13, 14):
-            arr = (_ffi.Contact * max(n.value, 1))()
-            _chk(lib().lco_debug_get(self._h, c, sel, arr, n.value, C.byref(n)), "debug_get")
-            v = np.array([list(arr[i].v) for i in range(n.value)], dtype=np.int32).reshape(-1, 4)
-            w = np.array([list(arr[i].w) for i in range(n.value)], dtype=np.float32).reshape(-1, 4)
-            return v, w
+            raw = np.empty((max(n.value, 1), 8), dtype=np.int32)
+            _chk(lib().lco_debug_get(self._h, c, sel, _p(raw), n.value, C.byref(n)), "debug_get")
+            raw = raw[:n.value]
+            return raw[:, :4].copy(), raw[:, 4:].copy().view(np.float32)
         dt, width = self._DT[sel]
         out = np.empty((n.value, width) if width > 1 else (n.value,), dtype=dt)
         _chk(lib().lco_debug_get(self._h, c, sel, _p(out), n.value, C.byref(n)), "debug_get")
         return out
+
+
+def lbvh_boxes(bmin, bmax, chunk: int = 64, mode: int = 0) -> dict:
+    """The restatement's LBVH over caller boxes ((T, 3) float32 min / max
+    corners): sorted Morton codes and order, lefts / rights / parents,
+    rightmost leaves, node boxes and pairs, in the layouts of the engine's
+    lc_lbvh_debug_get."""
+    lo = np.ascontiguousarray(bmin, np.float32).reshape(-1, 3)
+    hi = np.ascontiguousarray(bmax, np.float32).reshape(-1, 3)
+    T = lo.shape[0]
+    out = dict(MORTON=np.empty(T, np.uint64), PERM=np.empty(T, np.uint32), LEFTS=np.empty(T - 1, np.int32),
+               RIGHTS=np.empty(T - 1, np.int32), PARENTS=np.empty(2 * T - 1, np.int32),
+               RML=np.empty((T - 1, 2), np.int32), NODE_AABB=np.empty((2 * T - 1, 6), np.float32))
+    n = C.c_uint64()
+    args = [_p(out[k]) for k in ("MORTON", "PERM", "LEFTS", "RIGHTS", "PARENTS", "RML", "NODE_AABB")]
+    _chk(lib().lco_lbvh_boxes(_p(lo), _p(hi), T, chunk, mode, *args, None, 0, C.byref(n)), "lbvh_boxes")
+    pairs = np.empty((n.value, 2), np.uint32)
+    _chk(lib().lco_lbvh_boxes(_p(lo), _p(hi), T, chunk, mode, *([None] * 7), _p(pairs), n.value, C.byref(n)),
+         "lbvh_boxes")
+    out["PAIRS"] = pairs
+    return out
 
 
 def morton(x: float, y: float, z: float, mode: int = 0) -> int:

@@ -31,7 +31,11 @@ edits its sources) make its kernels compile with nvcc 13:
   change none, and a failed device assert would stop the GPU context instead
   of reporting a difference.
 
-Usage: python -m oracle.ref_pin.build_ref [reference-root]
+The reference root (the directory holding Collision/, Core/ and Physics/)
+comes from the command line or the LICENTA_REFERENCE environment variable;
+there is no built-in default.
+
+Usage: python -m oracle.ref_pin.build_ref REFERENCE_ROOT
 """
 from __future__ import annotations
 
@@ -47,7 +51,6 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 OUT = REPO / "oracle" / "_ref"
 CUBIN = OUT / "ref_kernels.cubin"
-DEFAULT_ROOT = Path("/root/reference/LicentaV2/LicentaV2")
 
 # The reference translation units of the cloth step's device code.
 SOURCES = [
@@ -63,9 +66,14 @@ SOURCES = [
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
-def reference_root() -> Path | None:
-    root = Path(os.environ.get("LICENTA_REFERENCE", DEFAULT_ROOT))
-    return root if (root / "Collision" / "CudaBVH.cu").exists() else None
+def reference_root(root: str | Path | None = None) -> Path | None:
+    """The reference root given, else LICENTA_REFERENCE; None when neither
+    names a checkout that holds the cloth step's sources."""
+    cand = root if root is not None else os.environ.get("LICENTA_REFERENCE")
+    if not cand:
+        return None
+    cand = Path(cand)
+    return cand if (cand / "Collision" / "CudaBVH.cu").exists() else None
 
 
 def _nvcc() -> str:
@@ -81,7 +89,7 @@ def _run(cmd):
 def build(root: Path | None = None, force: bool = False) -> Path | None:
     """Compile the reference kernels; returns the cubin path, or None when the
     reference checkout is not present (the cubin, if built earlier, stays)."""
-    root = root or reference_root()
+    root = reference_root(root)
     if root is None:
         return CUBIN if CUBIN.exists() or Path(str(CUBIN) + ".gz").exists() else None
     if CUBIN.exists() and not force:
@@ -115,5 +123,7 @@ def build(root: Path | None = None, force: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2 and not os.environ.get("LICENTA_REFERENCE"):
+        sys.exit("usage: python -m oracle.ref_pin.build_ref REFERENCE_ROOT (or set LICENTA_REFERENCE)")
     p = build(Path(sys.argv[1]) if len(sys.argv) > 1 else None, force=True)
     print(p if p else "reference checkout not found")

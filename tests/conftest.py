@@ -31,3 +31,22 @@ def cuda():
         pytest.skip("no CUDA device")
     torch.cuda.set_device(0)
     return torch
+
+
+# Measured figures that parity tests report (largest errors, steps excused by
+# the bend singularity, sizes checked), printed at the end of the run.
+_REPORT: list[tuple[str, dict]] = []
+
+
+@pytest.fixture
+def parity_report(request):
+    def add(**figures):
+        _REPORT.append((request.node.nodeid, figures))
+    return add
+
+
+def pytest_terminal_summary(terminalreporter):
+    if _REPORT:
+        terminalreporter.section("parity report")
+        for node, figures in _REPORT:
+            terminalreporter.write_line(f"{node}: " + ", ".join(f"{k}={v}" for k, v in figures.items()))

@@ -195,3 +195,29 @@ def test_rescaled_entry_matches_plain_entry():
             assert float((got - want).abs().max()) <= 2.0 ** -80
             assert torch.equal(a[n:], b[n:])
     cloth.close()
+
+
+def test_engine_adjoint_at_the_workload_size(parity_report):
+    """The differentiable-rollout workload as configured: a 64 x 64 cloth, 60
+    steps, 10 iterations, checkpoints every 10 steps; the target is the final
+    state of a forward run with stiffness 0.7 and wind (1.5, 0, 0.5) m/s^2;
+    the gradients with respect to the per-constraint stiffness (0.9) and the
+    initial velocities (zero) against the FP64 adjoint, each on its own
+    trajectory."""
+    spec = scenes.adjoint_cloth(seed=0)
+    tgt = scenes.adjoint_cloth(seed=0, stiffness=0.7, wind=(1.5, 0.0, 0.5))
+    steps = 60
+    o = Oracle([tgt], fp64=True)
+    o.step(steps, threads=1)
+    target = o.get_state(0)["x_prev"]
+    _, _, ne, nb = o.sizes(0)
+    o.close()
+    ks, kb = np.full(ne, 0.9), np.full(nb, 0.9)
+    v0 = np.zeros((spec.num_vertices, 3))
+    g = engine_grads(spec, steps, ks, kb, v0, target, every=10)
+    r = oracle_grads(spec, steps, ks, kb, v0, target)
+    errs = {k: rel_l2(g[k], r[k]) for k in ("ks", "kb", "v0", "x0")}
+    parity_report(final_dx_m=f"{np.abs(g['final'] - r['final']).max():.2e}",
+                  **{f"rel_l2_{k}": f"{v:.2e}" for k, v in errs.items()})
+    for k, e in errs.items():
+        assert e < 2e-3, f"{k}: relative error {e:.2e}"

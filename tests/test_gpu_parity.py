@@ -26,41 +26,8 @@ pytestmark = pytest.mark.gpu
 POS_TOL = 1e-5  # metres, on a 1 m cloth: the 1e-5 relative bound
 
 
-def run_parity(specs, steps, check_every=1, variant=0, friction=False, contact_gather=0):
-    batch = ClothBatch(specs, debug_capture=True, solver_variant=variant)
-    if contact_gather:
-        from licenta_gb300 import autotune
-        cfg = autotune.get_tuning(batch)
-        cfg["contact_gather"] = contact_gather
-        assert autotune.set_tuning(batch, cfg)
-    o32 = [Oracle([s], fp64=False) for s in specs]
-    o64 = [Oracle([s], fp64=True) for s in specs]
-    for o in o64:
-        o.track_bend(0)
-    bound = [parity.conditioning_bound(s, POS_TOL) for s in specs]
-    worst = 0.0
-    contacts = 0
-    singular = 0
-    for step in range(steps):
-        pre = [parity.capture_pre(batch, c) for c in range(len(specs))]
-        batch.step(1)
-        batch.sync()
-        for c, s in enumerate(specs):
-            if step % check_every == 0:
-                contacts += parity.check_collision(batch, c, o32[c], pre[c][0]["vn"], tag=f"cloth {c} step {step}")
-            err, err_v = parity.fp64_step_error(batch, c, o64[c], pre[c][0], pre[c][1], bool(s.params.sphereOn),
-                                                friction)
-            if err > POS_TOL and o64[c].bend_conditioning(0) < bound[c]:
-                # a bend passed the reference's d -> 1 singularity: the step's
-                # result is set by rounding, not by the scheme
-                singular += 1
-                continue
-            worst = max(worst, err)
-            assert err <= POS_TOL, f"cloth {c} step {step}: |x - x_fp64| = {err:.3e}"
-            if friction:  # friction changes velocities only
-                assert err_v <= POS_TOL / s.params.timestep, f"cloth {c} step {step}: |v - v_fp64| = {err_v:.3e}"
-    batch.close()
-    assert singular <= max(1, steps * len(specs) // 20), f"{singular} steps near the bend singularity"
+def run_parity(*args, **kw):
+    worst, contacts, _, _ = parity.run_parity(*args, tol=POS_TOL, **kw)
     return worst, contacts
 
 
