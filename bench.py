@@ -17,8 +17,10 @@ step, the per-phase profile, the roofline of the dominant kernel, sampled SM
 clocks, and the CPU oracle port timed on the host cores.
 
 --impl reference times the reference scheme's CPU restatement (the oracle,
-OpenMP over cloths on every host core) on a bounded sample of the same
-workload: the reference has no CPU implementation of its GPU cloth step.
+OpenMP over cloths on every host core) on the same workload and window (all
+256 cloths, the same warm-up and timed steps): the reference has no CPU
+implementation of its GPU cloth step.  It builds the workload without loading
+the CUDA library.
 """
 from __future__ import annotations
 
@@ -130,21 +132,6 @@ def measured_peak_gbs() -> tuple[float, str]:
         except (KeyError, ValueError):
             pass
     return 6800.0, "fallback"
-
-
-def ncu_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch from the committed ncu summary, if it covers this kernel/workload."""
-    p = ROOT / "profiles" / "traffic.json"
-    if not p.exists():
-        return None
-    try:
-        t = json.loads(p.read_text())
-        e = t.get(kernel)
-        if e and e.get("workload") == workload:
-            return float(e["bytes_per_launch"])
-    except (ValueError, KeyError):
-        return None
-    return None
 
 
 def save_state(batch, stream):
@@ -436,48 +423,76 @@ def lbvh_timing(seed: int, count: int = 1_000_000) -> dict:
             "l2": "flushed by a 256 MB write before each timed build"}
 
 
-def cpu_baseline(specs, seed: int, cloths: int = 256, steps: int = 5) -> dict:
+def cpu_baseline(batch, gspecs, members, state0, stream, warmup: int, steps: int = 4) -> dict:
     """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
-    cloths on every host core, on a bounded sample of the workload (every
-    cloth by default, for a few steps: about 10 s of host work)."""
+    cloths on every host core, on a bounded sample of the timed window: every
+    cloth of the workload, started from the GPU's state at the window's first
+    step (positions, previous positions, velocities, running normals,
+    triangle order) and stepped `steps` steps, about 20 s of host work.
+    gspecs: the specs in the batch's cloth order."""
     from oracle.oracle_ffi import Oracle, max_threads
-    rng = np.random.default_rng(seed + 7)
-    pick = sorted(rng.choice(len(specs), size=min(cloths, len(specs)), replace=False).tolist())
-    o = Oracle([specs[i] for i in pick], fp64=False)
-    o.step(1)  # warm-up
+    for m, st in zip(members, state0):
+        load_state(m, st, stream)
+    stream.synchronize()
+    o = Oracle(gspecs, fp64=False)
+    for c in range(len(gspecs)):
+        b, k = batch.locate(c) if hasattr(batch, "locate") else (batch, c)
+        st = b.get_state(k)
+        o.set_state(c, **{q: st[q].astype(np.float64) for q in ("x", "x_prev", "v", "vn")})
+        o.set_perm(c, b.triangle_order(k))
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": len(pick) * steps / dt, "unit": UNIT, "cores": max_threads(), "kind": "port",
-            "sample": f"{len(pick)} of {len(specs)} cloths (seeded) x {steps} steps after 1 warm-up step, "
-                      f"FP32 oracle port, OpenMP over cloths", "seconds": dt}
+    return {"value": len(gspecs) * steps / dt, "unit": UNIT, "cores": max_threads(), "kind": "port",
+            "sample": f"all {len(gspecs)} cloths, steps {warmup + 1}..{warmup + steps} (the first {steps} steps of "
+                      f"the timed window, from the GPU's state at step {warmup}), FP32 oracle port, OpenMP over "
+                      f"cloths", "seconds": dt}
+
+
+# Longest window the reference arm steps on every cloth: at about 2-5 s of
+# host time per 256-cloth step, 40 steps stay within a few minutes.
+REF_FULL_WINDOW = 40
 
 
 def run_reference(args, world, rank):
+    """The workload on the reference scheme's CPU restatement, OpenMP over
+    cloths on every host core: every cloth, W untimed warm-up steps, then K
+    timed steps (the window the GPU arm times).  Windows longer than
+    REF_FULL_WINDOW steps time a seeded sample of 32 cloths instead, so that
+    the run stays within a few minutes.  The workload is built by
+    licenta_gb300.scenes without loading the CUDA library."""
     if rank != 0:
         return
     from licenta_gb300 import scenes
     from oracle.oracle_ffi import Oracle, max_threads
-    specs = scenes.batched_cloths(seed=args.seed)
-    rng = np.random.default_rng(args.seed + 11)
-    sample = 32
-    pick = sorted(rng.choice(len(specs), size=sample, replace=False).tolist())
+    specs = scenes.batched_cloths(seed=args.seed, count=args.cloths)
+    if args.warmup + args.steps <= REF_FULL_WINDOW:
+        pick = list(range(len(specs)))
+    else:
+        rng = np.random.default_rng(args.seed + 11)
+        pick = sorted(rng.choice(len(specs), size=min(32, len(specs)), replace=False).tolist())
     o = Oracle([specs[i] for i in pick], fp64=False)
     o.step(args.warmup)
     t0 = time.perf_counter()
     o.step(args.steps)
     dt = time.perf_counter() - t0
+    o.close()
+    sample = len(pick)
     value = sample * args.steps / dt
     cores = max_threads()
+    what = (f"all {sample} cloths" if sample == len(specs) else f"{sample} of {len(specs)} cloths (seeded)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batched-256-uneven", "cloths_per_step": sample, "iterations": 10},
+        "config": {"workload": "batched-256-uneven" if args.cloths == NCLOTH else f"batched-{args.cloths}-uneven",
+                   "cloths_per_step": sample, "iterations": 10, "dt": 1.0 / 60.0,
+                   "window": f"steps {args.warmup + 1}..{args.warmup + args.steps} after {args.warmup} warm-up"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{sample} of 256 cloths (seeded) per step, FP32 restatement of the reference "
-                                   f"GPU scheme (the reference has no CPU implementation of it), OpenMP over cloths"},
+                         "sample": f"{what}, steps {args.warmup + 1}..{args.warmup + args.steps}, FP32 restatement "
+                                   f"of the reference GPU scheme (the reference has no CPU implementation of it), "
+                                   f"OpenMP over cloths", "seconds": dt},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -549,8 +564,11 @@ def run_ours(args, world, rank, local):
     value = world * args.cloths * args.steps / (ms / 1000.0)
 
     # ---- e2e through the public API: whole state host -> device -> host -----
+    # the same window as `value`: restart from the state at its first step
     V = sum(s.num_vertices for s in specs)
     host = [torch.empty((V, 3), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+    for m, st in zip(members, state0):
+        load_state(m, st, stream)
     batch.read_state(*(h.data_ptr() for h in host), True, stream)
     torch.cuda.synchronize()
     barrier()
@@ -570,6 +588,8 @@ def run_ours(args, world, rank, local):
     batch.sync()
     e2e = {"value": world * args.cloths * args.steps / (ms_e2e / 1000.0), "unit": UNIT,
            "h2d_bytes_per_step": 3 * 12 * V, "d2h_bytes_per_step": 3 * 12 * V,
+           "window": f"steps {args.warmup + 1}..{args.warmup + args.steps}, replayed from the saved state at "
+                     f"step {args.warmup} (the steps `value` times)",
            "what": ("lc_group_step_io: every step, per lane, lc_batch_write_state (x, x_prev, v from pinned "
                     "host) + lc_batch_step + lc_batch_read_state on the lane's stream" if args.lanes > 1 else
                     "lc_batch_write_state (x, x_prev, v from pinned host) + lc_batch_step + lc_batch_read_state")}
@@ -596,8 +616,7 @@ def run_ours(args, world, rank, local):
     achieved = alg[dom] / (launch_ms / 1000.0) / 1e9 if launch_ms > 0 else 0.0
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
-            "traffic": ncu_traffic(dom, "batched-256-uneven"), "algorithmic_bytes_per_launch": alg[dom],
-            "launch_ms": launch_ms}
+            "traffic": None, "algorithmic_bytes_per_launch": alg[dom], "launch_ms": launch_ms}
 
     # ---- plain path: the same engine one cloth per call ---------------------
     plain = None
@@ -635,7 +654,7 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(specs, args.seed)
+        cpu = cpu_baseline(batch, batch.specs if args.lanes > 1 else specs, members, state0, stream, args.warmup)
 
     T = sum(s.num_triangles for s in specs)
     state_mb = (V * 16 * 5) / 1e6

@@ -3,10 +3,15 @@
 The reference builds its cloth with VisualBodyFactory::CreateMeshProps
 (Rendering/VisualBodyFactory.cpp:343-391) and pins two corners
 (Managers/MastersSimulationManager.cpp:67-77); the triangle topology here is
-that generator's (lc_mesh_grid), placed as a 1 m x 1 m grid in the XZ plane at
-y = 1 m with a seeded uniform jitter on every coordinate.  Parameters the
-workloads leave open keep the reference defaults of
-Managers/MastersSimulationManager.cpp:33-62.
+that generator's, placed as a 1 m x 1 m grid in the XZ plane at y = 1 m with
+a seeded uniform jitter on every coordinate.  Parameters the workloads leave
+open keep the reference defaults of Managers/MastersSimulationManager.cpp
+:33-62.
+
+The grid topology and the default parameters are built here in numpy (the
+same values as the library's lc_mesh_grid and lc_default_params, which a CPU
+test holds byte for byte), so the workloads can be generated without loading
+the CUDA library; only the icosphere calls it.
 """
 from __future__ import annotations
 
@@ -36,10 +41,44 @@ class ClothSpec:
 
 
 def grid_indices(n: int) -> np.ndarray:
-    t = _ffi.lib().lc_mesh_grid(n, n, None)
-    out = np.empty((t, 3), dtype=np.uint32)
-    _ffi.lib().lc_mesh_grid(n, n, out.ctypes.data_as(C.c_void_p))
-    return out
+    """VisualBodyFactory::CreateMeshProps (Rendering/VisualBodyFactory.cpp
+    :343-391) for an n x n grid: two triangles per quad in row-major quad
+    order, the quad's diagonal alternating with the parity of i + j."""
+    if n < 2:
+        return np.zeros((0, 3), dtype=np.uint32)
+    i, j = np.meshgrid(np.arange(n - 1, dtype=np.int64), np.arange(n - 1, dtype=np.int64), indexing="ij")
+    a, b = n * i + j, n * (i + 1) + j
+    c, d = a + 1, b + 1
+    even = ((i + j) % 2 == 0)[..., None]
+    t0 = np.where(even, np.stack([a, b, c], -1), np.stack([a, b, d], -1))
+    t1 = np.where(even, np.stack([c, b, d], -1), np.stack([d, c, a], -1))
+    return np.stack([t0, t1], axis=2).reshape(-1, 3).astype(np.uint32)
+
+
+def default_params() -> _ffi.ClothParams:
+    """The reference's ClothParams defaults (Managers/MastersSimulationManager
+    .cpp:33-62, timestep from Core/Utils.hpp:18-19) plus the extension
+    defaults of lc_cloth_params: the values lc_default_params fills."""
+    f = np.float32
+    p = _ffi.ClothParams()
+    p.timestep = float(f(f(1000.0) / f(60.0)) / f(1000.0))
+    p.kFriction, p.kStretch, p.kShear, p.kBend = 0.1, 0.99, 0.7, 0.1
+    p.kDamp, p.kSpringDamp, p.thickness, p.objectMass = 0.05, 0.2, 0.0, 0.525
+    p.globalVelDamp, p.strainLimit = 0.01, 0.15
+    p.gravity[:] = (0.0, -0.0981, 0.0)
+    p.minWindDir[:] = (-0.04, -0.1, -0.1)
+    p.startWindDir[:] = (0.02, 0.095, 0.45)
+    p.maxWindDir[:] = (0.04, 0.135, 0.4)
+    p.windMinVariation, p.windMaxVariation, p.windOn = 0.0, 0.2, 1
+    p.worldMin[:] = (0.0, 0.0, 0.0)
+    p.worldMax[:] = (1.0, 1.0, 1.0)
+    p.dims[:] = (60, 60)
+    p.solverIterations, p.ccdIterations, p.BVHChunkSize, p.benchmarkSample = 6, 5, 64, 1000
+    p.useTriangleBending = p.colorContacts = p.useFriction = 0
+    p.thicknessFromMesh, p.mortonMode, p.refLeafAabbQuirk, p.groundOn = 1, _ffi.LC_MORTON_REF63, 1, 1
+    p.mortonOrigin[:] = (0.0, 0.0, 0.0)
+    p.mortonScale, p.windSeed, p.sphereOn, p.sphereRadius = 1.0, 0, 0, 0.0
+    return p
 
 
 def icosphere(depth: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
@@ -68,7 +107,7 @@ def corner_pins(n: int) -> np.ndarray:
 
 
 def base_params(iterations: int, stiffness: float, dt: float = 1.0 / 60.0) -> _ffi.ClothParams:
-    p = _ffi.default_params()
+    p = default_params()
     p.timestep = dt
     p.gravity[:] = (0.0, -9.81, 0.0)
     p.solverIterations = iterations

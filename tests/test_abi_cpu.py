@@ -56,6 +56,19 @@ def test_default_params_are_the_reference_defaults():
     assert p.thicknessFromMesh == 1
 
 
+def test_workload_generators_match_the_library():
+    """scenes builds grids and default parameters without the library (so the
+    CPU reference arm of the bench never loads it); they must be the
+    library's lc_mesh_grid and lc_default_params byte for byte."""
+    L = _ffi.lib()
+    for n in (2, 3, 4, 16, 33, 192):
+        t = L.lc_mesh_grid(n, n, None)
+        want = np.empty((t, 3), dtype=np.uint32)
+        L.lc_mesh_grid(n, n, want.ctypes.data_as(C.c_void_p))
+        assert np.array_equal(scenes.grid_indices(n), want), n
+    assert bytes(scenes.default_params()) == bytes(_ffi.default_params())
+
+
 def test_invalid_arguments_are_rejected_before_any_device_work():
     L = _ffi.lib()
     h = C.c_void_p()
