@@ -11,9 +11,13 @@
 // library, for the lifetime of the process.  Host code cannot use the symbol
 // itself as a device address (it names a host-side stand-in), so the first
 // call on each device looks the address up with cudaGetSymbolAddress while
-// that device is current; that first call should come before any stream
-// capture.  All calls share the one array: calls that overlap on the GPU (two
-// streams, two host threads) race and must be serialised by the caller.
+// that device is current and keeps it for the rest of the process; a
+// cudaDeviceReset invalidates it, so the entry point must not be called on a
+// device after that device was reset.  Every call ends by copying the pair
+// count to the host and waiting for its stream, so it cannot be issued on a
+// stream that is being captured.  All calls share the one array: calls that
+// overlap on the GPU (two streams, two host threads) race and must be
+// serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -117,14 +121,17 @@ __global__ void k_static_init(ClothDev *cd, int *tcloth, int *stile_cloth, int *
     if (t < T) tcloth[t] = 0;
 }
 
-// Pair compaction into the caller's buffer, never past its capacity.
+// Pair compaction into the caller's buffer, never past its capacity: one warp
+// per leaf, its lanes copying consecutive pairs of the leaf's chunk, so the
+// reads of the chunk and the writes of the output are coalesced.
 __global__ void k_static_compact(const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ off,
                                  const uint32_t *__restrict__ chunk_area, int T, int chunk, uint2 *__restrict__ out,
                                  uint64_t cap) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (s >= T) return;
     const uint32_t n = cnt[s], o = off[s];
-    for (uint32_t k = 0; k < n; ++k)
+    for (uint32_t k = lane; k < n; k += 32)
         if ((uint64_t)o + k < cap) out[o + k] = make_uint2((uint32_t)s, chunk_area[(size_t)s * chunk + k]);
 }
 
@@ -239,8 +246,9 @@ extern "C" lc_status lc_lbvh_pairs_static(const float *tri_min, const float *tri
     launch_refit(d, st);
     launch_traverse(d, 128, st);
     scan_u32(d.pair_cnt, d.pair_off, nullptr, (uint32_t)T, (uint32_t)T, d.scan_tmp, npairs, &d.counters[0], st);
-    if (cap) k_static_compact<<<nb, kThreads, 0, st>>>(d.pair_cnt, d.pair_off, d.pair_chunk, T, chunk,
-                                                        reinterpret_cast<uint2 *>(out_pairs), cap);
+    const int nwb = (T * 32 + kThreads - 1) / kThreads;  // one warp per leaf
+    if (cap) k_static_compact<<<nwb, kThreads, 0, st>>>(d.pair_cnt, d.pair_off, d.pair_chunk, T, chunk,
+                                                         reinterpret_cast<uint2 *>(out_pairs), cap);
     if (out_sorted_ids)
         LC_STATIC_CUDA(cudaMemcpyAsync(out_sorted_ids, d.perm, sizeof(uint32_t) * T, cudaMemcpyDeviceToDevice, st));
     LC_STATIC_CUDA(cudaGetLastError());

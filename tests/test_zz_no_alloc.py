@@ -72,6 +72,32 @@ def test_static_lbvh_matches_allocating_entry_point_twice(cuda):
         assert torch.equal(ids, want_ids)
 
 
+def test_static_lbvh_capacity_overflow_keeps_to_the_buffer(cuda):
+    """cap below the pair count: the call reports LC_ERR_CAPACITY_OVERFLOW with
+    the full count, writes exactly the first cap pairs of the allocating
+    path's list and nothing past them; run on a non-default stream."""
+    torch = cuda
+    L = _ffi.lib()
+    n, chunk = 1999, 64
+    lo, hi = dense_boxes(n, 3, 0.03, 1.0)
+    lo_t = torch.from_numpy(lo).cuda()
+    hi_t = torch.from_numpy(hi).cuda()
+    want_pairs, _, want_count = allocating_query(torch, lo_t, hi_t, n, chunk, _ffi.LC_MORTON_REF63)
+    cap = want_count // 2
+    buf = torch.full((want_count, 2), -7, dtype=torch.int32, device="cuda")
+    count = C.c_uint64()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    rc = L.lc_lbvh_pairs_static(C.c_void_p(lo_t.data_ptr()), C.c_void_p(hi_t.data_ptr()), n, chunk,
+                                _ffi.LC_MORTON_REF63, C.c_void_p(buf.data_ptr()), cap, C.byref(count), None,
+                                C.c_void_p(s.cuda_stream))
+    torch.cuda.synchronize()
+    assert rc == 3, L.lc_last_error_string()
+    assert count.value == want_count
+    assert torch.equal(buf[:cap], want_pairs[:cap])
+    assert bool((buf[cap:] == -7).all()), "a pair was written past cap"
+
+
 def test_static_lbvh_rejects_sizes_beyond_its_scratch(cuda):
     torch = cuda
     L = _ffi.lib()
