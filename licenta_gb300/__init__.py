@@ -6,10 +6,10 @@ need a GPU; stepping a cloth does.
 """
 from . import _ffi
 from ._ffi import LcError, ClothParams, default_params, default_options, LC_MORTON_REF63, LC_MORTON_K30
-from .cloth import ClothBatch, ClothBatchGroup, CudaDeformableBody, Lbvh
+from .cloth import ClothBatch, ClothBatchGroup, CudaDeformableBody, Lbvh, Narrowphase
 from .scenes import ClothSpec
 
 __all__ = [
     "_ffi", "LcError", "ClothParams", "default_params", "default_options", "LC_MORTON_REF63", "LC_MORTON_K30",
-    "ClothBatch", "ClothBatchGroup", "CudaDeformableBody", "Lbvh", "ClothSpec",
+    "ClothBatch", "ClothBatchGroup", "CudaDeformableBody", "Lbvh", "Narrowphase", "ClothSpec",
 ]

@@ -391,3 +391,41 @@ class Lbvh:
             self.close()
         except Exception:
             pass
+
+
+class Narrowphase:
+    """DeformableUtils::CreateTriangleTests + CCDTriangleTests on caller data
+    (lc_narrowphase_*): VF and EE contacts of broadphase pairs, in the
+    reference's order."""
+
+    def __init__(self, max_vertices: int, max_triangles: int, max_pairs: int, candidate_capacity: int = 0,
+                 contact_capacity: int = 0):
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().lc_narrowphase_create(max_vertices, max_triangles, max_pairs, candidate_capacity,
+                                                    contact_capacity, C.byref(h)), "lc_narrowphase_create")
+        self._h = h
+
+    def run(self, x_ptr: int | None, x_prev_ptr: int, v_ptr: int | None, num_vertices: int, tri_ptr: int,
+            feat_ptr: int | None, num_triangles: int, pair_ptr: int | None, num_pairs: int, thickness: float,
+            timestep: float, vf_ptr: int | None, vf_cap: int, ee_ptr: int | None, ee_cap: int, stream=None,
+            mode: int = _ffi.LC_NARROW_CCD) -> tuple[int, int, int]:
+        """Device pointers in, PrimitiveContact records (12 words) out;
+        returns (status, VF count, EE count)."""
+        nvf, nee = C.c_uint64(), C.c_uint64()
+        vp = lambda p: None if p is None else C.c_void_p(p)
+        rc = _ffi.lib().lc_narrowphase_run(self._h, mode, vp(x_ptr), vp(x_prev_ptr), vp(v_ptr), num_vertices, vp(tri_ptr),
+                                           vp(feat_ptr), num_triangles, vp(pair_ptr), num_pairs, thickness, timestep,
+                                           vp(vf_ptr), vf_cap, vp(ee_ptr), ee_cap, C.byref(nvf), C.byref(nee),
+                                           _stream_handle(stream))
+        return rc, nvf.value, nee.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _ffi.lib().lc_narrowphase_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

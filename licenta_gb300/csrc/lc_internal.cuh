@@ -113,10 +113,13 @@ struct DevPtrs {
     uint32_t *hit_q[2];                   // VF / EE hits in any order: candidate index ...
     float4 *hit_w[2];                     // ... and contact weights (capacity vf_cap / ee_cap)
     float4 *hit_nrm;                      // VF hits: unit face normal at the hit (friction; may be null)
+    float4 *hit_tn[2];                    // VF / EE hits: unit normal (xyz) and time of contact (w), the
+                                          // PrimitiveContact n and t (full contact records; may be null)
     uint32_t *hit_n;                      // [2] hit counts of the step
     uint4 *crange;         // per cloth: [vf0, vf1) and [ee0, ee1) contact ranges
     int4 *vf_v; float4 *vf_w;   // VF contacts (ids, weights)
     float4 *vf_n;               // VF contacts: face normal at the hit (friction; may be null)
+    float4 *vf_tn, *ee_tn;      // contacts: normal and time of contact (full contact records; may be null)
     int friction_any;           // some cloth of the batch uses friction
     int4 *ee_v; float4 *ee_w;   // EE contacts
     uint64_t vf_cap, ee_cap;

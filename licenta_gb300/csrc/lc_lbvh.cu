@@ -586,7 +586,10 @@ __global__ void k_pair_compact(DevPtrs d) {
 // feature AABB cull of Collision/CudaPrimitiveTests.cu:427-490, CCD of
 // :109-238 with Physics/CudaCubicSolver.cu:5-153 and the tests at :252-425.
 // ---------------------------------------------------------------------------
-struct Wts { float w0, w1, w2, w3; float3 n; };
+// A hit's weights, normal and time (Physics::PrimitiveContact w1..w4, n, t).
+// The tests write t where the reference's do (TestVF: 0; TestEE outside the
+// segments: 0); the caller starts it at the candidate's -1.
+struct Wts { float w0, w1, w2, w3; float3 n; float t; };
 
 __device__ __forceinline__ float triple(float3 x21, float3 x31, float3 x41, float3 v21, float3 v31, float3 v41,
                                         float t) {
@@ -637,6 +640,7 @@ __device__ bool test_vf(float3 x4, float3 x1, float3 x2, float3 x3, float th, Wt
         if (between(w1, lo, hi) && between(w2, lo, hi) && between(w3, lo, hi)) {
             w.w0 = 1.f; w.w1 = -w1; w.w2 = -w2; w.w3 = -w3;
             w.n = n;
+            w.t = 0.f;
             return true;
         }
     }
@@ -650,6 +654,7 @@ __device__ bool test_ee(float3 x1, float3 x2, float3 x3, float3 x4, float th, Wt
         const float3 m1 = add(x1, dvs(x21, 2.f)), m2 = add(x3, dvs(x43, 2.f));
         if (dist(m1, m2) <= th) {
             w.w0 = w.w1 = w.w2 = w.w3 = 0.5f;
+            w.n = normalize(sub(m1, m2));
             return true;
         }
         return false;
@@ -664,6 +669,9 @@ __device__ bool test_ee(float3 x1, float3 x2, float3 x3, float3 x4, float th, Wt
         const float3 cp1 = add(x1, mul(x21, a)), cp2 = add(x3, mul(x43, a));
         if (dist(cp1, cp2) <= th) {
             w.w0 = 1.f - a; w.w1 = a; w.w2 = -(1.f - b); w.w3 = -b;
+            // the normal measures the second point with b (Collision/CudaPrimitiveTests.cu:305-307)
+            const float3 dir = sub(add(x1, mul(x21, a)), add(x3, mul(x43, b)));
+            w.n = normalize(is_zero(dir) ? crs : dir);
             return true;
         }
     } else {
@@ -681,6 +689,8 @@ __device__ bool test_ee(float3 x1, float3 x2, float3 x3, float3 x4, float th, Wt
         }
         if (dist(cp1, cp2) <= th) {
             w.w0 = 1.f - a; w.w1 = a; w.w2 = -(1.f - b); w.w3 = -b;
+            w.n = normalize(sub(cp1, cp2));
+            w.t = 0.f;
             return true;
         }
     }
@@ -735,7 +745,7 @@ __device__ __forceinline__ int4 candidate_ids(const int vid[6], int s) {
 // AABB cull (Collision/CudaPrimitiveTests.cu:240-248, 427-490).  The checks
 // commute, so the surviving set is the reference's; the six vertex boxes are
 // built once per pair.
-__device__ __forceinline__ uint16_t pair_filter(const DevPtrs &d, uint2 pr) {
+__device__ __forceinline__ uint16_t pair_filter(const DevPtrs &d, uint2 pr, bool cull) {
     const int c = d.tcloth[pr.x];
     const float h = d.cloth[c].h;
     const int4 A = d.tri_slot[pr.x], B = d.tri_slot[pr.y];
@@ -761,7 +771,7 @@ __device__ __forceinline__ uint16_t pair_filter(const DevPtrs &d, uint2 pr) {
         if (e1 == e3 || e1 == e4 || e2 == e3 || e2 == e4) continue;
         want |= 1u << (6 + s);
     }
-    if (!want) return 0;
+    if (!want || !cull) return (uint16_t)want;
     // the six vertex boxes, the two face boxes and the six edge boxes once
     // (min / max are exact, so any grouping gives the reference's boxes)
     Box bx[6];
@@ -798,14 +808,18 @@ __device__ __forceinline__ uint16_t pair_filter(const DevPtrs &d, uint2 pr) {
 // group of kPairGroup consecutive pairs (one warp iteration: the stride is a
 // whole number of warps) the group's VF and EE candidate counts, whose scans
 // give every group its first candidate; the number of groups at ngroups.
-__global__ void __launch_bounds__(kThreads, 4) k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs) {
+// cull = 0 keeps the candidates the ownership bits and the sanity checks
+// leave, without the feature AABB cull (the discrete tests of
+// Collision/CudaCollisionDetection.cu:191-221 apply none).
+__global__ void __launch_bounds__(kThreads, 4) k_narrow_filter(DevPtrs d, const uint32_t *__restrict__ npairs,
+                                                               int cull) {
     static_assert(kPairGroup == 32, "a group is one warp iteration");
     const uint32_t n = *npairs, G = (n + kPairGroup - 1) / kPairGroup;
     if (blockIdx.x == 0 && threadIdx.x == 0) *d.ngroups = G;
     const int lane = threadIdx.x & 31;
     const uint32_t end = G * kPairGroup;  // whole warps stay in the loop together (pair counts stay below 2^31)
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < end; p += gridDim.x * blockDim.x) {
-        const uint16_t m = p < n ? pair_filter(d, d.pairs[p]) : (uint16_t)0;
+        const uint16_t m = p < n ? pair_filter(d, d.pairs[p], cull != 0) : (uint16_t)0;
         if (p < n) d.pair_mask[p] = m;
         const uint32_t vf = __reduce_add_sync(0xffffffffu, (unsigned)__popc((unsigned)(m & 0x3Fu)));
         const uint32_t ee = __reduce_add_sync(0xffffffffu, (unsigned)__popc((unsigned)(m >> 6)));
@@ -917,6 +931,8 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
     __shared__ CcdJob jobs[kCcdWarps][96];
     __shared__ uint8_t job_owner[kCcdWarps][96];  // lane << 2 | interval
     __shared__ float roots[kCcdWarps][3][32];
+    __shared__ float tq[kCcdWarps][6][32];        // each lane's times to test, in the reference's order
+    __shared__ int best[kCcdWarps][32];           // each lane's first hitting test (6: none)
     const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
     const int4 *list = VF ? d.cand : d.cand_e;
     // hit bits per group of 32 candidates (one warp iteration: base is a
@@ -1004,31 +1020,87 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
             roots[w][iv][own] = secant(x21, x31, x41, v21, v31, v41, jb.a, jb.b, jb.fa, jb.fb);
         }
         __syncwarp();
-        bool found = false;
+        // The ordered tests of every candidate (the reference advances the
+        // four positions by v t dt for each time in turn and tests after each
+        // advance, stopping at the first hit).  Every (candidate, time) test
+        // of the warp is a job of its own, spread evenly over the lanes: a
+        // job rebuilds its positions by the same sequence of advances and
+        // runs the same test, so it decides the same bits.  A candidate's
+        // first hit is its smallest hitting test index; its owner lane then
+        // runs that test once more for the weights.
+        int nt = 0;
+        float hq = 0.f, dtq = 0.f;
         if (valid) {
+            for (int i = 0; i <= ncp; ++i) {
+                const float a = i == 0 ? 0.f : (i == 1 ? e1 : e2);
+                if ((imm >> i) & 1u) tq[w][nt++][lane] = a;
+                if ((sec >> i) & 1u) {
+                    const float t = roots[w][i][lane];
+                    if (t != -15.f) tq[w][nt++][lane] = t;
+                }
+            }
             const ClothDev &cd = d.cloth[d.vcloth[ids.x]];
-            const int i1 = VF ? ids.y : ids.x, i2 = VF ? ids.z : ids.y, i3 = VF ? ids.w : ids.z, i4 = VF ? ids.x : ids.w;
-            float3 x1 = xyz(d.xp[i1]), x2 = xyz(d.xp[i2]), x3 = xyz(d.xp[i3]), x4 = xyz(d.xp[i4]);
-            const float3 v1 = xyz(d.v[i1]), v2 = xyz(d.v[i2]), v3 = xyz(d.v[i3]), v4 = xyz(d.v[i4]);
-            const float h = cd.h, dt = cd.dt;
-            Wts wt;
-            auto hit = [&](float t) {
-                const float tt = t * dt;
+            hq = cd.h;
+            dtq = cd.dt;
+        }
+        best[w][lane] = 6;
+        uint32_t ex = (uint32_t)nt;  // inclusive scan of the test counts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(full, ex, o);
+            if (lane >= o) ex += t;
+        }
+        const uint32_t ntests = __shfl_sync(full, ex, 31);
+        ex -= (uint32_t)nt;
+        __syncwarp();
+        // the four vertices of a candidate in test order (VF: face x1 x2 x3, vertex x4)
+        auto corners = [&](const int4 c, float3 &x1, float3 &x2, float3 &x3, float3 &x4, float3 &v1, float3 &v2,
+                           float3 &v3, float3 &v4) {
+            const int i1 = VF ? c.y : c.x, i2 = VF ? c.z : c.y, i3 = VF ? c.w : c.z, i4 = VF ? c.x : c.w;
+            x1 = xyz(d.xp[i1]); x2 = xyz(d.xp[i2]); x3 = xyz(d.xp[i3]); x4 = xyz(d.xp[i4]);
+            v1 = xyz(d.v[i1]); v2 = xyz(d.v[i2]); v3 = xyz(d.v[i3]); v4 = xyz(d.v[i4]);
+        };
+        // test m of lane L's candidate: the advances by its times 0..m, then the test
+        auto run_test = [&](const int4 c, int L, int m, float h, float dt, Wts &wt) {
+            float3 x1, x2, x3, x4, v1, v2, v3, v4;
+            corners(c, x1, x2, x3, x4, v1, v2, v3, v4);
+            float tt = 0.f;
+            for (int k = 0; k <= m; ++k) {
+                tt = tq[w][k][L] * dt;
                 x1 = add(x1, mul(v1, tt));
                 x2 = add(x2, mul(v2, tt));
                 x3 = add(x3, mul(v3, tt));
                 x4 = add(x4, mul(v4, tt));
-                if (!VF && ee_far(x1, x2, x3, x4, h)) return false;
-                return VF ? test_vf(x4, x1, x2, x3, h, wt) : test_ee(x1, x2, x3, x4, h, wt);
-            };
-            for (int i = 0; i <= ncp && !found; ++i) {
-                const float a = i == 0 ? 0.f : (i == 1 ? e1 : e2);
-                if (((imm >> i) & 1u) && hit(a)) { found = true; break; }
-                if ((sec >> i) & 1u) {
-                    const float t = roots[w][i][lane];
-                    if (t != -15.f && hit(t)) { found = true; break; }
-                }
             }
+            if (!VF && ee_far(x1, x2, x3, x4, h)) return false;
+            const bool r = VF ? test_vf(x4, x1, x2, x3, h, wt) : test_ee(x1, x2, x3, x4, h, wt);
+            wt.t = tt;  // the contact's time (Collision/CudaPrimitiveTests.cu:174, 228)
+            return r;
+        };
+        for (uint32_t j0 = 0; j0 < ntests; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            int L = 0;  // owner: the last lane whose first test is <= j
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int cand = L + step;
+                const uint32_t e = __shfl_sync(full, ex, cand & 31);
+                if (cand < 32 && e <= j) L = cand;
+            }
+            const uint32_t exL = __shfl_sync(full, ex, L);
+            const int4 c = make_int4(__shfl_sync(full, ids.x, L), __shfl_sync(full, ids.y, L),
+                                     __shfl_sync(full, ids.z, L), __shfl_sync(full, ids.w, L));
+            const float h = __shfl_sync(full, hq, L), dt = __shfl_sync(full, dtq, L);
+            if (j < ntests) {
+                const int m = (int)(j - exL);
+                Wts wt;
+                if (run_test(c, L, m, h, dt, wt)) atomicMin(&best[w][L], m);
+            }
+        }
+        __syncwarp();
+        bool found = false;
+        Wts wt;
+        if (valid && best[w][lane] < 6) found = run_test(ids, lane, best[w][lane], hq, dtq, wt);
+        if (valid) {
             if (found) {
                 // the contact's weights, placed at its final index by k_ccd_emit
                 const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
@@ -1037,6 +1109,7 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
                     d.hit_q[VF ? 0 : 1][slot] = q;
                     d.hit_w[VF ? 0 : 1][slot] = make_float4(wt.w0, wt.w1, wt.w2, wt.w3);
                     if (VF && d.hit_nrm) d.hit_nrm[slot] = make_float4(wt.n.x, wt.n.y, wt.n.z, 0.f);
+                    if (d.hit_tn[VF ? 0 : 1]) d.hit_tn[VF ? 0 : 1][slot] = make_float4(wt.n.x, wt.n.y, wt.n.z, wt.t);
                 } else {
                     atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
                 }
@@ -1048,6 +1121,51 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
             hcnt[base / 32] = (uint32_t)__popc(hb);
         }
         __syncwarp();
+    }
+}
+
+// The discrete tests (CudaPrimitiveTests::DCDTriangleTests,
+// Collision/CudaPrimitiveTests.cu:21-94): one TestVF / TestEE of every
+// candidate at x_prev, as HandleCollisionsDiscrete passes the previous
+// positions (Physics/CudaDeformableBody.cpp:428).  Hits are recorded as the
+// continuous kernel records them (per group of 32 candidates: the hit bits;
+// k_ccd_emit places them), with t as the tests leave it.
+template <bool VF>
+__global__ void __launch_bounds__(kThreads) k_dcd_warp(DevPtrs d, const uint32_t *__restrict__ ncand) {
+    const uint32_t n = (uint32_t)min((uint64_t)*ncand, d.cand_cap);
+    const int4 *list = VF ? d.cand : d.cand_e;
+    uint32_t *hmask = d.hitg_mask[VF ? 0 : 1], *hcnt = d.hitg_cnt[VF ? 0 : 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.hitg_n[VF ? 0 : 1] = (n + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warp0 * 32u; base < n; base += nwarps * 32u) {
+        const uint32_t q = base + lane;
+        bool found = false;
+        if (q < n) {
+            const int4 ids = list[q];
+            const float h = d.cloth[d.vcloth[ids.x]].h;
+            Wts wt;
+            wt.t = -1.f;  // the candidate's initial time (Physics/Structs.h:122-124)
+            found = VF ? test_vf(xyz(d.xp[ids.x]), xyz(d.xp[ids.y]), xyz(d.xp[ids.z]), xyz(d.xp[ids.w]), h, wt)
+                       : test_ee(xyz(d.xp[ids.x]), xyz(d.xp[ids.y]), xyz(d.xp[ids.z]), xyz(d.xp[ids.w]), h, wt);
+            if (found) {
+                const uint64_t cap = VF ? d.vf_cap : d.ee_cap;
+                const uint32_t slot = atomicAdd(&d.hit_n[VF ? 0 : 1], 1u);
+                if (slot < cap) {
+                    d.hit_q[VF ? 0 : 1][slot] = q;
+                    d.hit_w[VF ? 0 : 1][slot] = make_float4(wt.w0, wt.w1, wt.w2, wt.w3);
+                    if (d.hit_tn[VF ? 0 : 1])
+                        d.hit_tn[VF ? 0 : 1][slot] = make_float4(wt.n.x, wt.n.y, wt.n.z, wt.t);
+                } else {
+                    atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
+                }
+            }
+        }
+        const unsigned hb = __ballot_sync(0xffffffffu, found);
+        if (lane == 0) {
+            hmask[base / 32] = hb;
+            hcnt[base / 32] = (uint32_t)__popc(hb);
+        }
     }
 }
 
@@ -1077,8 +1195,12 @@ __global__ void k_ccd_emit(DevPtrs d) {
                 d.vf_v[o] = list[q];
                 d.vf_w[o] = d.hit_w[0][k];
                 if (d.vf_n) d.vf_n[o] = d.hit_nrm[k];
+                if (d.vf_tn) d.vf_tn[o] = d.hit_tn[0][k];
+            } else {
+                d.ee_v[o] = list[q];
+                d.ee_w[o] = d.hit_w[1][k];
+                if (d.ee_tn) d.ee_tn[o] = d.hit_tn[1][k];
             }
-            else { d.ee_v[o] = list[q]; d.ee_w[o] = d.hit_w[1][k]; }
         } else {
             atomicOr(d.err, VF ? ERR_VF_OVERFLOW : ERR_EE_OVERFLOW);
         }
@@ -1149,7 +1271,14 @@ void launch_pair_compact(const DevPtrs &d, cudaStream_t st) {
 }
 void launch_narrow(const DevPtrs &d, const uint32_t *npairs, const uint32_t *ncv, const uint32_t *nce, int grid,
                    int stage, cudaStream_t st) {
-    if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs);
+    if (stage == 0) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs, 1);
+    else if (stage == 6) k_narrow_filter<<<grid, kThreads, 0, st>>>(d, npairs, 0);  // no feature AABB cull
+    else if (stage == 7) {
+        cudaMemsetAsync(d.hit_n, 0, 2 * sizeof(uint32_t), st);
+        k_dcd_warp<true><<<grid, kThreads, 0, st>>>(d, ncv);
+    } else if (stage == 8) {
+        k_dcd_warp<false><<<grid, kThreads, 0, st>>>(d, nce);
+    }
     else if (stage == 1) k_narrow_expand<<<grid, kThreads, 0, st>>>(d, npairs);
     else if (stage == 2) {
         cudaMemsetAsync(d.hit_n, 0, 2 * sizeof(uint32_t), st);

@@ -335,6 +335,83 @@ struct Contact {
     float w[4];
 };
 
+// Physics::PrimitiveContact (Physics/Structs.h:106-129): ids, weights, time
+// of contact and unit normal, as the continuous and discrete tests leave them.
+struct ContactFull {
+    int v[4];
+    float w[4];
+    float t;
+    float n[3];
+};
+
+// CudaDeformableBody::SolveCollisions (Physics/CudaDeformableBody.cpp:523-548):
+// DeformableUtils::CreateImpulses then ApplyImpulses
+// (Collision/CudaCollisionResponse.cu:11-300), in float as the reference.
+// positions = x_prev (the reference passes m_dPrevPositions), velocities v;
+// on return v holds the velocities after the impulses and x the new
+// positions x_prev + v dt of every vertex that is not fixed (fixed vertices
+// keep both).  Each contact writes four impulses (its vertices, weights
+// times the impulse along its normal), the VF contacts first; they are
+// grouped by vertex with a stable sort (CUB's radix sort, unique result) and
+// summed per vertex in that order, then divided by the vertex's impulse
+// count.  AccumulateImpulses is launched over the contact count's grid,
+// ceil(contacts / 256) * 256 threads, one per run of equal vertex ids: the
+// runs past that many (vertices ranked by id) are never accumulated and get
+// no impulse (:132-136, the grid is not recomputed for the runs).
+inline void solve_collisions(std::vector<V3<float>> &x, const std::vector<V3<float>> &xp, std::vector<V3<float>> &v,
+                             const std::vector<u8> &fixed, const std::vector<ContactFull> &vf,
+                             const std::vector<ContactFull> &ee, float stiffness, float mass, float dt, float h) {
+    using V = V3<float>;
+    const size_t Vn = v.size(), C = vf.size() + ee.size();
+    std::vector<V> acc(Vn, mk<float>(0, 0, 0));
+    if (C) {
+        std::vector<std::pair<u32, V>> imp(4 * C);
+        for (size_t id = 0; id < C; ++id) {
+            const bool isvf = id < vf.size();
+            const ContactFull &c = isvf ? vf[id] : ee[id - vf.size()];
+            V vr;
+            if (isvf) {  // :179-189
+                V cv1 = v[c.v[0]] * c.w[0];
+                V cv2 = v[c.v[1]] * c.w[1] + v[c.v[2]] * c.w[2] + v[c.v[3]] * c.w[3];
+                vr = cv1 + cv2;
+            } else {     // :191-201
+                V cv1 = v[c.v[0]] * c.w[0] + v[c.v[1]] * c.w[1];
+                V cv2 = v[c.v[2]] * c.w[2] + v[c.v[3]] * c.w[3];
+                vr = cv1 + cv2;
+            }
+            // _CreateImpulse, :203-254
+            const V n = mk<float>(c.n[0], c.n[1], c.n[2]);
+            const V p = xp[c.v[0]] * c.w[0] + xp[c.v[1]] * c.w[1] + xp[c.v[2]] * c.w[2] + xp[c.v[3]] * c.w[3];
+            const float d = h - dot(p, n);
+            const float vn = dot(vr, n);
+            const float dts = (0.1f * d) / dt;
+            float i = 0.f;
+            if (vn < dts) i = -std::fmin(dt * stiffness * d, mass * (dts - vn));
+            if (vn < 0) i += mass * vn * 0.5f;
+            i = std::fmin(std::fmax(-mass * 0.1f * h, i), mass * 0.1f * h);
+            const float ip = (2 * i) / (c.w[0] * c.w[0] + c.w[1] * c.w[1] + c.w[2] * c.w[2] + c.w[3] * c.w[3]);
+            const V ipv = n * ip;
+            for (int k = 0; k < 4; ++k) imp[4 * id + k] = {(u32)c.v[k], ipv * c.w[k]};
+        }
+        std::stable_sort(imp.begin(), imp.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        const size_t threads = (C + 255) / 256 * 256;
+        size_t run = 0;
+        for (size_t s = 0; s < imp.size(); ++run) {
+            size_t e = s;
+            V sum = mk<float>(0, 0, 0);
+            while (e < imp.size() && imp[e].first == imp[s].first) sum = sum + imp[e++].second;
+            if (run < threads) acc[imp[s].first] = sum / (float)(int)(e - s);
+            s = e;
+        }
+    }
+    // ApplyImpulses, :262-300
+    for (size_t i = 0; i < Vn; ++i) {
+        if (fixed[i]) continue;
+        v[i] = v[i] + acc[i] / mass;
+        x[i] = xp[i] + v[i] * dt;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The cloth: state + one FixedUpdate (Physics/CudaDeformableBody.cpp:550-627).
 // ---------------------------------------------------------------------------
@@ -784,20 +861,23 @@ template <class R> class Cloth {
         return false;
     }
     // Collision/CudaPrimitiveTests.cu:408-425
-    static bool test_edge_degenerate(V x1, V x3, V x21, V x43, Contact &c, R th) {
+    // nout, tout (optional): the contact's normal and, where the reference's
+    // test writes it, its time (Physics::PrimitiveContact n and t).
+    static bool test_edge_degenerate(V x1, V x3, V x21, V x43, Contact &c, R th, V *nout = nullptr) {
         V m1 = x1 + x21 / R(2), m2 = x3 + x43 / R(2);
         if (dist(m1, m2) <= th) {
             c.w[0] = c.w[1] = c.w[2] = c.w[3] = 0.5f;
+            if (nout) *nout = normalize(m1 - m2);
             return true;
         }
         return false;
     }
     // Collision/CudaPrimitiveTests.cu:252-346 (the in-range branch measures
     // cp2 with a, not b, as the reference does).
-    static bool test_ee(V x1, V x2, V x3, V x4, Contact &c, R th) {
+    static bool test_ee(V x1, V x2, V x3, V x4, Contact &c, R th, V *nout = nullptr, R *tout = nullptr) {
         V x21 = x2 - x1, x31 = x3 - x1, x43 = x4 - x3;
         V crs = cross(x21, x43);
-        if (len(crs) < R(kEpsEE)) return test_edge_degenerate(x1, x3, x21, x43, c, th);
+        if (len(crs) < R(kEpsEE)) return test_edge_degenerate(x1, x3, x21, x43, c, th, nout);
         if (is_zero(crs)) return false;
         R dt = dot(-x21, x43);
         R m11 = dot(x21, x21), m12 = dt, m21 = dt, m22 = dot(x43, x43);
@@ -808,6 +888,10 @@ template <class R> class Cloth {
             V cp1 = x1 + a * x21, cp2 = x3 + a * x43;
             if (dist(cp1, cp2) <= th) {
                 c.w[0] = (float)(R(1) - a); c.w[1] = (float)a; c.w[2] = (float)(-(R(1) - b)); c.w[3] = (float)(-b);
+                if (nout) {
+                    V dir = (x1 + a * x21) - (x3 + b * x43);  // with b here (:305)
+                    *nout = normalize(is_zero(dir) ? crs : dir);
+                }
                 return true;
             }
         } else {
@@ -824,6 +908,8 @@ template <class R> class Cloth {
             }
             if (dist(cp1, cp2) <= th) {
                 c.w[0] = (float)(R(1) - a); c.w[1] = (float)a; c.w[2] = (float)(-(R(1) - b)); c.w[3] = (float)(-b);
+                if (nout) *nout = normalize(cp1 - cp2);
+                if (tout) *tout = R(0);
                 return true;
             }
         }

@@ -305,6 +305,140 @@ int lco_grid_indices(int rows, int cols, uint32_t *out) {
 // Morton code of one point, for golden-vector checks of the encoder.
 uint64_t lco_morton(float x, float y, float z, int mode) { return morton3d(x, y, z, mode); }
 
+// The narrowphase on caller data, with full contact records: for every pair
+// (triangle i, triangle j) the candidates of CreateTriangleTests
+// (Collision/CudaCollisionDetection.cu:53-189) in slot order, then
+//   mode 0 (CCDTriangleTests, :223-283): the feature AABB cull on the swept
+//     vertex boxes of x and x_prev (Collision/FeatureList.cu:134-162,
+//     Collision/CudaPrimitiveTests.cu:427-490), the sanity checks and the
+//     continuous tests on x_prev and v over dt (:128-238), t = the hit's
+//     coplanarity time times dt;
+//   mode 1 (DCDTriangleTests, :21-94): the sanity checks and one TestVF /
+//     TestEE at x_prev, t as those tests leave it (0, or the candidate's -1
+//     where TestEE does not write it).
+// Contacts go out as PrimitiveContact records, at most cap of each kind.
+int lco_narrow_contacts(int mode, const float *x, const float *xp, const float *v, int V, const uint32_t *tris,
+                        const uint8_t *feats, int T, const uint32_t *pairs, uint64_t P, float h, float dt,
+                        ContactFull *vf_out, uint64_t vf_cap, uint64_t *nvf, ContactFull *ee_out, uint64_t ee_cap,
+                        uint64_t *nee) {
+    using Cl = Cloth<float>;
+    using V3f = V3<float>;
+    if (!x || !xp || !v || !tris || V < 1 || T < 1 || (P && !pairs) || (mode != 0 && mode != 1)) return LC_ERR_INVALID_ARG;
+    for (int t = 0; t < 3 * T; ++t)
+        if (tris[t] >= (uint32_t)V) return LC_ERR_INVALID_ARG;
+    for (uint64_t q = 0; q < 2 * P; ++q)
+        if (pairs[q] >= (uint32_t)T) return LC_ERR_INVALID_ARG;
+    auto ld = [](const float *a, int i) { return mk<float>(a[3 * i], a[3 * i + 1], a[3 * i + 2]); };
+    std::vector<V3f> pmin(V), pmax(V);
+    for (int i = 0; i < V; ++i) {
+        pmin[i] = subc(vmin(ld(x, i), ld(xp, i)), h);
+        pmax[i] = addc(vmax(ld(x, i), ld(xp, i)), h);
+    }
+    uint64_t kv = 0, ke = 0;
+    auto emit = [](ContactFull *out, uint64_t cap, uint64_t &k, const Contact &c, float t, V3f n) {
+        if (k < cap) {
+            ContactFull &o = out[k];
+            for (int j = 0; j < 4; ++j) { o.v[j] = c.v[j]; o.w[j] = c.w[j]; }
+            o.t = t; o.n[0] = n.x; o.n[1] = n.y; o.n[2] = n.z;
+        }
+        ++k;
+    };
+    static const int ea_v[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    static const int ea_bit[3] = {2, 0, 1};
+    for (uint64_t q = 0; q < P; ++q) {
+        const uint32_t ta = pairs[2 * q], tb = pairs[2 * q + 1];
+        const int A[3] = {(int)tris[3 * ta], (int)tris[3 * ta + 1], (int)tris[3 * ta + 2]};
+        const int B[3] = {(int)tris[3 * tb], (int)tris[3 * tb + 1], (int)tris[3 * tb + 2]};
+        const uint8_t fa = feats ? feats[ta] : 0x3F, fb = feats ? feats[tb] : 0x3F;
+        for (int s = 0; s < 6; ++s) {
+            const int *P1 = s < 3 ? A : B, *F1 = s < 3 ? B : A;
+            if (!(((s < 3 ? fa : fb) >> (5 - s % 3)) & 1)) continue;
+            Contact c;
+            c.v[0] = P1[s % 3]; c.v[1] = F1[0]; c.v[2] = F1[1]; c.v[3] = F1[2];
+            c.w[0] = c.w[1] = c.w[2] = c.w[3] = -1.f;
+            if (mode == 0) {
+                V3f tmin = min3(pmin[c.v[1]], pmin[c.v[2]], pmin[c.v[3]]);
+                V3f tmax = max3(pmax[c.v[1]], pmax[c.v[2]], pmax[c.v[3]]);
+                if (!overlap(pmin[c.v[0]], pmax[c.v[0]], tmin, tmax)) continue;
+            }
+            if (c.v[0] == c.v[1] || c.v[0] == c.v[2] || c.v[0] == c.v[3]) continue;
+            V3f x4 = ld(xp, c.v[0]), x1 = ld(xp, c.v[1]), x2 = ld(xp, c.v[2]), x3 = ld(xp, c.v[3]);
+            V3f n = mk<float>(-1.f, -1.f, -1.f);
+            if (mode == 1) {
+                if (Cl::test_vf(x4, x1, x2, x3, c, h, &n)) emit(vf_out, vf_cap, kv, c, 0.f, n);
+                continue;
+            }
+            V3f v4 = ld(v, c.v[0]), v1 = ld(v, c.v[1]), v2 = ld(v, c.v[2]), v3 = ld(v, c.v[3]);
+            float times[8];
+            const int nt = Cl::coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+            for (int i = 0; i < nt; ++i) {
+                const float t = times[i] * dt;
+                x4 = x4 + v4 * t; x1 = x1 + v1 * t; x2 = x2 + v2 * t; x3 = x3 + v3 * t;
+                if (Cl::test_vf(x4, x1, x2, x3, c, h, &n)) { emit(vf_out, vf_cap, kv, c, t, n); break; }
+            }
+        }
+        for (int s = 0; s < 9; ++s) {
+            const int ia = s % 3, ib = s / 3;
+            if (!(((fa >> ea_bit[ia]) & 1) & ((fb >> ea_bit[ib]) & 1))) continue;
+            Contact c;
+            c.v[0] = A[ea_v[ia][0]]; c.v[1] = A[ea_v[ia][1]];
+            c.v[2] = B[ea_v[ib][0]]; c.v[3] = B[ea_v[ib][1]];
+            c.w[0] = c.w[1] = c.w[2] = c.w[3] = -1.f;
+            if (mode == 0) {
+                V3f e1min = vmin(pmin[c.v[0]], pmin[c.v[1]]), e1max = vmax(pmax[c.v[0]], pmax[c.v[1]]);
+                V3f e2min = vmin(pmin[c.v[2]], pmin[c.v[3]]), e2max = vmax(pmax[c.v[2]], pmax[c.v[3]]);
+                if (!overlap(e1min, e1max, e2min, e2max)) continue;
+            }
+            if (c.v[0] == c.v[2] || c.v[0] == c.v[3] || c.v[1] == c.v[2] || c.v[1] == c.v[3]) continue;
+            V3f x1 = ld(xp, c.v[0]), x2 = ld(xp, c.v[1]), x3 = ld(xp, c.v[2]), x4 = ld(xp, c.v[3]);
+            V3f n = mk<float>(-1.f, -1.f, -1.f);
+            if (mode == 1) {
+                float t = -1.f;
+                if (Cl::test_ee(x1, x2, x3, x4, c, h, &n, &t)) emit(ee_out, ee_cap, ke, c, t, n);
+                continue;
+            }
+            V3f v1 = ld(v, c.v[0]), v2 = ld(v, c.v[1]), v3 = ld(v, c.v[2]), v4 = ld(v, c.v[3]);
+            float times[8];
+            const int nt = Cl::coplanarity_times(x1, x2, x3, x4, v1, v2, v3, v4, times);
+            for (int i = 0; i < nt; ++i) {
+                const float t = times[i] * dt;
+                x1 = x1 + v1 * t; x2 = x2 + v2 * t; x3 = x3 + v3 * t; x4 = x4 + v4 * t;
+                if (Cl::test_ee(x1, x2, x3, x4, c, h, &n)) { emit(ee_out, ee_cap, ke, c, t, n); break; }
+            }
+        }
+    }
+    if (nvf) *nvf = kv;
+    if (nee) *nee = ke;
+    return LC_OK;
+}
+
+// CudaDeformableBody::SolveCollisions on caller data (lco::solve_collisions):
+// x (out), x_prev, v (in/out) 3 floats per vertex, fixed flags, contacts as
+// PrimitiveContact records (12 words each).
+int lco_solve_collisions(float *x, const float *xp, float *v, const uint8_t *fixed, int V, const ContactFull *vf,
+                         uint64_t nvf, const ContactFull *ee, uint64_t nee, float stiffness, float mass, float dt,
+                         float h) {
+    if (!x || !xp || !v || !fixed || V < 1 || (nvf && !vf) || (nee && !ee)) return LC_ERR_INVALID_ARG;
+    std::vector<V3<float>> X(V), XP(V), VV(V);
+    for (int i = 0; i < V; ++i) {
+        X[i] = mk<float>(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+        XP[i] = mk<float>(xp[3 * i], xp[3 * i + 1], xp[3 * i + 2]);
+        VV[i] = mk<float>(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    }
+    std::vector<u8> F(fixed, fixed + V);
+    std::vector<ContactFull> A(vf, vf + nvf), B(ee, ee + nee);
+    for (const auto *L : {&A, &B})
+        for (const auto &c : *L)
+            for (int k = 0; k < 4; ++k)
+                if (c.v[k] < 0 || c.v[k] >= V) return LC_ERR_INVALID_ARG;
+    solve_collisions(X, XP, VV, F, A, B, stiffness, mass, dt, h);
+    for (int i = 0; i < V; ++i) {
+        x[3 * i] = X[i].x; x[3 * i + 1] = X[i].y; x[3 * i + 2] = X[i].z;
+        v[3 * i] = VV[i].x; v[3 * i + 1] = VV[i].y; v[3 * i + 2] = VV[i].z;
+    }
+    return LC_OK;
+}
+
 // The LBVH chain over caller boxes that the engine's standalone entry points
 // (lc_lbvh_build + lc_lbvh_pairs) run: Morton code of each box's midpoint
 // min + (max - min) / 2 (identity frame, Core/CudaUtils.cu:278-325), a stable

@@ -64,6 +64,11 @@ def lib() -> C.CDLL:
             "lco_friction_on": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
             "lco_solve_decisions": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
             "lco_collide_all": (C.c_int, [VP, C.c_int]),
+            "lco_solve_collisions": (C.c_int, [VP, VP, VP, VP, C.c_int, VP, C.c_uint64, VP, C.c_uint64, C.c_float,
+                                               C.c_float, C.c_float, C.c_float]),
+            "lco_narrow_contacts": (C.c_int, [C.c_int, VP, VP, VP, C.c_int, VP, VP, C.c_int, VP, C.c_uint64,
+                                              C.c_float, C.c_float, VP, C.c_uint64, C.POINTER(C.c_uint64), VP,
+                                              C.c_uint64, C.POINTER(C.c_uint64)]),
             "lco_step_frozen_all": (C.c_int, [VP, C.c_int]),
             "lco_lbvh_boxes": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int] + [VP] * 8 +
                                [C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -380,6 +385,39 @@ def lbvh_boxes(bmin, bmax, chunk: int = 64, mode: int = 0) -> dict:
          "lbvh_boxes")
     out["PAIRS"] = pairs
     return out
+
+
+def solve_collisions(x, x_prev, v, fixed, vf, ee, *, stiffness: float, vertex_mass: float, dt: float,
+                     thickness: float):
+    """CudaDeformableBody::SolveCollisions restated (float): x, x_prev, v
+    (V, 3); fixed (V,) flags; vf, ee (N, 12) PrimitiveContact records.
+    Returns the new positions and velocities."""
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 3).copy()
+    xp = np.ascontiguousarray(x_prev, np.float32).reshape(-1, 3)
+    vel = np.ascontiguousarray(v, np.float32).reshape(-1, 3).copy()
+    fx = np.ascontiguousarray(fixed, np.uint8).reshape(-1)
+    a = np.ascontiguousarray(vf, np.int32).reshape(-1, 12)
+    b = np.ascontiguousarray(ee, np.int32).reshape(-1, 12)
+    _chk(lib().lco_solve_collisions(_p(x), _p(xp), _p(vel), _p(fx), x.shape[0], _p(a), len(a), _p(b), len(b),
+                                    stiffness, vertex_mass, dt, thickness), "solve_collisions")
+    return x, vel
+
+
+def narrow_contacts(mode: int, x, x_prev, v, triangles, features, pairs, thickness: float, dt: float):
+    """The narrowphase restated on caller data (mode 0: continuous tests,
+    1: discrete tests at x_prev), as (N, 12) PrimitiveContact records."""
+    xs = [np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (x, x_prev, v)]
+    tris = np.ascontiguousarray(triangles, np.uint32).reshape(-1, 3)
+    feats = np.ascontiguousarray(features, np.uint8).reshape(-1)
+    pr = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
+    nvf, nee = C.c_uint64(), C.c_uint64()
+    args = lambda a, ca, b, cb: (mode, _p(xs[0]), _p(xs[1]), _p(xs[2]), xs[1].shape[0], _p(tris), _p(feats),
+                                 len(tris), _p(pr), len(pr), thickness, dt, a, ca, C.byref(nvf), b, cb, C.byref(nee))
+    _chk(lib().lco_narrow_contacts(*args(None, 0, None, 0)), "narrow_contacts")
+    vf = np.zeros((nvf.value, 12), np.int32)
+    ee = np.zeros((nee.value, 12), np.int32)
+    _chk(lib().lco_narrow_contacts(*args(_p(vf), len(vf), _p(ee), len(ee))), "narrow_contacts")
+    return vf, ee
 
 
 def morton(x: float, y: float, z: float, mode: int = 0) -> int:

@@ -60,6 +60,7 @@ SOURCES = [
     "Collision/CudaPrimitiveTests.cu",
     "Collision/FeatureList.cu",
     "Collision/CudaCollisionDetection.cu",
+    "Collision/CudaCollisionResponse.cu",
     "Physics/CudaDeformableUtils.cu",
     "Physics/CudaPBD.cu",
 ]

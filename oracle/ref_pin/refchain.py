@@ -19,6 +19,11 @@ shapes of the reference's host code:
   DeformableUtils::CreateTriangleTests  Collision/CudaCollisionDetection.cu:6-51
   DeformableUtils::CCDTriangleTests     Collision/CudaCollisionDetection.cu:223-283
 
+and, for the other half of the step, the prediction (PBDStepExternal with
+UpdateVertexNormals), the solver (PBDStepSolver, PBDStepIntegration),
+friction (ApplyFriction), the impulse response (SolveCollisions) and the
+discrete triangle tests of HandleCollisionsDiscrete.
+
 Two host-side steps stand in for the reference's CUB calls: the stable radix
 sort of (Morton code, triangle) pairs (Core/CubWrappers.cuh:141-156) is a
 stable host sort of the same keys, whose result is unique, and
@@ -82,6 +87,13 @@ KERNELS = {
     "inertia": "ComputeIs",
     "update_vels": "UpdateVels",
     "euler": "ExplicitEuler",
+    # SolveCollisions (Physics/CudaDeformableBody.cpp:523-548) with
+    # Collision/CudaCollisionResponse.cu:11-300, and the discrete tests of
+    # HandleCollisionsDiscrete (Collision/CudaPrimitiveTests.cu:21-94)
+    "create_impulses": "_CreateImpulses",
+    "accumulate_impulses": "AccumulateImpulses",
+    "apply_impulses": "ApplyImpulses",
+    "dcd_tests": "DCDTriangleTests",
     # DeformableUtils::UpdateVertexNormals (Physics/CudaDeformableUtils.cu:190-249)
     "create_vns": "CreateVNs",
     "accumulate_vns": "AccumulateVNs",
@@ -439,6 +451,93 @@ class RefKernels:
         out["vf"] = vf[vff[:nvf].bool()].cpu().numpy()
         out["ee"] = ee[eef[:nee].bool()].cpu().numpy()
         return out
+
+    # ------------------------------------------------------------------
+    def solve_collisions(self, x, x_prev, v, fixed, vf, ee, *, stiffness: float, vertex_mass: float, dt: float,
+                         thickness: float) -> dict:
+        """CudaDeformableBody::SolveCollisions with the reference's kernels:
+        CreateImpulses (Collision/CudaCollisionResponse.cu:11-140: the
+        accumulators cleared, _CreateImpulses over the contacts, the CUB
+        stable sort by vertex id, run-length encoding and exclusive sum of the
+        counts on the host, AccumulateImpulses launched over the contacts'
+        grid as the reference launches it) then ApplyImpulses (:262-300).
+        x, x_prev, v: (V, 3) float32 positions, previous positions and
+        velocities (the reference passes m_dPrevPositions as the impulses'
+        positions; a fixed vertex keeps x); fixed: (V,) flags; vf, ee: (N, 12) int32
+        PrimitiveContact records.  Returns the new positions ``x``, the
+        velocities ``v`` and the accumulated impulses."""
+        torch = self.torch
+        f32, i32 = np.float32, np.int32
+        xp = np.ascontiguousarray(x_prev, f32)
+        V = xp.shape[0]
+        vel = np.ascontiguousarray(v, f32).reshape(V, 3)
+        vf = np.ascontiguousarray(vf, i32).reshape(-1, 12)
+        ee = np.ascontiguousarray(ee, i32).reshape(-1, 12)
+        for c in (vf, ee):
+            if len(c) and (c[:, :4].min() < 0 or c[:, :4].max() >= V):
+                raise ValueError("contact vertex out of range")
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        d_xp, d_v = dev(xp), dev(vel)
+        d_x = dev(np.ascontiguousarray(x, f32).reshape(V, 3))
+        acc = torch.zeros((V, 3), dtype=torch.float32, device="cuda")
+        nvf, nee = len(vf), len(ee)
+        C_ = nvf + nee
+        if C_:
+            ids = torch.zeros(4 * C_, dtype=torch.int32, device="cuda")
+            vals = torch.zeros((4 * C_, 3), dtype=torch.float32, device="cuda")
+            flags = torch.zeros(4 * C_, dtype=torch.uint8, device="cuda")
+            self.launch("create_impulses", C_, d_xp, d_v, dev(vf if nvf else np.zeros((1, 12), i32)), C.c_uint64(nvf),
+                        dev(ee if nee else np.zeros((1, 12), i32)), C.c_uint64(nee), ids, vals, flags,
+                        C.c_float(stiffness), C.c_float(vertex_mass), C.c_float(dt), C.c_float(thickness))
+            torch.cuda.synchronize()
+            h_ids = ids.cpu().numpy().view(np.uint32)
+            order = np.argsort(h_ids, kind="stable")
+            sids = h_ids[order]
+            starts = np.flatnonzero(np.r_[True, sids[1:] != sids[:-1]]).astype(i32)
+            runs = len(starts)
+            blocks = (C_ + THREADS - 1) // THREADS  # the contacts' grid (:132-136)
+            self.launch("accumulate_impulses", runs, C.c_int(runs), dev(sids[starts].view(i32)), dev(starts),
+                        dev(vals.cpu().numpy()[order]), C.c_uint64(4 * C_), acc, blocks=blocks)
+        self.launch("apply_impulses", V, C.c_int(V), d_x, d_xp, d_v, acc, dev(np.asarray(fixed) != 0),
+                    C.c_float(vertex_mass), C.c_float(dt))
+        torch.cuda.synchronize()
+        return dict(x=d_x.cpu().numpy(), v=d_v.cpu().numpy(), impulses=acc.cpu().numpy())
+
+    def dcd(self, positions, triangles, features, pairs, thickness: float) -> dict:
+        """HandleCollisionsDiscrete's tests (Physics/CudaDeformableBody.cpp:
+        419-438) on given broadphase pairs: CreateTriangleTests
+        (Collision/CudaCollisionDetection.cu:6-189) then DCDTriangleTests
+        (Collision/CudaPrimitiveTests.cu:21-94: the sanity checks and TestVF /
+        TestEE at the positions, no feature AABB cull) and the compaction.
+        positions: (V, 3) float32 (the reference passes m_dPrevPositions);
+        triangles: (T, 3) in the slot order the pairs index; features: (T,)
+        their ownership bytes; pairs: (P, 2).  Returns the VF / EE contacts
+        as (N, 12) PrimitiveContact records."""
+        torch = self.torch
+        f32, i32 = np.float32, np.int32
+        pos = np.ascontiguousarray(positions, f32)
+        V = pos.shape[0]
+        tris = np.ascontiguousarray(triangles, np.int64).reshape(-1, 3)
+        T = tris.shape[0]
+        pr = np.ascontiguousarray(pairs, i32).reshape(-1, 2)
+        P = pr.shape[0]
+        if tris.min() < 0 or tris.max() >= V or (P and (pr.min() < 0 or pr.max() >= T)):
+            raise ValueError("index out of range")
+        if P == 0:
+            return dict(vf=np.zeros((0, 12), i32), ee=np.zeros((0, 12), i32))
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        tri = np.zeros((T, 7), dtype=i32)
+        tri[:, :3] = tris
+        tri[:, 3] = np.asarray(features, np.uint8).astype(i32)
+        vf = torch.zeros((6 * P, 12), dtype=torch.int32, device="cuda")
+        ee = torch.zeros((9 * P, 12), dtype=torch.int32, device="cuda")
+        vff = torch.ones(6 * P, dtype=torch.uint8, device="cuda")
+        eef = torch.ones(9 * P, dtype=torch.uint8, device="cuda")
+        self.launch("tri_tests", P, C.c_int(P), dev(tri), dev(pr), vf, vff, ee, eef)
+        self.launch("dcd_tests", 15 * P, dev(tri), dev(pos), vf, vff, C.c_uint64(6 * P), ee, eef, C.c_uint64(9 * P),
+                    C.c_float(thickness))
+        torch.cuda.synchronize()
+        return dict(vf=vf[vff.bool()].cpu().numpy(), ee=ee[eef.bool()].cpu().numpy())
 
     # ------------------------------------------------------------------
     def solve(self, x, x_prev, topo: dict, vf, ee, *, iterations: int, k_stretch: float, k_bend: float,

@@ -84,6 +84,14 @@ def main(outdir: str) -> int:
             raise ValueError("the reference always projects ground constraints: keep groundOn")
         sol = ref.solve(x, xp, vf=r["vf"], ee=r["ee"], **golden_cases.solver_inputs(spec, data, o))
         data.update({"ref_solve_" + k: sol[k] for k in ("x", "v", "x_prev", "x_end")})
+        # the reference's other pipeline on the same state: SolveCollisions
+        # (impulses from the continuous contacts, with their normals) and the
+        # discrete tests of HandleCollisionsDiscrete at x_prev on the same pairs
+        imp = ref.solve_collisions(x, xp, v, spec.pinned, r["vf"], r["ee"], **golden_cases.impulse_params(spec, h))
+        data["ref_impulse_x"], data["ref_impulse_v"] = imp["x"], imp["v"]
+        slot = perm[r["order"].astype(np.int64)]
+        dcd = ref.dcd(xp, spec.indices.astype(np.int64)[slot], feats[slot], r["pairs"], h)
+        data["ref_dcd_vf"], data["ref_dcd_ee"] = dcd["vf"], dcd["ee"]
         # friction (CudaPBD::ApplyFriction) on the solver's velocities with the
         # step's ground flags and VF contacts
         data["ref_ground"] = sol["ground"]
@@ -98,6 +106,8 @@ def main(outdir: str) -> int:
         fdiff = golden_cases.compare_oracle_friction(spec, data)
         pdiff = golden_cases.compare_oracle_prediction(spec, data)
         print(f"{case['name']}: prediction vs oracle {pdiff}")
+        print(f"{case['name']}: dcd vf={len(dcd['vf'])} ee={len(dcd['ee'])}; response and contact records vs oracle "
+              f"{golden_cases.compare_oracle_response(spec, data)}")
         print(f"{case['name']}: T={len(perm)} pairs={len(r['pairs'])} vf={len(r['vf'])} ee={len(r['ee'])} "
               f"ground={sol['ground_flags']} lra={sol['lra_flags']} solver vs FP32 oracle {sdiff} friction {fdiff} "
               f"nodes raced in the unseeded refit={raced} "

@@ -119,6 +119,42 @@ def compare_oracle_prediction(spec, d: dict) -> dict:
     return out
 
 
+def impulse_params(spec, h: float) -> dict:
+    """The arguments SolveCollisions passes (Physics/CudaDeformableBody.cpp:
+    527-535): stiffness kStretch, the vertex mass objectMass / (dims.x
+    dims.y), the timestep and the thickness."""
+    p = spec.params
+    return dict(stiffness=float(p.kStretch),
+                vertex_mass=float(np.float32(p.objectMass) / np.float32(int(p.dims[0]) * int(p.dims[1]))),
+                dt=float(p.timestep), thickness=float(h))
+
+
+def slot_order(d: dict) -> np.ndarray:
+    """Original triangle of each sorted slot: the triangle order the
+    reference's pairs index."""
+    return d["perm_before"].astype(np.int64)[d["ref_order"].astype(np.int64)]
+
+
+def compare_oracle_response(spec, d: dict) -> dict:
+    """The oracle's impulse response (SolveCollisions) and its full contact
+    records (continuous and discrete tests on the golden's pairs) against
+    the reference's: largest position / velocity differences and whether
+    every record (ids, weights, time, normal) is identical."""
+    from oracle.oracle_ffi import narrow_contacts, solve_collisions
+    h = float(d["thickness"])
+    x, v = solve_collisions(d["x"], d["x_prev"], d["v"], spec.pinned, d["ref_vf"], d["ref_ee"],
+                            **impulse_params(spec, h))
+    slot = slot_order(d)
+    tris, feats = spec.indices[slot], d["features"][slot]
+    out = dict(impulse_dx=float(np.abs(x - d["ref_impulse_x"]).max()),
+               impulse_dv=float(np.abs(v - d["ref_impulse_v"]).max()))
+    for mode, tag, kv, ke in ((0, "ccd", "ref_vf", "ref_ee"), (1, "dcd", "ref_dcd_vf", "ref_dcd_ee")):
+        vf, ee = narrow_contacts(mode, d["x"], d["x_prev"], d["v"], tris, feats, d["ref_pairs"], h, float(d["dt"]))
+        out[f"{tag}_records_equal"] = bool(np.array_equal(vf, d[kv].astype(np.int32))
+                                            and np.array_equal(ee, d[ke].astype(np.int32)))
+    return out
+
+
 def solver_inputs(spec, d: dict, oracle) -> dict:
     """Arguments of the reference's solver chain (refchain.RefKernels.solve)
     for the golden's state: the oracle's topology and the cloth's parameters."""

@@ -120,3 +120,18 @@ def test_golden_prediction_is_the_collision_input(path):
     want = (d["x_prev"] + (dt * d["v"]).astype(np.float32)).astype(np.float32)
     assert np.array_equal(want.view(np.uint32), d["x"].view(np.uint32))
     assert np.array_equal(d["x_prev"], d["pre_x_prev"])
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_oracle_contact_records_and_response_match_reference_kernels(path):
+    """The oracle's full PrimitiveContact records (ids, weights, time, normal)
+    from the continuous tests (CCDTriangleTests) and the discrete tests
+    (DCDTriangleTests of HandleCollisionsDiscrete) on the reference's pairs,
+    and its impulse response (SolveCollisions: CreateImpulses +
+    ApplyImpulses) on the reference's contacts, against the reference's
+    kernels, bit for bit."""
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    r = golden_cases.compare_oracle_response(spec, d)
+    assert r["ccd_records_equal"] and r["dcd_records_equal"], r
+    assert r["impulse_dx"] == 0.0 and r["impulse_dv"] == 0.0, r

@@ -93,3 +93,105 @@ def test_engine_prediction_matches_reference_kernels(path):
         assert dvn <= golden_cases.VN_ATOL, dvn
     finally:
         b.close()
+
+
+def _narrowphase_inputs(torch, d):
+    """The golden's collision-stage state as the narrowphase entry takes it:
+    the triangles and ownership bytes in the sorted slot order the
+    reference's pairs index, on the device."""
+    spec = golden_cases.make_spec(d["case"])
+    slot = d["perm_before"].astype(np.int64)[d["ref_order"].astype(np.int64)]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return dict(spec=spec, x=dev(d["x"]), xp=dev(d["x_prev"]), v=dev(d["v"]),
+                tris=dev(spec.indices.astype(np.uint32)[slot]), feats=dev(d["features"].astype(np.uint8)[slot]),
+                pairs=dev(d["ref_pairs"].astype(np.uint32).reshape(-1, 2)))
+
+
+@pytest.mark.parametrize("mode", ["ccd", "dcd"])
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_narrowphase_entry_matches_reference_kernels(cuda, path, mode):
+    """lc_narrowphase_run on the reference's pairs of each golden state:
+    CreateTriangleTests + CCDTriangleTests (mode ccd) or + DCDTriangleTests
+    (mode dcd, the discrete tests of HandleCollisionsDiscrete at x_prev).
+    Its VF and EE contacts must be the reference kernels' PrimitiveContact
+    records (ids, weights, time, normal) bit for bit, in the same order."""
+    torch = cuda
+    from licenta_gb300 import Narrowphase, _ffi
+    d = golden_cases.load(path)
+    a = _narrowphase_inputs(torch, d)
+    V, T, P = a["spec"].num_vertices, a["spec"].num_triangles, len(a["pairs"])
+    np_ = Narrowphase(V, T, max(P, 1))
+    cap = 15 * max(P, 1)
+    vf = torch.zeros((cap, 12), dtype=torch.int32, device="cuda")
+    ee = torch.zeros((cap, 12), dtype=torch.int32, device="cuda")
+    ccd = mode == "ccd"
+    try:
+        rc, nvf, nee = np_.run(a["x"].data_ptr() if ccd else None, a["xp"].data_ptr(),
+                               a["v"].data_ptr() if ccd else None, V, a["tris"].data_ptr(), a["feats"].data_ptr(),
+                               T, a["pairs"].data_ptr(), P, float(d["thickness"]), float(d["dt"]), vf.data_ptr(), cap,
+                               ee.data_ptr(), cap, mode=_ffi.LC_NARROW_CCD if ccd else _ffi.LC_NARROW_DCD)
+        assert rc == 0
+        refs = (d["ref_vf"], d["ref_ee"]) if ccd else (d["ref_dcd_vf"], d["ref_dcd_ee"])
+        for got, n, ref in ((vf, nvf, refs[0]), (ee, nee, refs[1])):
+            assert n == len(ref)
+            assert np.array_equal(got[:n].cpu().numpy(), ref.astype(np.int32))
+    finally:
+        np_.close()
+
+
+@pytest.mark.parametrize("path", FILES, ids=[p.stem for p in FILES])
+def test_impulse_response_entry_matches_reference_kernels(cuda, path):
+    """lc_solve_collisions (SolveCollisions: CreateImpulses + ApplyImpulses)
+    on each golden state's continuous contacts: positions and velocities
+    bit for bit against the reference's kernels."""
+    torch = cuda
+    import ctypes as C
+    from licenta_gb300 import _ffi
+    d = golden_cases.load(path)
+    spec = golden_cases.make_spec(d["case"])
+    dev = lambda arr, dt=np.float32: torch.from_numpy(np.ascontiguousarray(arr, dt)).cuda()
+    x, xp, v = dev(d["x"]), dev(d["x_prev"]), dev(d["v"])
+    fixed = dev(spec.pinned, np.uint8)
+    vf = dev(d["ref_vf"].reshape(-1, 12), np.int32)
+    ee = dev(d["ref_ee"].reshape(-1, 12), np.int32)
+    prm = golden_cases.impulse_params(spec, float(d["thickness"]))
+    vp = lambda t: C.c_void_p(t.data_ptr())
+    rc = _ffi.lib().lc_solve_collisions(vp(x), vp(xp), vp(v), vp(fixed), spec.num_vertices, vp(vf), len(d["ref_vf"]),
+                                        vp(ee), len(d["ref_ee"]), prm["stiffness"], prm["vertex_mass"], prm["dt"],
+                                        prm["thickness"], None)
+    torch.cuda.synchronize()
+    assert rc == 0, _ffi.lib().lc_last_error_string()
+    assert np.array_equal(x.cpu().numpy().view(np.uint32), d["ref_impulse_x"].view(np.uint32))
+    assert np.array_equal(v.cpu().numpy().view(np.uint32), d["ref_impulse_v"].view(np.uint32))
+
+
+def test_narrowphase_entry_reports_capacity_and_bad_indices(cuda):
+    torch = cuda
+    from licenta_gb300 import Narrowphase, _ffi
+    d = golden_cases.load(golden_cases.GOLDEN / "cloth48_k06_step45.npz")
+    a = _narrowphase_inputs(torch, d)
+    V, T, P = a["spec"].num_vertices, a["spec"].num_triangles, len(a["pairs"])
+    np_ = Narrowphase(V, T, P)
+    n_ee = len(d["ref_ee"])
+    assert n_ee > 4
+    vf = torch.zeros((len(d["ref_vf"]) + 1, 12), dtype=torch.int32, device="cuda")
+    ee = torch.full((n_ee, 12), -3, dtype=torch.int32, device="cuda")
+    try:
+        # room for half the EE contacts: the first half written, the rest untouched, full count reported
+        half = n_ee // 2
+        rc, nvf, nee = np_.run(a["x"].data_ptr(), a["xp"].data_ptr(), a["v"].data_ptr(), V, a["tris"].data_ptr(),
+                               a["feats"].data_ptr(), T, a["pairs"].data_ptr(), P, float(d["thickness"]),
+                               float(d["dt"]), vf.data_ptr(), len(vf), ee.data_ptr(), half)
+        assert rc == 3 and nee == n_ee and nvf == len(d["ref_vf"])
+        g = ee.cpu().numpy()
+        assert np.array_equal(g[:half], d["ref_ee"][:half].astype(np.int32))
+        assert np.all(g[half:] == -3)
+        # a pair index past the triangle count is reported, not followed
+        bad = a["pairs"].clone()
+        bad[P // 2, 1] = T
+        rc, _, _ = np_.run(a["x"].data_ptr(), a["xp"].data_ptr(), a["v"].data_ptr(), V, a["tris"].data_ptr(),
+                           a["feats"].data_ptr(), T, bad.data_ptr(), P, float(d["thickness"]), float(d["dt"]),
+                           vf.data_ptr(), len(vf), ee.data_ptr(), n_ee)
+        assert rc == 1 and b"out of range" in _ffi.lib().lc_last_error_string()
+    finally:
+        np_.close()
