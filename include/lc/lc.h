@@ -316,6 +316,37 @@ typedef struct lc_tuning {
 lc_status lc_batch_get_tuning(const lc_batch *b, lc_tuning *t);
 lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t);
 
+/* The autotuner: every combination of the listed values (first n_* entries
+ * of each list) that changes the launches and that the batch accepts is
+ * timed with CUDA events over `steps` steps after `warmup` steps, each from
+ * the batch's current state (saved on entry, restored before every candidate
+ * and on return); the fastest is applied.  Combinations that differ only in a
+ * value the chosen solver does not read (the Jacobi block of the on-chip
+ * solvers, the cluster size of the global-memory one, the contact mode of
+ * solvers other than 3) are timed once.  allow_variants = 0 keeps the batch's
+ * solver variant (block, grid and cluster sizes never change results; the
+ * variant sums corrections in another order).  NULL space takes
+ * lc_default_autotune_space.  The winner goes to *best with its time per
+ * step; the first trials_cap trials (configuration, ms per step) to trials,
+ * their number to *num_trials.  Allocates one state buffer for the call;
+ * waits for the device. */
+typedef struct lc_autotune_space {
+    int32_t traverse_block[8];       int32_t n_traverse_block;
+    int32_t jacobi_block[8];         int32_t n_jacobi_block;
+    int32_t narrow_blocks_per_sm[8]; int32_t n_narrow_blocks_per_sm;
+    int32_t solver_variant[3];       int32_t n_solver_variant;
+    int32_t cluster_size[4];         int32_t n_cluster_size;
+    int32_t contact_gather[2];       int32_t n_contact_gather;
+} lc_autotune_space;
+typedef struct lc_autotune_trial {
+    lc_tuning config;
+    float ms_per_step;
+} lc_autotune_trial;
+void lc_default_autotune_space(lc_autotune_space *out);
+lc_status lc_batch_autotune(lc_batch *b, const lc_autotune_space *space, int32_t steps, int32_t warmup,
+                            int32_t allow_variants, void *stream, lc_tuning *best, float *best_ms,
+                            lc_autotune_trial *trials, int32_t trials_cap, int32_t *num_trials);
+
 /* ---- differentiation (no counterpart in the reference) -------------------
  * Per-constraint stiffness of the whole batch in the global constraint order
  * (cloth 0 first; lc_batch_constraint_counts gives each cloth's share), host
@@ -378,6 +409,82 @@ lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream);
  * checks, not for a hot loop. */
 lc_status lc_lbvh_debug_get(lc_lbvh *h, int32_t what, void *dst, uint64_t cap, uint64_t *count);
 lc_status lc_lbvh_destroy(lc_lbvh *h);
+
+/* Physics::PrimitiveContact (Physics/Structs.h:106-129) as the reference's
+ * contact tests leave it: vertex ids (VF: the vertex, then the face; EE: the
+ * two edges), weights, time of contact and unit normal. */
+typedef struct lc_primitive_contact {
+    int32_t v[4];
+    float w[4];
+    float t;
+    float n[3];
+} lc_primitive_contact;
+
+/* ----- impulse response ------------------------------------------------------
+ * CudaDeformableBody::SolveCollisions (Physics/CudaDeformableBody.cpp:523-548):
+ * DeformableUtils::CreateImpulses then ApplyImpulses
+ * (Collision/CudaCollisionResponse.cu:11-300).  Every contact gives an
+ * impulse along its normal from the penetration h - n.(sum w_i x_prev_i) and
+ * the relative normal velocity, clamped and spread over its four vertices by
+ * their weights; each vertex averages the impulses it received (the
+ * reference's grid quirk kept: of the vertices with impulses, ranked by id,
+ * only the first ceil(contacts / 256) * 256 are accumulated); then every
+ * vertex that is not fixed takes v += impulse / vertex_mass and
+ * x = x_prev + v timestep.  x (out), x_prev, v (in/out): device arrays of 3
+ * floats per vertex; fixed: device flags; vf, ee: device contacts (as
+ * lc_narrowphase_run writes them; VF first in the impulse order).  Stiffness
+ * is the reference's kStretch, vertex_mass objectMass / vertex count.
+ * Allocates its scratch in stream order (cudaMallocAsync) and, when there are
+ * contacts, waits for the stream once to validate their vertex ids. */
+lc_status lc_solve_collisions(float *x, const float *x_prev, float *v, const uint8_t *fixed, int32_t num_vertices,
+                              const lc_primitive_contact *vf, uint64_t num_vf, const lc_primitive_contact *ee,
+                              uint64_t num_ee, float stiffness, float vertex_mass, float timestep, float thickness,
+                              void *stream);
+
+/* ----- narrowphase on caller data ----------------------------------------
+ * DeformableUtils::CreateTriangleTests followed by
+ * DeformableUtils::CCDTriangleTests (mode LC_NARROW_CCD) or DCDTriangleTests
+ * (mode LC_NARROW_DCD) (Collision/CudaCollisionDetection.cuh:28-46,
+ * .cu:6-51, 191-221 and 223-283): for every broadphase pair (triangle i,
+ * triangle j) the 6 vertex-face and 9 edge-edge candidates of
+ * Collision/CudaCollisionDetection.cu:101-187 that the triangles' ownership
+ * bits and the shared-vertex sanity checks keep, then
+ *   CCD: the feature AABB cull on the swept vertex boxes of x and x_prev and
+ *        the continuous tests of Collision/CudaPrimitiveTests.cu:96-238 on
+ *        x_prev and v over one timestep (t = the hit's coplanarity time
+ *        times the timestep);
+ *   DCD: one TestVF / TestEE at x_prev (Collision/CudaPrimitiveTests.cu:
+ *        21-94, the positions HandleCollisionsDiscrete passes), no cull (t as
+ *        the tests leave it: 0, or -1 where TestEE does not write it).
+ * Contacts come out in the reference's order (pair, then candidate slot), as
+ * PrimitiveContact records.
+ *
+ * A handle owns the work buffers, sized for at most max_vertices,
+ * max_triangles and max_pairs; candidate_capacity (per kind) and
+ * contact_capacity (per kind) take 0 for the defaults of lc_batch_options.
+ * lc_narrowphase_run takes device arrays: x, x_prev, v (3 floats per vertex:
+ * predicted positions, previous positions, velocities; DCD reads x_prev
+ * only, x and v may be NULL), triangles (3 vertex ids each), features (one
+ * ownership byte per triangle: bits 5..3 own its vertices v1..v3, bits 2..0
+ * its edges v1v2, v2v3, v3v1, as Physics::CudaTriangle::m_features; NULL
+ * owns everything), pairs (2 triangle indices each, i < j as the traversal
+ * emits them) and the contact outputs (device arrays of vf_cap / ee_cap
+ * records).  The full contact counts go to *vf_count / *ee_count (host); more
+ * contacts than a cap return LC_ERR_CAPACITY_OVERFLOW with the first cap
+ * written.  An index out of range returns LC_ERR_INVALID_ARG (checked on the
+ * device; the offending triangle or pair takes no part).  The call waits for
+ * its stream. */
+enum { LC_NARROW_CCD = 0, LC_NARROW_DCD = 1 };
+typedef struct lc_narrowphase lc_narrowphase;
+lc_status lc_narrowphase_create(int32_t max_vertices, int32_t max_triangles, uint64_t max_pairs,
+                                uint64_t candidate_capacity, uint64_t contact_capacity, lc_narrowphase **out);
+lc_status lc_narrowphase_run(lc_narrowphase *h, int32_t mode, const float *x, const float *x_prev, const float *v,
+                             int32_t num_vertices, const uint32_t *triangles, const uint8_t *features,
+                             int32_t num_triangles, const uint32_t *pairs, uint64_t num_pairs, float thickness,
+                             float timestep, lc_primitive_contact *vf_out, uint64_t vf_cap,
+                             lc_primitive_contact *ee_out, uint64_t ee_cap, uint64_t *vf_count, uint64_t *ee_count,
+                             void *stream);
+lc_status lc_narrowphase_destroy(lc_narrowphase *h);
 
 /* ----- allocation-free LBVH query ---------------------------------------
  * No counterpart in the reference.  The same query as lc_lbvh_create +

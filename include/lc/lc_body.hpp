@@ -10,6 +10,8 @@
  *   Update()       — publishes the positions into *verts
  *                    (Physics/CudaDeformableBody.cpp:629-638, 473-495)
  *   SetSpherePos(pos, radius)   (Physics/CudaDeformableBody.cpp:640-643)
+ *   Autotune(steps, warmup, allow_variants) — picks the launch shapes with
+ *                    the library's autotuner (no counterpart in the reference)
  *
  * VertexT is any vertex record with a `m_position` member that has float x,
  * y, z fields — Rendering::VertexFormat (glm::vec3 m_position) qualifies.
@@ -96,6 +98,19 @@ public:
     void SetSpherePos(const Vec3 &pos, float radius) {
         const float p[3] = {pos.x, pos.y, pos.z};
         check(lc_batch_set_sphere(m_batch, 0, p, radius), "lc_batch_set_sphere");
+    }
+
+    // Times the library's default space of launch shapes on the body's
+    // current state (lc_batch_autotune; the state is restored) and keeps the
+    // fastest.  With allow_variants false the solver variant stays, and the
+    // body's trajectory is bit-identical to the untuned one.
+    lc_tuning Autotune(int steps = 3, int warmup = 1, bool allow_variants = false) {
+        lc_tuning best;
+        float ms = 0.f;
+        check(lc_batch_autotune(m_batch, nullptr, steps, warmup, allow_variants ? 1 : 0, nullptr, &best, &ms,
+                                nullptr, 0, nullptr),
+              "lc_batch_autotune");
+        return best;
     }
 
     lc_batch *batch() { return m_batch; }

@@ -19,6 +19,8 @@ STATUS_NAMES = {
 }
 LC_MORTON_REF63 = 0
 LC_MORTON_K30 = 1
+LC_NARROW_CCD = 0
+LC_NARROW_DCD = 1
 
 DBG = dict(PRED_X=1, PRED_XPREV=2, PRED_V=3, PERM_BEFORE=4, MORTON=5, PERM=6, LEFTS=7, RIGHTS=8,
            PARENTS=9, RML=10, NODE_AABB=11, PAIRS=12, VF=13, EE=14, FEATURES=15, GROUND=16,
@@ -65,6 +67,19 @@ class Tuning(C.Structure):
                 ("solver_variant", C.c_int32), ("cluster_size", C.c_int32), ("contact_gather", C.c_int32)]
 
 
+class AutotuneSpace(C.Structure):
+    _fields_ = [("traverse_block", C.c_int32 * 8), ("n_traverse_block", C.c_int32),
+                ("jacobi_block", C.c_int32 * 8), ("n_jacobi_block", C.c_int32),
+                ("narrow_blocks_per_sm", C.c_int32 * 8), ("n_narrow_blocks_per_sm", C.c_int32),
+                ("solver_variant", C.c_int32 * 3), ("n_solver_variant", C.c_int32),
+                ("cluster_size", C.c_int32 * 4), ("n_cluster_size", C.c_int32),
+                ("contact_gather", C.c_int32 * 2), ("n_contact_gather", C.c_int32)]
+
+
+class AutotuneTrial(C.Structure):
+    _fields_ = [("config", Tuning), ("ms_per_step", C.c_float)]
+
+
 class Profile(C.Structure):
     _fields_ = [("phase_ms", C.c_float * 7), ("jacobi_ms", C.c_float), ("traverse_ms", C.c_float),
                 ("narrow_ms", C.c_float), ("sort_ms", C.c_float), ("step_ms", C.c_float),
@@ -88,6 +103,10 @@ SIGNATURES = {
     "lc_batch_create": (C.c_int, [C.POINTER(ClothDesc), C.c_int32, C.POINTER(BatchOptions), C.POINTER(VP)]),
     "lc_batch_set_constraint_stiffness": (C.c_int, [VP, VP, VP, C.c_int32]),
     "lc_batch_get_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
+    "lc_default_autotune_space": (None, [C.POINTER(AutotuneSpace)]),
+    "lc_batch_autotune": (C.c_int, [VP, C.POINTER(AutotuneSpace), C.c_int32, C.c_int32, C.c_int32, VP,
+                                    C.POINTER(Tuning), C.POINTER(C.c_float), C.POINTER(AutotuneTrial), C.c_int32,
+                                    C.POINTER(C.c_int32)]),
     "lc_batch_set_tuning": (C.c_int, [VP, C.POINTER(Tuning)]),
     "lc_batch_write_vertex_records": (C.c_int, [VP, VP, C.c_int64, C.c_int32, C.c_int32, VP]),
     "lc_group_create": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
@@ -123,6 +142,14 @@ SIGNATURES = {
     "lc_lbvh_sorted_ids": (C.c_int, [VP, VP, VP]),
     "lc_lbvh_debug_get": (C.c_int, [VP, C.c_int32, VP, C.c_uint64, C.POINTER(C.c_uint64)]),
     "lc_lbvh_destroy": (C.c_int, [VP]),
+    "lc_narrowphase_create": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_uint64,
+                                        C.POINTER(VP)]),
+    "lc_narrowphase_run": (C.c_int, [VP, C.c_int32, VP, VP, VP, C.c_int32, VP, VP, C.c_int32, VP, C.c_uint64, C.c_float,
+                                     C.c_float, VP, C.c_uint64, VP, C.c_uint64, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint64), VP]),
+    "lc_narrowphase_destroy": (C.c_int, [VP]),
+    "lc_solve_collisions": (C.c_int, [VP, VP, VP, VP, C.c_int32, VP, C.c_uint64, VP, C.c_uint64, C.c_float,
+                                      C.c_float, C.c_float, C.c_float, VP]),
     "lc_lbvh_pairs_static": (C.c_int, [VP, VP, C.c_int32, C.c_int32, C.c_int32, VP, C.c_uint64,
                                        C.POINTER(C.c_uint64), VP, VP]),
     "lc_last_error_string": (C.c_char_p, []),

@@ -3,10 +3,11 @@
 For a given batch it times a small grid of launch shapes (traversal block,
 global-memory Jacobi block, narrowphase grid, Jacobi solver variant and the
 on-chip solver's cluster size) on the batch's current state and keeps the
-fastest.  Every candidate starts from the
-same saved state (lc_batch_save_state / lc_batch_load_state) and is timed
-with CUDA events over a few steps after a warm-up; the batch is left in the
-state it was given, with the winning shapes applied.
+fastest.  The timing loop is the library's own (lc_batch_autotune, which C++
+hosts call directly): every candidate starts from the same saved state and is
+timed with CUDA events over a few steps after a warm-up; the batch is left in
+the state it was given, with the winning shapes applied.  This module adds
+the search space as a dict and a cache of results.
 
 Block, grid and cluster sizes never change results.  The solver variant does
 (the variants sum the Jacobi corrections in different orders, all within the
@@ -19,7 +20,6 @@ stored shapes without timing.
 from __future__ import annotations
 
 import ctypes as C
-import itertools
 import json
 from pathlib import Path
 
@@ -64,20 +64,6 @@ def signature(batch) -> str:
                        "iterations": iters, "gpu": torch.cuda.get_device_name()}, sort_keys=True)
 
 
-def _time(batch, state, steps: int, warmup: int, stream) -> float:
-    L = _ffi.lib()
-    sp = C.c_void_p(stream.cuda_stream)
-    _ffi.check(L.lc_batch_load_state(batch._h, C.c_void_p(state.data_ptr()), sp), "lc_batch_load_state")
-    batch.step(warmup, stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    batch.step(steps, stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    batch.sync()
-    return e0.elapsed_time(e1) / steps
-
-
 def autotune(batch, *, steps: int = 3, warmup: int = 1, space: dict | None = None, allow_variants: bool = True,
              cache: Path | str | None = DEFAULT_CACHE, refresh: bool = False) -> dict:
     """Tunes `batch` in place and returns {"config": ..., "ms_per_step": ...,
@@ -93,44 +79,35 @@ def autotune(batch, *, steps: int = 3, warmup: int = 1, space: dict | None = Non
         return dict(store[key], cached=True)
 
     space = dict(DEFAULT_SPACE if space is None else space)
-    if not allow_variants:
-        space["solver_variant"] = (get_tuning(batch)["solver_variant"],)
-    L = _ffi.lib()
-    n = C.c_uint64()
-    _ffi.check(L.lc_batch_state_size(batch._h, C.byref(n)), "lc_batch_state_size")
-    state = torch.empty(n.value, dtype=torch.uint8, device="cuda")
+    current = get_tuning(batch)
+    sp = _ffi.AutotuneSpace()
+    for k in ("traverse_block", "jacobi_block", "narrow_blocks_per_sm", "solver_variant", "cluster_size",
+              "contact_gather"):
+        # a key the space leaves out is not searched: the cluster size stays
+        # automatic, the contact mode off, the others as the batch has them
+        held = (0,) if k in ("cluster_size", "contact_gather") else (current[k],)
+        vals = [int(v) for v in space.get(k, held)]
+        arr = getattr(sp, k)
+        if not 1 <= len(vals) <= len(arr):
+            raise ValueError(f"autotune space {k}: 1..{len(arr)} values")
+        arr[:len(vals)] = vals
+        setattr(sp, "n_" + k, len(vals))
+    cap = 1
+    for k in ("traverse_block", "jacobi_block", "narrow_blocks_per_sm", "solver_variant", "cluster_size",
+              "contact_gather"):
+        cap *= getattr(sp, "n_" + k)
+    trials = (_ffi.AutotuneTrial * cap)()
+    best_t, best_ms, n = _ffi.Tuning(), C.c_float(), C.c_int32()
     stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
-    _ffi.check(L.lc_batch_save_state(batch._h, C.c_void_p(state.data_ptr()), C.c_void_p(stream.cuda_stream)),
-               "lc_batch_save_state")
-    original = get_tuning(batch)
-    names = list(space)
-    tried = []
-    for values in itertools.product(*(space[k] for k in names)):
-        cfg = dict(zip(names, values))
-        cfg.setdefault("cluster_size", 0)
-        # the Jacobi block only matters for the global-memory solver, the
-        # cluster size only for the on-chip ones
-        if cfg["solver_variant"] != 1 and cfg["jacobi_block"] != space["jacobi_block"][0]:
-            continue
-        if cfg["solver_variant"] == 1 and cfg["cluster_size"] not in (0, space.get("cluster_size", (0,))[0]):
-            continue
-        if cfg["solver_variant"] == 1:
-            cfg["cluster_size"] = 0
-        # the contact mode only matters for the scatter solver
-        cfg.setdefault("contact_gather", 0)
-        if cfg["solver_variant"] != 3 and cfg["contact_gather"] != space.get("contact_gather", (0,))[0]:
-            continue
-        if cfg["solver_variant"] != 3:
-            cfg["contact_gather"] = 0
-        if not set_tuning(batch, cfg):
-            continue
-        tried.append({"config": cfg, "ms_per_step": _time(batch, state, steps, warmup, stream)})
-    best = min(tried, key=lambda r: r["ms_per_step"]) if tried else {"config": original, "ms_per_step": None}
-    set_tuning(batch, best["config"])
-    _ffi.check(L.lc_batch_load_state(batch._h, C.c_void_p(state.data_ptr()), C.c_void_p(stream.cuda_stream)),
-               "lc_batch_load_state")
+    _ffi.check(_ffi.lib().lc_batch_autotune(batch._h, C.byref(sp), steps, warmup, 1 if allow_variants else 0,
+                                            C.c_void_p(stream.cuda_stream), C.byref(best_t), C.byref(best_ms),
+                                            trials, cap, C.byref(n)), "lc_batch_autotune")
     torch.cuda.synchronize()
+    fields = [k for k, _ in _ffi.Tuning._fields_]
+    tried = [{"config": {k: getattr(trials[i].config, k) for k in fields}, "ms_per_step": trials[i].ms_per_step}
+             for i in range(min(n.value, cap))]
+    best = {"config": {k: getattr(best_t, k) for k in fields}, "ms_per_step": best_ms.value}
     result = {"config": best["config"], "ms_per_step": best["ms_per_step"], "tried": tried}
     if cache is not None and tried:
         store[key] = {"config": best["config"], "ms_per_step": best["ms_per_step"]}

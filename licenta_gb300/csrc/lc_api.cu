@@ -1238,6 +1238,101 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
     return LC_OK;
 }
 
+void lc_default_autotune_space(lc_autotune_space *s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    const int32_t tb[] = {64, 128, 256}, jb[] = {128, 256, 512}, nb[] = {4, 8, 16}, sv[] = {1, 2, 3},
+                  cs[] = {4, 8, 16}, cg[] = {0, 1};
+    std::memcpy(s->traverse_block, tb, sizeof(tb)); s->n_traverse_block = 3;
+    std::memcpy(s->jacobi_block, jb, sizeof(jb)); s->n_jacobi_block = 3;
+    std::memcpy(s->narrow_blocks_per_sm, nb, sizeof(nb)); s->n_narrow_blocks_per_sm = 3;
+    std::memcpy(s->solver_variant, sv, sizeof(sv)); s->n_solver_variant = 3;
+    std::memcpy(s->cluster_size, cs, sizeof(cs)); s->n_cluster_size = 3;
+    std::memcpy(s->contact_gather, cg, sizeof(cg)); s->n_contact_gather = 2;
+}
+
+lc_status lc_batch_autotune(lc_batch *b, const lc_autotune_space *space_in, int32_t steps, int32_t warmup,
+                            int32_t allow_variants, void *stream, lc_tuning *best, float *best_ms,
+                            lc_autotune_trial *trials, int32_t trials_cap, int32_t *num_trials) {
+    if (!b || steps < 1 || warmup < 0 || trials_cap < 0 || (trials_cap && !trials))
+        return fail(LC_ERR_INVALID_ARG, "lc_batch_autotune: bad arguments");
+    lc_autotune_space sp;
+    if (space_in) sp = *space_in; else lc_default_autotune_space(&sp);
+    const int32_t counts[6] = {sp.n_traverse_block, sp.n_jacobi_block, sp.n_narrow_blocks_per_sm,
+                               sp.n_solver_variant, sp.n_cluster_size, sp.n_contact_gather};
+    const int32_t caps[6] = {8, 8, 8, 3, 4, 2};
+    for (int k = 0; k < 6; ++k)
+        if (counts[k] < 1 || counts[k] > caps[k])
+            return fail(LC_ERR_INVALID_ARG, "lc_batch_autotune: every space list needs 1..its capacity values");
+    cudaStream_t st = (cudaStream_t)stream;
+    lc_tuning original;
+    LC_TRY(lc_batch_get_tuning(b, &original));
+    if (!allow_variants) { sp.solver_variant[0] = original.solver_variant; sp.n_solver_variant = 1; }
+    uint64_t nbytes = 0;
+    LC_TRY(lc_batch_state_size(b, &nbytes));
+    void *state = nullptr;
+    if (cudaMalloc(&state, nbytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(LC_ERR_OOM, "lc_batch_autotune: no room for the saved state");
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    struct Guard {
+        void *p; cudaEvent_t a, b;
+        ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (p) cudaFree(p); }
+    } guard{state, nullptr, nullptr};
+    LC_CUDA(cudaEventCreate(&e0)); guard.a = e0;
+    LC_CUDA(cudaEventCreate(&e1)); guard.b = e1;
+    LC_TRY(lc_batch_sync(b));
+    LC_TRY(lc_batch_save_state(b, state, st));
+    int32_t n = 0;
+    float best_t = 0.f;
+    lc_tuning best_cfg = original;
+    for (int i0 = 0; i0 < sp.n_traverse_block; ++i0)
+    for (int i1 = 0; i1 < sp.n_jacobi_block; ++i1)
+    for (int i2 = 0; i2 < sp.n_narrow_blocks_per_sm; ++i2)
+    for (int i3 = 0; i3 < sp.n_solver_variant; ++i3)
+    for (int i4 = 0; i4 < sp.n_cluster_size; ++i4)
+    for (int i5 = 0; i5 < sp.n_contact_gather; ++i5) {
+        lc_tuning c;
+        c.traverse_block = sp.traverse_block[i0];
+        c.jacobi_block = sp.jacobi_block[i1];
+        c.narrow_blocks_per_sm = sp.narrow_blocks_per_sm[i2];
+        c.solver_variant = sp.solver_variant[i3];
+        c.cluster_size = sp.cluster_size[i4];
+        c.contact_gather = sp.contact_gather[i5];
+        // the Jacobi block matters only to the global-memory solver, the
+        // cluster size only to the on-chip ones, the contact mode only to the
+        // scatter solver: other combinations would time the same launch twice
+        if (c.solver_variant != 1 && i1 != 0) continue;
+        if (c.solver_variant == 1 && i4 != 0) continue;
+        if (c.solver_variant == 1) c.cluster_size = 0;
+        if (c.solver_variant != 3 && i5 != 0) continue;
+        if (c.solver_variant != 3) c.contact_gather = 0;
+        if (lc_batch_set_tuning(b, &c) != LC_OK) continue;  // a shape the batch cannot take
+        LC_TRY(lc_batch_load_state(b, state, st));
+        LC_TRY(lc_batch_step(b, warmup, st));
+        LC_CUDA(cudaEventRecord(e0, st));
+        LC_TRY(lc_batch_step(b, steps, st));
+        LC_CUDA(cudaEventRecord(e1, st));
+        LC_CUDA(cudaEventSynchronize(e1));
+        LC_TRY(lc_batch_sync(b));
+        float ms = 0.f;
+        LC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= (float)steps;
+        if (n < trials_cap) { trials[n].config = c; trials[n].ms_per_step = ms; }
+        if (n == 0 || ms < best_t) { best_t = ms; best_cfg = c; }
+        ++n;
+    }
+    LC_TRY(lc_batch_set_tuning(b, &best_cfg));
+    LC_TRY(lc_batch_load_state(b, state, st));
+    LC_CUDA(cudaStreamSynchronize(st));
+    if (best) *best = best_cfg;
+    if (best_ms) *best_ms = n ? best_t : -1.f;
+    if (num_trials) *num_trials = n;
+    if (!n) return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_autotune: the batch took none of the shapes");
+    return LC_OK;
+}
+
 lc_status lc_batch_constraint_counts(const lc_batch *b, int32_t c, int32_t *ns, int32_t *nb) {
     if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
     if (ns) *ns = b->s_count[c];
@@ -1510,22 +1605,24 @@ lc_status lc_batch_counters(lc_batch *b, uint64_t out[4]) {
 
 lc_status lc_batch::cloth_contacts(int c, bool vf, std::vector<uint64_t> &gidx, std::vector<int4> &iv,
                                    std::vector<float4> &wv) {
+    // a cloth's contacts of each kind are one contiguous range of the batch's
+    // list (k_contact_ranges writes it every step)
     const ClothDev &cd = cds[c];
-    uint32_t tot = 0;
-    LC_CUDA(cudaMemcpy(&tot, vf ? nvf : nee, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    const uint64_t n = std::min<uint64_t>(tot, vf ? d.vf_cap : d.ee_cap);
-    std::vector<int4> all_v(n);
-    std::vector<float4> all_w(n);
+    uint4 cr;
+    LC_CUDA(cudaMemcpy(&cr, d.crange + c, sizeof(uint4), cudaMemcpyDeviceToHost));
+    const uint64_t a = vf ? cr.x : cr.z, e = vf ? cr.y : cr.w;
+    const uint64_t n = e > a ? e - a : 0;
+    std::vector<int4> v(n);
+    std::vector<float4> w(n);
     if (n) {
-        LC_CUDA(cudaMemcpy(all_v.data(), vf ? d.vf_v : d.ee_v, sizeof(int4) * n, cudaMemcpyDeviceToHost));
-        LC_CUDA(cudaMemcpy(all_w.data(), vf ? d.vf_w : d.ee_w, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+        LC_CUDA(cudaMemcpy(v.data(), (vf ? d.vf_v : d.ee_v) + a, sizeof(int4) * n, cudaMemcpyDeviceToHost));
+        LC_CUDA(cudaMemcpy(w.data(), (vf ? d.vf_w : d.ee_w) + a, sizeof(float4) * n, cudaMemcpyDeviceToHost));
     }
-    gidx.clear(); iv.clear(); wv.clear();
+    gidx.resize(n); iv.resize(n); wv.resize(n);
     for (uint64_t i = 0; i < n; ++i) {
-        if (all_v[i].x < cd.v_off || all_v[i].x >= cd.v_off + cd.V) continue;
-        gidx.push_back(i);
-        iv.push_back(make_int4(all_v[i].x - cd.v_off, all_v[i].y - cd.v_off, all_v[i].z - cd.v_off, all_v[i].w - cd.v_off));
-        wv.push_back(all_w[i]);
+        gidx[i] = a + i;
+        iv[i] = make_int4(v[i].x - cd.v_off, v[i].y - cd.v_off, v[i].z - cd.v_off, v[i].w - cd.v_off);
+        wv[i] = w[i];
     }
     return LC_OK;
 }
@@ -1616,15 +1713,15 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, ui
             std::vector<int4> iv;
             std::vector<float4> wv;
             LC_TRY(b->cloth_contacts(c, true, gi, iv, wv));
-            std::vector<float4> all(gi.empty() ? 0 : gi.back() + 1);
-            if (!all.empty())
-                LC_CUDA(cudaMemcpy(all.data(), d.vf_n, sizeof(float4) * all.size(), cudaMemcpyDeviceToHost));
+            std::vector<float4> nr(gi.size());
+            if (!nr.empty())
+                LC_CUDA(cudaMemcpy(nr.data(), d.vf_n + gi.front(), sizeof(float4) * nr.size(), cudaMemcpyDeviceToHost));
             if (count) *count = gi.size();
             if (dst)
                 for (uint64_t i = 0; i < std::min<uint64_t>(gi.size(), cap); ++i) {
-                    ((float *)dst)[3 * i] = all[gi[i]].x;
-                    ((float *)dst)[3 * i + 1] = all[gi[i]].y;
-                    ((float *)dst)[3 * i + 2] = all[gi[i]].z;
+                    ((float *)dst)[3 * i] = nr[i].x;
+                    ((float *)dst)[3 * i + 1] = nr[i].y;
+                    ((float *)dst)[3 * i + 2] = nr[i].z;
                 }
             return LC_OK;
         }
@@ -1654,17 +1751,15 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, ui
             LC_CUDA(cudaMemcpy(&nvf_tot, b->nvf, sizeof(uint32_t), cudaMemcpyDeviceToHost));
             nvf_tot = (uint32_t)std::min<uint64_t>(nvf_tot, d.vf_cap);
             const int iters = b->cds[c].iters;
-            const size_t per = (gvf.size() + gee.size()) * 4;
-            std::vector<uint8_t> all((size_t)b->max_iters * d.dyn_cap);
-            if (!all.empty())
-                LC_CUDA(cudaMemcpy(all.data(), d.dbg_dyn_nz, all.size(), cudaMemcpyDeviceToHost));
+            const size_t nv4 = 4 * gvf.size(), ne4 = 4 * gee.size(), per = nv4 + ne4;
+            // per iteration: the cloth's VF entries, then its EE entries (both contiguous)
             std::vector<uint8_t> outv((size_t)iters * per);
-            for (int it = 0; it < iters; ++it) {
-                size_t o = (size_t)it * per;
-                for (uint64_t g : gvf)
-                    for (int s = 0; s < 4; ++s) outv[o++] = all[(size_t)it * d.dyn_cap + 4 * g + s];
-                for (uint64_t g : gee)
-                    for (int s = 0; s < 4; ++s) outv[o++] = all[(size_t)it * d.dyn_cap + 4 * (nvf_tot + g) + s];
+            for (int it = 0; it < iters && per; ++it) {
+                const uint8_t *src = d.dbg_dyn_nz + (size_t)it * d.dyn_cap;
+                if (nv4) LC_CUDA(cudaMemcpy(outv.data() + (size_t)it * per, src + 4 * gvf.front(), nv4,
+                                            cudaMemcpyDeviceToHost));
+                if (ne4) LC_CUDA(cudaMemcpy(outv.data() + (size_t)it * per + nv4, src + 4 * (nvf_tot + gee.front()),
+                                            ne4, cudaMemcpyDeviceToHost));
             }
             if (count) *count = outv.size();
             if (dst && !outv.empty()) std::memcpy(dst, outv.data(), std::min<uint64_t>(outv.size(), cap));

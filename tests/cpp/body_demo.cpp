@@ -2,8 +2,10 @@
 // reference's scene code drives Physics::CudaDeformableBody: construct from a
 // vertex array, then FixedUpdate() and Update() once per frame.
 //
-// stdin:  int32 V, int32 T, int32 steps, float[3V] positions, uint32[3T]
-//         indices, uint8[V] pinned, lc_cloth_params (raw struct bytes)
+// stdin:  int32 V, int32 T, int32 steps, int32 tune, float[3V] positions,
+//         uint32[3T] indices, uint8[V] pinned, lc_cloth_params (raw struct
+//         bytes); tune = 1 runs the body's Autotune() (launch shapes only)
+//         before the first step
 // stdout: float[3V] published positions after the last Update()
 #include <cstdint>
 #include <cstdio>
@@ -25,8 +27,8 @@ template <class T> bool read(T *dst, size_t n) { return std::fread(dst, sizeof(T
 }  // namespace
 
 int main() {
-    int32_t V = 0, T = 0, steps = 0;
-    if (!read(&V, 1) || !read(&T, 1) || !read(&steps, 1) || V <= 0 || T <= 0) return 2;
+    int32_t V = 0, T = 0, steps = 0, tune = 0;
+    if (!read(&V, 1) || !read(&T, 1) || !read(&steps, 1) || !read(&tune, 1) || V <= 0 || T <= 0) return 2;
     std::vector<float> pos(3 * (size_t)V);
     std::vector<unsigned int> idx(3 * (size_t)T);
     std::vector<uint8_t> pin(V);
@@ -42,6 +44,7 @@ int main() {
     }
     try {
         lc::CudaDeformableBody<Vertex> body(&verts, &idx, params, fixed);
+        if (tune) body.Autotune(2, 1, false);
         for (int s = 0; s < steps; ++s) {
             body.FixedUpdate();
             body.Update();

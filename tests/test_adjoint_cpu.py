@@ -112,3 +112,46 @@ def test_adjoint_matches_finite_differences_through_contacts():
             # crosses the world clamp (many lie outside the unit box here)
             e = np.zeros((r.nv, 3)); e[i, d] = 1e-6
             check(gxp[i, d], r.fd(xp=lambda s, e=e: r.st0["x_prev"] + s * e), 1e-6)
+
+
+def test_adjoint_at_the_workload_size_matches_finite_differences():
+    """The differentiable-rollout workload's cloth (64 x 64, 10 iterations,
+    stiffness 0.9, zero initial velocities; the target is the final state of
+    a forward run with stiffness 0.7 and wind (1.5, 0, 0.5) m/s^2): the FP64
+    adjoint's directional derivatives along a random direction of the
+    per-constraint stiffnesses and one of the initial velocities against
+    central finite differences of the rollout replaying the recorded
+    decisions, over 50 steps.
+
+    The cloth folds onto itself and the rollout is chaotic: its gradient
+    grows from 6e-4 (10 steps) to 2e2 (50) and 8e5 (60) in the largest
+    stiffness entry, so a central difference with eps 1e-3 is far outside
+    the linear range past about 20 steps.  At 50 steps the difference
+    quotients converge to the adjoint as eps shrinks (eps 1e-7: 3e-5
+    relative); at 60 they scatter by 15% between eps 1e-8 and 1e-11 (the
+    curvature, then FP64 rounding of the loss, dominates), so no finite
+    difference resolves the 60-step gradient.  The engine's reverse pass is
+    compared with this adjoint step by step over all 60 steps
+    (tests/test_adjoint_gpu.py)."""
+    spec = scenes.adjoint_cloth(seed=0)
+    tgt = scenes.adjoint_cloth(seed=0, stiffness=0.7, wind=(1.5, 0.0, 0.5))
+    steps = 50
+    t = Oracle([tgt], fp64=True)
+    t.step(steps, threads=1)
+    target = t.get_state(0)["x_prev"]
+    t.close()
+    r = Rollout(spec)
+    r.ks0[:] = 0.9
+    r.kb0[:] = 0.9
+    r.v0 = np.zeros_like(r.v0)
+    r.target = target
+    gx, gxp, gv, gks, gkb = r.record(steps)
+    rng = np.random.default_rng(3)
+    eps = 1e-7
+    dk, db = rng.normal(size=r.ne), rng.normal(size=r.nb)
+    norm = np.sqrt((dk ** 2).sum() + (db ** 2).sum())
+    dk, db = dk / norm, db / norm
+    check(float(gks @ dk + gkb @ db), r.fd(ks=lambda s: r.ks0 + s * eps * dk, kb=lambda s: r.kb0 + s * eps * db), eps)
+    dv = rng.normal(size=(r.nv, 3)) * (spec.pinned == 0)[:, None]
+    dv /= np.linalg.norm(dv)
+    check(float((gv * dv).sum()), r.fd(v=lambda s: r.v0 + s * eps * dv), eps)

@@ -197,27 +197,58 @@ def test_rescaled_entry_matches_plain_entry():
     cloth.close()
 
 
-def test_engine_adjoint_at_the_workload_size(parity_report):
-    """The differentiable-rollout workload as configured: a 64 x 64 cloth, 60
-    steps, 10 iterations, checkpoints every 10 steps; the target is the final
-    state of a forward run with stiffness 0.7 and wind (1.5, 0, 0.5) m/s^2;
-    the gradients with respect to the per-constraint stiffness (0.9) and the
-    initial velocities (zero) against the FP64 adjoint, each on its own
-    trajectory."""
+def test_engine_reverse_steps_at_the_workload_size(parity_report):
+    """The reverse pass of every step of the differentiable-rollout workload
+    (a 64 x 64 cloth, 60 steps, 10 iterations, stiffness 0.9, zero initial
+    velocities) against the FP64 adjoint of the same step: before each step
+    the oracle takes the engine's state, and after it the engine's contacts
+    and discrete decisions, so both differentiate the same piecewise-smooth
+    branch from the same point; both reverse the step with the same random
+    seed gradients.  (Run freely, the FP32 and FP64 rollouts of this cloth
+    find different self-contacts after a few dozen steps and end centimetres
+    apart, so their whole-rollout gradients are gradients of different
+    trajectories; the whole-rollout comparison is the small case above.)"""
+    from oracle import parity
     spec = scenes.adjoint_cloth(seed=0)
-    tgt = scenes.adjoint_cloth(seed=0, stiffness=0.7, wind=(1.5, 0.0, 0.5))
     steps = 60
-    o = Oracle([tgt], fp64=True)
-    o.step(steps, threads=1)
-    target = o.get_state(0)["x_prev"]
+    cloth = DiffCloth([spec], checkpoint_every=10, debug_capture=True)
+    b = cloth.batch
+    V = spec.num_vertices
+    o = Oracle([spec], fp64=True)
     _, _, ne, nb = o.sizes(0)
-    o.close()
-    ks, kb = np.full(ne, 0.9), np.full(nb, 0.9)
-    v0 = np.zeros((spec.num_vertices, 3))
-    g = engine_grads(spec, steps, ks, kb, v0, target, every=10)
-    r = oracle_grads(spec, steps, ks, kb, v0, target)
-    errs = {k: rel_l2(g[k], r[k]) for k in ("ks", "kb", "v0", "x0")}
-    parity_report(final_dx_m=f"{np.abs(g['final'] - r['final']).max():.2e}",
-                  **{f"rel_l2_{k}": f"{v:.2e}" for k, v in errs.items()})
-    for k, e in errs.items():
-        assert e < 2e-3, f"{k}: relative error {e:.2e}"
+    o.set_stiffness_d(0, np.full(ne, 0.9), np.full(nb, 0.9))
+    cloth.set_stiffness(torch.full((cloth.E,), 0.9, device="cuda"), torch.full((cloth.B,), 0.9, device="cuda"))
+    x0 = torch.tensor(spec.positions, device="cuda")
+    cloth.set_initial(x0, torch.zeros_like(x0))
+    rng = np.random.default_rng(7)
+    worst = dict(x=0.0, gx=0.0, gxp=0.0, gv=0.0, gks=0.0, gkb=0.0)
+    contacts = 0
+    try:
+        for n in range(steps):
+            st, perm = parity.capture_pre(b, 0)
+            seeds = [rng.normal(size=(V, 3)).astype(np.float32) for _ in range(3)]
+            g = [torch.tensor(a, device="cuda") for a in seeds] + [torch.zeros(cloth.E, device="cuda"),
+                                                                   torch.zeros(cloth.B, device="cuda")]
+            cloth.adjoint_step(*g)
+            torch.cuda.synchronize()
+            vf, ee = b.debug(0, "VF"), b.debug(0, "EE")
+            contacts += len(vf[0]) + len(ee[0])
+            o.set_state(0, **{k: a.astype(np.float64) for k, a in st.items()})
+            o.set_perm(0, perm)
+            o.freeze_contacts(0, vf, ee)
+            o.force_decisions(0, b.debug(0, "GROUND"), b.debug(0, "GROUND_ACTIVE"), b.debug(0, "LRA"),
+                              b.debug(0, "DYN_ACTIVE"))
+            o.adj_clear(0)
+            o.adj_record(0, 1)
+            worst["x"] = max(worst["x"], float(np.abs(b.get_state(0)["x"] - o.get_state(0)["x"]).max()))
+            r = o.adj_backward(0, *seeds)
+            for k, got, want in zip(("gx", "gxp", "gv", "gks", "gkb"), g, r):
+                worst[k] = max(worst[k], rel_l2(got.cpu().numpy(), want))
+    finally:
+        cloth.close()
+        o.close()
+    parity_report(steps=steps, contacts=contacts, **{f"max_{k}": f"{v:.2e}" for k, v in worst.items()})
+    assert contacts > 0, "the rollout should reach self-contact"
+    assert worst["x"] <= 1e-5
+    for k in ("gx", "gxp", "gv", "gks", "gkb"):
+        assert worst[k] < 2e-3, f"{k}: relative error {worst[k]:.2e}"

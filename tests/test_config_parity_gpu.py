@@ -96,9 +96,10 @@ def test_lbvh_one_million_triangles_bit_exact(cuda, parity_report, mode):
     torch = cuda
     count = 1_000_000
     lo, hi = scenes.random_triangle_boxes(count, seed=0)
+    lo_t, hi_t = torch.from_numpy(lo).cuda(), torch.from_numpy(hi).cuda()  # held until the build has read them
     h = Lbvh(count, chunk_size=64, morton_mode=mode)
     try:
-        h.build(torch.from_numpy(lo).cuda().data_ptr(), torch.from_numpy(hi).cuda().data_ptr(), count)
+        h.build(lo_t.data_ptr(), hi_t.data_ptr(), count)
         n = h.pairs(None, 0)
         want = lbvh_boxes(lo, hi, chunk=64, mode=mode)
         for what in ("MORTON", "PERM", "LEFTS", "RIGHTS", "PARENTS", "RML", "NODE_AABB", "PAIRS"):

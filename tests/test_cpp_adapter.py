@@ -35,7 +35,8 @@ def test_adapter_header_compiles():
 
 
 @pytest.mark.gpu
-def test_adapter_steps_like_the_binding(tmp_path):
+@pytest.mark.parametrize("tune", [0, 1], ids=["default", "autotuned"])
+def test_adapter_steps_like_the_binding(tmp_path, tune):
     lib = _build.build()
     exe = tmp_path / "body_demo"
     r = subprocess.run([_gxx(), "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(SRC), "-o", str(exe),
@@ -44,7 +45,7 @@ def test_adapter_steps_like_the_binding(tmp_path):
     assert r.returncode == 0, r.stderr
     spec = scenes.small_cloth(seed=4, n=20)
     steps = 6
-    blob = (np.array([spec.num_vertices, spec.num_triangles, steps], np.int32).tobytes()
+    blob = (np.array([spec.num_vertices, spec.num_triangles, steps, tune], np.int32).tobytes()
             + spec.positions.astype(np.float32).tobytes() + spec.indices.astype(np.uint32).tobytes()
             + spec.pinned.astype(np.uint8).tobytes() + bytes(spec.params))
     r = subprocess.run([str(exe)], input=blob, capture_output=True)
