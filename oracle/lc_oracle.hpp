@@ -472,12 +472,18 @@ template <class R> class Cloth {
     };
     bool recording = false;
     Record rec;
-    // Smallest 1 - n1.n2 over the bends and the solver iterates of the last
-    // solve (when track_bend): how close a bend came to the d -> 1
-    // singularity of the reference's formula, where the correction is 0 * inf
-    // and rounding alone moves it by a finite amount.
+    // Smallest 1 - n1.n2 (bend_min) and 1 + n1.n2 (bend_min_neg) over the
+    // bends and the solver iterates of the last solve (when track_bend): how
+    // close a bend came to a singularity of the reference's formula.  At
+    // d -> 1 the correction itself is 0 * inf and rounding alone moves it by
+    // a finite amount; at d -> -1 (phi -> phi0 = pi) the correction is a
+    // 0 / 0 ratio that goes to zero with a bounded rounding error, but whose
+    // derivative grows like (1 + d)^-1/2, so only the reverse pass is
+    // ill-conditioned there.  The formula takes raw positions, so every bend
+    // of a cloth lying in a plane through the origin (on the ground plane
+    // y = 0) sits at d = -1.
     bool track_bend = false;
-    double bend_min = 1e300;
+    double bend_min = 1e300, bend_min_neg = 1e300;
     std::vector<Record> records;  // one per recorded step of a rollout
 
     void init(const lc_cloth_desc &d) {
@@ -1050,7 +1056,7 @@ template <class R> class Cloth {
             rec.dyn.assign((size_t)prm.solverIterations * corr_dyn.size(), 0);
             rec.xk.assign(1, x);
         }
-        bend_min = 1e300;
+        bend_min = bend_min_neg = 1e300;
         for (int it = 0; it < prm.solverIterations; ++it) {
             if (track_bend) track_bend_conditioning();
             for (int i = 0; i < Vn; ++i) { acc[i] = mk<R>(0, 0, 0); cnt[i] = 0; }
@@ -1126,7 +1132,9 @@ template <class R> class Cloth {
             const double lu = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
             const double lw = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
             if (lu <= 0 || lw <= 0) continue;
-            bend_min = std::min(bend_min, 1.0 - (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) / (lu * lw));
+            const double d = (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) / (lu * lw);
+            bend_min = std::min(bend_min, 1.0 - d);
+            bend_min_neg = std::min(bend_min_neg, 1.0 + d);
         }
     }
 

@@ -298,12 +298,14 @@ class Oracle:
     def track_bend(self, c: int, on: bool = True) -> None:
         _chk(lib().lco_track_bend(self._h, c, 1 if on else 0), "track_bend")
 
-    def bend_conditioning(self, c: int) -> float:
+    def bend_conditioning(self, c: int, reverse: bool = False) -> float:
         """min over bends and solver iterates of 1 - n1.n2 in the last solve
-        (tracked after track_bend)."""
-        out = C.c_double()
-        _chk(lib().lco_bend_conditioning(self._h, c, C.byref(out)), "bend_conditioning")
-        return out.value
+        or step (tracked after track_bend): the forward singularity of the
+        reference's bend formula.  reverse=True: min of 1 - |n1.n2|, which
+        adds the d -> -1 end where only the derivative is singular."""
+        out = (C.c_double * 2)()
+        _chk(lib().lco_bend_conditioning(self._h, c, out), "bend_conditioning")
+        return min(out[0], out[1]) if reverse else out[0]
 
     def friction_on(self, c: int, v, ground, vf: tuple, normals) -> np.ndarray:
         """Friction (CudaPBD::ApplyFriction) on given velocities with the given
