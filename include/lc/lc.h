@@ -246,6 +246,38 @@ lc_status lc_batch_profile(lc_batch *b, int32_t nsteps, void *stream, lc_profile
 /* CudaPBD::SetSpherePos for one cloth (Physics/CudaPBD.cu:460-472). */
 lc_status lc_batch_set_sphere(lc_batch *b, int32_t cloth, const float pos[3], float radius);
 
+/* Static triangle collider of one cloth (no counterpart in the reference,
+ * whose only collider is the analytic sphere of CudaPBD::SetSpherePos): a
+ * mesh that does not move (vertices: 3 floats each, host memory; indices: 3
+ * per triangle; num_triangles = 0 removes the cloth's collider).  winding
+ * names the free side: LC_WINDING_CCW when the faces turn counter-clockwise
+ * seen from it ((b - a) x (c - a) points there), LC_WINDING_CW for the
+ * opposite, which is how lc_mesh_icosphere winds its sphere.  Every step,
+ * after the self-collision narrowphase, each cloth vertex is tested against
+ * the collider triangles whose boxes meet its swept box inflated by 5 h (h
+ * the cloth's thickness).  With n the face's unit normal towards the free
+ * side and the vertex's heights s0 = n . (x_prev - a), s1 = n . (x - a) (x
+ * the prediction), the face is a contact when s1 < 5 h, s0 > -4 h, and the
+ * point where the vertex crosses the face's plane (without a crossing, the
+ * prediction) lies on the triangle within the barycentric tolerance of the
+ * reference's TestVF (h / perimeter, Collision/CudaPrimitiveTests.cu:
+ * 348-406).  The reach beyond the contact layer lets the constraint act on a
+ * vertex that the solver iterations drag towards the face, and brings back
+ * one that ended a step behind it.  The hits (at most LC_COLLIDER_SLOTS per
+ * vertex, the lowest triangle indices; more is a capacity error reported by
+ * lc_batch_sync) are one-sided constraints n . x >= n . a + h on the vertex
+ * alone.  The vertex is projected onto them, in slot order, before the first
+ * solver iteration and at the end of every iteration, after the Jacobi
+ * average, so collisions are projected last; pinned vertices do not move.
+ * (The reference's two-sided VF projection, averaged with the other
+ * corrections, leaves a vertex that crossed a face within one step on the
+ * far side; a static face has a side.)  A BVH over the triangles is built on
+ * the host once per call.  Not for batches created with adjoint. */
+#define LC_COLLIDER_SLOTS 8
+enum { LC_WINDING_CCW = 0, LC_WINDING_CW = 1 };
+lc_status lc_batch_set_collider(lc_batch *b, int32_t cloth, const float *vertices, int32_t num_vertices,
+                                const uint32_t *indices, int32_t num_triangles, int32_t winding);
+
 /* Per-constraint stiffness override (stretch: E values, bend: B values). */
 lc_status lc_batch_set_stiffness(lc_batch *b, int32_t cloth, const float *k_stretch,
                                  const float *k_bend);
@@ -279,8 +311,11 @@ enum {
     LC_DBG_DYN_ACTIVE = 19,   /* u8 per iteration x (VF contacts, then EE contacts) x 4 slots:
                                  correction non-zero, i.e. counted (:1466) */
     LC_DBG_SPHERE = 20,       /* i8 per vertex: ray-sphere outcome -1/0/1 (:1523) */
-    LC_DBG_VF_NORMAL = 21     /* float3 per vertex-face contact: face normal at the hit, which friction
+    LC_DBG_VF_NORMAL = 21,    /* float3 per vertex-face contact: face normal at the hit, which friction
                                  uses (Collision/CudaPrimitiveTests.cu:393); batches with friction only */
+    LC_DBG_COLLIDER = 22      /* lc_contact per vertex x LC_COLLIDER_SLOTS: static-collider contacts of the
+                                 step, v = (vertex, collider triangle or -1, 0, 0), w = the contact's plane
+                                 (unit normal towards the free side, then n . a) */
 };
 
 /* A contact as the solver consumes it: the ids/weights of

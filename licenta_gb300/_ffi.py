@@ -13,6 +13,9 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "_lib" / "liblicenta_gb300.so"
 
 LC_OK = 0
+LC_ERR_INVALID_ARG = 1
+LC_ERR_CAPACITY_OVERFLOW = 3
+LC_ERR_NOT_SUPPORTED = 6
 STATUS_NAMES = {
     0: "LC_OK", 1: "LC_ERR_INVALID_ARG", 2: "LC_ERR_OOM", 3: "LC_ERR_CAPACITY_OVERFLOW",
     4: "LC_ERR_TIMEOUT", 5: "LC_ERR_CUDA", 6: "LC_ERR_NOT_SUPPORTED", 7: "LC_ERR_STACK_OVERFLOW",
@@ -21,10 +24,13 @@ LC_MORTON_REF63 = 0
 LC_MORTON_K30 = 1
 LC_NARROW_CCD = 0
 LC_NARROW_DCD = 1
+LC_WINDING_CCW = 0
+LC_WINDING_CW = 1
+COLLIDER_SLOTS = 8
 
 DBG = dict(PRED_X=1, PRED_XPREV=2, PRED_V=3, PERM_BEFORE=4, MORTON=5, PERM=6, LEFTS=7, RIGHTS=8,
            PARENTS=9, RML=10, NODE_AABB=11, PAIRS=12, VF=13, EE=14, FEATURES=15, GROUND=16,
-           GROUND_ACTIVE=17, LRA=18, DYN_ACTIVE=19, SPHERE=20, VF_NORMAL=21)
+           GROUND_ACTIVE=17, LRA=18, DYN_ACTIVE=19, SPHERE=20, VF_NORMAL=21, COLLIDER=22)
 
 F3 = C.c_float * 3
 
@@ -129,6 +135,7 @@ SIGNATURES = {
     "lc_batch_set_triangle_order": (C.c_int, [VP, C.c_int32, VP]),
     "lc_batch_read_positions": (C.c_int, [VP, VP, C.c_int32, VP]),
     "lc_batch_set_sphere": (C.c_int, [VP, C.c_int32, C.POINTER(C.c_float), C.c_float]),
+    "lc_batch_set_collider": (C.c_int, [VP, C.c_int32, VP, C.c_int32, VP, C.c_int32, C.c_int32]),
     "lc_batch_set_stiffness": (C.c_int, [VP, C.c_int32, VP, VP]),
     "lc_batch_constraint_counts": (C.c_int, [VP, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lc_batch_debug_get": (C.c_int, [VP, C.c_int32, C.c_int32, VP, C.c_uint64, C.POINTER(C.c_uint64)]),

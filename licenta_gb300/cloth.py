@@ -69,6 +69,9 @@ class ClothBatch:
         self._keep.clear()
         self.num_vertices = [s.num_vertices for s in self.specs]
         self.num_triangles = [s.num_triangles for s in self.specs]
+        for k, s in enumerate(self.specs):
+            if getattr(s, "collider", None) is not None:
+                self.set_collider(k, *s.collider)
 
     # -- lifetime -----------------------------------------------------------
     def close(self) -> None:
@@ -161,6 +164,17 @@ class ClothBatch:
         p = (C.c_float * 3)(*[float(v) for v in pos])
         _ffi.check(_ffi.lib().lc_batch_set_sphere(self._h, cloth, p, float(radius)), "lc_batch_set_sphere")
 
+    def set_collider(self, cloth: int, vertices, indices, winding: str = "ccw") -> None:
+        """A static triangle collider for one cloth (lc_batch_set_collider);
+        an empty index array removes it.  winding: "ccw" when the faces turn
+        counter-clockwise seen from the free side, "cw" for the opposite
+        (scenes.icosphere)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        w = {"ccw": _ffi.LC_WINDING_CCW, "cw": _ffi.LC_WINDING_CW}[winding]
+        _ffi.check(_ffi.lib().lc_batch_set_collider(self._h, cloth, _ptr(v), len(v), _ptr(i), len(i), w),
+                   "lc_batch_set_collider")
+
     def constraint_counts(self, cloth: int) -> tuple[int, int]:
         a, b = C.c_int32(), C.c_int32()
         _ffi.check(_ffi.lib().lc_batch_constraint_counts(self._h, cloth, C.byref(a), C.byref(b)), "constraint_counts")
@@ -187,8 +201,8 @@ class ClothBatch:
         L = _ffi.lib()
         n = C.c_uint64()
         _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, None, 0, C.byref(n)), "lc_batch_debug_get")
-        if sel in (13, 14):
-            # lc_contact records: 4 int32 ids then 4 float32 weights
+        if sel in (13, 14, 22):
+            # lc_contact records: 4 int32 ids then 4 float32 weights (collider: plane)
             raw = np.empty((max(n.value, 1), 8), dtype=np.int32)
             _ffi.check(L.lc_batch_debug_get(self._h, cloth, sel, _ptr(raw), n.value, C.byref(n)), "lc_batch_debug_get")
             raw = raw[:n.value]

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <numeric>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
@@ -20,6 +21,7 @@
 namespace lc {
 // launchers (lc_lbvh.cu, lc_step.cu, lc_scan.cu)
 void launch_triangles(const DevPtrs &d, cudaStream_t st);
+void launch_collider(const DevPtrs &d, int grid, cudaStream_t st);
 void launch_leaves_from_boxes(const DevPtrs &d, const float *bmin, const float *bmax, int T, int mode,
                               cudaStream_t st);
 void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream_t st);
@@ -366,10 +368,30 @@ struct lc_batch {
     lc_status cloth_contacts(int c, bool vf, std::vector<uint64_t> &gidx, std::vector<int4> &iv,
                              std::vector<float4> &wv);
 
+    // static triangle colliders (lc_batch_set_collider): host copies per
+    // cloth, and the device arrays built from all of them
+    struct Collider {
+        std::vector<float> verts;
+        std::vector<uint32_t> tris;
+        int tbase = 0;    // first triangle in the flat device arrays
+        bool cw = false;  // faces clockwise seen from the free side
+    };
+    std::vector<Collider> colliders;
+    std::vector<void *> coll_mem;  // device arrays of the current colliders (rebuilt on every set)
+    int *coll_slots_cnt = nullptr; // per-vertex contact slots (arena), allocated with the first collider
+    int *coll_slots_face = nullptr;
+    float4 *coll_slots_w = nullptr;
+
+    void free_collider_arrays() {
+        for (void *q : coll_mem) cudaFree(q);
+        coll_mem.clear();
+    }
+
     ~lc_batch() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         if (cap_stream) cudaStreamDestroy(cap_stream);
+        free_collider_arrays();
     }
 
     void invalidate_graph() {
@@ -453,6 +475,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     scan_u32(d.hitg_cnt[1], d.hitg_off[1], d.hitg_n + 1, 0, hcap, d.scan_tmp, nee, &d.counters[2], st);
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 3, st);  // write contacts
     launch_narrow(d, npairs, ncand, ncand_e, narrow_grid, 4, st);  // per-cloth ranges
+    launch_collider(d, narrow_grid, st);                            // static colliders (lc_batch_set_collider)
     LC_PHASE(5);
     // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
     // per-vertex contact CSR feeds the gather solvers; the scatter solver
@@ -626,6 +649,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
         cd.lra_off = LRA;
         cd.s_off = (int)E; cd.s_cnt = (int)hc.s_ids.size();
         cd.b_off = (int)B; cd.b_cnt = (int)hc.b_ids.size();
+        cd.coll_root = -1;
+        cd.coll_cw = 0;
         b->e_off[c] = (int)E; b->b_off[c] = (int)B;
         b->s_count[c] = (int)hc.s_ids.size();
         b->b_count[c] = (int)hc.b_ids.size();
@@ -1166,11 +1191,12 @@ lc_status lc_batch_sync(lc_batch *b) {
     LC_CUDA(cudaDeviceSynchronize());
     uint32_t err = 0;
     LC_CUDA(cudaMemcpy(&err, b->d.err, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err & (ERR_VF_OVERFLOW | ERR_EE_OVERFLOW | ERR_DYN_OVERFLOW | ERR_CAND_OVERFLOW)) {
+    if (err & (ERR_VF_OVERFLOW | ERR_EE_OVERFLOW | ERR_DYN_OVERFLOW | ERR_CAND_OVERFLOW | ERR_COLL_OVERFLOW)) {
         cudaMemset(b->d.err, 0, sizeof(uint32_t));
-        return fail(LC_ERR_CAPACITY_OVERFLOW, (err & ERR_CAND_OVERFLOW)
-                                                  ? "narrowphase candidate capacity exceeded; raise lc_batch_options.cand_capacity"
-                                                  : "contact capacity exceeded; raise lc_batch_options.vf/ee_capacity");
+        return fail(LC_ERR_CAPACITY_OVERFLOW,
+                    (err & ERR_CAND_OVERFLOW)   ? "narrowphase candidate capacity exceeded; raise lc_batch_options.cand_capacity"
+                    : (err & ERR_COLL_OVERFLOW) ? "more static-collider contacts at a vertex than LC_COLLIDER_SLOTS"
+                                                : "contact capacity exceeded; raise lc_batch_options.vf/ee_capacity");
     }
     if (err & ERR_STACK) {
         cudaMemset(b->d.err, 0, sizeof(uint32_t));
@@ -1460,6 +1486,129 @@ lc_status lc_batch_set_sphere(lc_batch *b, int32_t c, const float pos[3], float 
     return LC_OK;
 }
 
+extern "C++" {
+// A median-split BVH over one collider's triangles, appended to the flat node
+// arrays: leaves hold one triangle each with the triangle's box (the query
+// inflates the vertex's box instead), internal nodes the union of their
+// children's boxes.  Returns the root's index.
+static int build_collider_node(const std::vector<float3> &bmin, const std::vector<float3> &bmax,
+                               const std::vector<float3> &cen, std::vector<int> &idx, int b, int e, int tri_base,
+                               std::vector<float4> &nmin, std::vector<float4> &nmax, std::vector<int2> &child) {
+    const int node = (int)nmin.size();
+    nmin.emplace_back();
+    nmax.emplace_back();
+    child.emplace_back();
+    if (e - b == 1) {
+        const int t = idx[b];
+        nmin[node] = f4(bmin[t], 0.f);
+        nmax[node] = f4(bmax[t], 0.f);
+        child[node] = make_int2(-(tri_base + t) - 1, -1);
+        return node;
+    }
+    float3 lo = cen[idx[b]], hi = lo;
+    for (int k = b + 1; k < e; ++k) { lo = vmin(lo, cen[idx[k]]); hi = vmax(hi, cen[idx[k]]); }
+    const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+    const int axis = ex >= ey && ex >= ez ? 0 : (ey >= ez ? 1 : 2);
+    const int mid = (b + e) / 2;
+    auto key = [&](int t) { return axis == 0 ? cen[t].x : (axis == 1 ? cen[t].y : cen[t].z); };
+    std::nth_element(idx.begin() + b, idx.begin() + mid, idx.begin() + e,
+                     [&](int p, int q) { return key(p) < key(q) || (key(p) == key(q) && p < q); });
+    const int l = build_collider_node(bmin, bmax, cen, idx, b, mid, tri_base, nmin, nmax, child);
+    const int r = build_collider_node(bmin, bmax, cen, idx, mid, e, tri_base, nmin, nmax, child);
+    nmin[node] = f4(vmin(xyz(nmin[l]), xyz(nmin[r])), 0.f);
+    nmax[node] = f4(vmax(xyz(nmax[l]), xyz(nmax[r])), 0.f);
+    child[node] = make_int2(l, r);
+    return node;
+}
+
+// A host vector in a fresh device array whose pointer `owner` keeps.
+template <class T>
+static lc_status upload_owned(std::vector<void *> &owner, const std::vector<T> &vec, const T *&dst) {
+    void *q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * std::max<size_t>(vec.size(), 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(LC_ERR_OOM, "lc_batch_set_collider: cudaMalloc failed");
+    }
+    owner.push_back(q);
+    if (!vec.empty()) LC_CUDA(cudaMemcpy(q, vec.data(), sizeof(T) * vec.size(), cudaMemcpyHostToDevice));
+    dst = static_cast<const T *>(q);
+    return LC_OK;
+}
+}  // extern "C++"
+
+lc_status lc_batch_set_collider(lc_batch *b, int32_t c, const float *vertices, int32_t num_vertices,
+                                const uint32_t *indices, int32_t num_triangles, int32_t winding) {
+    if (!b || c < 0 || c >= b->C || num_vertices < 0 || num_triangles < 0 ||
+        (winding != LC_WINDING_CCW && winding != LC_WINDING_CW) ||
+        (num_triangles > 0 && (!vertices || !indices || num_vertices < 3)))
+        return fail(LC_ERR_INVALID_ARG, "lc_batch_set_collider: bad arguments");
+    for (int64_t k = 0; k < 3 * (int64_t)num_triangles; ++k)
+        if (indices[k] >= (uint32_t)num_vertices)
+            return fail(LC_ERR_INVALID_ARG, "lc_batch_set_collider: index out of range");
+    if (b->opt.adjoint && num_triangles > 0)
+        return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_collider: colliders are not differentiated");
+    LC_CUDA(cudaDeviceSynchronize());
+    if (b->colliders.empty()) b->colliders.resize(b->C);
+    b->colliders[c].verts.assign(vertices, vertices + 3 * (size_t)(num_triangles ? num_vertices : 0));
+    b->colliders[c].tris.assign(indices, indices + 3 * (size_t)num_triangles);
+    b->colliders[c].cw = winding == LC_WINDING_CW;
+    // every cloth's collider into flat arrays, one BVH per cloth
+    std::vector<float4> cv, nmin, nmax;
+    std::vector<int4> ct;
+    std::vector<int2> child;
+    bool any = false;
+    for (int k = 0; k < b->C; ++k) {
+        ClothDev &cd = b->cds[k];
+        lc_batch::Collider &col = b->colliders[k];
+        const int T = (int)(col.tris.size() / 3);
+        cd.coll_cw = col.cw ? 1 : 0;
+        if (!T) { cd.coll_root = -1; continue; }
+        any = true;
+        const int vbase = (int)cv.size(), tbase = (int)ct.size();
+        col.tbase = tbase;
+        const int NV = (int)(col.verts.size() / 3);
+        for (int v = 0; v < NV; ++v)
+            cv.push_back(make_float4(col.verts[3 * v], col.verts[3 * v + 1], col.verts[3 * v + 2], 0.f));
+        std::vector<float3> bmin(T), bmax(T), cen(T);
+        for (int t = 0; t < T; ++t) {
+            const uint32_t *q = &col.tris[3 * (size_t)t];
+            ct.push_back(make_int4(vbase + (int)q[0], vbase + (int)q[1], vbase + (int)q[2], k));
+            const float3 p0 = xyz(cv[vbase + q[0]]), p1 = xyz(cv[vbase + q[1]]), p2 = xyz(cv[vbase + q[2]]);
+            bmin[t] = min3(p0, p1, p2);
+            bmax[t] = max3(p0, p1, p2);
+            cen[t] = f3((bmin[t].x + bmax[t].x) * 0.5f, (bmin[t].y + bmax[t].y) * 0.5f, (bmin[t].z + bmax[t].z) * 0.5f);
+        }
+        std::vector<int> idx(T);
+        std::iota(idx.begin(), idx.end(), 0);
+        cd.coll_root = build_collider_node(bmin, bmax, cen, idx, 0, T, tbase, nmin, nmax, child);
+    }
+    b->free_collider_arrays();
+    DevPtrs &d = b->d;
+    d.cv = nullptr; d.ct = nullptr; d.cnmin = d.cnmax = nullptr; d.cnchild = nullptr;
+    if (any) {
+        LC_TRY(upload_owned(b->coll_mem, cv, d.cv));
+        LC_TRY(upload_owned(b->coll_mem, ct, d.ct));
+        LC_TRY(upload_owned(b->coll_mem, nmin, d.cnmin));
+        LC_TRY(upload_owned(b->coll_mem, nmax, d.cnmax));
+        LC_TRY(upload_owned(b->coll_mem, child, d.cnchild));
+        if (!b->coll_slots_cnt) {
+            const size_t V = (size_t)d.Vtot;
+            LC_TRY(b->arena.alloc(b->coll_slots_cnt, V, "collider counts"));
+            LC_TRY(b->arena.alloc(b->coll_slots_face, V * kColliderSlots, "collider faces"));
+            LC_TRY(b->arena.alloc(b->coll_slots_w, V * kColliderSlots, "collider planes"));
+            LC_CUDA(cudaMemset(b->coll_slots_cnt, 0, sizeof(int) * V));
+        }
+    }
+    d.ccnt = b->coll_slots_cnt;
+    d.cface = b->coll_slots_face;
+    d.cw = b->coll_slots_w;
+    d.any_collider = any ? 1 : 0;
+    if (b->coll_slots_cnt && !any) LC_CUDA(cudaMemset(b->coll_slots_cnt, 0, sizeof(int) * (size_t)d.Vtot));
+    LC_CUDA(cudaMemcpy(b->cloth_dev, b->cds.data(), sizeof(ClothDev) * b->cds.size(), cudaMemcpyHostToDevice));
+    b->invalidate_graph();
+    return LC_OK;
+}
+
 lc_status lc_batch_set_stiffness(lc_batch *b, int32_t c, const float *ks, const float *kb) {
     if (!b || c < 0 || c >= b->C) return fail(LC_ERR_INVALID_ARG, "bad cloth index");
     const HostCloth &hc = b->hosts[c];
@@ -1705,6 +1854,33 @@ lc_status lc_batch_debug_get(lc_batch *b, int32_t c, int32_t what, void *dst, ui
             }
             if (count) *count = outv.size();
             if (dst && !outv.empty()) std::memcpy(dst, outv.data(), sizeof(lc_contact) * std::min<uint64_t>(outv.size(), cap));
+            return LC_OK;
+        }
+        case LC_DBG_COLLIDER: {
+            const size_t K = kColliderSlots, n = (size_t)cd.V * K;
+            std::vector<lc_contact> outv(n);
+            for (size_t i = 0; i < n; ++i) {
+                outv[i] = lc_contact{};
+                outv[i].v[0] = (int)(i / K);
+                outv[i].v[1] = -1;
+            }
+            if (d.any_collider && b->coll_slots_cnt) {
+                std::vector<int> cnt(cd.V), face(n);
+                std::vector<float4> w(n);
+                LC_CUDA(cudaMemcpy(cnt.data(), d.ccnt + cd.v_off, sizeof(int) * cd.V, cudaMemcpyDeviceToHost));
+                LC_CUDA(cudaMemcpy(face.data(), d.cface + (size_t)cd.v_off * K, sizeof(int) * n, cudaMemcpyDeviceToHost));
+                LC_CUDA(cudaMemcpy(w.data(), d.cw + (size_t)cd.v_off * K, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+                const int tbase = b->colliders.empty() ? 0 : b->colliders[c].tbase;
+                for (int v = 0; v < cd.V; ++v)
+                    for (int k = 0; k < cnt[v] && k < (int)K; ++k) {
+                        lc_contact &o = outv[(size_t)v * K + k];
+                        o.v[1] = face[(size_t)v * K + k] - tbase;
+                        const float4 q = w[(size_t)v * K + k];
+                        o.w[0] = q.x; o.w[1] = q.y; o.w[2] = q.z; o.w[3] = q.w;
+                    }
+            }
+            if (count) *count = n;
+            if (dst) std::memcpy(dst, outv.data(), sizeof(lc_contact) * std::min<uint64_t>(n, cap));
             return LC_OK;
         }
         case LC_DBG_VF_NORMAL: {

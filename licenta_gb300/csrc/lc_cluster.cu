@@ -230,7 +230,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
                 }
             }
             // FinalCorrectionStep, Physics/CudaPBD.cu:1690-1698
-            xb[i] = f4(add(xi, dvs(acc, (float)cnt)), xi4.w);
+            float3 xn = add(xi, dvs(acc, (float)cnt));
+            if (d.any_collider && xi4.w != 0.f) xn = collider_project(d, g, xn, h);
+            xb[i] = f4(xn, xi4.w);
         }
         cluster.sync();
         float4 *t = xa;
@@ -499,6 +501,7 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             x4.x += (__int2float_rn(sx) * kFixInv) / n;
             x4.y += (__int2float_rn(sy) * kFixInv) / n;
             x4.z += (__int2float_rn(sz) * kFixInv) / n;
+            if (d.any_collider && x4.w != 0.f) x4 = f4(collider_project(d, g, xyz(x4), h), x4.w);
             xs[i] = x4;
             axc[i] = ayz[i] = 0ull;
         }

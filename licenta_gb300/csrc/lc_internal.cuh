@@ -19,6 +19,9 @@ constexpr int kTraverseStack = 64;       // Collision/CudaBVH.cu:38
 constexpr int kTraverseBlockMax = 256;   // largest traversal block (the packet kernel is bounded for 6 of them per SM)
 constexpr int kScanBlocks = 1024;        // fixed grid of the device-count scans
 constexpr int kPairGroup = 32;           // consecutive pairs per narrowphase expansion warp (one per lane)
+constexpr int kColliderSlots = LC_COLLIDER_SLOTS;  // static-collider contacts kept per cloth vertex and step
+constexpr int kColliderStack = 64;       // collider BVH traversal stack
+constexpr float kColliderMargin = 4.f;   // collider detection reach beyond the contact layer, in thicknesses
 
 // Device error word bits (latched, reported by lc_batch_sync).
 enum : uint32_t {
@@ -28,6 +31,7 @@ enum : uint32_t {
     ERR_TREE = 1u << 3,
     ERR_DYN_OVERFLOW = 1u << 4,
     ERR_CAND_OVERFLOW = 1u << 5,
+    ERR_COLL_OVERFLOW = 1u << 6,   // more static-collider contacts at a vertex than kColliderSlots
 };
 
 // Per-cloth descriptor in device memory.
@@ -57,6 +61,8 @@ struct ClothDev {
     float wind_var_min, wind_var_max;
     int s_off, s_cnt;      // stretch constraints of the cloth (global range)
     int b_off, b_cnt;      // bend constraints
+    int coll_root;         // root node of the cloth's static collider BVH, -1 without one
+    int coll_cw;           // 1: the collider's faces turn clockwise seen from its free side
 };
 
 // Mutable per-cloth state that kernels update on the device (wind + RNG).
@@ -157,6 +163,15 @@ struct DevPtrs {
     uint8_t *dbg_dyn_nz;      // per iteration x dynamic entry: correction was non-zero
     int8_t *dbg_sphere;       // per vertex: ray-sphere outcome (-1, 0, 1)
     float kpi_gap;            // pi - (float)3.14159265359f, rest-angle offset of the bend term
+    // static triangle colliders (lc_batch_set_collider), all cloths' in flat arrays
+    const float4 *cv;         // collider vertices
+    const int4 *ct;           // collider triangles: global vertex ids, w = cloth
+    const float4 *cnmin, *cnmax;  // collider BVH node boxes
+    const int2 *cnchild;      // children, or (-(triangle + 1), -1) at a leaf
+    int *ccnt;                // per cloth vertex: collider contacts of the step (<= kColliderSlots)
+    int *cface;               // per cloth vertex x slot: collider triangle (global), ascending
+    float4 *cw;               // per cloth vertex x slot: the contact's plane (unit normal to the free side, n . a)
+    int any_collider;
 };
 
 // Reverse pass of one step (lc_adjoint.cu): the recorded step's tape and the

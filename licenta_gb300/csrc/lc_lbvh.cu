@@ -1224,10 +1224,108 @@ __global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncv, co
 }
 
 // ---------------------------------------------------------------------------
+// Static triangle colliders (lc_batch_set_collider; no counterpart in the
+// reference, whose sphere is analytic).  One thread per cloth vertex walks
+// its cloth's collider BVH with the vertex's swept box inflated by h + m
+// (m = kColliderMargin h).  For a face with unit normal n towards the free
+// side (the winding given to lc_batch_set_collider) and d0 = n . a, the
+// vertex's signed heights s0 = n . x_prev - d0 and s1 = n . x - d0 (x the
+// prediction) make it a contact when it ends within reach of the face's
+// layer (s1 < h + m) without having started far behind it (s0 > -m), and the
+// point where it crosses the plane (without a crossing, its prediction) lies
+// on the triangle: barycentric coordinates >= -h / perimeter, the tolerance
+// of the reference's TestVF (Collision/CudaPrimitiveTests.cu:348-406).  The
+// motion is the prediction's straight line, so the test is exact.  The reach
+// lets the constraint act on a vertex that the solver iterations drag
+// towards the face after this test, and brings back one that ended a step
+// behind it; a contact above its layer is inactive, the constraint being
+// one-sided.  A contact records the face and its plane (n, d0): the
+// constraint n . x >= d0 + h, onto which the vertex is projected here, in
+// slot order, and again at the end of every solver iteration.  The
+// kColliderSlots lowest faces are kept, ascending, so the result does not
+// depend on the traversal order.
+// ---------------------------------------------------------------------------
+__device__ bool collider_hit(float3 xp, float3 x, float3 a, float3 b, float3 c, float3 n, float d0, float h,
+                             float m) {
+    const float s0 = dot(n, xp) - d0, s1 = dot(n, x) - d0;
+    if (!(s1 < h + m) || !(s0 > -m)) return false;
+    const float3 q = (s0 > 0.f && s1 < 0.f) ? add(xp, mul(sub(x, xp), s0 / (s0 - s1))) : x;
+    const float3 e1 = sub(b, a), e2 = sub(c, a), e3 = sub(c, b), r = sub(q, a);
+    const float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2), d20 = dot(r, e1), d21 = dot(r, e2);
+    const float den = d00 * d11 - d01 * d01;
+    if (!(den > 0.f)) return false;
+    const float wb = (d11 * d20 - d01 * d21) / den, wc = (d00 * d21 - d01 * d20) / den;
+    const float wa = 1.f - wb - wc;
+    const float del = h / (len(e1) + len(e2) + len(e3));
+    return wa >= -del && wb >= -del && wc >= -del;
+}
+
+__global__ void k_collider_query(DevPtrs d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.Vtot; i += gridDim.x * blockDim.x) {
+        const ClothDev &cd = d.cloth[d.vcloth[i]];
+        int n = 0;
+        int face[kColliderSlots];
+        float4 pln[kColliderSlots];
+        const float4 x4 = d.x[i];
+        const float h = cd.h;
+        if (cd.coll_root >= 0) {
+            const float m = kColliderMargin * h, hm = h + m;
+            const float3 xi = xyz(x4), xpi = xyz(d.xp[i]);
+            const float3 lo = subc(vmin(xi, xpi), hm), hi = addc(vmax(xi, xpi), hm);
+            int stack[kColliderStack];
+            int top = 0;
+            stack[top++] = cd.coll_root;
+            while (top > 0) {
+                const int node = stack[--top];
+                if (!overlap(lo, hi, xyz(d.cnmin[node]), xyz(d.cnmax[node]))) continue;
+                const int2 ch = d.cnchild[node];
+                if (ch.x >= 0) {
+                    if (top + 2 > kColliderStack) { atomicOr(d.err, ERR_STACK); break; }
+                    stack[top++] = ch.y;
+                    stack[top++] = ch.x;
+                    continue;
+                }
+                const int tri = -(ch.x + 1);
+                const int4 t = d.ct[tri];
+                const float3 x1 = xyz(d.cv[t.x]), x2 = xyz(d.cv[t.y]), x3 = xyz(d.cv[t.z]);
+                float3 nf = normalize(cross(sub(x2, x1), sub(x3, x1)));
+                if (cd.coll_cw) nf = mul(nf, -1.f);
+                const float d0 = dot(nf, x1);
+                if (!collider_hit(xpi, xi, x1, x2, x3, nf, d0, h, m)) continue;
+                // keep the kColliderSlots lowest faces, ascending
+                if (n == kColliderSlots && tri > face[n - 1]) { atomicOr(d.err, ERR_COLL_OVERFLOW); continue; }
+                if (n == kColliderSlots) atomicOr(d.err, ERR_COLL_OVERFLOW);
+                int k = n < kColliderSlots ? n++ : kColliderSlots - 1;
+                while (k > 0 && face[k - 1] > tri) {
+                    face[k] = face[k - 1];
+                    pln[k] = pln[k - 1];
+                    --k;
+                }
+                face[k] = tri;
+                pln[k] = f4(nf, d0);
+            }
+        }
+        d.ccnt[i] = n;
+        if (!n) continue;
+        float3 xn = xyz(x4);
+        for (int k = 0; k < n; ++k) {
+            d.cface[(size_t)i * kColliderSlots + k] = face[k];
+            d.cw[(size_t)i * kColliderSlots + k] = pln[k];
+            const float c = dot(xyz(pln[k]), xn) - pln[k].w - h;
+            if (c < 0.f) xn = add(xn, mul(xyz(pln[k]), -c));
+        }
+        if (x4.w != 0.f) d.x[i] = f4(xn, x4.w);  // pinned vertices do not move
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
 static inline int nblk(int64_t n, int b = kThreads) { return (int)((n + b - 1) / b); }
 
+void launch_collider(const DevPtrs &d, int grid, cudaStream_t st) {
+    if (d.Vtot && d.any_collider) k_collider_query<<<grid, kThreads, 0, st>>>(d);
+}
 void launch_triangles(const DevPtrs &d, cudaStream_t st) {
     if (d.Ttot) k_triangles<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
 }

@@ -178,4 +178,21 @@ __device__ __forceinline__ void contact_all_pos(float4 A, float4 B, float4 C, fl
     out[3] = mul(mul(neg(n), b[3]), -s * D.w);
 }
 
+// Static-collider contacts of vertex i (lc_batch_set_collider): each slot's
+// plane (unit normal n towards the free side, d0 = n . a) is the one-sided
+// constraint n . x >= d0 + h on the vertex alone (the face does not move).
+// The vertex is projected onto them in slot order at the end of every solver
+// iteration, after the Jacobi average: collisions are projected last, so the
+// averaged stretch and bend corrections cannot pull a vertex that crossed a
+// face back through it.  The caller skips pinned vertices.
+__device__ __forceinline__ float3 collider_project(const DevPtrs &d, int i, float3 x, float h) {
+    const int nc = d.ccnt[i];
+    for (int k = 0; k < nc; ++k) {
+        const float4 pl = d.cw[(size_t)i * kColliderSlots + k];
+        const float c = dot(xyz(pl), x) - pl.w - h;
+        if (c < 0.f) x = add(x, mul(xyz(pl), -c));
+    }
+    return x;
+}
+
 }  // namespace lc

@@ -423,7 +423,9 @@ __global__ void k_jacobi(DevPtrs d, const float4 *__restrict__ xa, float4 *__res
         }
     }
     // FinalCorrectionStep, Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
-    xb[i] = f4(add(xi, dvs(acc, (float)cnt)), xi4.w);
+    float3 xn = add(xi, dvs(acc, (float)cnt));
+    if (d.any_collider && xi4.w != 0.f) xn = collider_project(d, i, xn, cd.h);
+    xb[i] = f4(xn, xi4.w);
 }
 
 // _FinalUpdate (Physics/CudaPBD.cu:1916-1932) then _WorldConstraints

@@ -30,6 +30,9 @@ class ClothSpec:
     pinned: np.ndarray         # (V,) uint8
     params: _ffi.ClothParams
     meta: dict = field(default_factory=dict)
+    # static triangle collider: (vertices (N, 3) float32, indices (M, 3)
+    # uint32, winding "ccw" | "cw" seen from the free side)
+    collider: tuple | None = None
 
     @property
     def num_vertices(self) -> int:
@@ -82,7 +85,8 @@ def default_params() -> _ffi.ClothParams:
 
 
 def icosphere(depth: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
-    """Rendering/VisualBodyFactory.cpp:259-341 (unwelded vertices)."""
+    """Rendering/VisualBodyFactory.cpp:259-341 (unwelded vertices; the faces
+    turn clockwise seen from outside)."""
     t = _ffi.lib().lc_mesh_icosphere(depth, None, None)
     v = np.empty((3 * t // 4 * 2, 3), dtype=np.float32)
     idx = np.empty((t, 3), dtype=np.uint32)
@@ -157,6 +161,26 @@ def large_cloth(seed: int = 0, n: int = 512, iterations: int = 20, stiffness: fl
     pos = grid_positions(n, rng, origin=(-0.5, -0.5))
     return ClothSpec(pos, grid_indices(n), np.zeros(n * n, dtype=np.uint8), p,
                      dict(workload="plain-large", n=n, steps=300))
+
+
+def icosphere_cloth(seed: int = 0, n: int = 32, depth: int = 3, radius: float = 0.3, iterations: int = 10,
+                    stiffness: float = 0.9, height: float = 0.5, span: float = 1.0) -> ClothSpec:
+    """An n x n cloth `span` metres wide centred over the origin at y =
+    `height` (no pins), dropped onto a static icosphere of subdivision
+    `depth` and radius `radius` at the origin, given as a triangle collider
+    (lc_batch_set_collider); the analytic sphere is off.  World box and
+    Morton frame [-1, 1]^3."""
+    rng = np.random.default_rng(seed)
+    p = base_params(iterations, stiffness)
+    p.dims[:] = (n, n)
+    p.worldMin[:] = (-1.0, -1.0, -1.0)
+    p.worldMax[:] = (1.0, 1.0, 1.0)
+    p.mortonOrigin[:] = (-1.0, -1.0, -1.0)
+    p.mortonScale = 0.5
+    pos = grid_positions(n, rng, y=height, span=span, origin=(-span / 2, -span / 2))
+    return ClothSpec(pos, grid_indices(n), np.zeros(n * n, dtype=np.uint8), p,
+                     dict(workload="icosphere", n=n, depth=depth, r=radius),
+                     collider=(*icosphere(depth, radius), "cw"))
 
 
 def batched_cloths(seed: int = 0, count: int = 256, n_min: int = 16, n_max: int = 192,

@@ -441,6 +441,22 @@ template <class R> class Cloth {
     u64 dropped = 0;
     int stack_overflow = 0;
 
+    // Static triangle collider of the engine's lc_batch_set_collider (no
+    // counterpart in the reference): its mesh and winding, and per vertex the
+    // step's contacts (kCollSlots, ascending triangle; triangle -1 unused; a
+    // contact's w holds its plane: unit normal towards the free side, n . a).
+    static constexpr int kCollSlots = 8;
+    static constexpr float kCollMargin = 4.0f;  // detection reach beyond the contact layer, in thicknesses
+    std::vector<V> coll_v;
+    std::vector<int> coll_t;
+    bool coll_cw = false;  // faces clockwise seen from the free side
+    std::vector<int> coll_tri;
+    std::vector<Contact> coll_c;
+    bool coll_overflow = false;
+    bool have_frozen_coll = false;
+    std::vector<int> frozen_coll_tri;
+    std::vector<Contact> frozen_coll_c;
+
     bool have_frozen = false;
     std::vector<Contact> frozen_vf, frozen_ee;
     std::vector<V> frozen_vf_n;  // their face normals, for friction (empty: no friction on frozen contacts)
@@ -669,6 +685,89 @@ template <class R> class Cloth {
         refit();
         traverse();
         narrowphase();
+        collider_contacts();
+    }
+
+    // The static collider's contacts of every vertex (the engine's
+    // k_collider_query; no counterpart in the reference).  For a face with
+    // unit normal n towards the free side and d0 = n . a, the signed heights
+    // s0 = n . x_prev - d0, s1 = n . x - d0 (x the prediction) make it a
+    // contact when s1 < h + m and s0 > -m (m = kCollMargin h) and the point
+    // where the vertex crosses the plane (without a crossing, the
+    // prediction) has barycentric coordinates >= -h / perimeter (TestVF's
+    // tolerance, Collision/CudaPrimitiveTests.cu:348-406).  The reach lets
+    // the constraint act on a vertex the solver iterations drag towards the
+    // face after detection, and brings back one that ended a step behind it;
+    // the constraint is one-sided, so a contact above its layer is inactive.
+    // Only faces whose boxes meet the vertex's swept box inflated by h + m
+    // are tested (the engine's BVH culls the same way).  The hits in
+    // ascending triangle order, at most kCollSlots (more sets coll_overflow).
+    static bool collider_hit(V xp, V x, V a, V b, V c, V n, R d0, R h, R m) {
+        const R s0 = dot(n, xp) - d0, s1 = dot(n, x) - d0;
+        if (!(s1 < h + m) || !(s0 > -m)) return false;
+        const V q = (s0 > R(0) && s1 < R(0)) ? xp + (x - xp) * (s0 / (s0 - s1)) : x;
+        const V e1 = b - a, e2 = c - a, e3 = c - b, r = q - a;
+        const R d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2), d20 = dot(r, e1), d21 = dot(r, e2);
+        const R den = d00 * d11 - d01 * d01;
+        if (!(den > R(0))) return false;
+        const R wb = (d11 * d20 - d01 * d21) / den, wc = (d00 * d21 - d01 * d20) / den;
+        const R wa = R(1) - wb - wc;
+        const R del = h / (len(e1) + len(e2) + len(e3));
+        return wa >= -del && wb >= -del && wc >= -del;
+    }
+    void collider_contacts() {
+        const int Vn = tp.V, K = kCollSlots, T = (int)(coll_t.size() / 3);
+        coll_tri.assign((size_t)Vn * K, -1);
+        coll_c.assign((size_t)Vn * K, Contact{});
+        coll_overflow = false;
+        if (!T) return;
+        const R hh = R(h), mm = R(kCollMargin) * hh, hm = hh + mm;
+        for (int i = 0; i < Vn; ++i) {
+            const V lo = subc(vmin(x[i], xp[i]), hm), hi = addc(vmax(x[i], xp[i]), hm);
+            int n = 0;
+            for (int t = 0; t < T; ++t) {
+                const V a = coll_v[coll_t[3 * t]], b = coll_v[coll_t[3 * t + 1]], c = coll_v[coll_t[3 * t + 2]];
+                if (!overlap(lo, hi, min3(a, b, c), max3(a, b, c))) continue;
+                V nf = normalize(cross(b - a, c - a));
+                if (coll_cw) nf = nf * R(-1);
+                const R d0 = dot(nf, a);
+                if (!collider_hit(xp[i], x[i], a, b, c, nf, d0, hh, mm)) continue;
+                if (n == K) { coll_overflow = true; break; }
+                Contact k;
+                k.v[0] = i; k.v[1] = k.v[2] = k.v[3] = 0;
+                k.w[0] = float(nf.x); k.w[1] = float(nf.y); k.w[2] = float(nf.z); k.w[3] = float(d0);
+                coll_tri[(size_t)i * K + n] = t;
+                coll_c[(size_t)i * K + n] = k;
+                ++n;
+            }
+        }
+    }
+
+    // A vertex projected onto its collider contacts' one-sided constraints
+    // n . x >= d0 + h, in slot order (this step's contacts, or the frozen
+    // ones); pinned vertices do not move.  Done before the solver (as the
+    // reference projects onto its analytic sphere before the iterations,
+    // Physics/CudaPBD.cu:1509-1569) and at the end of every iteration, after
+    // the Jacobi average: collisions are projected last, so the averaged
+    // stretch and bend corrections cannot pull a vertex that crossed a face
+    // back through it.
+    void coll_project_vertex(int i) {
+        if (invm[i] == R(0)) return;
+        const int K = kCollSlots;
+        const std::vector<int> &ctri = have_frozen_coll ? frozen_coll_tri : coll_tri;
+        const std::vector<Contact> &cc = have_frozen_coll ? frozen_coll_c : coll_c;
+        if (ctri.size() < (size_t)(i + 1) * K) return;
+        const R th = R(h);
+        for (int k = 0; k < K && ctri[(size_t)i * K + k] >= 0; ++k) {
+            const Contact &q = cc[(size_t)i * K + k];
+            const V n = mk<R>(R(q.w[0]), R(q.w[1]), R(q.w[2]));
+            const R c = dot(n, x[i]) - R(q.w[3]) - th;
+            if (c < R(0)) x[i] = x[i] + n * (-c);
+        }
+    }
+    void coll_project() {
+        if (coll_t.empty()) return;
+        for (int i = 0; i < tp.V; ++i) coll_project_vertex(i);
     }
 
     // Collision/CudaBVH.cu:163-188.  Two internal nodes may claim the same
@@ -1116,6 +1215,8 @@ template <class R> class Cloth {
             }
             // Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
             for (int i = 0; i < Vn; ++i) x[i] = x[i] + acc[i] / R(cnt[i]);
+            if (!coll_t.empty())
+                for (int i = 0; i < Vn; ++i) coll_project_vertex(i);
             if (recording) rec.xk.push_back(x);
         }
     }
@@ -1605,12 +1706,14 @@ template <class R> class Cloth {
         external();
         pred_x = x; pred_xp = xp; pred_v = v;
         if (!(have_frozen && skip_collide)) collide();
+        coll_project();
         if (have_frozen)
             solve(frozen_vf, frozen_ee);
         else
             solve(vf, ee);
         const bool frozen = have_frozen;
         have_frozen = false;
+        have_frozen_coll = false;
         forced.on = false;
         integrate();
         if (prm.useFriction) {

@@ -190,6 +190,44 @@ int lco_step_one(lco_world *w, int c) {
     return with_cloth(w, c, [&](auto &cl) { cl.step(); return LC_OK; });
 }
 
+// The static triangle collider of lc_batch_set_collider (cw: faces clockwise
+// seen from the free side); nt = 0 removes it.
+int lco_set_collider(lco_world *w, int c, const float *verts, int nv, const uint32_t *tris, int nt, int cw) {
+    return with_cloth(w, c, [&](auto &cl) {
+        using R = std::remove_reference_t<decltype(cl.wind.x)>;
+        if (nt < 0 || nv < 0 || (nt && (!verts || !tris))) return (int)LC_ERR_INVALID_ARG;
+        for (int k = 0; k < 3 * nt; ++k)
+            if (tris[k] >= (uint32_t)nv) return (int)LC_ERR_INVALID_ARG;
+        cl.coll_cw = cw != 0;
+        cl.coll_v.resize(nt ? nv : 0);
+        for (int i = 0; i < (nt ? nv : 0); ++i)
+            cl.coll_v[i] = mk<R>(R(verts[3 * i]), R(verts[3 * i + 1]), R(verts[3 * i + 2]));
+        cl.coll_t.assign(tris, tris + 3 * (size_t)nt);
+        return (int)LC_OK;
+    });
+}
+
+// The next step uses these collider contacts (lc_contact records of the
+// engine's LC_DBG_COLLIDER: v[1] the triangle or -1, w the plane) instead of
+// its own.
+int lco_set_frozen_collider(lco_world *w, int c, const lc_contact *rec, uint64_t n) {
+    return with_cloth(w, c, [&](auto &cl) {
+        const int K = cl.kCollSlots;
+        if (n != (uint64_t)cl.tp.V * K) return (int)LC_ERR_INVALID_ARG;
+        cl.frozen_coll_tri.assign(n, -1);
+        cl.frozen_coll_c.assign(n, Contact{});
+        for (uint64_t i = 0; i < n; ++i) {
+            cl.frozen_coll_tri[i] = rec[i].v[1];
+            Contact k;
+            k.v[0] = (int)(i / K); k.v[1] = k.v[2] = k.v[3] = 0;
+            for (int j = 0; j < 4; ++j) k.w[j] = rec[i].w[j];
+            cl.frozen_coll_c[i] = k;
+        }
+        cl.have_frozen_coll = true;
+        return (int)LC_OK;
+    });
+}
+
 // The next step of cloth c uses these contacts instead of the ones its own
 // collision stage finds (contact sets frozen for position comparisons).
 int lco_set_frozen_contacts(lco_world *w, int c, const lc_contact *vf, uint64_t nvf, const lc_contact *ee,
@@ -239,7 +277,8 @@ int lco_counters(lco_world *w, int c, uint64_t out[4]) {
         out[1] = cl.vf.size();
         out[2] = cl.ee.size();
         out[3] = cl.dropped;
-        return cl.stack_overflow ? LC_ERR_STACK_OVERFLOW : LC_OK;
+        if (cl.stack_overflow) return (int)LC_ERR_STACK_OVERFLOW;
+        return cl.coll_overflow ? (int)LC_ERR_CAPACITY_OVERFLOW : (int)LC_OK;
     });
 }
 
@@ -288,6 +327,22 @@ int lco_debug_get(lco_world *w, int c, int what, void *dst, uint64_t cap, uint64
             }
             case LC_DBG_VF: return copy_out(cl.vf.data(), cl.vf.size(), dst, cap, count);
             case LC_DBG_EE: return copy_out(cl.ee.data(), cl.ee.size(), dst, cap, count);
+            case LC_DBG_COLLIDER: {
+                const int K = cl.kCollSlots;
+                const size_t n = (size_t)cl.tp.V * K;
+                std::vector<Contact> out(n);
+                for (size_t i = 0; i < n; ++i) {
+                    Contact k{};
+                    k.v[0] = (int)(i / K);
+                    k.v[1] = -1;
+                    if (i < cl.coll_tri.size() && cl.coll_tri[i] >= 0) {
+                        k.v[1] = cl.coll_tri[i];
+                        for (int j = 0; j < 4; ++j) k.w[j] = cl.coll_c[i].w[j];
+                    }
+                    out[i] = k;
+                }
+                return copy_out(out.data(), out.size(), dst, cap, count);
+            }
             case LC_DBG_FEATURES: return copy_out(cl.tp.features.data(), cl.tp.features.size(), dst, cap, count);
             default: return LC_ERR_INVALID_ARG;
         }
@@ -557,6 +612,7 @@ extern "C" int lco_adj_backward(lco_world *w, int c, double *gx, double *gxp, do
             av[i] = mk<R>(R(gv[3 * i]), R(gv[3 * i + 1]), R(gv[3 * i + 2]));
         }
         if (cl.tp.tri_bend) return (int)LC_ERR_NOT_SUPPORTED;  // triangle bending is not differentiated
+        if (!cl.coll_t.empty()) return (int)LC_ERR_NOT_SUPPORTED;  // nor are static colliders
         std::vector<double> ks(cl.tp.s1.size(), 0.0), kb(cl.tp.b1.size(), 0.0);
         for (int s = (int)cl.records.size() - 1; s >= 0; --s) cl.backward(cl.records[s], ax, axp, av, ks, kb);
         for (int i = 0; i < Vn; ++i) {

@@ -42,6 +42,8 @@ def lib() -> C.CDLL:
             "lco_collide": (C.c_int, [VP, C.c_int]),
             "lco_step_one": (C.c_int, [VP, C.c_int]),
             "lco_set_frozen_contacts": (C.c_int, [VP, C.c_int, VP, C.c_uint64, VP, C.c_uint64]),
+            "lco_set_collider": (C.c_int, [VP, C.c_int, VP, C.c_int, VP, C.c_int, C.c_int]),
+            "lco_set_frozen_collider": (C.c_int, [VP, C.c_int, VP, C.c_uint64]),
             "lco_set_stiffness": (C.c_int, [VP, C.c_int, VP, VP]),
             "lco_set_forced": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, C.c_uint64, VP]),
             "lco_thickness": (C.c_int, [VP, C.c_int, VP]),
@@ -118,6 +120,9 @@ class Oracle:
         self.n = len(specs)
         self.V = [s.num_vertices for s in specs]
         self.T = [s.num_triangles for s in specs]
+        for k, s in enumerate(specs):
+            if getattr(s, "collider", None) is not None:
+                self.set_collider(k, *s.collider)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -179,6 +184,23 @@ class Oracle:
     def set_wind(self, c: int, wind, rng: int) -> None:
         w = np.ascontiguousarray(wind, dtype=np.float64)
         _chk(lib().lco_set_wind(self._h, c, _p(w), rng), "set_wind")
+
+    def set_collider(self, c: int, vertices, indices, winding: str = "ccw") -> None:
+        """The static triangle collider of lc_batch_set_collider; winding
+        "cw" when the faces turn clockwise seen from the free side."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        cw = {"ccw": 0, "cw": 1}[winding]
+        _chk(lib().lco_set_collider(self._h, c, _p(v), len(v), _p(i), len(i), cw), "set_collider")
+
+    def freeze_collider(self, c: int, records) -> None:
+        """The next step takes these collider contacts (the engine's
+        LC_DBG_COLLIDER records as (ids, planes))."""
+        ids, w = records
+        rec = np.zeros((len(ids), 8), np.int32)
+        rec[:, :4] = np.asarray(ids, np.int32).reshape(-1, 4)
+        rec[:, 4:] = np.asarray(w, np.float32).reshape(-1, 4).view(np.int32)
+        _chk(lib().lco_set_frozen_collider(self._h, c, _p(rec), len(rec)), "set_frozen_collider")
 
     def freeze_contacts(self, c: int, vf: tuple, ee: tuple, vf_normals=None) -> None:
         def pack(t):  # lc_contact records: 4 int32 ids then 4 float32 weights
@@ -351,13 +373,14 @@ class Oracle:
     def counters(self, c: int) -> dict:
         out = (C.c_uint64 * 4)()
         rc = lib().lco_counters(self._h, c, out)
-        return dict(pairs=out[0], vf=out[1], ee=out[2], dropped=out[3], stack_overflow=rc != 0)
+        return dict(pairs=out[0], vf=out[1], ee=out[2], dropped=out[3], stack_overflow=rc == 7,
+                    collider_overflow=rc == 3)
 
     def debug(self, c: int, what: str):
         sel = _ffi.DBG[what]
         n = C.c_uint64()
         _chk(lib().lco_debug_get(self._h, c, sel, None, 0, C.byref(n)), "debug_get")
-        if sel in (13, 14):
+        if sel in (13, 14, 22):
             raw = np.empty((max(n.value, 1), 8), dtype=np.int32)
             _chk(lib().lco_debug_get(self._h, c, sel, _p(raw), n.value, C.byref(n)), "debug_get")
             raw = raw[:n.value]

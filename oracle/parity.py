@@ -43,6 +43,12 @@ def check_collision(batch, c, o32, pre_vn, tag=""):
         if not (np.array_equal(gv, rv) and np.array_equal(gw, rw)):
             raise AssertionError(f"{tag}: {what} contacts differ ({len(gv)} vs {len(rv)})")
         n += len(gv)
+    if getattr(batch.specs[c], "collider", None) is not None:
+        (gv, gw), (rv, rw) = batch.debug(c, "COLLIDER"), o32.debug(0, "COLLIDER")
+        if not (np.array_equal(gv, rv) and np.array_equal(gw, rw)):
+            raise AssertionError(f"{tag}: collider contacts differ ({int((gv[:, 1] >= 0).sum())} vs "
+                                 f"{int((rv[:, 1] >= 0).sum())})")
+        n += int((gv[:, 1] >= 0).sum())
     return n
 
 
@@ -54,6 +60,8 @@ def fp64_step_error(batch, c, o64, pre, perm, sphere: bool, friction: bool = Fal
     o64.freeze_contacts(0, vf, ee, batch.debug(c, "VF_NORMAL") if friction else None)
     o64.force_decisions(0, batch.debug(c, "GROUND"), batch.debug(c, "GROUND_ACTIVE"), batch.debug(c, "LRA"),
                         batch.debug(c, "DYN_ACTIVE"), batch.debug(c, "SPHERE") if sphere else None)
+    if getattr(batch.specs[c], "collider", None) is not None:
+        o64.freeze_collider(0, batch.debug(c, "COLLIDER"))
     o64.step_one(0)
     g = batch.get_state(c)
     r = o64.get_state(0)
@@ -153,6 +161,12 @@ def check_all_cloths(batch, specs, o32, o64, pre, tol=1e-5):
             if not (np.array_equal(gv, rv) and np.array_equal(gw, rw)):
                 raise AssertionError(f"cloth {c}: {what} contacts differ ({len(gv)} vs {len(rv)})")
             contacts += len(gv)
+        if getattr(specs[c], "collider", None) is not None:
+            (gv, gw), (rv, rw) = batch.debug(c, "COLLIDER"), o32.debug(c, "COLLIDER")
+            if not (np.array_equal(gv, rv) and np.array_equal(gw, rw)):
+                raise AssertionError(f"cloth {c}: collider contacts differ ({int((gv[:, 1] >= 0).sum())} vs "
+                                     f"{int((rv[:, 1] >= 0).sum())})")
+            contacts += int((gv[:, 1] >= 0).sum())
     for c, s in enumerate(specs):
         st, perm = pre[c]
         o64.set_state(c, **{k: v.astype(np.float64) for k, v in st.items()})
@@ -160,6 +174,8 @@ def check_all_cloths(batch, specs, o32, o64, pre, tol=1e-5):
         o64.freeze_contacts(c, batch.debug(c, "VF"), batch.debug(c, "EE"))
         o64.force_decisions(c, batch.debug(c, "GROUND"), batch.debug(c, "GROUND_ACTIVE"), batch.debug(c, "LRA"),
                             batch.debug(c, "DYN_ACTIVE"), batch.debug(c, "SPHERE") if s.params.sphereOn else None)
+        if getattr(s, "collider", None) is not None:
+            o64.freeze_collider(c, batch.debug(c, "COLLIDER"))
     o64.step_frozen_all()
     worst, excused = 0.0, 0
     for c, s in enumerate(specs):
