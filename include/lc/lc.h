@@ -272,7 +272,9 @@ lc_status lc_batch_set_sphere(lc_batch *b, int32_t cloth, const float pos[3], fl
  * (The reference's two-sided VF projection, averaged with the other
  * corrections, leaves a vertex that crossed a face within one step on the
  * far side; a static face has a side.)  A BVH over the triangles is built on
- * the host once per call.  Not for batches created with adjoint. */
+ * the host once per call.  In batches created with adjoint the reverse pass
+ * differentiates through the projections, with the contact planes held
+ * fixed as the recorded step found them. */
 #define LC_COLLIDER_SLOTS 8
 enum { LC_WINDING_CCW = 0, LC_WINDING_CW = 1 };
 lc_status lc_batch_set_collider(lc_batch *b, int32_t cloth, const float *vertices, int32_t num_vertices,

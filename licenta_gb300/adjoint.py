@@ -36,10 +36,19 @@ def _p(t: torch.Tensor | None):
 class DiffCloth:
     """A batch prepared for differentiable rollouts (adjoint tape kept)."""
 
-    def __init__(self, specs: Sequence[ClothSpec], checkpoint_every: int = 10, **batch_kw):
+    def __init__(self, specs: Sequence[ClothSpec], checkpoint_every: int = 10, unscale: bool = True, **batch_kw):
+        """unscale=False: ClothRollout's backward returns each cloth's
+        gradients as the reverse pass kept them, scaled by 2^(-60 e) with e =
+        grad_exponent[cloth] after the call.  They stay finite (and their
+        direction exact) where the true gradient of a long contact-rich
+        rollout is beyond float range, which is what per-cloth normalised
+        descent needs; unscale=True multiplies the scale back in (inf where
+        the true value exceeds float)."""
         self.batch = ClothBatch(specs, adjoint=True, use_graph=True, **batch_kw)
         self.h = self.batch._h
         self.every = max(1, int(checkpoint_every))
+        self.unscale = unscale
+        self.grad_exponent = torch.zeros(len(specs), dtype=torch.int32, device="cuda")
         L = _ffi.lib()
         n = C.c_uint64()
         _ffi.check(L.lc_batch_state_size(self.h, C.byref(n)), "lc_batch_state_size")
@@ -162,7 +171,11 @@ class ClothRollout(torch.autograd.Function):
                 # beyond float range).
                 cloth.adjoint_step(gx, gxp, gv, gks, gkb, exp60)
 
+        cloth.grad_exponent = exp60.clone()
+
         def unscale(t, idx):
+            if not cloth.unscale:
+                return t
             sc = torch.pow(torch.tensor(2.0 ** 60, device="cuda"), exp60.to(torch.float32))[idx]
             if t.dim() == 2:
                 sc = sc.unsqueeze(1)

@@ -2,7 +2,8 @@
 // global-memory solver path, with the step's discrete decisions held fixed as
 // the recorded forward step took them: the contact set and its weights, ground
 // and LRA activation, and the dynamic terms counted in each Jacobi iteration.
-// The analytic sphere and the wind term's vertex normals are held fixed.
+// The analytic sphere and the wind term's vertex normals are held fixed; the
+// static colliders' contact planes are fixed, their projections reversed.
 //
 // Given dL/d(x, x_prev, v) after the step, the kernels produce dL/d(x, x_prev,
 // v) before it and add dL/dk of every stretch and bend constraint.  Order:
@@ -347,6 +348,25 @@ __global__ void k_adj_fixed_add(DevPtrs d, AdjPtrs A, float4 *g, int nfixed) {
     A.fixed[3 * k] = A.fixed[3 * k + 1] = A.fixed[3 * k + 2] = 0.f;
 }
 
+// The static-collider projections of one pass reversed (lc_batch_set_collider):
+// each projected slot maps x to x - (n . x - d0 - h) n, whose Jacobian
+// I - n n^T is symmetric; the slots were applied in order, so their
+// transposes apply last slot first.  pass 0 is the projection before the
+// solver, pass it + 1 the one ending iteration it.
+__global__ void k_adj_collider(DevPtrs d, float4 *a, int pass) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.Vtot) return;
+    const uint32_t m = d.coll_act[(size_t)pass * d.Vtot + i];
+    if (!m) return;
+    float3 g = xyz(a[i]);
+    for (int k = kColliderSlots - 1; k >= 0; --k)
+        if ((m >> k) & 1u) {
+            const float3 n = xyz(d.cw[(size_t)i * kColliderSlots + k]);
+            g = sub(g, mul(n, dot(n, g)));
+        }
+    a[i] = f4(g, 0.f);
+}
+
 // ExplicitEuler reversed (x_p = x_prev + dt v_c) and the sums the damping
 // reverse needs: S1 = sum dL/dv_c, S2 = sum r x dL/dv_c, r = x - xcm.
 __global__ void k_adj_damp1(DevPtrs d, AdjPtrs A, const float4 *a) {
@@ -522,8 +542,10 @@ void launch_adj_rescale(const DevPtrs &d, float *gx, float *gxp, float *gv, floa
 void launch_adjoint(const DevPtrs &d, const AdjPtrs &A, float4 *a, float4 *g, const uint32_t *nvf, const uint32_t *nee,
                     int grid, int nfixed, float *gk_stretch, float *gk_bend, cudaStream_t st) {
     if (!d.Vtot) return;
+    const bool coll = d.any_collider && d.coll_act;
     k_adj_integrate<<<nb(d.Vtot), kThreads, 0, st>>>(d, A, a);
     for (int it = A.K - 1; it >= 0; --it) {
+        if (coll) k_adj_collider<<<nb(d.Vtot), kThreads, 0, st>>>(d, a, it + 1);
         k_adj_u<<<nb(d.Vtot), kThreads, 0, st>>>(d, A, a, it);
         if (A.E) k_adj_stretch<<<nb(A.E), kThreads, 0, st>>>(d, A, it, gk_stretch);
         if (A.B) k_adj_bend<<<nb(A.B, 128), 128, 0, st>>>(d, A, it, gk_bend);
@@ -532,6 +554,7 @@ void launch_adjoint(const DevPtrs &d, const AdjPtrs &A, float4 *a, float4 *g, co
         if (nfixed) k_adj_fixed_add<<<nb(nfixed), kThreads, 0, st>>>(d, A, g, nfixed);
         float4 *t = a; a = g; g = t;
     }
+    if (coll) k_adj_collider<<<nb(d.Vtot), kThreads, 0, st>>>(d, a, 0);
     k_adj_damp1<<<d.nvblk, kThreads, 0, st>>>(d, A, a);
     k_adj_totals<<<d.C, 32, 0, st>>>(d, A);
     k_adj_damp2<<<d.nvblk, kThreads, 0, st>>>(d, A);

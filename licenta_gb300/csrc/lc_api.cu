@@ -1545,8 +1545,6 @@ lc_status lc_batch_set_collider(lc_batch *b, int32_t c, const float *vertices, i
     for (int64_t k = 0; k < 3 * (int64_t)num_triangles; ++k)
         if (indices[k] >= (uint32_t)num_vertices)
             return fail(LC_ERR_INVALID_ARG, "lc_batch_set_collider: index out of range");
-    if (b->opt.adjoint && num_triangles > 0)
-        return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_collider: colliders are not differentiated");
     LC_CUDA(cudaDeviceSynchronize());
     if (b->colliders.empty()) b->colliders.resize(b->C);
     b->colliders[c].verts.assign(vertices, vertices + 3 * (size_t)(num_triangles ? num_vertices : 0));
@@ -1597,6 +1595,10 @@ lc_status lc_batch_set_collider(lc_batch *b, int32_t c, const float *vertices, i
             LC_TRY(b->arena.alloc(b->coll_slots_face, V * kColliderSlots, "collider faces"));
             LC_TRY(b->arena.alloc(b->coll_slots_w, V * kColliderSlots, "collider planes"));
             LC_CUDA(cudaMemset(b->coll_slots_cnt, 0, sizeof(int) * V));
+            if (b->opt.adjoint) {  // the reverse pass's record of the projections
+                LC_TRY(b->arena.alloc(d.coll_act, (size_t)(b->max_iters + 1) * V, "collider projection masks"));
+                LC_CUDA(cudaMemset(d.coll_act, 0, (size_t)(b->max_iters + 1) * V));
+            }
         }
     }
     d.ccnt = b->coll_slots_cnt;

@@ -171,6 +171,8 @@ struct DevPtrs {
     int *ccnt;                // per cloth vertex: collider contacts of the step (<= kColliderSlots)
     int *cface;               // per cloth vertex x slot: collider triangle (global), ascending
     float4 *cw;               // per cloth vertex x slot: the contact's plane (unit normal to the free side, n . a)
+    uint8_t *coll_act;        // adjoint batches: (iterations + 1) x vertex bit masks of the collider slots
+                              // projected, [0] before the solver, [it + 1] in iteration it (else null)
     int any_collider;
 };
 

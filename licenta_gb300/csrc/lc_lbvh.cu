@@ -1306,15 +1306,20 @@ __global__ void k_collider_query(DevPtrs d) {
             }
         }
         d.ccnt[i] = n;
-        if (!n) continue;
         float3 xn = xyz(x4);
+        uint32_t act = 0;
         for (int k = 0; k < n; ++k) {
             d.cface[(size_t)i * kColliderSlots + k] = face[k];
             d.cw[(size_t)i * kColliderSlots + k] = pln[k];
             const float c = dot(xyz(pln[k]), xn) - pln[k].w - h;
-            if (c < 0.f) xn = add(xn, mul(xyz(pln[k]), -c));
+            if (c < 0.f) {
+                xn = add(xn, mul(xyz(pln[k]), -c));
+                act |= 1u << k;
+            }
         }
-        if (x4.w != 0.f) d.x[i] = f4(xn, x4.w);  // pinned vertices do not move
+        if (x4.w == 0.f) act = 0;                  // pinned vertices do not move
+        else if (n) d.x[i] = f4(xn, x4.w);
+        if (d.coll_act) d.coll_act[i] = (uint8_t)act;  // the adjoint's record of the projection
     }
 }
 

@@ -185,13 +185,20 @@ __device__ __forceinline__ void contact_all_pos(float4 A, float4 B, float4 C, fl
 // iteration, after the Jacobi average: collisions are projected last, so the
 // averaged stretch and bend corrections cannot pull a vertex that crossed a
 // face back through it.  The caller skips pinned vertices.
-__device__ __forceinline__ float3 collider_project(const DevPtrs &d, int i, float3 x, float h) {
+// act (adjoint batches): receives the bit mask of the slots projected.
+__device__ __forceinline__ float3 collider_project(const DevPtrs &d, int i, float3 x, float h,
+                                                  uint8_t *act = nullptr) {
     const int nc = d.ccnt[i];
+    uint32_t m = 0;
     for (int k = 0; k < nc; ++k) {
         const float4 pl = d.cw[(size_t)i * kColliderSlots + k];
         const float c = dot(xyz(pl), x) - pl.w - h;
-        if (c < 0.f) x = add(x, mul(xyz(pl), -c));
+        if (c < 0.f) {
+            x = add(x, mul(xyz(pl), -c));
+            m |= 1u << k;
+        }
     }
+    if (act) *act = (uint8_t)m;
     return x;
 }
 

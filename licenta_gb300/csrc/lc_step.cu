@@ -357,7 +357,11 @@ __global__ void k_jacobi(DevPtrs d, const float4 *__restrict__ xa, float4 *__res
     const int c = d.vcloth[i];
     const ClothDev &cd = d.cloth[c];
     const float4 xi4 = xa[i];
-    if (it >= cd.iters) { xb[i] = xi4; return; }
+    if (it >= cd.iters) {
+        xb[i] = xi4;
+        if (d.coll_act) d.coll_act[(size_t)(it + 1) * d.Vtot + i] = 0;
+        return;
+    }
     const float3 xi = xyz(xi4);
     float3 acc = f3(0.f, 0.f, 0.f);
     int cnt = 0;
@@ -424,7 +428,11 @@ __global__ void k_jacobi(DevPtrs d, const float4 *__restrict__ xa, float4 *__res
     }
     // FinalCorrectionStep, Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
     float3 xn = add(xi, dvs(acc, (float)cnt));
-    if (d.any_collider && xi4.w != 0.f) xn = collider_project(d, i, xn, cd.h);
+    if (d.any_collider) {
+        uint8_t *act = d.coll_act ? d.coll_act + (size_t)(it + 1) * d.Vtot + i : nullptr;
+        if (xi4.w != 0.f) xn = collider_project(d, i, xn, cd.h, act);
+        else if (act) *act = 0;
+    }
     xb[i] = f4(xn, xi4.w);
 }
 

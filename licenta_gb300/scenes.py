@@ -144,10 +144,12 @@ def small_cloth(seed: int = 0, n: int = 32, iterations: int = 10, stiffness: flo
 
 
 def large_cloth(seed: int = 0, n: int = 512, iterations: int = 20, stiffness: float = 0.9,
-                sphere_radius: float = 0.3) -> ClothSpec:
+                sphere_radius: float = 0.3, mesh: bool = False) -> ClothSpec:
     """512x512 grid centred over a sphere of radius 0.3 m at the origin,
     dropped from y = 1 m (no pins), 20 iterations.  The sphere is the
-    reference's analytic sphere collider (CudaPBD::SetSpherePos)."""
+    reference's analytic sphere collider (CudaPBD::SetSpherePos), or with
+    mesh=True the icosphere of subdivision 5 (20,480 faces) as a static
+    triangle collider instead."""
     rng = np.random.default_rng(seed)
     p = base_params(iterations, stiffness)
     p.dims[:] = (n, n)
@@ -159,8 +161,12 @@ def large_cloth(seed: int = 0, n: int = 512, iterations: int = 20, stiffness: fl
     p.spherePos[:] = (0.0, 0.0, 0.0)
     p.sphereRadius = sphere_radius
     pos = grid_positions(n, rng, origin=(-0.5, -0.5))
+    coll = None
+    if mesh:
+        p.sphereOn = 0
+        coll = (*icosphere(5, sphere_radius), "cw")
     return ClothSpec(pos, grid_indices(n), np.zeros(n * n, dtype=np.uint8), p,
-                     dict(workload="plain-large", n=n, steps=300))
+                     dict(workload="plain-large", n=n, steps=300, mesh=mesh), collider=coll)
 
 
 def icosphere_cloth(seed: int = 0, n: int = 32, depth: int = 3, radius: float = 0.3, iterations: int = 10,
@@ -203,12 +209,14 @@ def batched_cloths(seed: int = 0, count: int = 256, n_min: int = 16, n_max: int 
 
 
 def batched_sphere_cloths(seed: int = 0, count: int = 128, n_min: int = 32, n_max: int = 128,
-                          iterations: int = 10) -> list[ClothSpec]:
+                          iterations: int = 10, mesh: bool = False) -> list[ClothSpec]:
     """The batched differentiable workload: 128 unpinned cloths, side drawn
     from U{32..128}, 1 m square centred over the origin at y = 1 m, each
     dropped onto its own sphere at the origin with radius U[0.2, 0.4] m (the
     reference's analytic sphere collider, CudaPBD::SetSpherePos), stiffness
-    0.9, 10 iterations."""
+    0.9, 10 iterations.  mesh=True: each sphere is an icosphere of
+    subdivision 4 (5,120 faces) given as a static triangle collider, the
+    analytic sphere off."""
     rng = np.random.default_rng(seed)
     sides = rng.integers(n_min, n_max + 1, size=count)
     radii = rng.uniform(0.2, 0.4, size=count)
@@ -224,9 +232,14 @@ def batched_sphere_cloths(seed: int = 0, count: int = 128, n_min: int = 32, n_ma
         p.sphereOn = 1
         p.spherePos[:] = (0.0, 0.0, 0.0)
         p.sphereRadius = float(radii[c])
+        coll = None
+        if mesh:
+            p.sphereOn = 0
+            coll = (*icosphere(4, float(radii[c])), "cw")
         out.append(ClothSpec(grid_positions(n, rng, origin=(-0.5, -0.5)), grid_indices(n),
                              np.zeros(n * n, dtype=np.uint8), p, dict(workload="batched-sphere", n=n,
-                                                                      r=float(radii[c]))))
+                                                                      r=float(radii[c]), mesh=mesh),
+                             collider=coll))
     return out
 
 

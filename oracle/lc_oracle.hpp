@@ -484,6 +484,9 @@ template <class R> class Cloth {
         std::vector<int8_t> sphere;  // V: ray-sphere outcome -1 / 0 / 1
         std::vector<V> x_in, v_b;    // damping inputs: state x, velocity after the global damping
         std::vector<std::vector<V>> xk;  // solver iterates x^0 .. x^K
+        std::vector<int> coll_tri;       // static-collider contacts of the step (V x kCollSlots) ...
+        std::vector<Contact> coll_c;     // ... and their planes
+        std::vector<u8> coll_act;        // (iterations + 1) x V: slots projected, [0] before the solver
         double M = 0, xcm[3] = {0, 0, 0}, vcm[3] = {0, 0, 0}, om[3] = {0, 0, 0}, I[3][3] = {};
     };
     bool recording = false;
@@ -751,23 +754,51 @@ template <class R> class Cloth {
     // the Jacobi average: collisions are projected last, so the averaged
     // stretch and bend corrections cannot pull a vertex that crossed a face
     // back through it.
-    void coll_project_vertex(int i) {
+    // pass (recording): 0 before the solver, it + 1 at the end of iteration
+    // it; the slots projected go to rec.coll_act for the reverse pass.
+    void coll_project_vertex(int i, int pass) {
         if (invm[i] == R(0)) return;
         const int K = kCollSlots;
         const std::vector<int> &ctri = have_frozen_coll ? frozen_coll_tri : coll_tri;
         const std::vector<Contact> &cc = have_frozen_coll ? frozen_coll_c : coll_c;
         if (ctri.size() < (size_t)(i + 1) * K) return;
         const R th = R(h);
+        u8 m = 0;
         for (int k = 0; k < K && ctri[(size_t)i * K + k] >= 0; ++k) {
             const Contact &q = cc[(size_t)i * K + k];
             const V n = mk<R>(R(q.w[0]), R(q.w[1]), R(q.w[2]));
             const R c = dot(n, x[i]) - R(q.w[3]) - th;
-            if (c < R(0)) x[i] = x[i] + n * (-c);
+            if (c < R(0)) {
+                x[i] = x[i] + n * (-c);
+                m |= (u8)(1u << k);
+            }
         }
+        if (recording && !rec.coll_act.empty()) rec.coll_act[(size_t)pass * tp.V + i] = m;
     }
     void coll_project() {
+        if (recording) { rec.coll_tri.clear(); rec.coll_c.clear(); rec.coll_act.clear(); }
         if (coll_t.empty()) return;
-        for (int i = 0; i < tp.V; ++i) coll_project_vertex(i);
+        if (recording) {
+            rec.coll_tri = have_frozen_coll ? frozen_coll_tri : coll_tri;
+            rec.coll_c = have_frozen_coll ? frozen_coll_c : coll_c;
+            rec.coll_act.assign((size_t)(prm.solverIterations + 1) * tp.V, 0);
+        }
+        for (int i = 0; i < tp.V; ++i) coll_project_vertex(i, 0);
+    }
+    // The projections of one pass reversed: each projected slot's Jacobian
+    // I - n n^T is symmetric, and the slots apply last first.
+    void coll_project_reverse(const Record &r, int pass, std::vector<V> &a) const {
+        if (r.coll_act.empty()) return;
+        const int K = kCollSlots;
+        for (int i = 0; i < tp.V; ++i) {
+            const u8 m = r.coll_act[(size_t)pass * tp.V + i];
+            for (int k = K - 1; k >= 0; --k)
+                if ((m >> k) & 1u) {
+                    const Contact &q = r.coll_c[(size_t)i * K + k];
+                    const V n = mk<R>(R(q.w[0]), R(q.w[1]), R(q.w[2]));
+                    a[i] = a[i] - n * dot(n, a[i]);
+                }
+        }
     }
 
     // Collision/CudaBVH.cu:163-188.  Two internal nodes may claim the same
@@ -1216,7 +1247,7 @@ template <class R> class Cloth {
             // Physics/CudaPBD.cu:1690-1698 (no zero-count guard)
             for (int i = 0; i < Vn; ++i) x[i] = x[i] + acc[i] / R(cnt[i]);
             if (!coll_t.empty())
-                for (int i = 0; i < Vn; ++i) coll_project_vertex(i);
+                for (int i = 0; i < Vn; ++i) coll_project_vertex(i, it + 1);
             if (recording) rec.xk.push_back(x);
         }
     }
@@ -1519,6 +1550,7 @@ template <class R> class Cloth {
         std::vector<int> cnt(Vn);
         for (int it = K - 1; it >= 0; --it) {
             const std::vector<V> &X = r.xk[it];
+            coll_project_reverse(r, it + 1, a);
             for (int i = 0; i < Vn; ++i) cnt[i] = stat_cnt[i] + lra_cnt[i] + (int)((r.ground_it[i] >> it) & 1u);
             for (size_t c = 0; c < nvf + nee; ++c) {
                 const Contact &k = c < nvf ? r.vf[c] : r.ee[c - nvf];
@@ -1603,6 +1635,7 @@ template <class R> class Cloth {
             }
             a.swap(g);
         }
+        coll_project_reverse(r, 0, a);
         // ExplicitEuler (Physics/CudaPBD.cu:2005-2012): x = x_prev + dt v
         std::vector<V> gvc(Vn);
         for (int i = 0; i < Vn; ++i) { gxp0[i] = gxp0[i] + a[i]; gvc[i] = a[i] * dt; }

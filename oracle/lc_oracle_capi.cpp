@@ -588,6 +588,11 @@ extern "C" int lco_adj_replay(lco_world *w, int c, int first, int nsteps) {
             cl.forced.dyn = r.dyn;
             cl.forced.sphere.assign(cl.tp.V, 0);
             cl.forced.on = true;
+            if (!r.coll_tri.empty()) {
+                cl.frozen_coll_tri = r.coll_tri;
+                cl.frozen_coll_c = r.coll_c;
+                cl.have_frozen_coll = true;
+            }
             cl.step();
         }
         return (int)LC_OK;
@@ -612,7 +617,6 @@ extern "C" int lco_adj_backward(lco_world *w, int c, double *gx, double *gxp, do
             av[i] = mk<R>(R(gv[3 * i]), R(gv[3 * i + 1]), R(gv[3 * i + 2]));
         }
         if (cl.tp.tri_bend) return (int)LC_ERR_NOT_SUPPORTED;  // triangle bending is not differentiated
-        if (!cl.coll_t.empty()) return (int)LC_ERR_NOT_SUPPORTED;  // nor are static colliders
         std::vector<double> ks(cl.tp.s1.size(), 0.0), kb(cl.tp.b1.size(), 0.0);
         for (int s = (int)cl.records.size() - 1; s >= 0; --s) cl.backward(cl.records[s], ax, axp, av, ks, kb);
         for (int i = 0; i < Vn; ++i) {

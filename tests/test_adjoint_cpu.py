@@ -209,3 +209,29 @@ def test_fp32_reverse_steps_differ_from_fp64_only_at_singular_hinges():
     assert contacts > 0
     assert not unexplained, f"steps differing at well-conditioned hinges: {unexplained}"
     assert worst > 1e-1, "the singular hinges should show in FP32"
+
+
+def test_adjoint_matches_finite_differences_on_a_static_collider():
+    """A 12 x 12 cloth warmed for 14 steps until it lies on an icosphere
+    collider (lc_batch_set_collider), then 6 recorded steps: the reverse of
+    the collider's projections (the contact planes held as recorded) against
+    finite differences that replay the recorded contacts."""
+    spec = scenes.icosphere_cloth(seed=4, n=12, depth=2, radius=0.3, height=0.45, span=0.6)
+    r = Rollout(spec, warm_steps=14, seed=3)
+    r.record(1)
+    ids, _ = r.o.debug(0, "COLLIDER")
+    assert (ids[:, 1] >= 0).sum() > 10, "the cloth should touch the collider"
+    gx, gxp, gv, gks, gkb = r.record(6)
+    rng = np.random.default_rng(8)
+    eps = 1e-4
+    for c in rng.choice(r.ne, 5, replace=False):
+        check(gks[c], r.fd(ks=lambda s, c=c: r.ks0 + s * eps * (np.arange(r.ne) == c)), eps)
+    for c in rng.choice(r.nb, 3, replace=False):
+        check(gkb[c], r.fd(kb=lambda s, c=c: r.kb0 + s * eps * (np.arange(r.nb) == c)), eps)
+    touching = np.unique(ids[ids[:, 1] >= 0][:, 0])
+    for i in rng.choice(touching, 3, replace=False):
+        for d in range(3):
+            e = np.zeros((r.nv, 3)); e[i, d] = eps
+            check(gv[i, d], r.fd(v=lambda s, e=e: r.v0 + s * e), eps)
+            e = np.zeros((r.nv, 3)); e[i, d] = 1e-6
+            check(gxp[i, d], r.fd(xp=lambda s, e=e: r.st0["x_prev"] + s * e), 1e-6)

@@ -76,13 +76,52 @@ def test_more_contacts_than_slots_is_a_capacity_error():
         b.close()
 
 
-def test_adjoint_batches_refuse_colliders():
-    spec = scenes.adjoint_cloth(seed=0, n=8)
-    b = ClothBatch([spec], adjoint=True)
+def test_reverse_pass_through_the_collider_matches_the_fp64_adjoint():
+    """A 12 x 12 cloth dropped onto an icosphere collider over 14 steps
+    (collider contacts from step 3): the engine's gradients of the loss on the final
+    positions with respect to the per-constraint stiffness, the initial
+    positions and velocities, against the FP64 adjoint of the oracle, whose
+    reverse of the collider projections is checked by finite differences in
+    tests/test_adjoint_cpu.py."""
+    import torch
+    from licenta_gb300.adjoint import ClothRollout, DiffCloth
+    from oracle.oracle_ffi import Oracle
+
+    spec = scenes.icosphere_cloth(seed=4, n=12, depth=2, radius=0.3, height=0.4, span=0.6)
+    steps = 14
+    o = Oracle([spec], fp64=True)
+    _, _, ne, nb = o.sizes(0)
+    rng = np.random.default_rng(4)
+    ks, kb = 0.9 + rng.uniform(-0.1, 0.05, ne), 0.9 + rng.uniform(-0.1, 0.05, nb)
+    v0 = rng.normal(scale=0.2, size=(spec.num_vertices, 3))
+    target = spec.positions + rng.normal(scale=0.05, size=(spec.num_vertices, 3)) - np.array([0.0, 0.3, 0.0])
+    st = o.get_state(0)
+    o.set_state(0, x=st["x"], x_prev=st["x"], v=v0, vn=st["vn"])
+    o.set_stiffness_d(0, ks, kb)
+    o.adj_record(0, steps)
+    ids, _ = o.debug(0, "COLLIDER")
+    xp = o.get_state(0)["x_prev"]
+    z = np.zeros_like(xp)
+    gx, gxp, gv, gks, gkb = o.adj_backward(0, z, 2 * (xp - target), z)
+    o.close()
+    want = dict(ks=gks, kb=gkb, x0=gx + gxp, v0=gv)
+
+    cloth = DiffCloth([spec], checkpoint_every=5)
     try:
-        v, i = scenes.icosphere(2, 0.3)
-        with pytest.raises(_ffi.LcError) as e:
-            b.set_collider(0, v, i, "cw")
-        assert e.value.status == _ffi.LC_ERR_NOT_SUPPORTED
+        t = dict(ks=torch.tensor(ks, dtype=torch.float32, device="cuda", requires_grad=True),
+                 kb=torch.tensor(kb, dtype=torch.float32, device="cuda", requires_grad=True),
+                 x0=torch.tensor(spec.positions, dtype=torch.float32, device="cuda", requires_grad=True),
+                 v0=torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True))
+        out = ClothRollout.apply(cloth, steps, t["ks"], t["kb"], t["x0"], t["v0"])
+        loss = ((out - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        final = out.detach().cpu().numpy()
+        got = {k: v.grad.cpu().numpy() for k, v in t.items()}
     finally:
-        b.close()
+        cloth.close()
+    assert (ids[:, 1] >= 0).sum() > 20, "the cloth should lie on the collider at the end"
+    assert np.abs(final - xp).max() < 1e-5
+    for k in ("ks", "kb", "v0", "x0"):
+        e = float(np.linalg.norm(got[k] - want[k]) / np.linalg.norm(want[k]))
+        assert e < 2e-3, f"{k}: relative error {e:.2e}"
