@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--only-lbvh", action="store_true",
                     help="run only the LBVH microbenchmark and print its line (for profiling it alone)")
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--rollout-1m", action="store_true",
+                    help="also run the million-vertex 300-step checkpointed rollout and report its device memory")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--lanes", type=int, default=2,
                     help="concurrent batches the workload is cut into (lc_group_step)")
@@ -336,15 +338,68 @@ def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20) -> dict
                     "beyond float range come out as inf (never NaN)"}
 
 
-def large_cloth_timing(seed: int, steps: int = 30, warmup: int = 5) -> dict:
+def rollout_1m_memory(seed: int, n: int = 1024, steps: int = 300, every: int = 20) -> dict:
+    """The checkpointed differentiable rollout at a million vertices: one
+    n x n cloth (n = 1024: 1,048,576 vertices, 2,093,058 triangles) hanging
+    from its two pinned corners with self-collision, 300 steps, 10
+    iterations, checkpoints every 20 steps; loss = summed squared distance of
+    the final positions to a target.  Reports the engine's own device
+    allocation (the drop in free device memory when the batch is created),
+    the peak of the torch-allocated checkpoints, segment states and
+    gradients, and the forward / backward times."""
+    import torch
+    from licenta_gb300 import scenes
+    from licenta_gb300.adjoint import ClothRollout, DiffCloth
+
+    spec = scenes.adjoint_cloth(seed=seed, n=n)
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    cloth = DiffCloth([spec], checkpoint_every=every)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
+    kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
+    x0 = torch.tensor(spec.positions, device="cuda", requires_grad=True)
+    v0 = torch.zeros_like(x0, requires_grad=True)
+    target = x0.detach() - torch.tensor([0.0, 0.3, 0.0], device="cuda")
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    out = ClothRollout.apply(cloth, steps, ks, kb, x0, v0)
+    loss = ((out - target) ** 2).sum()
+    e[1].record()
+    loss.backward()
+    e[2].record()
+    torch.cuda.synchronize()
+    free2, _ = torch.cuda.mem_get_info()
+    finite = float(torch.isfinite(ks.grad).float().mean())
+    peak_torch = torch.cuda.max_memory_allocated() - base
+    engine = free0 - free1
+    res = {"workload": f"checkpointed differentiable rollout: one {n}x{n} cloth ({spec.num_vertices} vertices, "
+                       f"{spec.num_triangles} triangles), {steps} steps, 10 iterations, checkpoints every {every}",
+           "engine_device_bytes": int(engine), "torch_peak_bytes": int(peak_torch),
+           "peak_device_bytes": int(engine + peak_torch), "device_total_bytes": int(total),
+           "min_free_after_bytes": int(free2),
+           "forward_ms_per_step": e[0].elapsed_time(e[1]) / steps,
+           "backward_ms_per_step": e[1].elapsed_time(e[2]) / steps,
+           "dL_dk_stretch_finite_share": finite}
+    cloth.close()
+    return res
+
+
+def large_cloth_timing(seed: int, steps: int = 30, warmup: int = 5, mesh: bool = True) -> dict:
     """The plain large workload: one 512x512 cloth (262,144 vertices) dropped
-    from y = 1 m onto the analytic sphere of radius 0.3 m, 20 iterations,
-    dt = 1/60 s, self-collision on.  The cloth is too large to keep on chip,
-    so the global-memory Jacobi solver runs.  CUDA events around `steps`
-    steps after `warmup`; the cloth's pair slots alone (134 MB) exceed L2."""
+    from y = 1 m onto a sphere of radius 0.3 m at the origin, 20 iterations,
+    dt = 1/60 s, self-collision on.  mesh=True (the workload as configured):
+    the sphere is the icosphere of subdivision 5 (20,480 faces) as a static
+    triangle collider; mesh=False: the reference's analytic sphere.  The
+    cloth is too large to keep on chip, so the global-memory Jacobi solver
+    runs.  CUDA events around `steps` steps after `warmup`; the cloth's pair
+    slots alone (134 MB) exceed L2."""
     import torch
     from licenta_gb300 import ClothBatch, scenes
-    b = ClothBatch([scenes.large_cloth(seed=seed)])
+    b = ClothBatch([scenes.large_cloth(seed=seed, mesh=mesh)])
     s = torch.cuda.Stream()
     b.step(warmup, s)
     b.sync()
@@ -357,7 +412,9 @@ def large_cloth_timing(seed: int, steps: int = 30, warmup: int = 5) -> dict:
     prof = b.profile(1, s)
     cnt = b.counters()
     b.close()
-    return {"workload": "512x512 cloth onto the analytic sphere (r 0.3 m), 20 iterations", "steps": steps,
+    what = "the icosphere of subdivision 5 (r 0.3 m) as a static collider" if mesh else \
+        "the analytic sphere (r 0.3 m)"
+    return {"workload": f"512x512 cloth onto {what}, 20 iterations", "steps": steps,
             "warmup": warmup, "ms_per_step": ms, "cloth_steps_per_s": 1000.0 / ms,
             "solver_variant": prof["solver_variant"], "phases_ms": prof["phases"],
             "pairs": cnt["pairs"], "contacts": cnt["vf"] + cnt["ee"]}
@@ -645,12 +702,16 @@ def run_ours(args, world, rank, local):
     lbvh = None
     if rank == 0 and not args.no_lbvh:
         lbvh = lbvh_timing(args.seed)
-    large = None
+    large = large_analytic = None
     if rank == 0 and not args.no_large:
-        large = large_cloth_timing(args.seed)
+        large = large_cloth_timing(args.seed, mesh=True)
+        large_analytic = large_cloth_timing(args.seed, mesh=False)
     adj_batched = None
     if rank == 0 and not args.no_adjoint:
         adj_batched = adjoint_batched_timing(args.seed)
+    roll_1m = None
+    if rank == 0 and args.rollout_1m:
+        roll_1m = rollout_1m_memory(args.seed)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -682,7 +743,9 @@ def run_ours(args, world, rank, local):
         "adjoint": adj,
         "lbvh": lbvh,
         "large_cloth": large,
+        "large_cloth_analytic_sphere": large_analytic,
         "adjoint_batched": adj_batched,
+        "rollout_1m": roll_1m,
         "tuning": tuning,
     }
     if rank == 0:

@@ -447,6 +447,63 @@ lc_status lc_lbvh_sorted_ids(lc_lbvh *h, uint32_t *out_ids, void *stream);
 lc_status lc_lbvh_debug_get(lc_lbvh *h, int32_t what, void *dst, uint64_t cap, uint64_t *count);
 lc_status lc_lbvh_destroy(lc_lbvh *h);
 
+/* ---- Object-level broadphase: the Collision::ICollisionMethod family ------
+ * Replaces the reference's object-level methods behind ICollisionMethod
+ * (Collision/ICollisionMethod.h:15-87: BVH, SweepAndPrune, SpatialGrid,
+ * SpatialHashing, Collision/BVH.cpp etc.), which run on the CPU over SceneObjects.
+ * Here an object is its axis-aligned box, and lc_broadphase_update (the
+ * interface's Update) takes all boxes at once: box_min / box_max, 3 floats per
+ * object, in device memory, which must stay valid until the
+ * lc_broadphase_test that follows (TestCollision) has returned.  Every method
+ * returns the same set, all pairs (a, b), a < b, of objects whose closed boxes
+ * overlap (BoundingBox::Collides), with nothing dropped; the methods differ in
+ * the work they do:
+ *   LC_BP_BRUTE every pair;
+ *   LC_BP_SAP   sorted by lower x, each object sweeps forward;
+ *   LC_BP_GRID  a uniform grid of cells_per_axis^3 cells over the world box
+ *               (boxes outside it are clamped into the border cells);
+ *   LC_BP_HASH  an unbounded grid of cell_size cells hashed into table_size
+ *               buckets (a power of two);
+ *   LC_BP_BVH   a linear BVH over the box centres.
+ * The reference's SweepAndPrune keeps its pair set across frames and tests
+ * bounding spheres, and its SpatialHashing files objects by points of their
+ * boxes; these members all report the exact box-overlap set.  The grid and
+ * hash members hold up to max_entries (object, cell) entries (0: 8 per
+ * object); more is LC_ERR_CAPACITY_OVERFLOW from lc_broadphase_update.
+ * lc_broadphase_test writes at most cap pairs (2 uint32 each, device memory,
+ * NULL with cap 0 to count only) and the full count into *count (host),
+ * returning LC_ERR_CAPACITY_OVERFLOW when more exist; it synchronizes the
+ * stream.  Object add / move / remove (ObjectAdded / ObjectMoved /
+ * ObjectRemoved) edit the caller's box array between updates; the host
+ * adapters (licenta_gb300.broadphase.CollisionMethod, lc::CollisionMethod in
+ * lc_body.hpp) keep that bookkeeping.  lc_broadphase_get_criteria gives the last
+ * frame's criteria (Collision/ICollisionMethod.h:61-85): structure and
+ * collision times (ms, CUDA events), box tests made and the bytes held. */
+enum { LC_BP_BRUTE = 0, LC_BP_SAP = 1, LC_BP_GRID = 2, LC_BP_HASH = 3, LC_BP_BVH = 4 };
+typedef struct lc_broadphase_desc {
+    int32_t method;
+    int32_t max_objects;
+    uint64_t max_entries;               /* grid / hash */
+    float world_min[3], world_max[3];   /* grid */
+    int32_t cells_per_axis;             /* grid, 1..1024 */
+    float cell_size;                    /* hash */
+    int32_t table_size;                 /* hash */
+} lc_broadphase_desc;
+typedef struct lc_broadphase_criteria {
+    float structure_ms;                 /* last update */
+    float collision_ms;                 /* last test */
+    uint64_t intersection_tests;        /* box tests of the last test */
+    uint64_t pairs;                     /* pairs of the last test */
+    uint64_t memory_bytes;              /* device memory held */
+} lc_broadphase_criteria;
+typedef struct lc_broadphase lc_broadphase;
+lc_status lc_broadphase_create(const lc_broadphase_desc *desc, lc_broadphase **out);
+lc_status lc_broadphase_update(lc_broadphase *b, const float *box_min, const float *box_max, int32_t num_objects,
+                               void *stream);
+lc_status lc_broadphase_test(lc_broadphase *b, uint32_t *pairs, uint64_t cap, uint64_t *count, void *stream);
+lc_status lc_broadphase_get_criteria(lc_broadphase *b, lc_broadphase_criteria *out);
+lc_status lc_broadphase_destroy(lc_broadphase *b);
+
 /* Physics::PrimitiveContact (Physics/Structs.h:106-129) as the reference's
  * contact tests leave it: vertex ids (VF: the vertex, then the face; EE: the
  * two edges), weights, time of contact and unit normal. */

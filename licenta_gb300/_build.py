@@ -21,7 +21,7 @@ LIB = OUT / "liblicenta_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 SOURCES = ["lc_api.cu", "lc_lbvh.cu", "lc_step.cu", "lc_scan.cu", "lc_cluster.cu", "lc_static.cu", "lc_adjoint.cu",
-           "lc_narrow_api.cu", "lc_response.cu"]
+           "lc_narrow_api.cu", "lc_response.cu", "lc_broadphase.cu"]
 # lc_lbvh.cu carries the bit-exact stages and lc_response.cu the impulse
 # response: no FMA contraction, IEEE div/sqrt.
 # The solver translation units are compared against FP64 within a tolerance

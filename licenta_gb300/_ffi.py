@@ -24,6 +24,20 @@ LC_MORTON_REF63 = 0
 LC_MORTON_K30 = 1
 LC_NARROW_CCD = 0
 LC_NARROW_DCD = 1
+LC_BP_BRUTE, LC_BP_SAP, LC_BP_GRID, LC_BP_HASH, LC_BP_BVH = 0, 1, 2, 3, 4
+
+
+class BroadphaseDesc(C.Structure):
+    _fields_ = [("method", C.c_int32), ("max_objects", C.c_int32), ("max_entries", C.c_uint64),
+                ("world_min", C.c_float * 3), ("world_max", C.c_float * 3), ("cells_per_axis", C.c_int32),
+                ("cell_size", C.c_float), ("table_size", C.c_int32)]
+
+
+class BroadphaseCriteria(C.Structure):
+    _fields_ = [("structure_ms", C.c_float), ("collision_ms", C.c_float), ("intersection_tests", C.c_uint64),
+                ("pairs", C.c_uint64), ("memory_bytes", C.c_uint64)]
+
+
 LC_WINDING_CCW = 0
 LC_WINDING_CW = 1
 COLLIDER_SLOTS = 8
@@ -136,6 +150,11 @@ SIGNATURES = {
     "lc_batch_read_positions": (C.c_int, [VP, VP, C.c_int32, VP]),
     "lc_batch_set_sphere": (C.c_int, [VP, C.c_int32, C.POINTER(C.c_float), C.c_float]),
     "lc_batch_set_collider": (C.c_int, [VP, C.c_int32, VP, C.c_int32, VP, C.c_int32, C.c_int32]),
+    "lc_broadphase_create": (C.c_int, [VP, C.POINTER(C.c_void_p)]),
+    "lc_broadphase_update": (C.c_int, [VP, VP, VP, C.c_int32, VP]),
+    "lc_broadphase_test": (C.c_int, [VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
+    "lc_broadphase_get_criteria": (C.c_int, [VP, VP]),
+    "lc_broadphase_destroy": (C.c_int, [VP]),
     "lc_batch_set_stiffness": (C.c_int, [VP, C.c_int32, VP, VP]),
     "lc_batch_constraint_counts": (C.c_int, [VP, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lc_batch_debug_get": (C.c_int, [VP, C.c_int32, C.c_int32, VP, C.c_uint64, C.POINTER(C.c_uint64)]),

@@ -503,6 +503,11 @@ template <class R> class Cloth {
     // y = 0) sits at d = -1.
     bool track_bend = false;
     double bend_min = 1e300, bend_min_neg = 1e300;
+    // Smallest |n| / h over the contacts of the last solve's iterates (when
+    // track_bend), n the contact vector of Physics/CudaPBD.cu:1212-1415: the
+    // correction's Jacobian I - (h / |n|)(I - n n^T / |n|^2) grows without
+    // bound as a vertex comes to lie on its face or two edges cross.
+    double contact_min = 1e300;
     std::vector<Record> records;  // one per recorded step of a rollout
 
     void init(const lc_cloth_desc &d) {
@@ -1186,7 +1191,7 @@ template <class R> class Cloth {
             rec.dyn.assign((size_t)prm.solverIterations * corr_dyn.size(), 0);
             rec.xk.assign(1, x);
         }
-        bend_min = bend_min_neg = 1e300;
+        bend_min = bend_min_neg = contact_min = 1e300;
         for (int it = 0; it < prm.solverIterations; ++it) {
             if (track_bend) track_bend_conditioning();
             for (int i = 0; i < Vn; ++i) { acc[i] = mk<R>(0, 0, 0); cnt[i] = 0; }
@@ -1229,6 +1234,7 @@ template <class R> class Cloth {
             // dynamic, Physics/CudaPBD.cu:1190-1415 and :1448-1475
             for (size_t c = 0; c < nvf; ++c) vf_corr(cvf[c], th, &corr_dyn[c * 4]);
             for (size_t c = 0; c < nee; ++c) ee_corr(cee[c], th, &corr_dyn[(nvf + c) * 4]);
+            if (track_bend) track_contact_conditioning(cvf, cee, th);
             for (int i = 0; i < Vn; ++i) {
                 if (dyn[i].empty()) continue;
                 V a = mk<R>(0, 0, 0);
@@ -1249,6 +1255,20 @@ template <class R> class Cloth {
             if (!coll_t.empty())
                 for (int i = 0; i < Vn; ++i) coll_project_vertex(i, it + 1);
             if (recording) rec.xk.push_back(x);
+        }
+    }
+
+    void track_contact_conditioning(const std::vector<Contact> &cvf, const std::vector<Contact> &cee, R th) {
+        for (const Contact &k : cvf) {
+            const R b0 = clampf(R(-k.w[1]), R(0), R(1)), b1 = clampf(R(-k.w[2]), R(0), R(1)),
+                    b2 = clampf(R(-k.w[3]), R(0), R(1));
+            const V n = x[k.v[0]] - (x[k.v[1]] * b0 + x[k.v[2]] * b1 + x[k.v[3]] * b2);
+            contact_min = std::min(contact_min, double(len(n) / th));
+        }
+        for (const Contact &k : cee) {
+            const V n = (x[k.v[0]] * R(k.w[0]) + x[k.v[1]] * R(k.w[1])) -
+                        (x[k.v[2]] * R(-k.w[2]) + x[k.v[3]] * R(-k.w[3]));
+            contact_min = std::min(contact_min, double(len(n) / th));
         }
     }
 

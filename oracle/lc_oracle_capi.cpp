@@ -788,11 +788,13 @@ extern "C" int lco_set_frozen_normals(lco_world *w, int c, const float *n, uint6
 extern "C" int lco_track_bend(lco_world *w, int c, int on) {
     return with_cloth(w, c, [&](auto &cl) { cl.track_bend = on != 0; return (int)LC_OK; });
 }
-// out[0] = smallest 1 - n1.n2, out[1] = smallest 1 + n1.n2 (Cloth::bend_min).
+// out[0] = smallest 1 - n1.n2, out[1] = smallest 1 + n1.n2 (Cloth::bend_min),
+// out[2] = smallest |n| / h over the contacts (Cloth::contact_min).
 extern "C" int lco_bend_conditioning(lco_world *w, int c, double *out) {
     return with_cloth(w, c, [&](auto &cl) {
         out[0] = cl.bend_min;
         out[1] = cl.bend_min_neg;
+        out[2] = cl.contact_min;
         return (int)LC_OK;
     });
 }

@@ -325,9 +325,24 @@ class Oracle:
         or step (tracked after track_bend): the forward singularity of the
         reference's bend formula.  reverse=True: min of 1 - |n1.n2|, which
         adds the d -> -1 end where only the derivative is singular."""
-        out = (C.c_double * 2)()
+        out = (C.c_double * 3)()
         _chk(lib().lco_bend_conditioning(self._h, c, out), "bend_conditioning")
         return min(out[0], out[1]) if reverse else out[0]
+
+    def hinge_conditioning(self, c: int) -> tuple[float, float]:
+        """(min 1 - n1.n2, min 1 + n1.n2) over the bends and solver iterates
+        of the last solve or step (tracked after track_bend)."""
+        out = (C.c_double * 3)()
+        _chk(lib().lco_bend_conditioning(self._h, c, out), "bend_conditioning")
+        return out[0], out[1]
+
+    def contact_conditioning(self, c: int) -> float:
+        """min over the contacts and solver iterates of the last solve or
+        step of |n| / h (tracked after track_bend), n the contact vector: the
+        contact correction's derivative grows like h / |n|."""
+        out = (C.c_double * 3)()
+        _chk(lib().lco_bend_conditioning(self._h, c, out), "bend_conditioning")
+        return out[2]
 
     def friction_on(self, c: int, v, ground, vf: tuple, normals) -> np.ndarray:
         """Friction (CudaPBD::ApplyFriction) on given velocities with the given

@@ -22,6 +22,16 @@ import numpy as np
 COLLISION_ARRAYS = ("MORTON", "PERM", "LEFTS", "RIGHTS", "PARENTS", "RML", "NODE_AABB", "PAIRS")
 
 
+# A step's solve is near a singularity of the reference's raw-position bend
+# formula when a hinge comes within 1 - n1.n2 < SINGULAR_FWD of d = 1 (the
+# correction is 0 * inf there, in the forward step as in its derivative) or
+# within 1 + n1.n2 < SINGULAR_NEG of d = -1 (the correction is a 0 / 0 ratio
+# whose derivative grows like (1 + d)^-1/2).  Reverse-pass comparisons excuse
+# such steps.
+SINGULAR_FWD = 1e-7
+SINGULAR_NEG = 1e-11
+
+
 def capture_pre(batch, c):
     st = batch.get_state(c)
     return st, batch.triangle_order(c)

@@ -39,6 +39,9 @@ def test_struct_layout_matches_header():
     # lc_cloth_params: 11 floats, 4 float3, 2 floats + int, 2 float3, int2, 3 ints,
     # u64, 3 ints, then the extension block
     assert C.sizeof(_ffi.Contact) == 32
+    # lc_broadphase_desc: int, int, u64, 2 float3, int, float, int (+ tail padding to 8)
+    assert _ffi.BroadphaseDesc.max_entries.offset == 8 and _ffi.BroadphaseDesc.table_size.offset == 48
+    assert C.sizeof(_ffi.BroadphaseDesc) == 56 and C.sizeof(_ffi.BroadphaseCriteria) == 32
     assert _ffi.ClothParams.benchmarkSample.offset % 8 == 0
     assert _ffi.ClothDesc.params.offset % 8 == 0
 

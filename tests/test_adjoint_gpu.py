@@ -209,20 +209,19 @@ def test_engine_reverse_steps_at_the_workload_size(parity_report):
     apart, so their whole-rollout gradients are gradients of different
     trajectories; the whole-rollout comparison is the small case above.)
 
-    The reference's bend formula takes raw positions, and it is singular
-    where n1.n2 -> +-1; every hinge of a cloth lying on the ground plane
-    y = 0 (a plane through the origin) is there, and near such a hinge an
-    FP32 reverse of the formula differs from the FP64 one by as much as the
-    gradient itself.  The yardstick for each step is therefore the FP32
-    restatement of the oracle, taught the same state, contacts and decisions
-    and reversed with the same seeds: where it agrees with FP64 to 1e-3 the
-    step is well conditioned and the engine must agree to 2e-3; elsewhere
-    the engine's error is reported beside the FP32 restatement's and must not
-    be systematically larger (median ratio <= 3).  The state gradients
-    (x, x_prev, v) are compared as one vector, so that a part that cancels to
-    nothing in FP64 (dL/dx of the first step from rest) is measured on the
-    scale of the others."""
+    The reference's bend formula takes raw positions and is singular where
+    a hinge reaches n1.n2 = +-1 (a cloth lying on the ground plane y = 0, a
+    plane through the origin, puts hinges there).  A step whose solve brings
+    a hinge within 1 - n1.n2 < 1e-7 or 1 + n1.n2 < 1e-11 is excused
+    (test_adjoint_cpu.py shows the FP32 restatement failing at such steps
+    and only there); every other step must agree to 2e-3 (relative L2, the
+    state gradients (x, x_prev, v) as one vector, so that a part that
+    cancels to nothing in FP64 is measured on the scale of the others).  On
+    the excused steps the engine's error is set beside the FP32
+    restatement's, taught the same state: it must be finite and not
+    systematically larger (median ratio <= 3)."""
     from oracle import parity
+    from oracle.parity import SINGULAR_FWD, SINGULAR_NEG
     spec = scenes.adjoint_cloth(seed=0)
     steps = 60
     cloth = DiffCloth([spec], checkpoint_every=10, debug_capture=True)
@@ -232,6 +231,7 @@ def test_engine_reverse_steps_at_the_workload_size(parity_report):
     _, _, ne, nb = o64.sizes(0)
     for o in (o64, o32):
         o.set_stiffness_d(0, np.full(ne, 0.9), np.full(nb, 0.9))
+    o64.track_bend(0, True)
     cloth.set_stiffness(torch.full((cloth.E,), 0.9, device="cuda"), torch.full((cloth.B,), 0.9, device="cuda"))
     x0 = torch.tensor(spec.positions, device="cuda")
     cloth.set_initial(x0, torch.zeros_like(x0))
@@ -267,22 +267,24 @@ def test_engine_reverse_steps_at_the_workload_size(parity_report):
                 o.adj_record(0, 1)
                 want[tag] = o.adj_backward(0, *seeds)
             worst_x = max(worst_x, float(np.abs(b.get_state(0)["x"] - o64.get_state(0)["x"]).max()))
-            e_engine, e_fp32 = err(got, want["64"]), err(want["32"], want["64"])
-            if e_fp32 < 1e-3:
+            fwd, neg = o64.hinge_conditioning(0)
+            e_engine = err(got, want["64"])
+            if fwd >= SINGULAR_FWD and neg >= SINGULAR_NEG:
                 ok_steps += 1
                 ok_contacts += nc
                 worst_ok = max(worst_ok, e_engine)
             else:
-                ratios.append(e_engine / e_fp32)
+                ratios.append(e_engine / max(err(want["32"], want["64"]), 1e-30))
     finally:
         cloth.close()
         o64.close()
         o32.close()
     med = float(np.median(ratios)) if ratios else 0.0
     parity_report(steps=steps, contacts=contacts, well_conditioned_steps=ok_steps, ok_contacts=ok_contacts,
-                  max_rel_well_conditioned=f"{worst_ok:.2e}", ill_conditioned_steps=len(ratios),
-                  median_engine_over_fp32=f"{med:.2f}", max_x=f"{worst_x:.2e}")
+                  max_rel_well_conditioned=f"{worst_ok:.2e}", singular_steps=len(ratios),
+                  median_engine_over_fp32_singular=f"{med:.2f}", max_x=f"{worst_x:.2e}")
     assert ok_contacts > 0, "the well-conditioned steps should include self-contact"
+    assert ok_steps >= steps // 2, f"only {ok_steps} steps clear of the bend singularities"
     assert worst_x <= 1e-5
     assert worst_ok < 2e-3, f"well-conditioned step: relative error {worst_ok:.2e}"
-    assert med <= 3.0, f"engine error {med:.2f} x the FP32 restatement's at ill-conditioned steps"
+    assert med <= 3.0, f"engine error {med:.2f} x the FP32 restatement's on the singular steps"
