@@ -7,8 +7,9 @@ U[0.5, 1.0], constant wind U[-2, 2] m/s^2 on x and z, two pinned corners,
 10 solver iterations, dt = 1/60 s, self-collision on.  One "step" advances
 every cloth of the batch by one CudaDeformableBody::FixedUpdate.  value =
 cloth-steps/s = cloths x steps / device time.  With --gpus N (torchrun, one
-rank per GPU) every rank steps its own 256-cloth workload (seed + rank): weak
-scaling with no collective on the data path.
+rank per GPU) one seeded workload of 256 N cloths is split across the ranks
+by licenta_gb300.shard.my_share, about 256 cloths each: weak scaling with no
+collective on the data path.
 
 Also reported: the plain path (the same engine stepping one cloth per call,
 on a seeded sample of the workload's cloths), e2e through the public API with
@@ -577,7 +578,13 @@ def run_ours(args, world, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    specs = scenes.batched_cloths(seed=args.seed + rank, count=args.cloths)
+    # one seeded workload of `cloths` cloths per GPU, split across the ranks
+    # by the balancing helper (greedy on the per-step cost), so each rank
+    # steps about `cloths` cloths (weak scaling); at one GPU the workload is
+    # the 256 cloths themselves
+    from licenta_gb300 import shard
+    everything = scenes.batched_cloths(seed=args.seed, count=args.cloths * world)
+    specs = [everything[i] for i in shard.my_share(everything, rank, world)] if world > 1 else everything
     # the workload as `lanes` concurrent batches: ranges of the cloths ordered
     # by size, so each lane holds cloths of like size and is tuned on its own
     batch = ClothBatchGroup(specs, lanes=args.lanes, order="size") if args.lanes > 1 else ClothBatch(specs)
@@ -727,6 +734,8 @@ def run_ours(args, world, rank, local):
                    "global_batch": world * args.cloths, "cloths_per_gpu": args.cloths,
                    "vertices_per_gpu": V, "triangles_per_gpu": T, "iterations": 10, "dt": 1.0 / 60.0,
                    "parallelism": f"shard-by-cloth x{world}",
+                   "sharding": f"one seeded workload of {args.cloths * world} cloths split across the ranks by "
+                               "licenta_gb300.shard.my_share (greedy per-step cost balance), no collective in the step",
                    "concurrent_batches": args.lanes,
                    "lane_order": "cloths by vertex count, largest first" if args.lanes > 1 else None,
                    "l2": f"inputs larger than L2 (vertex state {state_mb:.0f} MB + constraints + pair buffers)"},

@@ -500,7 +500,15 @@ typedef struct lc_broadphase lc_broadphase;
 lc_status lc_broadphase_create(const lc_broadphase_desc *desc, lc_broadphase **out);
 lc_status lc_broadphase_update(lc_broadphase *b, const float *box_min, const float *box_max, int32_t num_objects,
                                void *stream);
+/* The boxes from host memory, copied into the handle's own device buffers
+ * (which the following test reads). */
+lc_status lc_broadphase_update_host(lc_broadphase *b, const float *box_min, const float *box_max,
+                                    int32_t num_objects, void *stream);
 lc_status lc_broadphase_test(lc_broadphase *b, uint32_t *pairs, uint64_t cap, uint64_t *count, void *stream);
+/* The same into host memory (through a device staging buffer the handle grows
+ * to the largest pair count it has seen). */
+lc_status lc_broadphase_test_host(lc_broadphase *b, uint32_t *pairs, uint64_t cap, uint64_t *count,
+                                  void *stream);
 lc_status lc_broadphase_get_criteria(lc_broadphase *b, lc_broadphase_criteria *out);
 lc_status lc_broadphase_destroy(lc_broadphase *b);
 

@@ -13,6 +13,9 @@
  *   Autotune(steps, warmup, allow_variants) — picks the launch shapes with
  *                    the library's autotuner (no counterpart in the reference)
  *
+ * and lc::CollisionMethod<Id>, Collision::ICollisionMethod over the engine's
+ * object-level broadphase (lc_broadphase_*).
+ *
  * VertexT is any vertex record with a `m_position` member that has float x,
  * y, z fields — Rendering::VertexFormat (glm::vec3 m_position) qualifies.
  * As in the reference, the caller owns *verts and *indices and the body keeps
@@ -26,8 +29,11 @@
  */
 #pragma once
 
+#include <algorithm>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "lc.h"
@@ -119,6 +125,82 @@ private:
     std::vector<VertexT> *m_verts;
     lc_batch *m_batch = nullptr;
     std::vector<float> m_published;
+};
+
+// Collision::ICollisionMethod (Collision/ICollisionMethod.h:15-87) over an
+// lc_broadphase: objects are ids of type Id with an axis-aligned box each.
+// ObjectAdded / ObjectMoved / ObjectRemoved edit a host box table, Update()
+// copies it to the device and builds the method's structure, TestCollision()
+// returns the pairs of ids whose boxes overlap, and GetLastFrameCriteria()
+// the reference's per-frame criteria under its keys (Core/Utils.hpp:42-46).
+template <class Id>
+class CollisionMethod {
+public:
+    explicit CollisionMethod(const lc_broadphase_desc &desc) : max_(desc.max_objects) {
+        check(lc_broadphase_create(&desc, &h_), "lc_broadphase_create");
+    }
+    ~CollisionMethod() { lc_broadphase_destroy(h_); }
+    CollisionMethod(const CollisionMethod &) = delete;
+    CollisionMethod &operator=(const CollisionMethod &) = delete;
+
+    void ObjectAdded(const Id &id, const float box_min[3], const float box_max[3]) {
+        if (slot_.count(id)) throw std::invalid_argument("ObjectAdded: id already present");
+        if ((int)ids_.size() >= max_) throw std::length_error("ObjectAdded: more objects than max_objects");
+        slot_[id] = ids_.size();
+        ids_.push_back(id);
+        lo_.insert(lo_.end(), box_min, box_min + 3);
+        hi_.insert(hi_.end(), box_max, box_max + 3);
+    }
+    void ObjectMoved(const Id &id, const float box_min[3], const float box_max[3]) {
+        const size_t s = slot_.at(id);
+        std::copy(box_min, box_min + 3, lo_.begin() + 3 * s);
+        std::copy(box_max, box_max + 3, hi_.begin() + 3 * s);
+    }
+    void ObjectRemoved(const Id &id) {
+        const size_t s = slot_.at(id), last = ids_.size() - 1;
+        slot_.erase(id);
+        if (s != last) {  // the last object takes the freed slot
+            ids_[s] = ids_[last];
+            slot_[ids_[s]] = s;
+            std::copy(lo_.begin() + 3 * last, lo_.begin() + 3 * last + 3, lo_.begin() + 3 * s);
+            std::copy(hi_.begin() + 3 * last, hi_.begin() + 3 * last + 3, hi_.begin() + 3 * s);
+        }
+        ids_.pop_back();
+        lo_.resize(3 * last);
+        hi_.resize(3 * last);
+    }
+    void Update() {
+        check(lc_broadphase_update_host(h_, lo_.data(), hi_.data(), (int32_t)ids_.size(), nullptr),
+              "lc_broadphase_update_host");
+    }
+    std::vector<std::pair<Id, Id>> TestCollision() {
+        uint64_t n = 0;
+        lc_status s = lc_broadphase_test_host(h_, host_.data(), host_.size() / 2, &n, nullptr);
+        if (s == LC_ERR_CAPACITY_OVERFLOW) {  // grow to the count and ask again
+            host_.resize(2 * n);
+            s = lc_broadphase_test_host(h_, host_.data(), n, &n, nullptr);
+        }
+        check(s, "lc_broadphase_test_host");
+        std::vector<std::pair<Id, Id>> out(n);
+        for (uint64_t k = 0; k < n; ++k) out[k] = {ids_[host_[2 * k]], ids_[host_[2 * k + 1]]};
+        lc_broadphase_criteria c{};
+        check(lc_broadphase_get_criteria(h_, &c), "lc_broadphase_get_criteria");
+        criteria_ = {{"Time Spent - Collisions", c.collision_ms},
+                     {"Time Spent - Structure Update", c.structure_ms},
+                     {"Intersection Tests", (float)c.intersection_tests},
+                     {"Memory Used (KB)", (float)c.memory_bytes / 1024.f}};
+        return out;
+    }
+    std::unordered_map<std::string, float> GetLastFrameCriteria() const { return criteria_; }
+
+private:
+    lc_broadphase *h_ = nullptr;
+    int max_;
+    std::vector<Id> ids_;
+    std::unordered_map<Id, size_t> slot_;
+    std::vector<float> lo_, hi_;
+    std::vector<uint32_t> host_;
+    std::unordered_map<std::string, float> criteria_;
 };
 
 }  // namespace lc

@@ -152,7 +152,9 @@ SIGNATURES = {
     "lc_batch_set_collider": (C.c_int, [VP, C.c_int32, VP, C.c_int32, VP, C.c_int32, C.c_int32]),
     "lc_broadphase_create": (C.c_int, [VP, C.POINTER(C.c_void_p)]),
     "lc_broadphase_update": (C.c_int, [VP, VP, VP, C.c_int32, VP]),
+    "lc_broadphase_update_host": (C.c_int, [VP, VP, VP, C.c_int32, VP]),
     "lc_broadphase_test": (C.c_int, [VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
+    "lc_broadphase_test_host": (C.c_int, [VP, VP, C.c_uint64, C.POINTER(C.c_uint64), VP]),
     "lc_broadphase_get_criteria": (C.c_int, [VP, VP]),
     "lc_broadphase_destroy": (C.c_int, [VP]),
     "lc_batch_set_stiffness": (C.c_int, [VP, C.c_int32, VP, VP]),

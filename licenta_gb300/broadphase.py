@@ -138,9 +138,11 @@ class CollisionMethod:
         pairs = self.bp.test().cpu().numpy()
         ids = self._ids
         c = self.bp.criteria()
-        self._criteria = {"Collision Time": c["collision_ms"], "Structure Time": c["structure_ms"],
+        # the keys of Core/Utils.hpp:42-46
+        self._criteria = {"Time Spent - Collisions": c["collision_ms"],
+                          "Time Spent - Structure Update": c["structure_ms"],
                           "Intersection Tests": float(c["intersection_tests"]),
-                          "Memory": c["memory_bytes"] / 1024.0}
+                          "Memory Used (KB)": c["memory_bytes"] / 1024.0}
         return {(ids[a], ids[b]) for a, b in pairs}
 
     def GetLastFrameCriteria(self) -> dict:

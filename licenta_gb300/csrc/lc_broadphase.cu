@@ -394,6 +394,9 @@ struct lc_broadphase {
     int4 *ecell = nullptr;
     int ne = 0;                      // grid / hash entries of the last update
     BvhPtrs bvh{};
+    float *hlo = nullptr, *hhi = nullptr;  // device copies of host boxes (lc_broadphase_update_host)
+    uint32_t *stage = nullptr;             // pairs on their way to host memory (lc_broadphase_test_host)
+    uint64_t stage_cap = 0;
     GridSpec grid{};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     uint64_t last_tests = 0, last_pairs = 0;
@@ -411,6 +414,7 @@ struct lc_broadphase {
         return LC_OK;
     }
     ~lc_broadphase() {
+        if (stage) cudaFree(stage);
         for (void *q : mem) cudaFree(q);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
@@ -515,6 +519,8 @@ lc_status lc_broadphase_create(const lc_broadphase_desc *desc, lc_broadphase **o
         LC_TRY_BP(b.alloc(B.visit, N, "arrival counters"));
         LC_TRY_BP(b.alloc(B.bounds, 6, "scene box"));
     }
+    LC_TRY_BP(b.alloc(b.hlo, 3 * N, "host box copies"));
+    LC_TRY_BP(b.alloc(b.hhi, 3 * N, "host box copies"));
     for (cudaEvent_t &e : b.ev) LC_BP_CUDA(cudaEventCreate(&e));
     *out = h.release();
     return LC_OK;
@@ -565,6 +571,18 @@ lc_status lc_broadphase_update(lc_broadphase *b, const float *box_min, const flo
     return LC_OK;
 }
 
+lc_status lc_broadphase_update_host(lc_broadphase *b, const float *box_min, const float *box_max, int32_t n,
+                                    void *stream) {
+    if (!b || n < 0 || n > b->desc.max_objects || (n > 0 && (!box_min || !box_max)))
+        return bp_fail(LC_ERR_INVALID_ARG, "lc_broadphase_update_host: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0) {
+        LC_BP_CUDA(cudaMemcpyAsync(b->hlo, box_min, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        LC_BP_CUDA(cudaMemcpyAsync(b->hhi, box_max, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+    }
+    return lc_broadphase_update(b, b->hlo, b->hhi, n, stream);
+}
+
 lc_status lc_broadphase_test(lc_broadphase *b, uint32_t *pairs, uint64_t cap, uint64_t *count, void *stream) {
     if (!b || !count || (cap > 0 && !pairs)) return bp_fail(LC_ERR_INVALID_ARG, "lc_broadphase_test: bad arguments");
     cudaStream_t st = (cudaStream_t)stream;
@@ -613,6 +631,34 @@ lc_status lc_broadphase_test(lc_broadphase *b, uint32_t *pairs, uint64_t cap, ui
     if (tot > cap && pairs)
         return bp_fail(LC_ERR_CAPACITY_OVERFLOW, "lc_broadphase_test: more pairs than cap (" + std::to_string(tot) + ")");
     return LC_OK;
+}
+
+lc_status lc_broadphase_test_host(lc_broadphase *b, uint32_t *pairs, uint64_t cap, uint64_t *count, void *stream) {
+    if (!b || !count || (cap > 0 && !pairs))
+        return bp_fail(LC_ERR_INVALID_ARG, "lc_broadphase_test_host: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    uint64_t n = 0;
+    LC_TRY_BP(lc_broadphase_test(b, nullptr, 0, &n, stream));
+    const uint64_t want = std::min(n, cap);
+    if (want == 0) {
+        *count = n;
+        return n > cap ? bp_fail(LC_ERR_CAPACITY_OVERFLOW, "lc_broadphase_test_host: more pairs than cap") : LC_OK;
+    }
+    if (n > b->stage_cap) {
+        if (b->stage) cudaFree(b->stage);
+        b->stage = nullptr;
+        b->stage_cap = 0;
+        if (cudaMalloc((void **)&b->stage, sizeof(uint32_t) * 2 * n) != cudaSuccess) {
+            cudaGetLastError();
+            return bp_fail(LC_ERR_OOM, "lc_broadphase_test_host: cudaMalloc failed for the pair staging buffer");
+        }
+        b->stage_cap = n;
+    }
+    LC_TRY_BP(lc_broadphase_test(b, b->stage, b->stage_cap, &n, stream));
+    LC_BP_CUDA(cudaMemcpyAsync(pairs, b->stage, sizeof(uint32_t) * 2 * want, cudaMemcpyDeviceToHost, st));
+    LC_BP_CUDA(cudaStreamSynchronize(st));
+    *count = n;
+    return n > cap ? bp_fail(LC_ERR_CAPACITY_OVERFLOW, "lc_broadphase_test_host: more pairs than cap") : LC_OK;
 }
 
 lc_status lc_broadphase_get_criteria(lc_broadphase *b, lc_broadphase_criteria *out) {

@@ -66,4 +66,5 @@ def test_adapter_keeps_ids_through_add_move_remove():
     want = {tuple(sorted((names[a], names[b])))
             for a, b in box_pairs(np.array([boxes[n][0] for n in names]), np.array([boxes[n][1] for n in names]))}
     assert {tuple(sorted(p)) for p in got} == want
-    assert set(m.GetLastFrameCriteria()) == {"Collision Time", "Structure Time", "Intersection Tests", "Memory"}
+    assert set(m.GetLastFrameCriteria()) == {"Time Spent - Collisions", "Time Spent - Structure Update",
+                                             "Intersection Tests", "Memory Used (KB)"}

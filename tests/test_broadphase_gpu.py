@@ -75,8 +75,8 @@ def test_hash_buckets_shared_by_many_cells():
 @pytest.mark.parametrize("n", [0, 1, 2])
 def test_tiny_inputs(method, n):
     lo = np.zeros((n, 3), np.float32)
-    hi = np.ones((n, 3), np.float32)
-    got, _ = run(method, lo, hi)
+    hi = np.ones((n, 3), np.float32)  # each box covers the whole 24^3 grid
+    got, _ = run(method, lo, hi, max_entries=60_000)
     assert np.array_equal(got, box_pairs(lo, hi))
 
 
@@ -130,6 +130,6 @@ def test_collision_method_object_lifecycle(method):
             want = {(keys[a], keys[b]) for a, b in box_pairs(np.array([boxes[k][0] for k in keys]),
                                                             np.array([boxes[k][1] for k in keys]))}
             assert got == want, f"frame {frame}"
-            assert m.GetLastFrameCriteria()["Memory"] > 0
+            assert m.GetLastFrameCriteria()["Memory Used (KB)"] > 0
     finally:
         m.close()
