@@ -293,19 +293,25 @@ def adjoint_timing(seed: int) -> dict:
             "what": "backward = segment re-run from checkpoints + recorded step + reverse pass, per step"}
 
 
-def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20) -> dict:
+def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20, fit_steps: int = 50,
+                           fit_iters: int = 8) -> dict:
     """The batched differentiable rollout: 128 cloths (sides U{32..128}), each
-    dropped onto its own analytic sphere, 100 steps, 10 iterations,
-    checkpoints every 20 steps; loss = summed squared distance of the final
-    positions to a target.  One forward rollout and its backward pass after
-    one warm-up pair, CUDA events; the sphere projection is held fixed in the
-    reverse pass."""
+    dropped onto its own icosphere of subdivision 4 (radius U[0.2, 0.4] m) as
+    a static collider, 10 iterations, checkpoints every 20 steps.  Times one
+    100-step forward rollout and its backward pass (loss = summed squared
+    distance of the final positions to a target) after one warm-up pair,
+    with CUDA events.  Then recovers each cloth's stiffness by gradient
+    descent from 0.9 toward seeded targets U[0.5, 0.8]
+    (adjoint.fit_cloth_stiffness, the targets' final positions from forward
+    runs) over a `fit_steps` horizon: past about 50 steps the drapes fold
+    chaotically and the exact gradient no longer predicts the loss."""
     import torch
     from licenta_gb300 import scenes
-    from licenta_gb300.adjoint import ClothRollout, DiffCloth
+    from licenta_gb300.adjoint import ClothRollout, DiffCloth, fit_cloth_stiffness
 
-    specs = scenes.batched_sphere_cloths(seed=seed)
-    cloth = DiffCloth(specs, checkpoint_every=every)
+    specs = scenes.batched_sphere_cloths(seed=seed, mesh=True)
+    cloth = DiffCloth(specs, checkpoint_every=every, unscale=False)
+    C = len(specs)
     ks = torch.full((cloth.E,), 0.9, device="cuda", requires_grad=True)
     kb = torch.full((cloth.B,), 0.9, device="cuda", requires_grad=True)
     x0 = torch.tensor(np.concatenate([s.positions for s in specs]), device="cuda", requires_grad=True)
@@ -321,22 +327,45 @@ def adjoint_batched_timing(seed: int, steps: int = 100, every: int = 20) -> dict
         loss.backward()
         e[2].record()
         torch.cuda.synchronize()
-        g = ks.grad.abs()
-        fin = torch.isfinite(g)
-        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), float(fin.float().mean()), \
-            float(g[fin].max()) if bool(fin.any()) else 0.0
+        fin = float(torch.isfinite(ks.grad).float().mean())
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), fin, int(cloth.grad_exponent.max())
 
     once()
-    fwd, bwd, finite, gmax = once()
+    fwd, bwd, finite, exp_max = once()
     V = cloth.V
+    # stiffness recovery over the fit horizon
+    counts = [cloth.batch.constraint_counts(c) for c in range(C)]
+    kstar = torch.tensor(np.random.default_rng(seed + 1).uniform(0.5, 0.8, C), dtype=torch.float32, device="cuda")
+    ecl = torch.repeat_interleave(torch.arange(C, device="cuda"), torch.tensor([e for e, _ in counts], device="cuda"))
+    bcl = torch.repeat_interleave(torch.arange(C, device="cuda"), torch.tensor([b for _, b in counts], device="cuda"))
+    xs = x0.detach()
+    vs = torch.zeros_like(xs)
+    with torch.no_grad():
+        tgt = ClothRollout.apply(cloth, fit_steps, kstar[ecl], kstar[bcl], xs, vs).clone()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    k, hist = fit_cloth_stiffness(cloth, fit_steps, xs, vs, tgt, iters=fit_iters)
+    t1.record()
+    torch.cuda.synchronize()
+    err0 = float((0.9 - kstar).abs().mean())
+    err1 = float((k - kstar).abs().mean())
+    closer = float(((k - kstar).abs() < (0.9 - kstar).abs()).float().mean())
     cloth.close()
-    return {"workload": f"batched differentiable rollout: {len(specs)} cloths (sides 32..128, {V} vertices) onto "
-                        f"their own spheres, {steps} steps, 10 iterations, checkpoints every {every}",
+    return {"workload": f"batched differentiable rollout: {C} cloths (sides 32..128, {V} vertices) onto their own "
+                        f"icospheres (subdivision 4) as static colliders, {steps} steps, 10 iterations, "
+                        f"checkpoints every {every}",
             "forward_ms_per_step": fwd / steps, "backward_ms_per_step": bwd / steps,
-            "adjoint_over_forward": bwd / fwd, "cloth_steps_per_s_forward": len(specs) * steps / (fwd / 1000.0),
-            "dL_dk_stretch_finite_share": finite, "max_finite_abs_dL_dk_stretch": gmax,
-            "note": "the exact reverse pass grows ~1e14 per 20 steps in these contact-rich drapes; gradients "
-                    "beyond float range come out as inf (never NaN)"}
+            "adjoint_over_forward": bwd / fwd, "cloth_steps_per_s_forward": C * steps / (fwd / 1000.0),
+            "dL_dk_stretch_finite_share": finite, "max_gradient_exponent_2pow60": exp_max,
+            "stiffness_recovery": {"horizon_steps": fit_steps, "iterations": fit_iters,
+                                   "mean_abs_k_error_start": err0, "mean_abs_k_error_end": err1,
+                                   "cloths_closer_share": closer, "loss_start": hist[0][0], "loss_end": hist[-1][0],
+                                   "seconds": t0.elapsed_time(t1) / 1000.0,
+                                   "method": "per-cloth k, sign of dL/dk (scaled reverse pass), step 0.1 halved "
+                                             "on sign flips"},
+            "note": "gradients are the reverse pass's per-cloth scaled values (x 2^(-60 e)), all finite; the "
+                    "exact gradient of a 100-step contact-rich drape reaches 2^60 and beyond"}
 
 
 def rollout_1m_memory(seed: int, n: int = 1024, steps: int = 300, every: int = 20) -> dict:

@@ -181,3 +181,42 @@ class ClothRollout(torch.autograd.Function):
                 sc = sc.unsqueeze(1)
             return torch.where(t == 0, t, t * sc)
         return (None, None, unscale(gks, ecl), unscale(gkb, bcl), unscale(gx + gxp, vcl), unscale(gv, vcl))
+
+
+def fit_cloth_stiffness(cloth: DiffCloth, steps: int, x0: torch.Tensor, v0: torch.Tensor, target: torch.Tensor,
+                        k0: float = 0.9, iters: int = 8, step0: float = 0.1, k_range=(0.3, 0.98)):
+    """Per-cloth stiffness recovered by gradient descent: every cloth of the
+    batch has one stiffness k_c (its stretch and bend constraints share it),
+    starting at k0; the loss is the summed squared distance of the positions
+    after `steps` steps to `target`, each cloth's part depending only on its
+    own k_c.  Each iteration runs the rollout and its reverse pass and moves
+    every k_c by its own step against the sign of dL/dk_c (summed over the
+    cloth's constraints), halving the step when the sign flips.  The
+    direction comes from the reverse pass's scaled gradients
+    (DiffCloth(unscale=False)), so it stays exact where the gradient's
+    magnitude is beyond float range.  Returns (k, history) with history a
+    list of (total loss, per-cloth losses) before each update."""
+    C = len(cloth.batch.num_vertices)
+    counts = [cloth.batch.constraint_counts(c) for c in range(C)]
+    ecl = torch.repeat_interleave(torch.arange(C, device="cuda"), torch.tensor([e for e, _ in counts], device="cuda"))
+    bcl = torch.repeat_interleave(torch.arange(C, device="cuda"), torch.tensor([b for _, b in counts], device="cuda"))
+    vcl = torch.repeat_interleave(torch.arange(C, device="cuda"),
+                                  torch.tensor(cloth.batch.num_vertices, device="cuda"))
+    k = torch.full((C,), float(k0), device="cuda")
+    step = torch.full((C,), float(step0), device="cuda")
+    prev = torch.zeros(C, device="cuda")
+    history = []
+    for _ in range(iters):
+        ks = k[ecl].clone().requires_grad_(True)
+        kb = k[bcl].clone().requires_grad_(True)
+        out = ClothRollout.apply(cloth, steps, ks, kb, x0, v0)
+        per = torch.zeros(C, device="cuda").index_add_(0, vcl, ((out - target) ** 2).sum(dim=1))
+        per.sum().backward()
+        history.append((float(per.sum().detach()), per.detach().cpu().numpy()))
+        with torch.no_grad():
+            g = torch.zeros(C, device="cuda").index_add_(0, ecl, ks.grad).index_add_(0, bcl, kb.grad)
+            sgn = torch.sign(g)
+            step = torch.where(sgn * prev < 0, step * 0.5, step)
+            k = torch.clamp(k - step * sgn, *k_range)
+            prev = sgn
+    return k, history

@@ -388,15 +388,28 @@ struct lc_batch {
     }
 
     ~lc_batch() {
-        if (gexec) cudaGraphExecDestroy(gexec);
-        if (graph) cudaGraphDestroy(graph);
+        invalidate_graph();
         if (cap_stream) cudaStreamDestroy(cap_stream);
         free_collider_arrays();
     }
 
+    // graphs of the adjoint step (the recorded step and its reverse pass),
+    // one per set of gradient buffers and rescale parity, most recent first
+    struct AdjGraph {
+        uintptr_t key[7];
+        cudaGraph_t g;
+        cudaGraphExec_t e;
+    };
+    std::vector<AdjGraph> adj_graphs;
+
     void invalidate_graph() {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        for (AdjGraph &a : adj_graphs) {
+            cudaGraphExecDestroy(a.e);
+            cudaGraphDestroy(a.g);
+        }
+        adj_graphs.clear();
     }
 
     lc_status enqueue_step(cudaStream_t st);
@@ -480,8 +493,11 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
     // per-vertex contact CSR feeds the gather solvers; the scatter solver
     // walks the cloth's contact ranges instead.
-    const bool ordered = !(use_cluster && cluster_scatter) || d.friction_any;  // float sums in entry order
-    if (ordered || (use_cluster && cluster_scatter && ca.contact_gather)) {
+    // the recorded step of an adjoint batch runs on the global-memory solver,
+    // whose iterates the reverse pass replays
+    const bool on_chip = use_cluster && !recording;
+    const bool ordered = !(on_chip && cluster_scatter) || d.friction_any;  // float sums in entry order
+    if (ordered || (on_chip && cluster_scatter && ca.contact_gather)) {
         LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         launch_dyn(d, nvf, nee, narrow_grid, 0, st);
@@ -489,7 +505,7 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
         launch_dyn(d, nvf, nee, narrow_grid, 1, st);
         if (ordered) launch_dyn(d, nvf, nee, narrow_grid, 2, st);
     }
-    if (use_cluster) {
+    if (on_chip) {
         LC_KEV(0);
         LC_TRY(enqueue_cluster_solver(this, st));
         LC_KEV(1);
@@ -524,7 +540,15 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
 
 // Solver + integration on the cluster-resident path (one launch).
 static lc_status enqueue_cluster_solver(lc_batch *b, cudaStream_t st) {
-    LC_CUDA(launch_solve_cluster(b->d, b->ca, b->cluster_cs, b->cluster_scatter, b->C, st));
+    DevPtrs d = b->d;
+    if (b->opt.adjoint && !b->opt.debug_capture) {
+        // an adjoint batch keeps the decision records for its recorded step
+        // (global-memory solver); the on-chip steps need not write them
+        d.dbg_ground_it = nullptr;
+        d.dbg_dyn_nz = nullptr;
+        d.dbg_sphere = nullptr;
+    }
+    LC_CUDA(launch_solve_cluster(d, b->ca, b->cluster_cs, b->cluster_scatter, b->C, st));
     return LC_OK;
 }
 
@@ -617,11 +641,10 @@ static void fill_cloth_dev(const HostCloth &hc, ClothDev &cd) {
 
 static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, const lc_batch_options &opt_in) {
     lc_batch_options opt = opt_in;
-    if (opt.adjoint) {
-        // the reverse pass replays the global-memory Jacobi iterations
-        if (opt.solver_variant >= 2) return fail(LC_ERR_NOT_SUPPORTED, "adjoint: needs solver_variant 0 or 1");
-        opt.solver_variant = 1;
-    }
+    // adjoint batches: the reverse pass replays the global-memory Jacobi
+    // iterations, so the recorded step runs on that solver; the steps that
+    // are not recorded (the forward rollout, the segment re-runs) take the
+    // on-chip solver when the cloths fit
     b->C = n;
     b->opt = opt;
     b->hosts.resize(n);
@@ -1240,8 +1263,6 @@ lc_status lc_batch_set_tuning(lc_batch *b, const lc_tuning *t) {
         (t->cluster_size != 0 && t->cluster_size != 4 && t->cluster_size != 8 && t->cluster_size != 16) ||
         t->contact_gather < 0 || t->contact_gather > 1)
         return fail(LC_ERR_INVALID_ARG, "lc_batch_set_tuning: value out of range");
-    if (b->opt.adjoint && t->solver_variant != 1)
-        return fail(LC_ERR_NOT_SUPPORTED, "lc_batch_set_tuning: an adjoint batch keeps solver variant 1");
     LC_CUDA(cudaDeviceSynchronize());
     b->traverse_block = t->traverse_block;
     b->jacobi_block = t->jacobi_block;
@@ -1716,21 +1737,62 @@ static lc_status adjoint_step(lc_batch *b, float *gx, float *gxp, float *gv, flo
     if (!b->opt.adjoint) return fail(LC_ERR_INVALID_ARG, std::string(who) + ": batch created without the adjoint option");
     cudaStream_t st = (cudaStream_t)stream;
     b->last_stream = st;
-    b->recording = true;
-    const lc_status s = b->enqueue_step(st);
-    b->recording = false;
-    if (s != LC_OK) return s;
     const int V = b->d.Vtot;
-    uint32_t *flag = exponent ? b->adj_flag + (size_t)b->adj_flip * b->C : nullptr;
-    launch_adj_unpack(b->adj, gx, gxp, gv, V, st);
-    launch_adjoint(b->d, b->adj, b->adj_a, b->adj_g, b->nvf, b->nee, b->narrow_grid, b->nfixed, gk_stretch, gk_bend, st);
-    launch_adj_pack(b->d, b->adj, gx, gxp, gv, flag, V, st);
-    if (exponent) {
-        uint32_t *next = b->adj_flag + (size_t)(1 - b->adj_flip) * b->C;
-        launch_adj_rescale(b->d, gx, gxp, gv, gk_stretch, gk_bend, flag, next, exponent, b->adj.E, b->adj.B, st);
-        b->adj_flip = 1 - b->adj_flip;
+    // the recorded step, then its reverse pass, on stream s
+    auto enqueue = [&](cudaStream_t s) -> lc_status {
+        b->recording = true;
+        const lc_status r = b->enqueue_step(s);
+        b->recording = false;
+        if (r != LC_OK) return r;
+        uint32_t *flag = exponent ? b->adj_flag + (size_t)b->adj_flip * b->C : nullptr;
+        launch_adj_unpack(b->adj, gx, gxp, gv, V, s);
+        launch_adjoint(b->d, b->adj, b->adj_a, b->adj_g, b->nvf, b->nee, b->narrow_grid, b->nfixed, gk_stretch,
+                       gk_bend, s);
+        launch_adj_pack(b->d, b->adj, gx, gxp, gv, flag, V, s);
+        if (exponent) {
+            uint32_t *next = b->adj_flag + (size_t)(1 - b->adj_flip) * b->C;
+            launch_adj_rescale(b->d, gx, gxp, gv, gk_stretch, gk_bend, flag, next, exponent, b->adj.E, b->adj.B, s);
+        }
+        LC_CUDA(cudaGetLastError());
+        return LC_OK;
+    };
+    if (!b->opt.use_graph || b->opt.debug_capture) {
+        LC_TRY(enqueue(st));
+    } else {
+        // about 130 short launches for a small cloth: replayed as one graph,
+        // captured once per set of gradient buffers and rescale parity
+        const uintptr_t key[7] = {(uintptr_t)gx, (uintptr_t)gxp, (uintptr_t)gv, (uintptr_t)gk_stretch,
+                                  (uintptr_t)gk_bend, (uintptr_t)exponent, (uintptr_t)b->adj_flip};
+        size_t k = 0;
+        while (k < b->adj_graphs.size() && std::memcmp(b->adj_graphs[k].key, key, sizeof(key)) != 0) ++k;
+        if (k == b->adj_graphs.size()) {
+            LC_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+            const lc_status s = enqueue(b->cap_stream);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+            if (s != LC_OK) { if (g) cudaGraphDestroy(g); return s; }
+            LC_CUDA(e);
+            lc_batch::AdjGraph a{};
+            std::memcpy(a.key, key, sizeof(key));
+            a.g = g;
+            if (cudaGraphInstantiate(&a.e, g, 0) != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return fail(LC_ERR_CUDA, std::string(who) + ": graph instantiation failed");
+            }
+            if (b->adj_graphs.size() == 4) {
+                cudaGraphExecDestroy(b->adj_graphs.back().e);
+                cudaGraphDestroy(b->adj_graphs.back().g);
+                b->adj_graphs.pop_back();
+            }
+            b->adj_graphs.insert(b->adj_graphs.begin(), a);
+            k = 0;
+        } else if (k) {
+            std::rotate(b->adj_graphs.begin(), b->adj_graphs.begin() + k, b->adj_graphs.begin() + k + 1);
+            k = 0;
+        }
+        LC_CUDA(cudaGraphLaunch(b->adj_graphs[k].e, st));
     }
-    LC_CUDA(cudaGetLastError());
+    if (exponent) b->adj_flip = 1 - b->adj_flip;
     return LC_OK;
 }
 
