@@ -171,9 +171,7 @@ __global__ void k_adj_u(DevPtrs d, AdjPtrs A, const float4 *a, int it) {
 
 // Stretch (Physics/CudaPBD.cu:986-1022): corr1 = -w1 kp/ws f(x1 - x2),
 // corr2 = +w2 kp/ws f(x1 - x2).
-__global__ void k_adj_stretch(DevPtrs d, AdjPtrs A, int it, float *gk) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.E) return;
+__device__ __forceinline__ void adj_stretch_one(const DevPtrs &d, const AdjPtrs &A, int it, float *gk, int c) {
     const int2 id = d.s_ids[c];
     const float2 par = d.s_par[c];
     const ClothDev &cd = d.cloth[d.vcloth[id.x]];
@@ -197,9 +195,7 @@ __global__ void k_adj_stretch(DevPtrs d, AdjPtrs A, int it, float *gk) {
 }
 
 // Bend (Physics/CudaPBD.cu:1024-1147).
-__global__ void k_adj_bend(DevPtrs d, AdjPtrs A, int it, float *gk) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.B) return;
+__device__ __forceinline__ void adj_bend_one(const DevPtrs &d, const AdjPtrs &A, int it, float *gk, int c) {
     const int4 id = d.b_ids[c];
     const ClothDev &cd = d.cloth[d.vcloth[id.x]];
     float3 g2 = f3(0.f, 0.f, 0.f), g3 = g2, g4 = g2;
@@ -223,11 +219,12 @@ __global__ void k_adj_bend(DevPtrs d, AdjPtrs A, int it, float *gk) {
 // (frozen) barycentric weights b_s and signs, n = sum_s sgn_s b_s x_s and
 // corr_s = -(w_s sgn_s b_s / sum_s w_s b_s^2) f(n) with l0 = thickness; only
 // the entries counted in this iteration contribute.
-__global__ void k_adj_contact(DevPtrs d, AdjPtrs A, int it, const uint32_t *nvf_dev, const uint32_t *nee_dev) {
+__device__ __forceinline__ void adj_contacts(const DevPtrs &d, const AdjPtrs &A, int it, const uint32_t *nvf_dev,
+                                             const uint32_t *nee_dev, uint32_t first, uint32_t stride) {
     const uint32_t nvf = (uint32_t)min((uint64_t)*nvf_dev, d.vf_cap);
     const uint32_t nee = (uint32_t)min((uint64_t)*nee_dev, d.ee_cap);
     const uint8_t *nz = d.dbg_dyn_nz + (size_t)it * d.dyn_cap;
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nvf + nee; c += gridDim.x * blockDim.x) {
+    for (uint32_t c = first; c < nvf + nee; c += stride) {
         const bool isvf = c < nvf;
         const int4 v4 = isvf ? d.vf_v[c] : d.ee_v[c - nvf];
         const float4 w4 = isvf ? d.vf_w[c] : d.ee_w[c - nvf];
@@ -272,6 +269,27 @@ __global__ void k_adj_contact(DevPtrs d, AdjPtrs A, int it, const uint32_t *nvf_
         }
 #pragma unroll
         for (int s = 0; s < 4; ++s) A.dyn[c * 4 + s] = f4(out[s], 0.f);
+    }
+}
+
+// One iteration's vector-Jacobian products in one launch: blocks [0, nbs)
+// take the stretch constraints, the next nbb blocks the bends and the rest
+// the contacts (grid-stride).  They write disjoint buffers (the constraints'
+// CSR slots, the contact entries) from the same inputs.
+constexpr int kAdjBlock = 128;
+__global__ void __launch_bounds__(kAdjBlock) k_adj_constraints(DevPtrs d, AdjPtrs A, int it, float *gks, float *gkb,
+                                                               const uint32_t *nvf, const uint32_t *nee, int nbs,
+                                                               int nbb) {
+    const int bx = blockIdx.x;
+    if (bx < nbs) {
+        const int c = bx * kAdjBlock + threadIdx.x;
+        if (c < A.E) adj_stretch_one(d, A, it, gks, c);
+    } else if (bx < nbs + nbb) {
+        const int c = (bx - nbs) * kAdjBlock + threadIdx.x;
+        if (c < A.B) adj_bend_one(d, A, it, gkb, c);
+    } else {
+        const uint32_t nbc = gridDim.x - (uint32_t)(nbs + nbb);
+        adj_contacts(d, A, it, nvf, nee, (uint32_t)(bx - nbs - nbb) * kAdjBlock + threadIdx.x, nbc * kAdjBlock);
     }
 }
 
@@ -543,13 +561,12 @@ void launch_adjoint(const DevPtrs &d, const AdjPtrs &A, float4 *a, float4 *g, co
                     int grid, int nfixed, float *gk_stretch, float *gk_bend, cudaStream_t st) {
     if (!d.Vtot) return;
     const bool coll = d.any_collider && d.coll_act;
+    const int nbs = nb(A.E, kAdjBlock), nbb = nb(A.B, kAdjBlock);
     k_adj_integrate<<<nb(d.Vtot), kThreads, 0, st>>>(d, A, a);
     for (int it = A.K - 1; it >= 0; --it) {
         if (coll) k_adj_collider<<<nb(d.Vtot), kThreads, 0, st>>>(d, a, it + 1);
         k_adj_u<<<nb(d.Vtot), kThreads, 0, st>>>(d, A, a, it);
-        if (A.E) k_adj_stretch<<<nb(A.E), kThreads, 0, st>>>(d, A, it, gk_stretch);
-        if (A.B) k_adj_bend<<<nb(A.B, 128), 128, 0, st>>>(d, A, it, gk_bend);
-        k_adj_contact<<<grid, kThreads, 0, st>>>(d, A, it, nvf, nee);
+        k_adj_constraints<<<nbs + nbb + grid, kAdjBlock, 0, st>>>(d, A, it, gk_stretch, gk_bend, nvf, nee, nbs, nbb);
         k_adj_gather<<<d.nvblk, kThreads, 0, st>>>(d, A, a, g, it);
         if (nfixed) k_adj_fixed_add<<<nb(nfixed), kThreads, 0, st>>>(d, A, g, nfixed);
         float4 *t = a; a = g; g = t;

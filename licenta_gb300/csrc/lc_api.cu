@@ -22,6 +22,7 @@ namespace lc {
 // launchers (lc_lbvh.cu, lc_step.cu, lc_scan.cu)
 void launch_triangles(const DevPtrs &d, cudaStream_t st);
 void launch_collider(const DevPtrs &d, int grid, cudaStream_t st);
+void launch_collider_faces(const DevPtrs &d, int ntri, cudaStream_t st);
 void launch_leaves_from_boxes(const DevPtrs &d, const float *bmin, const float *bmax, int T, int mode,
                               cudaStream_t st);
 void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream_t st);
@@ -785,6 +786,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(sts, stile_start.size(), "stile_start")); LC_TRY(A.alloc(tf, n + 1, "tile_first"));
     d.stile_cloth = stc; d.stile_start = sts; b->tile_first = tf;
     LC_TRY(A.alloc(d.shist, (size_t)stile_cloth.size() * kSortBuckets, "shist"));
+    LC_TRY(A.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
     int *vbc, *vbs, *vbf; LC_TRY(A.alloc(vbc, vblk_cloth.size(), "vblk_cloth")); LC_TRY(A.alloc(vbs, vblk_start.size(), "vblk_start"));
     LC_TRY(A.alloc(vbf, vb_first.size(), "vb_first"));
     d.vblk_cloth = vbc; d.vblk_start = vbs; d.vb_first = vbf;
@@ -1603,13 +1605,22 @@ lc_status lc_batch_set_collider(lc_batch *b, int32_t c, const float *vertices, i
     }
     b->free_collider_arrays();
     DevPtrs &d = b->d;
-    d.cv = nullptr; d.ct = nullptr; d.cnmin = d.cnmax = nullptr; d.cnchild = nullptr;
+    d.cv = nullptr; d.ct = nullptr; d.cnmin = d.cnmax = nullptr; d.cnchild = nullptr; d.cface_geo = nullptr;
     if (any) {
         LC_TRY(upload_owned(b->coll_mem, cv, d.cv));
         LC_TRY(upload_owned(b->coll_mem, ct, d.ct));
         LC_TRY(upload_owned(b->coll_mem, nmin, d.cnmin));
         LC_TRY(upload_owned(b->coll_mem, nmax, d.cnmax));
         LC_TRY(upload_owned(b->coll_mem, child, d.cnchild));
+        {
+            void *q = nullptr;
+            if (cudaMalloc(&q, sizeof(float4) * 5 * ct.size()) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(LC_ERR_OOM, "lc_batch_set_collider: cudaMalloc failed");
+            }
+            b->coll_mem.push_back(q);
+            d.cface_geo = static_cast<float4 *>(q);
+        }
         if (!b->coll_slots_cnt) {
             const size_t V = (size_t)d.Vtot;
             LC_TRY(b->arena.alloc(b->coll_slots_cnt, V, "collider counts"));
@@ -1628,6 +1639,10 @@ lc_status lc_batch_set_collider(lc_batch *b, int32_t c, const float *vertices, i
     d.any_collider = any ? 1 : 0;
     if (b->coll_slots_cnt && !any) LC_CUDA(cudaMemset(b->coll_slots_cnt, 0, sizeof(int) * (size_t)d.Vtot));
     LC_CUDA(cudaMemcpy(b->cloth_dev, b->cds.data(), sizeof(ClothDev) * b->cds.size(), cudaMemcpyHostToDevice));
+    if (any) {  // the faces' planes and barycentric set-up, once (they read the windings just copied)
+        launch_collider_faces(d, (int)ct.size(), nullptr);
+        LC_CUDA(cudaDeviceSynchronize());
+    }
     b->invalidate_graph();
     return LC_OK;
 }
@@ -2147,6 +2162,7 @@ lc_status lc_lbvh_create(int32_t max_triangles, int32_t chunk_size, int32_t mort
     LC_TRY(A.alloc(stc, tiles, "stile_cloth")); LC_TRY(A.alloc(sts, tiles, "stile_start")); LC_TRY(A.alloc(tf, 2, "tile_first"));
     d.stile_cloth = stc; d.stile_start = sts; b.tile_first = tf;
     LC_TRY(A.alloc(d.shist, tiles * kSortBuckets, "shist"));
+    LC_TRY(A.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
     LC_TRY(A.alloc(b.npairs, 1, "npairs"));
     d.pair_cap = (uint64_t)PC;
     LC_CUDA(cudaMemset(d.err, 0, sizeof(uint32_t)));

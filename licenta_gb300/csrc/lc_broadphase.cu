@@ -501,6 +501,7 @@ lc_status lc_broadphase_create(const lc_broadphase_desc *desc, lc_broadphase **o
         d.stile_cloth = stc;
         d.stile_start = sts;
         LC_TRY_BP(b.alloc(d.shist, tiles * kSortBuckets, "sort histograms"));
+        LC_TRY_BP(b.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
         LC_TRY_BP(b.alloc(d.keys, keys, "keys"));
         LC_TRY_BP(b.alloc(d.keys_alt, keys, "keys"));
         LC_TRY_BP(b.alloc(d.payload, keys, "payload"));

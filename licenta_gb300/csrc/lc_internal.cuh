@@ -154,6 +154,7 @@ struct DevPtrs {
     const int *stile_start;   // sort tile -> first slot (global)
     int nstiles;
     uint32_t *shist;          // per tile x bucket counts / offsets
+    uint32_t *sdigit;         // kSortBuckets digit totals / bases: one segment of many tiles (may be null)
     const int *vblk_cloth, *vblk_start;  // vertex blocks never straddle cloths
     const int *vb_first;                 // per cloth: first vertex block (C+1 entries)
     double *damp_part;                   // 16 partial sums per vertex block
@@ -168,6 +169,8 @@ struct DevPtrs {
     const int4 *ct;           // collider triangles: global vertex ids, w = cloth
     const float4 *cnmin, *cnmax;  // collider BVH node boxes
     const int2 *cnchild;      // children, or (-(triangle + 1), -1) at a leaf
+    float4 *cface_geo;        // per collider triangle, 5 float4: (n, d0) (a, perimeter) (e1, d00) (e2, d11)
+                              // (d01, den, -, -): its plane towards the free side and the barycentric set-up
     int *ccnt;                // per cloth vertex: collider contacts of the step (<= kColliderSlots)
     int *cface;               // per cloth vertex x slot: collider triangle (global), ascending
     float4 *cw;               // per cloth vertex x slot: the contact's plane (unit normal to the free side, n . a)

@@ -170,6 +170,61 @@ __global__ void __launch_bounds__(kSortBuckets * kOffsetsSplit) k_sort_offsets(D
     }
 }
 
+// One segment of many tiles (the standalone LBVH, the broadphase, one large
+// cloth): its offsets spread over the digits instead of one block.  Block
+// `digit` scans that digit's counts over the tiles (an exclusive prefix,
+// in place) and keeps the digit's total; k_sort_digit_base turns the totals
+// into each digit's first position (after the segment's t_off) and
+// k_sort_add_base adds it to every tile's prefix.  The offsets are the same
+// numbers k_sort_offsets writes.
+__global__ void __launch_bounds__(kThreads) k_sort_col_scan(DevPtrs d, int ntiles) {
+    __shared__ uint32_t wsum[kThreads / 32];
+    const int dig = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (int t0 = 0; t0 < ntiles; t0 += kThreads) {
+        const int t = t0 + threadIdx.x;
+        const uint32_t v = t < ntiles ? d.shist[(size_t)t * kSortBuckets + dig] : 0u;
+        uint32_t x = v;  // inclusive scan in the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[wid] = x;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int k = 0; k < kThreads / 32; ++k) {
+            const uint32_t ws = wsum[k];
+            before += k < wid ? ws : 0u;
+            total += ws;
+        }
+        if (t < ntiles) d.shist[(size_t)t * kSortBuckets + dig] = carry + before + x - v;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) d.sdigit[dig] = carry;
+}
+__global__ void __launch_bounds__(kSortBuckets) k_sort_digit_base(DevPtrs d) {
+    __shared__ uint32_t s[kSortBuckets];
+    const int dig = threadIdx.x;
+    const uint32_t tot = d.sdigit[dig];
+    s[dig] = tot;
+    __syncthreads();
+    for (int o = 1; o < kSortBuckets; o <<= 1) {
+        const uint32_t y = dig >= o ? s[dig - o] : 0u;
+        __syncthreads();
+        s[dig] += y;
+        __syncthreads();
+    }
+    d.sdigit[dig] = (uint32_t)d.cloth[0].t_off + s[dig] - tot;
+}
+__global__ void k_sort_add_base(DevPtrs d, int ntiles) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)ntiles * kSortBuckets) return;
+    d.shist[i] += d.sdigit[i % kSortBuckets];
+}
+
 // One tile per block, ranked without block-wide rounds: warp w takes the
 // tile's keys [256 w, 256 w + 256) in 8 steps of 32 and ranks each key among
 // the warp's earlier keys of its digit (warp-private counts, no block
@@ -1245,18 +1300,45 @@ __global__ void k_contact_ranges(DevPtrs d, const uint32_t *__restrict__ ncv, co
 // kColliderSlots lowest faces are kept, ascending, so the result does not
 // depend on the traversal order.
 // ---------------------------------------------------------------------------
-__device__ bool collider_hit(float3 xp, float3 x, float3 a, float3 b, float3 c, float3 n, float d0, float h,
-                             float m) {
+// The per-face part of the test, computed once per lc_batch_set_collider
+// (the same operations in the same order as a per-test evaluation, so the
+// same bits): plane (n towards the free side, d0 = n . a), corner a and the
+// perimeter, the edges and their dot products.
+__global__ void k_collider_faces(DevPtrs d, int ntri) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const int4 tv = d.ct[t];
+    const float3 a = xyz(d.cv[tv.x]), b = xyz(d.cv[tv.y]), c = xyz(d.cv[tv.z]);
+    float3 nf = normalize(cross(sub(b, a), sub(c, a)));
+    if (d.cloth[tv.w].coll_cw) nf = mul(nf, -1.f);
+    const float3 e1 = sub(b, a), e2 = sub(c, a), e3 = sub(c, b);
+    const float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2);
+    float4 *g = d.cface_geo + (size_t)5 * t;
+    g[0] = f4(nf, dot(nf, a));
+    g[1] = f4(a, len(e1) + len(e2) + len(e3));
+    g[2] = f4(e1, d00);
+    g[3] = f4(e2, d11);
+    g[4] = make_float4(d01, d00 * d11 - d01 * d01, 0.f, 0.f);
+}
+void launch_collider_faces(const DevPtrs &d, int ntri, cudaStream_t st) {
+    if (ntri) k_collider_faces<<<(ntri + kThreads - 1) / kThreads, kThreads, 0, st>>>(d, ntri);
+}
+
+__device__ bool collider_hit(float3 xp, float3 x, const float4 *__restrict__ g, float h, float m) {
+    const float4 pl = g[0];
+    const float3 n = xyz(pl);
+    const float d0 = pl.w;
     const float s0 = dot(n, xp) - d0, s1 = dot(n, x) - d0;
     if (!(s1 < h + m) || !(s0 > -m)) return false;
+    const float4 ga = g[1], g1 = g[2], g2 = g[3], g3 = g[4];
     const float3 q = (s0 > 0.f && s1 < 0.f) ? add(xp, mul(sub(x, xp), s0 / (s0 - s1))) : x;
-    const float3 e1 = sub(b, a), e2 = sub(c, a), e3 = sub(c, b), r = sub(q, a);
-    const float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2), d20 = dot(r, e1), d21 = dot(r, e2);
-    const float den = d00 * d11 - d01 * d01;
+    const float3 r = sub(q, xyz(ga));
+    const float d00 = g1.w, d01 = g3.x, d11 = g2.w, d20 = dot(r, xyz(g1)), d21 = dot(r, xyz(g2));
+    const float den = g3.y;
     if (!(den > 0.f)) return false;
     const float wb = (d11 * d20 - d01 * d21) / den, wc = (d00 * d21 - d01 * d20) / den;
     const float wa = 1.f - wb - wc;
-    const float del = h / (len(e1) + len(e2) + len(e3));
+    const float del = h / ga.w;
     return wa >= -del && wb >= -del && wc >= -del;
 }
 
@@ -1286,12 +1368,8 @@ __global__ void k_collider_query(DevPtrs d) {
                     continue;
                 }
                 const int tri = -(ch.x + 1);
-                const int4 t = d.ct[tri];
-                const float3 x1 = xyz(d.cv[t.x]), x2 = xyz(d.cv[t.y]), x3 = xyz(d.cv[t.z]);
-                float3 nf = normalize(cross(sub(x2, x1), sub(x3, x1)));
-                if (cd.coll_cw) nf = mul(nf, -1.f);
-                const float d0 = dot(nf, x1);
-                if (!collider_hit(xpi, xi, x1, x2, x3, nf, d0, h, m)) continue;
+                const float4 *g = d.cface_geo + (size_t)5 * tri;
+                if (!collider_hit(xpi, xi, g, h, m)) continue;
                 // keep the kColliderSlots lowest faces, ascending
                 if (n == kColliderSlots && tri > face[n - 1]) { atomicOr(d.err, ERR_COLL_OVERFLOW); continue; }
                 if (n == kColliderSlots) atomicOr(d.err, ERR_COLL_OVERFLOW);
@@ -1302,7 +1380,7 @@ __global__ void k_collider_query(DevPtrs d) {
                     --k;
                 }
                 face[k] = tri;
-                pln[k] = f4(nf, d0);
+                pln[k] = g[0];
             }
         }
         d.ccnt[i] = n;
@@ -1347,7 +1425,13 @@ void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream
         const uint32_t *pin = even ? d.payload : d.payload_alt;
         uint32_t *pout = even ? d.payload_alt : d.payload;
         k_sort_hist<<<d.nstiles, kThreads, 0, st>>>(d, kin, p * kSortBits);
-        k_sort_offsets<<<d.C, kSortBuckets * kOffsetsSplit, 0, st>>>(d, tile_first);
+        if (d.C == 1 && d.sdigit && d.nstiles >= 16) {
+            k_sort_col_scan<<<kSortBuckets, kThreads, 0, st>>>(d, d.nstiles);
+            k_sort_digit_base<<<1, kSortBuckets, 0, st>>>(d);
+            k_sort_add_base<<<nblk((int64_t)d.nstiles * kSortBuckets), kThreads, 0, st>>>(d, d.nstiles);
+        } else {
+            k_sort_offsets<<<d.C, kSortBuckets * kOffsetsSplit, 0, st>>>(d, tile_first);
+        }
         k_sort_scatter<<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits);
     }
 }
