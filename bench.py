@@ -42,6 +42,12 @@ sys.path.insert(0, str(ROOT))
 METRIC = "cloth-steps/s, 256 uneven cloths (16..192 side) batched, 10 iterations, self-collision"
 UNIT = "cloth-steps/s"
 NCLOTH = 256
+# DRAM bytes of the solver's launches in one step of the 256-cloth workload
+# (both lanes, default launch shapes, steps 6 and 7): dram__bytes_read.sum +
+# dram__bytes_write.sum of k_solve_cluster_scatter from one single-pass ncu
+# capture of `bench.py --steps 2 --warmup 5 --no-plain --no-cpu-baseline
+# --no-adjoint --no-lbvh --no-large --no-autotune` (684.1 and 682.6 MB).
+SOLVER_DRAM_BYTES_PER_STEP = 683.4e6
 
 
 def parse():
@@ -707,9 +713,13 @@ def run_ours(args, world, rank, local):
                  "what": "compulsory bytes of one whole step (68V + 16E + 24B + 213T + 16P + 96C, pairs and "
                          "contacts averaged over the sampled steps) / measured time per step"}
     achieved = alg[dom] / (launch_ms / 1000.0) / 1e9 if launch_ms > 0 else 0.0
+    measured = dom == "solver" and args.cloths == NCLOTH and args.lanes == 2
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
-            "traffic": None, "algorithmic_bytes_per_launch": alg[dom], "launch_ms": launch_ms}
+            "traffic": SOLVER_DRAM_BYTES_PER_STEP if measured else None,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the solver launches of steps 6-7 "
+                               "(both lanes), this workload" if measured else "not captured for this configuration"),
+            "algorithmic_bytes_per_launch": alg[dom], "launch_ms": launch_ms}
 
     # ---- plain path: the same engine one cloth per call ---------------------
     plain = None

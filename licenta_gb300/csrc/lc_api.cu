@@ -736,6 +736,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(d.parent, N, "parent")); LC_TRY(A.alloc(d.child, I, "child"));
     LC_TRY(A.alloc(d.rml, I, "rml"));
     LC_TRY(A.alloc(d.wnode, 4 * std::max<int64_t>(I, 1), "wnode")); LC_TRY(A.alloc(d.visit, I, "visit"));
+    LC_TRY(A.alloc(d.nend, I, "node range ends"));
+    LC_TRY(A.alloc(d.rexit, 2 * std::max<int64_t>(I, 1), "refit exits")); LC_TRY(A.alloc(d.nrexit, 1, "refit exit count"));
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.pair_mask, PC, "pair_mask"));
@@ -786,7 +788,8 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(sts, stile_start.size(), "stile_start")); LC_TRY(A.alloc(tf, n + 1, "tile_first"));
     d.stile_cloth = stc; d.stile_start = sts; b->tile_first = tf;
     LC_TRY(A.alloc(d.shist, (size_t)stile_cloth.size() * kSortBuckets, "shist"));
-    LC_TRY(A.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
+    LC_TRY(A.alloc(d.sseg, kSortPassesMax + (size_t)n * kSortPassesMax * kSortBuckets, "sort segment totals"));
+    LC_TRY(A.alloc(d.sstat, (size_t)kSortPassesMax * stile_cloth.size() * kSortBuckets, "sort look-back status"));
     int *vbc, *vbs, *vbf; LC_TRY(A.alloc(vbc, vblk_cloth.size(), "vblk_cloth")); LC_TRY(A.alloc(vbs, vblk_start.size(), "vblk_start"));
     LC_TRY(A.alloc(vbf, vb_first.size(), "vb_first"));
     d.vblk_cloth = vbc; d.vblk_start = vbs; d.vb_first = vbf;
@@ -1226,6 +1229,10 @@ lc_status lc_batch_sync(lc_batch *b) {
     if (err & ERR_STACK) {
         cudaMemset(b->d.err, 0, sizeof(uint32_t));
         return fail(LC_ERR_STACK_OVERFLOW, "BVH traversal stack (64) exceeded");
+    }
+    if (err & ERR_SORT) {
+        cudaMemset(b->d.err, 0, sizeof(uint32_t));
+        return fail(LC_ERR_TIMEOUT, "sort look-back wait exceeded its bound");
     }
     return LC_OK;
 }
@@ -2153,7 +2160,8 @@ lc_status lc_lbvh_create(int32_t max_triangles, int32_t chunk_size, int32_t mort
     LC_TRY(A.alloc(d.nmin, N, "nmin")); LC_TRY(A.alloc(d.nmax, N, "nmax"));
     LC_TRY(A.alloc(d.leaf_tmp_min, T, "leaf_tmp_min")); LC_TRY(A.alloc(d.leaf_tmp_max, T, "leaf_tmp_max"));
     LC_TRY(A.alloc(d.parent, N, "parent")); LC_TRY(A.alloc(d.child, I, "child"));
-    LC_TRY(A.alloc(d.rml, I, "rml")); LC_TRY(A.alloc(d.visit, I, "visit"));
+    LC_TRY(A.alloc(d.rml, I, "rml")); LC_TRY(A.alloc(d.visit, I, "visit")); LC_TRY(A.alloc(d.nend, I, "node range ends"));
+    LC_TRY(A.alloc(d.rexit, 2 * std::max<int64_t>(I, 1), "refit exits")); LC_TRY(A.alloc(d.nrexit, 1, "refit exit count"));
     LC_TRY(A.alloc(d.pair_cnt, T, "pair_cnt")); LC_TRY(A.alloc(d.pair_off, T + 1, "pair_off"));
     LC_TRY(A.alloc(d.pair_chunk, PC, "pair_chunk")); LC_TRY(A.alloc(d.pairs, PC, "pairs"));
     LC_TRY(A.alloc(d.counters, 4, "counters")); LC_TRY(A.alloc(d.err, 1, "err"));
@@ -2162,7 +2170,8 @@ lc_status lc_lbvh_create(int32_t max_triangles, int32_t chunk_size, int32_t mort
     LC_TRY(A.alloc(stc, tiles, "stile_cloth")); LC_TRY(A.alloc(sts, tiles, "stile_start")); LC_TRY(A.alloc(tf, 2, "tile_first"));
     d.stile_cloth = stc; d.stile_start = sts; b.tile_first = tf;
     LC_TRY(A.alloc(d.shist, tiles * kSortBuckets, "shist"));
-    LC_TRY(A.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
+    LC_TRY(A.alloc(d.sseg, kSortPassesMax + (size_t)kSortPassesMax * kSortBuckets, "sort segment totals"));
+    LC_TRY(A.alloc(d.sstat, (size_t)kSortPassesMax * tiles * kSortBuckets, "sort look-back status"));
     LC_TRY(A.alloc(b.npairs, 1, "npairs"));
     d.pair_cap = (uint64_t)PC;
     LC_CUDA(cudaMemset(d.err, 0, sizeof(uint32_t)));
@@ -2227,6 +2236,7 @@ lc_status lc_lbvh_pairs(lc_lbvh *h, uint32_t *out_pairs, uint64_t cap, uint64_t 
     uint32_t err = 0;
     LC_CUDA(cudaMemcpy(&err, d.err, sizeof(err), cudaMemcpyDeviceToHost));
     if (err & ERR_STACK) return fail(LC_ERR_STACK_OVERFLOW, "BVH traversal stack (64) exceeded");
+    if (err & ERR_SORT) return fail(LC_ERR_TIMEOUT, "sort look-back wait exceeded its bound");
     return LC_OK;
 }
 

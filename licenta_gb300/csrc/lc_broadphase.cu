@@ -434,6 +434,7 @@ struct lc_broadphase {
         // the host arrays above are read by the copies before the sort starts
         LC_BP_CUDA(cudaStreamSynchronize(st));
         sd.nstiles = (int)starts.size();
+        sd.Ttot = (int)std::min<uint64_t>(count, 0x7FFFFFFFull);  // the one-sweep's 30-bit count check
         launch_sort(sd, tile_first, sort_passes, st);
         return LC_OK;
     }
@@ -501,7 +502,9 @@ lc_status lc_broadphase_create(const lc_broadphase_desc *desc, lc_broadphase **o
         d.stile_cloth = stc;
         d.stile_start = sts;
         LC_TRY_BP(b.alloc(d.shist, tiles * kSortBuckets, "sort histograms"));
-        LC_TRY_BP(b.alloc(d.sdigit, kSortBuckets, "sort digit bases"));
+        LC_TRY_BP(b.alloc(d.sseg, kSortPassesMax + (size_t)kSortPassesMax * kSortBuckets, "sort segment totals"));
+        LC_TRY_BP(b.alloc(d.sstat, (size_t)kSortPassesMax * tiles * kSortBuckets, "sort look-back status"));
+        d.err = b.err;
         LC_TRY_BP(b.alloc(d.keys, keys, "keys"));
         LC_TRY_BP(b.alloc(d.keys_alt, keys, "keys"));
         LC_TRY_BP(b.alloc(d.payload, keys, "payload"));
@@ -627,6 +630,7 @@ lc_status lc_broadphase_test(lc_broadphase *b, uint32_t *pairs, uint64_t cap, ui
     *count = tot;
     if (err) {
         LC_BP_CUDA(cudaMemset(b->err, 0, sizeof(uint32_t)));
+        if (err & ERR_SORT) return bp_fail(LC_ERR_TIMEOUT, "lc_broadphase_update: sort look-back wait exceeded its bound");
         return bp_fail(LC_ERR_STACK_OVERFLOW, "lc_broadphase_test: BVH traversal stack exceeded");
     }
     if (tot > cap && pairs)

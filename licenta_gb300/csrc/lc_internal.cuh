@@ -15,6 +15,7 @@ constexpr int kThreads = 256;
 constexpr int kSortBits = 8;
 constexpr int kSortBuckets = 1 << kSortBits;
 constexpr int kSortTile = 2048;          // keys per sort tile (256 threads x 8)
+constexpr int kSortPassesMax = 8;        // 8-bit digits of a 63-bit key
 constexpr int kTraverseStack = 64;       // Collision/CudaBVH.cu:38
 constexpr int kTraverseBlockMax = 256;   // largest traversal block (the packet kernel is bounded for 6 of them per SM)
 constexpr int kScanBlocks = 1024;        // fixed grid of the device-count scans
@@ -32,6 +33,7 @@ enum : uint32_t {
     ERR_DYN_OVERFLOW = 1u << 4,
     ERR_CAND_OVERFLOW = 1u << 5,
     ERR_COLL_OVERFLOW = 1u << 6,   // more static-collider contacts at a vertex than kColliderSlots
+    ERR_SORT = 1u << 7,            // a sort look-back wait ran past its bound
 };
 
 // Per-cloth descriptor in device memory.
@@ -100,6 +102,9 @@ struct DevPtrs {
     int2 *child;
     int2 *rml;
     int *visit;
+    int *nend;             // per internal node: the other end j of its leaf range (may be null)
+    int2 *rexit;           // refit: (cloth, node) arrivals left for the upper pass (2 x internal nodes)
+    uint32_t *nrexit;      // their count (cleared by k_karras)
     float4 *wnode;         // 4 per internal node: {lmin, left} {lmax, rmll} {rmin, right} {rmax, rmlr} (may be null)
     uint32_t *pair_cnt;    // per slot
     uint32_t *pair_off;    // per slot (exclusive scan), + total at [Ttot]
@@ -154,7 +159,10 @@ struct DevPtrs {
     const int *stile_start;   // sort tile -> first slot (global)
     int nstiles;
     uint32_t *shist;          // per tile x bucket counts / offsets
-    uint32_t *sdigit;         // kSortBuckets digit totals / bases: one segment of many tiles (may be null)
+    // one-sweep scratch (both null: per-pass histograms and k_sort_offsets):
+    // sseg = kSortPassesMax tile tickets, then per segment x pass x digit the
+    // segment's digit totals; sstat = per pass x tile x digit look-back status
+    uint32_t *sseg, *sstat;
     const int *vblk_cloth, *vblk_start;  // vertex blocks never straddle cloths
     const int *vb_first;                 // per cloth: first vertex block (C+1 entries)
     double *damp_part;                   // 16 partial sums per vertex block

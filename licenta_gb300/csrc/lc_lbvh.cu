@@ -170,59 +170,55 @@ __global__ void __launch_bounds__(kSortBuckets * kOffsetsSplit) k_sort_offsets(D
     }
 }
 
-// One segment of many tiles (the standalone LBVH, the broadphase, one large
-// cloth): its offsets spread over the digits instead of one block.  Block
-// `digit` scans that digit's counts over the tiles (an exclusive prefix,
-// in place) and keeps the digit's total; k_sort_digit_base turns the totals
-// into each digit's first position (after the segment's t_off) and
-// k_sort_add_base adds it to every tile's prefix.  The offsets are the same
-// numbers k_sort_offsets writes.
-__global__ void __launch_bounds__(kThreads) k_sort_col_scan(DevPtrs d, int ntiles) {
-    __shared__ uint32_t wsum[kThreads / 32];
-    const int dig = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t carry = 0;
-    for (int t0 = 0; t0 < ntiles; t0 += kThreads) {
-        const int t = t0 + threadIdx.x;
-        const uint32_t v = t < ntiles ? d.shist[(size_t)t * kSortBuckets + dig] : 0u;
-        uint32_t x = v;  // inclusive scan in the warp
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) wsum[wid] = x;
-        __syncthreads();
-        uint32_t before = 0, total = 0;
-#pragma unroll
-        for (int k = 0; k < kThreads / 32; ++k) {
-            const uint32_t ws = wsum[k];
-            before += k < wid ? ws : 0u;
-            total += ws;
-        }
-        if (t < ntiles) d.shist[(size_t)t * kSortBuckets + dig] = carry + before + x - v;
-        carry += total;
-        __syncthreads();
+// One-sweep offsets (every sort with look-back scratch; the allocation-free
+// entry keeps the per-pass histogram above).  k_sort_hist_all reads each
+// tile's keys once and adds the digit counts of every pass to its segment's
+// totals, so the digits' first positions in the segment are known before
+// the first pass; the scatter of a pass then finds a tile's place among its
+// segment's earlier tiles by a decoupled look-back over per-tile, per-digit
+// status words (flag in the top two bits: aggregate of the tile alone, or
+// inclusive prefix from the segment's first tile).  Tiles take their
+// position from a ticket counter, so a block only ever waits on blocks that
+// started before it.  The offsets are the numbers k_sort_offsets gives.
+constexpr uint32_t kStatAgg = 1u << 30, kStatPre = 2u << 30, kStatCount = kStatAgg - 1;
+constexpr uint32_t kLookbackSpins = 1u << 22;  // bound on the status waits of one look-back (then ERR_SORT)
+constexpr int kLookbackWindow = 8;               // earlier tiles' statuses read per look-back step
+__global__ void __launch_bounds__(kThreads) k_sort_hist_all(DevPtrs d, const unsigned long long *__restrict__ keys,
+                                                            int passes) {
+    static_assert(kThreads == kSortBuckets, "one thread per digit");
+    constexpr int R = kSortTile / kThreads;
+    __shared__ uint32_t h[kSortPassesMax][kSortBuckets];
+    const int tile = blockIdx.x, t = threadIdx.x, lane = t & 31;
+    const int c = d.stile_cloth[tile];
+    const int start = d.stile_start[tile];
+    const ClothDev &cd = d.cloth[c];
+    const int n = min(kSortTile, cd.t_off + cd.T - start);
+    for (int p = 0; p < passes; ++p) {
+        h[p][t] = 0;
+        d.sstat[((size_t)p * d.nstiles + tile) * kSortBuckets + t] = 0;
     }
-    if (threadIdx.x == 0) d.sdigit[dig] = carry;
-}
-__global__ void __launch_bounds__(kSortBuckets) k_sort_digit_base(DevPtrs d) {
-    __shared__ uint32_t s[kSortBuckets];
-    const int dig = threadIdx.x;
-    const uint32_t tot = d.sdigit[dig];
-    s[dig] = tot;
     __syncthreads();
-    for (int o = 1; o < kSortBuckets; o <<= 1) {
-        const uint32_t y = dig >= o ? s[dig - o] : 0u;
-        __syncthreads();
-        s[dig] += y;
-        __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int li = r * kThreads + t;
+        const bool valid = li < n;
+        const unsigned long long key = valid ? keys[start + li] : 0ull;
+        for (int p = 0; p < passes; ++p) {
+            // a digit common to the whole warp (the high digits of nearby
+            // Morton codes) is one atomic; otherwise one per lane
+            const uint32_t dig = valid ? (uint32_t)(key >> (p * kSortBits)) & (kSortBuckets - 1) : kSortBuckets;
+            const uint32_t d0 = __shfl_sync(0xffffffffu, dig, 0);
+            if (__all_sync(0xffffffffu, dig == d0)) {
+                if (lane == 0 && d0 < kSortBuckets) atomicAdd(&h[p][d0], 32u);
+            } else if (valid) {
+                atomicAdd(&h[p][dig], 1u);
+            }
+        }
     }
-    d.sdigit[dig] = (uint32_t)d.cloth[0].t_off + s[dig] - tot;
-}
-__global__ void k_sort_add_base(DevPtrs d, int ntiles) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)ntiles * kSortBuckets) return;
-    d.shist[i] += d.sdigit[i % kSortBuckets];
+    __syncthreads();
+    uint32_t *seg = d.sseg + kSortPassesMax + (size_t)c * kSortPassesMax * kSortBuckets;
+    for (int p = 0; p < passes; ++p)
+        if (h[p][t]) atomicAdd(&seg[p * kSortBuckets + t], h[p][t]);
 }
 
 // One tile per block, ranked without block-wide rounds: warp w takes the
@@ -231,27 +227,39 @@ __global__ void k_sort_add_base(DevPtrs d, int ntiles) {
 // barrier); one scan per digit over the warps then gives every key its slot
 // in the tile sorted by digit, stable because index order is (warp, step,
 // lane).  The sorted tile is staged in shared memory and written out with
-// consecutive threads on consecutive slots of each digit's run.
-__global__ void __launch_bounds__(kThreads) k_sort_scatter(DevPtrs d, const unsigned long long *__restrict__ kin,
+// consecutive threads on consecutive slots of each digit's run.  With
+// kLookback the tile's global slots come from the one-sweep look-back
+// (tiles in ticket order), otherwise from k_sort_offsets.
+template <bool kLookback>
+__global__ void __launch_bounds__(kThreads, 4) k_sort_scatter(DevPtrs d, const unsigned long long *__restrict__ kin,
                                                            const uint32_t *__restrict__ pin,
                                                            unsigned long long *__restrict__ kout,
-                                                           uint32_t *__restrict__ pout, int shift) {
+                                                           uint32_t *__restrict__ pout, int shift, int pass,
+                                                           const int *__restrict__ tile_first) {
     constexpr int W = kThreads / 32;
     constexpr int R = kSortTile / kThreads;  // keys per lane
     static_assert(kThreads == kSortBuckets && kSortTile == W * 32 * R, "one thread per digit, 32 R keys per warp");
     __shared__ uint32_t wcnt[W][kSortBuckets];  // per warp: keys of each digit (then: first tile slot)
     __shared__ uint32_t lbase[kSortBuckets];    // first tile slot per digit
-    __shared__ uint32_t gbase[kSortBuckets];    // first global slot per digit (from k_sort_offsets)
-    __shared__ uint32_t wsum[W];
+    __shared__ uint32_t gbase[kSortBuckets];    // first global slot per digit
+    __shared__ uint32_t wsum[W], wseg[W];
     __shared__ unsigned long long skey[kSortTile];
     __shared__ uint32_t spay[kSortTile];
-    const int tile = blockIdx.x;
+    __shared__ int s_tile, s_bad;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    if (kLookback) {
+        if (t == 0) {
+            s_tile = (int)atomicAdd(&d.sseg[pass], 1u);
+            s_bad = 0;
+        }
+        __syncthreads();
+    }
+    const int tile = kLookback ? s_tile : (int)blockIdx.x;
     const int c = d.stile_cloth[tile];
     const int start = d.stile_start[tile];
     const ClothDev &cd = d.cloth[c];
     const int n = min(kSortTile, cd.t_off + cd.T - start);
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    gbase[t] = d.shist[(size_t)tile * kSortBuckets + t];
+    if (!kLookback) gbase[t] = d.shist[(size_t)tile * kSortBuckets + t];
 #pragma unroll
     for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
     __syncthreads();
@@ -278,13 +286,32 @@ __global__ void __launch_bounds__(kThreads) k_sort_scatter(DevPtrs d, const unsi
     uint32_t tot = 0;
 #pragma unroll
     for (int w = 0; w < W; ++w) tot += wcnt[w][t];
+    // one-sweep: publish the tile's count of digit t, and scan the segment's
+    // digit totals (the digits' first positions in the segment)
+    uint32_t *stat = nullptr;
+    int first = 0;
+    uint32_t segtot = 0, segincl = 0;
+    if (kLookback) {
+        first = tile_first[c];
+        stat = d.sstat + (size_t)pass * d.nstiles * kSortBuckets;
+        cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(stat[(size_t)tile * kSortBuckets + t])
+            .store((tile == first ? kStatPre : kStatAgg) | tot, cuda::memory_order_relaxed);
+        segtot = segincl = d.sseg[kSortPassesMax + ((size_t)c * kSortPassesMax + pass) * kSortBuckets + t];
+    }
     uint32_t incl = tot;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += v;
+        if (kLookback) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, segincl, o);
+            if (lane >= o) segincl += u;
+        }
     }
-    if (lane == 31) wsum[wid] = incl;
+    if (lane == 31) {
+        wsum[wid] = incl;
+        if (kLookback) wseg[wid] = segincl;
+    }
     __syncthreads();
     uint32_t run = incl - tot;
     for (int w = 0; w < wid; ++w) run += wsum[w];
@@ -306,11 +333,64 @@ __global__ void __launch_bounds__(kThreads) k_sort_scatter(DevPtrs d, const unsi
             spay[pos] = pr[r];
         }
     }
+    if (kLookback) {
+        // the tile's place among the segment's earlier tiles, digit t: sum
+        // the aggregates back to the first inclusive prefix
+        // A window of kLookbackWindow earlier tiles is read at once (the
+        // segment's first tile always holds its inclusive prefix, so the
+        // walk never passes it); a window that meets an unpublished tile
+        // resumes there.
+        uint32_t excl = 0;
+        if (tile != first) {
+            uint32_t spins = 0;
+            for (int j = tile - 1;;) {
+                uint32_t sv[kLookbackWindow];
+#pragma unroll
+                for (int k = 0; k < kLookbackWindow; ++k)
+                    sv[k] = j - k >= first ? cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(
+                                                 stat[(size_t)(j - k) * kSortBuckets + t])
+                                                 .load(cuda::memory_order_relaxed)
+                                           : kStatPre;
+                bool done = false;
+                int k = 0;
+                for (; k < kLookbackWindow; ++k) {
+                    if (sv[k] == 0) break;  // not published yet
+                    excl += sv[k] & kStatCount;
+                    if ((sv[k] & ~kStatCount) == kStatPre || j - k == first) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (done) break;
+                j -= k;
+                if (k == 0) {
+                    if (++spins > kLookbackSpins) {
+                        s_bad = 1;
+                        atomicOr(d.err, ERR_SORT);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            // published even after a failed wait, so that later tiles end
+            cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(stat[(size_t)tile * kSortBuckets + t])
+                .store(kStatPre | (excl + tot), cuda::memory_order_relaxed);
+        }
+        uint32_t dbase = segincl - segtot;
+        for (int w = 0; w < wid; ++w) dbase += wseg[w];
+        gbase[t] = (uint32_t)cd.t_off + dbase + excl;
+    }
     __syncthreads();
+    if (kLookback && s_bad) return;
+    const uint32_t lo = (uint32_t)cd.t_off, hi = (uint32_t)(cd.t_off + cd.T);
     for (int i = t; i < n; i += kThreads) {
         const unsigned long long key = skey[i];
         const uint32_t dig = (uint32_t)(key >> shift) & (kSortBuckets - 1);
         const uint32_t g = gbase[dig] + (uint32_t)i - lbase[dig];
+        if (kLookback && (g < lo || g >= hi)) {  // only after a failed wait elsewhere
+            atomicOr(d.err, ERR_SORT);
+            continue;
+        }
         kout[g] = key;
         pout[g] = spay[i];
     }
@@ -346,6 +426,7 @@ __device__ __forceinline__ int sgn_ref(int a) { return signbit((float)a) ? -1 : 
 
 __global__ void k_karras(DevPtrs d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0 && d.nrexit) *d.nrexit = 0;  // k_refit_local appends to it
     if (s >= d.Ttot) return;
     const int c = d.tcloth[s];
     const ClothDev &cd = d.cloth[c];
@@ -383,6 +464,7 @@ __global__ void k_karras(DevPtrs d) {
     const int left = split == first ? In + split : split;
     const int right = split + 1 == last ? In + split + 1 : split + 1;
     d.child[cd.i_off + id] = make_int2(left, right);
+    if (d.nend) d.nend[cd.i_off + id] = j;
     // An internal node that the refit never reaches (possible only when a run
     // of >= 3 equal codes makes two nodes claim one child) keeps stale data in
     // the reference; here it keeps zeros, deterministically.
@@ -398,15 +480,9 @@ __global__ void k_karras(DevPtrs d) {
 // Bottom-up refit: Collision/CudaBVH.cu:128-149.  The second arrival at a
 // node unions its children; the arrival counter is an acq_rel atomic, which
 // orders the child writes before it, and the children are re-read from L2.
-__global__ void k_refit(DevPtrs d) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.Ttot) return;
-    const int c = d.tcloth[s];
-    const ClothDev &cd = d.cloth[c];
-    const int id = s - cd.t_off;
+// refit_climb starts at node pid, arriving from a child whose box is written.
+__device__ __forceinline__ void refit_climb(const DevPtrs &d, const ClothDev &cd, int pid) {
     const int In = cd.T - 1;
-    if (In <= 0) return;
-    int pid = d.parent[cd.n_off + In + id];
     for (int guard = 0; guard <= cd.T; ++guard) {
         if (pid < 0 || pid >= In) {
             if (pid != 0) atomicOr(d.err, ERR_TREE);
@@ -436,6 +512,121 @@ __global__ void k_refit(DevPtrs d) {
         pid = up;
     }
     atomicOr(d.err, ERR_TREE);
+}
+
+// One thread per leaf, the whole climb in L2 (the allocation-free entry).
+__global__ void k_refit(DevPtrs d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.Ttot) return;
+    const ClothDev &cd = d.cloth[d.tcloth[s]];
+    const int id = s - cd.t_off;
+    const int In = cd.T - 1;
+    if (In <= 0) return;
+    refit_climb(d, cd, d.parent[cd.n_off + In + id]);
+}
+
+// The same refit in two launches.  k_refit_local: block b owns the slots
+// [256 b, 256 b + 256); an internal node whose leaf range [min(i, j),
+// max(i, j)] lies inside one block (node i sits at one end of its range, so
+// its slot is inside too) is "local": its arrival counter, box and rightmost
+// leaves live in that block's shared memory (block-scope acq_rel counter),
+// and its box is also written out.  A thread that reaches a node whose
+// range crosses a block boundary stops there and leaves the arrival to
+// k_refit_upper (each thread leaves at most one); the block writes its
+// arrivals out densely, one global atomic per block.  k_refit_upper then
+// climbs from the few left arrivals in L2 as k_refit does, so no block of
+// the launch over all leaves waits on a climb to the root.
+// Every arrival at a local node comes from inside its block: the ranges
+// come from the index-tiebroken prefix (unique keys), so any two ranges are
+// nested or disjoint, and an internal child is strictly inside its
+// parent's range (a child at the range's end is a leaf), so its own range
+// lies inside too -- also where equal codes make two nodes claim one child.
+// Shared boxes start at zero, like the global ones k_karras clears.
+__global__ void __launch_bounds__(kThreads) k_refit_local(DevPtrs d) {
+    __shared__ float4 s_lmin[kThreads], s_lmax[kThreads];  // the block's leaves
+    __shared__ float4 s_min[kThreads], s_max[kThreads];    // local internal nodes, by slot
+    __shared__ int2 s_rml[kThreads];
+    __shared__ int s_visit[kThreads];
+    __shared__ int2 s_exit[kThreads];
+    __shared__ uint32_t s_nexit, s_base;
+    const int tid = threadIdx.x;
+    const int B0 = blockIdx.x * kThreads, B1 = min(B0 + kThreads, d.Ttot);
+    const int s = B0 + tid;
+    const bool valid = s < d.Ttot;
+    int c = 0, id = 0, In = 0;
+    const ClothDev *cdp = nullptr;
+    s_visit[tid] = 0;
+    s_min[tid] = s_max[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s_rml[tid] = make_int2(0, 0);
+    if (tid == 0) s_nexit = 0;
+    if (valid) {
+        c = d.tcloth[s];
+        cdp = &d.cloth[c];
+        id = s - cdp->t_off;
+        In = cdp->T - 1;
+        s_lmin[tid] = __ldg(&d.nmin[cdp->n_off + In + id]);
+        s_lmax[tid] = __ldg(&d.nmax[cdp->n_off + In + id]);
+    }
+    __syncthreads();
+    if (valid && In > 0) {
+        const ClothDev &cd = *cdp;
+        const int base = cd.t_off - B0;  // cloth-local index -> block slot
+        int pid = d.parent[cd.n_off + In + id];
+        for (int guard = 0;; ++guard) {
+            if (guard > cd.T) {
+                atomicOr(d.err, ERR_TREE);
+                break;
+            }
+            if (pid < 0 || pid >= In) {
+                if (pid != 0) atomicOr(d.err, ERR_TREE);
+                break;
+            }
+            const int je = __ldg(&d.nend[cd.i_off + pid]);
+            const int lo = min(pid, je) + base, hi = max(pid, je) + base;
+            if (lo < 0 || hi >= B1 - B0) {  // crosses a block boundary: the upper pass arrives
+                const uint32_t e = atomicAdd(&s_nexit, 1u);
+                s_exit[e] = make_int2(c, pid);
+                break;
+            }
+            const int2 ch = __ldg(&d.child[cd.i_off + pid]);
+            const int up = pid ? __ldg(&d.parent[cd.n_off + pid]) : 0;
+            cuda::atomic_ref<int, cuda::thread_scope_block> visit(s_visit[pid + base]);
+            if (visit.fetch_add(1, cuda::memory_order_acq_rel) == 0) break;
+            const bool la = ch.x >= In, lb = ch.y >= In;
+            const int ia = (la ? ch.x - In : ch.x) + base, ib = (lb ? ch.y - In : ch.y) + base;
+            if (ia < 0 || ia >= B1 - B0 || ib < 0 || ib >= B1 - B0) {  // children outside the range: not a tree
+                atomicOr(d.err, ERR_TREE);
+                break;
+            }
+            const float4 amn = la ? s_lmin[ia] : s_min[ia], amx = la ? s_lmax[ia] : s_max[ia];
+            const float4 bmn = lb ? s_lmin[ib] : s_min[ib], bmx = lb ? s_lmax[ib] : s_max[ib];
+            const float4 mn = f4(vmin(xyz(amn), xyz(bmn)), 0.f), mx = f4(vmax(xyz(amx), xyz(bmx)), 0.f);
+            int rl, rr;
+            if (la) rl = ch.x;
+            else { const int2 q = s_rml[ia]; rl = max(q.x, q.y); }
+            if (lb) rr = ch.y;
+            else { const int2 q = s_rml[ib]; rr = max(q.x, q.y); }
+            s_min[pid + base] = mn;
+            s_max[pid + base] = mx;
+            s_rml[pid + base] = make_int2(rl, rr);
+            d.nmin[cd.n_off + pid] = mn;
+            d.nmax[cd.n_off + pid] = mx;
+            d.rml[cd.i_off + pid] = make_int2(rl, rr);
+            if (pid == 0) break;
+            pid = up;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) s_base = s_nexit ? atomicAdd(d.nrexit, s_nexit) : 0u;
+    __syncthreads();
+    if ((uint32_t)tid < s_nexit) d.rexit[s_base + tid] = s_exit[tid];
+}
+__global__ void k_refit_upper(DevPtrs d) {
+    const uint32_t n = *d.nrexit;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int2 x = d.rexit[e];
+        refit_climb(d, d.cloth[x.x], x.y);
+    }
 }
 
 // Wide node records for the traversal: per internal node both children's
@@ -1418,21 +1609,28 @@ void launch_leaves_from_boxes(const DevPtrs &d, const float *bmin, const float *
 }
 void launch_sort(const DevPtrs &d, const int *tile_first, int passes, cudaStream_t st) {
     if (!d.nstiles) return;
+    // One-sweep wherever the scratch exists (not in the allocation-free
+    // entry, whose one tile needs no look-back) and the digit counts fit the
+    // status word's 30 bits; the per-pass histogram and per-segment offsets
+    // block remain for the rest.
+    const bool sweep = d.sstat && d.sseg && d.Ttot <= (int64_t)kStatCount && passes <= kSortPassesMax;
+    if (sweep) {
+        cudaMemsetAsync(d.sseg, 0, sizeof(uint32_t) * (kSortPassesMax + (size_t)d.C * kSortPassesMax * kSortBuckets), st);
+        k_sort_hist_all<<<d.nstiles, kThreads, 0, st>>>(d, d.keys, passes);
+    }
     for (int p = 0; p < passes; ++p) {
         const bool even = (p & 1) == 0;
         const unsigned long long *kin = even ? d.keys : d.keys_alt;
         unsigned long long *kout = even ? d.keys_alt : d.keys;
         const uint32_t *pin = even ? d.payload : d.payload_alt;
         uint32_t *pout = even ? d.payload_alt : d.payload;
-        k_sort_hist<<<d.nstiles, kThreads, 0, st>>>(d, kin, p * kSortBits);
-        if (d.C == 1 && d.sdigit && d.nstiles >= 16) {
-            k_sort_col_scan<<<kSortBuckets, kThreads, 0, st>>>(d, d.nstiles);
-            k_sort_digit_base<<<1, kSortBuckets, 0, st>>>(d);
-            k_sort_add_base<<<nblk((int64_t)d.nstiles * kSortBuckets), kThreads, 0, st>>>(d, d.nstiles);
+        if (sweep) {
+            k_sort_scatter<true><<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits, p, tile_first);
         } else {
+            k_sort_hist<<<d.nstiles, kThreads, 0, st>>>(d, kin, p * kSortBits);
             k_sort_offsets<<<d.C, kSortBuckets * kOffsetsSplit, 0, st>>>(d, tile_first);
+            k_sort_scatter<false><<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits, p, tile_first);
         }
-        k_sort_scatter<<<d.nstiles, kThreads, 0, st>>>(d, kin, pin, kout, pout, p * kSortBits);
     }
 }
 void launch_post_sort(const DevPtrs &d, cudaStream_t st) {
@@ -1442,7 +1640,15 @@ void launch_karras(const DevPtrs &d, cudaStream_t st) {
     if (d.Ttot) k_karras<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
 }
 void launch_refit(const DevPtrs &d, cudaStream_t st) {
-    if (d.Ttot) k_refit<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+    if (!d.Ttot) return;
+    if (d.nend) {
+        // the upper pass: a grid-stride loop over the arrivals left, sized to
+        // be resident at once
+        k_refit_local<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+        k_refit_upper<<<std::min(nblk(2 * (int64_t)std::max(d.Itot, 1)), 1024), kThreads, 0, st>>>(d);
+    } else {
+        k_refit<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
+    }
 }
 void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
     if (!d.Ttot) return;
