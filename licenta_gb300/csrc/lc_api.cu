@@ -494,17 +494,18 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
     // 6. PBD Solver (+ 7. integration fused on the cluster path).  The
     // per-vertex contact CSR feeds the gather solvers; the scatter solver
     // walks the cloth's contact ranges instead.
-    // the recorded step of an adjoint batch runs on the global-memory solver,
-    // whose iterates the reverse pass replays
-    const bool on_chip = use_cluster && !recording;
+    // The recorded step of an adjoint batch writes its iterates to the tape
+    // and its decisions to the records the reverse pass replays, on either
+    // solver; the reverse pass walks the per-vertex contact lists.
+    const bool on_chip = use_cluster;
     const bool ordered = !(on_chip && cluster_scatter) || d.friction_any;  // float sums in entry order
-    if (ordered || (on_chip && cluster_scatter && ca.contact_gather)) {
+    if (ordered || recording || (on_chip && cluster_scatter && ca.contact_gather)) {
         LC_CUDA(cudaMemsetAsync(d.dyn_cnt, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         LC_CUDA(cudaMemsetAsync(d.dyn_cur, 0, sizeof(uint32_t) * (size_t)d.Vtot, st));
         launch_dyn(d, nvf, nee, narrow_grid, 0, st);
         scan_u32(d.dyn_cnt, d.dyn_off, nullptr, (uint32_t)d.Vtot, (uint32_t)d.Vtot, d.scan_tmp, nullptr, nullptr, st);
         launch_dyn(d, nvf, nee, narrow_grid, 1, st);
-        if (ordered) launch_dyn(d, nvf, nee, narrow_grid, 2, st);
+        if (ordered || recording) launch_dyn(d, nvf, nee, narrow_grid, 2, st);
     }
     if (on_chip) {
         LC_KEV(0);
@@ -542,12 +543,16 @@ lc_status lc_batch::enqueue_step(cudaStream_t st) {
 // Solver + integration on the cluster-resident path (one launch).
 static lc_status enqueue_cluster_solver(lc_batch *b, cudaStream_t st) {
     DevPtrs d = b->d;
-    if (b->opt.adjoint && !b->opt.debug_capture) {
-        // an adjoint batch keeps the decision records for its recorded step
-        // (global-memory solver); the on-chip steps need not write them
+    if (b->recording) {
+        // the recorded step of an adjoint batch: iterates to the tape
+        d.tape_x = b->tape_x;
+        d.tape_K = b->max_iters;
+    } else if (b->opt.adjoint && !b->opt.debug_capture) {
+        // the other steps of an adjoint batch keep no records
         d.dbg_ground_it = nullptr;
         d.dbg_dyn_nz = nullptr;
         d.dbg_sphere = nullptr;
+        d.coll_act = nullptr;
     }
     LC_CUDA(launch_solve_cluster(d, b->ca, b->cluster_cs, b->cluster_scatter, b->C, st));
     return LC_OK;

@@ -37,6 +37,19 @@ struct ClusterArgs {
     int contact_gather;      // scatter solver: contacts gathered per owned vertex (no remote atomics)
 };
 
+// A recorded step's iterations past a cloth's own count (the tape holds the
+// batch's largest): the iterate repeats and no collider slot is projected,
+// as the global-memory solver records them.
+__device__ __forceinline__ void record_tail(const DevPtrs &d, const ClothDev &cd, int g0, int n_own,
+                                            const float4 *xs, int tid, int bs) {
+    if (!d.tape_x) return;
+    for (int it = cd.iters; it < d.tape_K; ++it)
+        for (int i = tid; i < n_own; i += bs) {
+            d.tape_x[(size_t)(it + 1) * d.Vtot + g0 + i] = xs[i];
+            if (d.coll_act) d.coll_act[(size_t)(it + 1) * d.Vtot + g0 + i] = 0;
+        }
+}
+
 template <int CS>
 __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, ClusterArgs a) {
     cg::cluster_group cluster = cg::this_cluster();
@@ -146,6 +159,8 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
 
     const uint32_t nvf = (uint32_t)min((uint64_t)*a.nvf, d.vf_cap);
     const float h = cd.h;
+    if (d.tape_x)  // a recorded step: x^0 = the prediction after the set-up
+        for (int i = tid; i < n_own; i += bs) d.tape_x[vo + lo + i] = buf0[i];
     float4 *xa = buf0, *xb = buf1;
     for (int it = 0; it < cd.iters; ++it) {
         for (int i = tid; i < n_own; i += bs) {
@@ -231,14 +246,20 @@ __global__ void __launch_bounds__(kClusterBlock, 1) k_solve_cluster(DevPtrs d, C
             }
             // FinalCorrectionStep, Physics/CudaPBD.cu:1690-1698
             float3 xn = add(xi, dvs(acc, (float)cnt));
-            if (d.any_collider && xi4.w != 0.f) xn = collider_project(d, g, xn, h);
+            if (d.any_collider) {
+                uint8_t *act = d.coll_act ? d.coll_act + (size_t)(it + 1) * d.Vtot + g : nullptr;
+                if (xi4.w != 0.f) xn = collider_project(d, g, xn, h, act);
+                else if (act) *act = 0;
+            }
             xb[i] = f4(xn, xi4.w);
+            if (d.tape_x) d.tape_x[(size_t)(it + 1) * d.Vtot + g] = xb[i];
         }
         cluster.sync();
         float4 *t = xa;
         xa = xb;
         xb = t;
     }
+    record_tail(d, cd, vo + lo, n_own, xa, tid, bs);
 
     // ---- integration + world box (Physics/CudaPBD.cu:1916-1932,
     //      Physics/CudaDeformableUtils.cu:260-269) -----------------------------
@@ -396,6 +417,8 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
     const int s_per = (cd.s_cnt + CS - 1) / CS, b_per = (cd.b_cnt + CS - 1) / CS;
     const int sb = cd.s_off + min(cd.s_cnt, r * s_per), se = cd.s_off + min(cd.s_cnt, (r + 1) * s_per);
     const int bb = cd.b_off + min(cd.b_cnt, r * b_per), be = cd.b_off + min(cd.b_cnt, (r + 1) * b_per);
+    if (d.tape_x)  // a recorded step: x^0 = the prediction after the set-up
+        for (int i = tid; i < n_own; i += bs) d.tape_x[vo + lo + i] = xs[i];
     for (int it = 0; it < cd.iters; ++it) {
         for (int k = sb + tid; k < se; k += bs) {
             const int2 id = __ldg(&d.s_ids[k]);
@@ -501,12 +524,18 @@ __global__ void __launch_bounds__(kClusterBlock, 2) k_solve_cluster_scatter(DevP
             x4.x += (__int2float_rn(sx) * kFixInv) / n;
             x4.y += (__int2float_rn(sy) * kFixInv) / n;
             x4.z += (__int2float_rn(sz) * kFixInv) / n;
-            if (d.any_collider && x4.w != 0.f) x4 = f4(collider_project(d, g, xyz(x4), h), x4.w);
+            if (d.any_collider) {
+                uint8_t *act = d.coll_act ? d.coll_act + (size_t)(it + 1) * d.Vtot + g : nullptr;
+                if (x4.w != 0.f) x4 = f4(collider_project(d, g, xyz(x4), h, act), x4.w);
+                else if (act) *act = 0;
+            }
             xs[i] = x4;
+            if (d.tape_x) d.tape_x[(size_t)(it + 1) * d.Vtot + g] = x4;
             axc[i] = ayz[i] = 0ull;
         }
         cluster.sync();
     }
+    record_tail(d, cd, vo + lo, n_own, xs, tid, bs);
     for (int i = tid; i < n_own; i += bs) {
         const int g = vo + lo + i;
         const float4 x4 = xs[i];

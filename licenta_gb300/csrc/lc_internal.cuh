@@ -185,6 +185,8 @@ struct DevPtrs {
     uint8_t *coll_act;        // adjoint batches: (iterations + 1) x vertex bit masks of the collider slots
                               // projected, [0] before the solver, [it + 1] in iteration it (else null)
     int any_collider;
+    float4 *tape_x;           // a recorded step on the cluster solver: (tape_K + 1) x Vtot iterates (else null)
+    int tape_K;
 };
 
 // Reverse pass of one step (lc_adjoint.cu): the recorded step's tape and the
