@@ -799,6 +799,7 @@ static lc_status batch_build(lc_batch *b, const lc_cloth_desc *descs, int n, con
     LC_TRY(A.alloc(vbf, vb_first.size(), "vb_first"));
     d.vblk_cloth = vbc; d.vblk_start = vbs; d.vb_first = vbf;
     LC_TRY(A.alloc(d.damp_part, 16 * vblk_cloth.size(), "damp_part"));
+    LC_TRY(A.alloc(d.vbox, 2 * std::max<int64_t>(V, 1), "vertex swept boxes"));
     LC_TRY(A.alloc(b->npairs, 1, "npairs")); LC_TRY(A.alloc(b->nvf, 1, "nvf")); LC_TRY(A.alloc(b->nee, 1, "nee"));
     LC_TRY(A.alloc(b->ncand, 1, "ncand")); LC_TRY(A.alloc(b->ncand_e, 1, "ncand_e"));
     if (opt.debug_capture) {

@@ -186,6 +186,8 @@ struct DevPtrs {
                               // projected, [0] before the solver, [it + 1] in iteration it (else null)
     int any_collider;
     float4 *tape_x;           // a recorded step on the cluster solver: (tape_K + 1) x Vtot iterates (else null)
+    float4 *vbox;             // per vertex, written by the prediction: the swept box of x_prev and x widened by
+                              // the thickness, lo at [2 v], hi at [2 v + 1] (may be null: computed in place)
     int tape_K;
 };
 

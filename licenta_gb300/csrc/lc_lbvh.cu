@@ -960,6 +960,7 @@ __device__ __forceinline__ bool ee_far(float3 a, float3 b, float3 c, float3 d, f
 // x and x_prev (min/max are exact, so this equals the stored boxes).
 struct Box { float3 lo, hi; };
 __device__ __forceinline__ Box pbox(const DevPtrs &d, int v, float h) {
+    if (d.vbox) return Box{xyz(d.vbox[2 * (size_t)v]), xyz(d.vbox[2 * (size_t)v + 1])};  // the same operations, once per vertex
     const float3 p = xyz(d.x[v]), q = xyz(d.xp[v]);
     return Box{subc(vmin(p, q), h), addc(vmax(p, q), h)};
 }

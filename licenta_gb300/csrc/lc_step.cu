@@ -170,8 +170,13 @@ __global__ void k_damp_apply(DevPtrs d) {
     // the predicted positions the collision stages see are reproducible.
     const float4 p = d.xp[i];
     const float dt = cd.dt;
-    d.x[i] = make_float4(__fadd_rn(p.x, __fmul_rn(vel.x, dt)), __fadd_rn(p.y, __fmul_rn(vel.y, dt)),
-                         __fadd_rn(p.z, __fmul_rn(vel.z, dt)), x4.w);
+    const float4 xn = make_float4(__fadd_rn(p.x, __fmul_rn(vel.x, dt)), __fadd_rn(p.y, __fmul_rn(vel.y, dt)),
+                                  __fadd_rn(p.z, __fmul_rn(vel.z, dt)), x4.w);
+    d.x[i] = xn;
+    if (d.vbox) {  // the narrowphase's vertex boxes, once per vertex instead of once per pair
+        d.vbox[2 * (size_t)i] = f4(subc(vmin(xyz(xn), xyz(p)), cd.h), 0.f);
+        d.vbox[2 * (size_t)i + 1] = f4(addc(vmax(xyz(xn), xyz(p)), cd.h), 0.f);
+    }
 }
 
 // UpdateVertexNormals (Physics/CudaDeformableUtils.cu:190-249) as a gather
