@@ -26,6 +26,7 @@ the CUDA library.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -64,6 +65,8 @@ def parse():
     ap.add_argument("--only-lbvh", action="store_true",
                     help="run only the LBVH microbenchmark and print its line (for profiling it alone)")
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-next", action="store_true",
+                    help="skip the broadphase family, narrowphase entry and impulse response timings")
     ap.add_argument("--rollout-1m", action="store_true",
                     help="also run the million-vertex 300-step checkpointed rollout and report its device memory")
     ap.add_argument("--no-autotune", action="store_true")
@@ -516,6 +519,148 @@ def lbvh_timing(seed: int, count: int = 1_000_000) -> dict:
             "l2": "flushed by a 256 MB write before each timed build"}
 
 
+def _cuda_ms(fn, reps: int = 10, warmup: int = 3) -> float:
+    """Median CUDA-event time of fn() on the current stream."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def next_rows_timing(seed: int, cpu: bool = True) -> dict:
+    """The rows beside the step, each on one GPU, CUDA events on the
+    launching stream (median of 10 after 3 warm-up calls):
+    - the ICollisionMethod family (lc_broadphase_*): 200,000 random boxes
+      (lower corner uniform in the unit cube, sides U[1, 10] mm) resident on
+      the device; one call = update (structure build) + test (pair count and
+      pairs); the methods' pair sets must agree;
+    - the alternative collision pipeline on the 512x512 cloth (262,144
+      vertices, 522,242 triangles) 10 steps into its drop onto the analytic
+      sphere: its swept triangle boxes (the engine's thickness for this mesh,
+      the first edge's length / 3; the world box mapped onto the unit cube) through lc_lbvh_build and lc_lbvh_pairs, then
+      lc_narrowphase_run (CCD and DCD) on those pairs
+      and lc_solve_collisions (the impulse response) on the CCD contacts.
+    cpu: the oracle's restatements on the same inputs, one host thread (the
+    narrowphase on the first 200,000 pairs), as a reported baseline."""
+    import torch
+    from licenta_gb300 import ClothBatch, Lbvh, Narrowphase, _ffi, scenes
+    from licenta_gb300.broadphase import Broadphase
+    out = {}
+    rng = np.random.default_rng(seed + 11)
+    N = 200_000
+    lo = rng.random((N, 3)).astype(np.float32)
+    hi = lo + rng.uniform(1e-3, 1e-2, (N, 3)).astype(np.float32)
+    lo_t, hi_t = torch.from_numpy(lo).cuda(), torch.from_numpy(hi).cuda()
+    kw = {"sap": {}, "bvh": {},
+          "grid": dict(world_min=(0.0, 0.0, 0.0), world_max=(1.02, 1.02, 1.02), cells_per_axis=128, max_entries=8 * N),
+          "hash": dict(cell_size=0.01, table_size=1 << 20, max_entries=8 * N)}
+    bp_out, counts = {}, set()
+    for name, k in kw.items():
+        b = Broadphase(name, N, **k)
+        pairs = [None]
+        def call():
+            b.update(lo_t, hi_t)
+            pairs[0] = b.test()
+        ms = _cuda_ms(call)
+        counts.add(int(pairs[0].shape[0]))
+        bp_out[name] = {"ms_per_update_and_test": ms, "pairs": int(pairs[0].shape[0]),
+                        "objects_per_s": N / (ms / 1000.0)}
+        b.close()
+    out["broadphase"] = {"workload": f"{N} random boxes (sides 1..10 mm) in the unit cube", "methods": bp_out,
+                         "pair_sets_agree": len(counts) == 1}
+    # the alternative pipeline on the large cloth's own pairs
+    spec = scenes.large_cloth(seed=seed)
+    cb = ClothBatch([spec])
+    cb.step(10)
+    cb.sync()
+    st = cb.get_state(0)
+    cb.close()
+    # the engine's thickness for this mesh: the first edge's length / 3
+    h = float(np.linalg.norm(spec.positions[1].astype(np.float64) - spec.positions[0]) / 3.0)
+    dt = float(spec.params.timestep)
+    tri = spec.indices.astype(np.int64).reshape(-1, 3)
+    T = tri.shape[0]
+    P3 = np.stack([st["x"][tri], st["x_prev"][tri]], 1).reshape(T, 6, 3)
+    # the world box [-1, 1]^3 mapped onto the unit cube the Morton codes cover
+    tlo = ((P3.min(1) - h + 1.0) * 0.5).astype(np.float32)
+    thi = ((P3.max(1) + h + 1.0) * 0.5).astype(np.float32)
+    lb = Lbvh(T, chunk_size=64)
+    tlo_t, thi_t = torch.from_numpy(tlo).cuda(), torch.from_numpy(thi).cuda()
+    lb.build(tlo_t.data_ptr(), thi_t.data_ptr(), T)
+    npairs = lb.pairs(None, 0)
+    pairs_t = torch.empty((max(npairs, 1), 2), dtype=torch.int32, device="cuda")
+    lb.pairs(pairs_t.data_ptr(), npairs)
+    ids = torch.empty(T, dtype=torch.int32, device="cuda")
+    lb.sorted_ids(ids.data_ptr())
+    torch.cuda.synchronize()
+    lb.close()
+    tris_t = torch.from_numpy(tri.astype(np.int32)).cuda()[ids.long()].contiguous()
+    x_t, xp_t, v_t = (torch.from_numpy(st[q]).cuda() for q in ("x", "x_prev", "v"))
+    cap = 15 * max(npairs, 1)
+    vf = torch.zeros((min(cap, 1 << 24), 12), dtype=torch.int32, device="cuda")
+    ee = torch.zeros((min(cap, 1 << 24), 12), dtype=torch.int32, device="cuda")
+    nph = Narrowphase(spec.num_vertices, T, max(npairs, 1), candidate_capacity=9 * max(npairs, 1),
+                      contact_capacity=len(vf))
+    res = {}
+    for mode, name in ((_ffi.LC_NARROW_CCD, "ccd"), (_ffi.LC_NARROW_DCD, "dcd")):
+        got = [0, 0, 0]
+        ccd = mode == _ffi.LC_NARROW_CCD
+        def call():
+            got[:] = nph.run(x_t.data_ptr() if ccd else None, xp_t.data_ptr(), v_t.data_ptr() if ccd else None,
+                             spec.num_vertices, tris_t.data_ptr(), None, T, pairs_t.data_ptr(), npairs, h, dt,
+                             vf.data_ptr(), len(vf), ee.data_ptr(), len(ee), mode=mode)
+        ms = _cuda_ms(call)
+        res[name] = {"ms": ms, "pairs_per_s": npairs / (ms / 1000.0), "vf": got[1], "ee": got[2], "status": got[0]}
+    # the CCD contacts for the impulse response
+    rc, nvf, nee = nph.run(x_t.data_ptr(), xp_t.data_ptr(), v_t.data_ptr(), spec.num_vertices, tris_t.data_ptr(),
+                           None, T, pairs_t.data_ptr(), npairs, h, dt, vf.data_ptr(), len(vf), ee.data_ptr(), len(ee))
+    nph.close()
+    p = spec.params
+    vmass = float(np.float32(p.objectMass) / np.float32(int(p.dims[0]) * int(p.dims[1])))
+    fixed = torch.zeros(spec.num_vertices, dtype=torch.uint8, device="cuda")
+    xw = x_t.clone()
+    vw = v_t.clone()
+    vp = lambda t: C.c_void_p(t.data_ptr())
+    def resp():
+        xw.copy_(x_t)
+        vw.copy_(v_t)
+        _ffi.check(_ffi.lib().lc_solve_collisions(vp(xw), vp(xp_t), vp(vw), vp(fixed), spec.num_vertices, vp(vf),
+                                                  nvf, vp(ee), nee, float(p.kStretch), vmass, dt, h, None),
+                   "lc_solve_collisions")
+    ms_r = _cuda_ms(resp)
+    out["collision_pipeline"] = {
+        "workload": f"512x512 cloth, step 10 of its drop onto the analytic sphere: {npairs} LBVH pairs of its "
+                    f"swept triangle boxes (thickness {h:.3g} m)",
+        "narrowphase": res,
+        "impulse_response": {"ms": ms_r, "contacts": nvf + nee, "note": "includes re-copying x and v (6 MB)"}}
+    if cpu:
+        from oracle import oracle_ffi
+        from oracle.broadphase import box_pairs
+        nb = 20_000
+        t0 = time.perf_counter()
+        box_pairs(lo[:nb], hi[:nb])
+        out["broadphase"]["cpu_baseline"] = {"objects_per_s": nb / (time.perf_counter() - t0), "cores": 1,
+                                             "kind": "port", "sample": f"brute force over the first {nb} boxes"}
+        k = min(npairs, 200_000)
+        pr = pairs_t[:k].cpu().numpy()
+        tr = tris_t.cpu().numpy()
+        t0 = time.perf_counter()
+        oracle_ffi.narrow_contacts(0, st["x"], st["x_prev"], st["v"], tr, np.full(T, 0x3F, np.uint8), pr, h, dt)
+        out["collision_pipeline"]["cpu_baseline"] = {
+            "narrowphase_ccd_pairs_per_s": k / (time.perf_counter() - t0), "cores": 1, "kind": "port",
+            "sample": f"the first {k} pairs, the oracle's narrowphase restatement"}
+    return out
+
+
 def cpu_baseline(batch, gspecs, members, state0, stream, warmup: int, steps: int = 4) -> dict:
     """The oracle port (FP32 mirror of the reference GPU scheme), OpenMP over
     cloths on every host core, on a bounded sample of the timed window: every
@@ -758,6 +903,9 @@ def run_ours(args, world, rank, local):
     roll_1m = None
     if rank == 0 and args.rollout_1m:
         roll_1m = rollout_1m_memory(args.seed)
+    next_rows = None
+    if rank == 0 and not args.no_next:
+        next_rows = next_rows_timing(args.seed, cpu=world == 1 and not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -794,6 +942,7 @@ def run_ours(args, world, rank, local):
         "large_cloth_analytic_sphere": large_analytic,
         "adjoint_batched": adj_batched,
         "rollout_1m": roll_1m,
+        "next_rows": next_rows,
         "tuning": tuning,
     }
     if rank == 0:
