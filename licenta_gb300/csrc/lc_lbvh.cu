@@ -794,36 +794,52 @@ __global__ void __launch_bounds__(kTraverseBlockMax, 6) k_traverse_packet(DevPtr
 
 
 // Order-preserving compaction of the per-leaf chunks into the pair list:
-// each warp takes 32 consecutive leaves and copies them one leaf at a time
-// with all 32 lanes, so reads and writes are coalesced.
+// each warp takes 32 consecutive leaves, whose outputs are one contiguous
+// range, and spreads that range over its lanes (output j belongs to the
+// last leaf whose prefix count is <= j), so the loads are independent and
+// both reads and writes are coalesced runs.
 __global__ void k_pair_compact(DevPtrs d) {
     const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int base = warp0 * 32; base < d.Ttot; base += nwarps * 32) {
         const int s = base + lane;
-        uint32_t n = 0, o = 0;
+        uint32_t n = 0;
         int t0 = 0;
         const uint32_t *src = nullptr;
         if (s < d.Ttot) {
             n = d.pair_cnt[s];
             if (n) {
                 const ClothDev &cd = d.cloth[d.tcloth[s]];
-                o = d.pair_off[s];
                 t0 = cd.t_off;
                 src = d.pair_chunk + cd.pc_off + (int64_t)(s - cd.t_off) * cd.chunk;
             }
         }
-        unsigned live = __ballot_sync(0xffffffffu, n != 0);
-        while (live) {
-            const int j = __ffs(live) - 1;
-            live &= live - 1;
-            const uint32_t nj = __shfl_sync(0xffffffffu, n, j), oj = __shfl_sync(0xffffffffu, o, j);
-            const int tj = __shfl_sync(0xffffffffu, t0, j);
-            const uint32_t *sj = reinterpret_cast<const uint32_t *>(
-                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), j));
-            for (uint32_t k = lane; k < nj; k += 32)
-                d.pairs[oj + k] = make_uint2((uint32_t)(base + j), (uint32_t)tj + sj[k]);
+        uint32_t ex = n;  // inclusive scan over the warp's leaves
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(full, ex, o);
+            if (lane >= o) ex += t;
+        }
+        const uint32_t total = __shfl_sync(full, ex, 31);
+        ex -= n;
+        if (total == 0) continue;
+        const uint32_t o0 = d.pair_off[base];
+        for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            int L = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int cand = L + step;
+                const uint32_t e = __shfl_sync(full, ex, cand & 31);
+                if (cand < 32 && e <= j) L = cand;
+            }
+            const uint32_t exL = __shfl_sync(full, ex, L);
+            const int tL = __shfl_sync(full, t0, L);
+            const uint32_t *sL = reinterpret_cast<const uint32_t *>(
+                __shfl_sync(full, reinterpret_cast<unsigned long long>(src), L));
+            if (j < total) d.pairs[o0 + j] = make_uint2((uint32_t)(base + L), (uint32_t)tL + sL[j - exL]);
         }
     }
 }
