@@ -35,7 +35,8 @@ typedef enum lc_status {
     LC_ERR_INVALID_ARG = 1,
     LC_ERR_OOM = 2,
     LC_ERR_CAPACITY_OVERFLOW = 3,
-    LC_ERR_TIMEOUT = 4,
+    LC_ERR_TIMEOUT = 4,            /* a bounded device-side wait gave up (a sort or look-back status
+                                      that never arrived); reported by the next synchronising call */
     LC_ERR_CUDA = 5,
     LC_ERR_NOT_SUPPORTED = 6,
     LC_ERR_STACK_OVERFLOW = 7
