@@ -1190,7 +1190,7 @@ struct CcdJob { float a, b, fa, fb; };
 // words spill to L1): measured 0.83 -> 0.80 ms per step for VF, EE unchanged.
 template <bool VF>
 __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const uint32_t *__restrict__ ncand) {
-    __shared__ float geom[kCcdWarps][18][33];     // x21 x31 x41 v21 v31 v41 per lane (padded)
+    __shared__ float geom[kCcdWarps][24][33];     // x1..x4 then v1..v4 (test order) per lane (padded)
     __shared__ CcdJob jobs[kCcdWarps][96];
     __shared__ uint8_t job_owner[kCcdWarps][96];  // lane << 2 | interval
     __shared__ float roots[kCcdWarps][3][32];
@@ -1221,10 +1221,10 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
             const float3 v1 = xyz(d.v[i1]), v2 = xyz(d.v[i2]), v3 = xyz(d.v[i3]), v4 = xyz(d.v[i4]);
             const float3 x21 = sub(x2, x1), x31 = sub(x3, x1), x41 = sub(x4, x1);
             const float3 v21 = sub(v2, v1), v31 = sub(v3, v1), v41 = sub(v4, v1);
-            const float g[18] = {x21.x, x21.y, x21.z, x31.x, x31.y, x31.z, x41.x, x41.y, x41.z,
-                                 v21.x, v21.y, v21.z, v31.x, v31.y, v31.z, v41.x, v41.y, v41.z};
+            const float g[24] = {x1.x, x1.y, x1.z, x2.x, x2.y, x2.z, x3.x, x3.y, x3.z, x4.x, x4.y, x4.z,
+                                 v1.x, v1.y, v1.z, v2.x, v2.y, v2.z, v3.x, v3.y, v3.z, v4.x, v4.y, v4.z};
 #pragma unroll
-            for (int k = 0; k < 18; ++k) geom[w][k][lane] = g[k];
+            for (int k = 0; k < 24; ++k) geom[w][k][lane] = g[k];
             const float3 v21v31 = cross(v21, v31), x21v31 = cross(x21, v31), v21x31 = cross(v21, x31),
                          x21x31 = cross(x21, x31);
             const float v1v2v3 = dot(v21v31, v41), x1v2v3 = dot(x21v31, v41), v1x2v3 = dot(v21x31, v41),
@@ -1274,12 +1274,15 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
         for (int j = lane; j < njobs; j += 32) {
             const CcdJob jb = jobs[w][j];
             const int own = job_owner[w][j] >> 2, iv = job_owner[w][j] & 3;
-            const float3 x21 = f3(geom[w][0][own], geom[w][1][own], geom[w][2][own]);
-            const float3 x31 = f3(geom[w][3][own], geom[w][4][own], geom[w][5][own]);
-            const float3 x41 = f3(geom[w][6][own], geom[w][7][own], geom[w][8][own]);
-            const float3 v21 = f3(geom[w][9][own], geom[w][10][own], geom[w][11][own]);
-            const float3 v31 = f3(geom[w][12][own], geom[w][13][own], geom[w][14][own]);
-            const float3 v41 = f3(geom[w][15][own], geom[w][16][own], geom[w][17][own]);
+            // the set-up's differences, from the same operands
+            const float3 p1 = f3(geom[w][0][own], geom[w][1][own], geom[w][2][own]);
+            const float3 u1 = f3(geom[w][12][own], geom[w][13][own], geom[w][14][own]);
+            const float3 x21 = sub(f3(geom[w][3][own], geom[w][4][own], geom[w][5][own]), p1);
+            const float3 x31 = sub(f3(geom[w][6][own], geom[w][7][own], geom[w][8][own]), p1);
+            const float3 x41 = sub(f3(geom[w][9][own], geom[w][10][own], geom[w][11][own]), p1);
+            const float3 v21 = sub(f3(geom[w][15][own], geom[w][16][own], geom[w][17][own]), u1);
+            const float3 v31 = sub(f3(geom[w][18][own], geom[w][19][own], geom[w][20][own]), u1);
+            const float3 v41 = sub(f3(geom[w][21][own], geom[w][22][own], geom[w][23][own]), u1);
             roots[w][iv][own] = secant(x21, x31, x41, v21, v31, v41, jb.a, jb.b, jb.fa, jb.fb);
         }
         __syncwarp();
@@ -1316,17 +1319,20 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
         const uint32_t ntests = __shfl_sync(full, ex, 31);
         ex -= (uint32_t)nt;
         __syncwarp();
-        // the four vertices of a candidate in test order (VF: face x1 x2 x3, vertex x4)
-        auto corners = [&](const int4 c, float3 &x1, float3 &x2, float3 &x3, float3 &x4, float3 &v1, float3 &v2,
+        // the four vertices of lane L's candidate in test order (VF: face x1 x2 x3,
+        // vertex x4), as its set-up loaded them
+        auto corners = [&](int L, float3 &x1, float3 &x2, float3 &x3, float3 &x4, float3 &v1, float3 &v2,
                            float3 &v3, float3 &v4) {
-            const int i1 = VF ? c.y : c.x, i2 = VF ? c.z : c.y, i3 = VF ? c.w : c.z, i4 = VF ? c.x : c.w;
-            x1 = xyz(d.xp[i1]); x2 = xyz(d.xp[i2]); x3 = xyz(d.xp[i3]); x4 = xyz(d.xp[i4]);
-            v1 = xyz(d.v[i1]); v2 = xyz(d.v[i2]); v3 = xyz(d.v[i3]); v4 = xyz(d.v[i4]);
+            const float(*gm)[33] = geom[w];
+            x1 = f3(gm[0][L], gm[1][L], gm[2][L]); x2 = f3(gm[3][L], gm[4][L], gm[5][L]);
+            x3 = f3(gm[6][L], gm[7][L], gm[8][L]); x4 = f3(gm[9][L], gm[10][L], gm[11][L]);
+            v1 = f3(gm[12][L], gm[13][L], gm[14][L]); v2 = f3(gm[15][L], gm[16][L], gm[17][L]);
+            v3 = f3(gm[18][L], gm[19][L], gm[20][L]); v4 = f3(gm[21][L], gm[22][L], gm[23][L]);
         };
         // test m of lane L's candidate: the advances by its times 0..m, then the test
-        auto run_test = [&](const int4 c, int L, int m, float h, float dt, Wts &wt) {
+        auto run_test = [&](int L, int m, float h, float dt, Wts &wt) {
             float3 x1, x2, x3, x4, v1, v2, v3, v4;
-            corners(c, x1, x2, x3, x4, v1, v2, v3, v4);
+            corners(L, x1, x2, x3, x4, v1, v2, v3, v4);
             float tt = 0.f;
             for (int k = 0; k <= m; ++k) {
                 tt = tq[w][k][L] * dt;
@@ -1350,19 +1356,17 @@ __global__ void __launch_bounds__(kCcdWarps * 32, 4) k_ccd_warp(DevPtrs d, const
                 if (cand < 32 && e <= j) L = cand;
             }
             const uint32_t exL = __shfl_sync(full, ex, L);
-            const int4 c = make_int4(__shfl_sync(full, ids.x, L), __shfl_sync(full, ids.y, L),
-                                     __shfl_sync(full, ids.z, L), __shfl_sync(full, ids.w, L));
             const float h = __shfl_sync(full, hq, L), dt = __shfl_sync(full, dtq, L);
             if (j < ntests) {
                 const int m = (int)(j - exL);
                 Wts wt;
-                if (run_test(c, L, m, h, dt, wt)) atomicMin(&best[w][L], m);
+                if (run_test(L, m, h, dt, wt)) atomicMin(&best[w][L], m);
             }
         }
         __syncwarp();
         bool found = false;
         Wts wt;
-        if (valid && best[w][lane] < 6) found = run_test(ids, lane, best[w][lane], hq, dtq, wt);
+        if (valid && best[w][lane] < 6) found = run_test(lane, best[w][lane], hq, dtq, wt);
         if (valid) {
             if (found) {
                 // the contact's weights, placed at its final index by k_ccd_emit
