@@ -543,6 +543,9 @@ def next_rows_timing(seed: int, cpu: bool = True) -> dict:
       (lower corner uniform in the unit cube, sides U[1, 10] mm) resident on
       the device; one call = update (structure build) + test (pair count and
       pairs); the methods' pair sets must agree;
+    - friction and triangle bending (batched step time with the option on,
+      against off) and the render-format vertex record write, on the first
+      32 cloths of the batched workload;
     - the alternative collision pipeline on the 512x512 cloth (262,144
       vertices, 522,242 triangles) 10 steps into its drop onto the analytic
       sphere: its swept triangle boxes (the engine's thickness for this mesh,
@@ -642,6 +645,33 @@ def next_rows_timing(seed: int, cpu: bool = True) -> dict:
                     f"swept triangle boxes (thickness {h:.3g} m)",
         "narrowphase": res,
         "impulse_response": {"ms": ms_r, "contacts": nvf + nee, "note": "includes re-copying x and v (6 MB)"}}
+    # the solver options and the render-format write on the first 32 cloths of
+    # the batched workload, steps 6-15 (5 warm-up)
+    import dataclasses
+    base_specs = scenes.batched_cloths(seed=seed)[:32]
+    opts = {}
+    for name, fld in (("base", None), ("friction", "useFriction"), ("triangle_bending", "useTriangleBending")):
+        sp = [dataclasses.replace(x, params=type(x.params).from_buffer_copy(x.params)) for x in base_specs]
+        if fld:
+            for x in sp:
+                setattr(x.params, fld, 1)
+        bb = ClothBatch(sp)
+        bb.step(5)
+        bb.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bb.step(10)
+        e1.record()
+        torch.cuda.synchronize()
+        opts[name] = {"ms_per_step": e0.elapsed_time(e1) / 10}
+        if name == "base":
+            Vb = sum(x.num_vertices for x in sp)
+            rec = torch.zeros((Vb, 12), dtype=torch.float32, device="cuda")
+            ms_rec = _cuda_ms(lambda: bb.write_vertex_records(rec.data_ptr()))
+            opts["vertex_records"] = {"ms": ms_rec, "vertices": Vb, "bytes_written": 48 * Vb,
+                                      "gb_per_s": 48 * Vb / (ms_rec / 1000.0) / 1e9}
+        bb.close()
+    out["solver_options"] = {"workload": "the first 32 cloths of the batched workload, steps 6-15", **opts}
     if cpu:
         from oracle import oracle_ffi
         from oracle.broadphase import box_pairs
