@@ -718,10 +718,11 @@ __global__ void k_traverse(DevPtrs d) {
 // waits on dependent node fetches, and 12 resident 4-warp blocks hide more of
 // that latency than the 10 that 41 registers allowed.
 __global__ void __launch_bounds__(kTraverseBlockMax, 6) k_traverse_packet(DevPtrs d) {
-    extern __shared__ int wstack_all[];  // kTraverseStack slots per warp of the block (sized at launch)
+    static_assert(kTraverseStack == 64, "two stack slots per lane");
     const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int *wstack = wstack_all + w * kTraverseStack;
+    const int lane = threadIdx.x & 31;
+    // the warp's stack in registers: slot k in lane k % 32, register k / 32
+    int stk0 = 0, stk1 = 0;
     const int s = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 + lane;
     const bool valid = s < d.Ttot;
     int c = -1, me = 0, got = 0, chunk = 0;
@@ -753,8 +754,7 @@ __global__ void __launch_bounds__(kTraverseBlockMax, 6) k_traverse_packet(DevPtr
         const int In = cd.T - 1;
         const float4 *W = d.wnode + 4 * (size_t)cd.i_off;
         int top = 1, node = 0;
-        if (lane == 0) wstack[0] = -1;
-        __syncwarp();
+        if (lane == 0) stk0 = -1;
         const int guard_max = 4 * cd.T + 64;
         for (int guard = 0; guard < guard_max; ++guard) {
             const float4 *r = W + 4 * (size_t)node;
@@ -773,16 +773,20 @@ __global__ void __launch_bounds__(kTraverseBlockMax, 6) k_traverse_packet(DevPtr
             }
             const bool tl = chx < In && __any_sync(full, ol), tr = chy < In && __any_sync(full, orr);
             if (!tl && !tr) {
-                node = wstack[--top];
+                --top;
+                const int a = __shfl_sync(full, stk0, top & 31), b = __shfl_sync(full, stk1, top & 31);
+                node = top < 32 ? a : b;
             } else {
                 node = tl ? chx : chy;
                 if (tl && tr) {
                     if (top >= kTraverseStack) { overflow = true; break; }
-                    if (lane == 0) wstack[top] = chy;
+                    if (lane == (top & 31)) {
+                        if (top < 32) stk0 = chy;
+                        else stk1 = chy;
+                    }
                     ++top;
                 }
             }
-            __syncwarp();
             if (top == 0) break;
         }
         __syncwarp();
@@ -1675,7 +1679,7 @@ void launch_traverse(const DevPtrs &d, int block, cudaStream_t st) {
     if (!d.Ttot) return;
     if (d.wnode) {
         k_pack_nodes<<<nblk(d.Ttot), kThreads, 0, st>>>(d);
-        k_traverse_packet<<<nblk(d.Ttot, block), block, (size_t)(block / 32) * kTraverseStack * sizeof(int), st>>>(d);
+        k_traverse_packet<<<nblk(d.Ttot, block), block, 0, st>>>(d);
     } else {
         k_traverse<<<nblk(d.Ttot, block), block, 0, st>>>(d);
     }
