@@ -51,6 +51,23 @@ def test_scattered_boxes(method, parity_report):
     assert np.array_equal(got, want)
 
 
+def test_methods_agree_at_scale(parity_report):
+    """200,000 boxes (sorts of about a hundred tiles and more, the one-sweep
+    look-back across many of them): the four sublinear methods return the
+    same pair set, and the pairs of its first 20,000 boxes are the oracle's
+    brute-force pairs of those boxes."""
+    lo, hi = scattered(200_000, seed=11, size=(0.001, 0.01))
+    kw = dict(cells_per_axis=128, cell_size=0.01, table_size=1 << 20, max_entries=8 * len(lo))
+    got = {m: run(m, lo, hi, **kw)[0] for m in ("sap", "grid", "hash", "bvh")}
+    ref = got["bvh"]
+    for m, g in got.items():
+        assert np.array_equal(g, ref), m
+    k = 20_000
+    sub = ref[(ref[:, 0] < k) & (ref[:, 1] < k)]
+    assert np.array_equal(sub, box_pairs(lo[:k], hi[:k]))
+    parity_report(objects=len(lo), pairs=len(ref), checked_subset=k, subset_pairs=len(sub))
+
+
 @pytest.mark.parametrize("method", METHODS)
 def test_coincident_and_large_boxes(method):
     lo, hi = scattered(1500, seed=2)

@@ -115,6 +115,33 @@ def test_lbvh_one_million_triangles_bit_exact(cuda, parity_report, mode):
         h.close()
 
 
+def test_lbvh_awkward_sizes_bit_exact(cuda):
+    """One handle built at awkward sizes in turn, largest first (the tile
+    table is rebuilt when the count changes): a single key, one tile exactly,
+    one key past a tile, a last tile of one key, counts that are not a
+    multiple of the refit's 256-leaf blocks.  Codes, order, hierarchy, boxes
+    and pairs must equal the oracle's for each (one-sweep sort over 1 to 49
+    tiles, two-pass refit)."""
+    torch = cuda
+    sizes = [100_001, 32_769, 4_097, 2_049, 2_048, 2_047, 257, 2]
+    h = Lbvh(max(sizes), chunk_size=64)
+    try:
+        for count in sizes:
+            lo, hi = scenes.random_triangle_boxes(count, seed=count)
+            lo_t, hi_t = torch.from_numpy(lo).cuda(), torch.from_numpy(hi).cuda()
+            h.build(lo_t.data_ptr(), hi_t.data_ptr(), count)
+            n = h.pairs(None, 0)
+            want = lbvh_boxes(lo, hi, chunk=64, mode=_ffi.LC_MORTON_REF63)
+            for what in ("MORTON", "PERM", "LEFTS", "RIGHTS", "PARENTS", "RML", "NODE_AABB", "PAIRS"):
+                got, exp = h.debug(what), want[what]
+                if what == "NODE_AABB":
+                    got, exp = got.view(np.uint32), exp.view(np.uint32)
+                assert got.shape == exp.shape and np.array_equal(got, exp), (count, what)
+            assert n == len(want["PAIRS"]), count
+    finally:
+        h.close()
+
+
 def test_free_rollout_drift_report(parity_report):
     """The untethered drift of the plain small cloth: the engine (FP32) and
     the FP64 oracle each run the 120-step rollout on their own, with no
