@@ -54,8 +54,8 @@ def oracle_grads(spec, steps, ks, kb, v0, target):
     return dict(loss=float(((xp - target) ** 2).sum()), ks=gks, kb=gkb, x0=gx + gxp, v0=gv, final=xp)
 
 
-def case(seed, n, steps, v_scale):
-    spec = scenes.small_cloth(seed=seed, n=n)
+def case(seed, n, steps, v_scale, iterations=10):
+    spec = scenes.small_cloth(seed=seed, n=n, iterations=iterations)
     o = Oracle([spec], fp64=True)
     _, _, ne, nb = o.sizes(0)
     o.close()
@@ -74,6 +74,40 @@ def test_engine_adjoint_matches_fp64_adjoint():
     assert np.abs(g["final"] - r["final"]).max() < 1e-5
     for k in ("ks", "kb", "v0", "x0"):
         assert rel_l2(g[k], r[k]) < 2e-3, f"{k}: relative error {rel_l2(g[k], r[k]):.2e}"
+
+
+def test_batch_of_unequal_iteration_counts_matches_fp64():
+    """Two cloths in one differentiable batch, with 10 and 6 solver
+    iterations: the recorded step runs on the batch's solver and, for the
+    shorter cloth, repeats its last iterate in the tape for the iterations it
+    does not run.  Each cloth's gradients must match the FP64 adjoint of that
+    cloth alone (the cloths are independent)."""
+    a = case(1, 12, 10, 0.3)
+    b = case(5, 10, 10, 0.3, iterations=6)
+    specs = [a[0], b[0]]
+    cloth = DiffCloth(specs, checkpoint_every=4)
+    cat = lambda i: np.concatenate([a[i], b[i]]).astype(np.float32)
+    ks_t = torch.tensor(cat(1), device="cuda", requires_grad=True)
+    kb_t = torch.tensor(cat(2), device="cuda", requires_grad=True)
+    x0 = torch.tensor(np.concatenate([x.positions for x in specs]), device="cuda", requires_grad=True)
+    v0_t = torch.tensor(cat(3), device="cuda", requires_grad=True)
+    out = ClothRollout.apply(cloth, 10, ks_t, kb_t, x0, v0_t)
+    loss = ((out - torch.tensor(cat(4), device="cuda")) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    got = dict(ks=ks_t.grad.cpu().numpy(), kb=kb_t.grad.cpu().numpy(), x0=x0.grad.cpu().numpy(),
+               v0=v0_t.grad.cpu().numpy(), final=out.detach().cpu().numpy())
+    cloth.close()
+    off = dict(ks=0, kb=0, x0=0, v0=0, final=0)
+    for spec, (sp, ks, kb, v0, target) in zip(specs, (a, b)):
+        r = oracle_grads(sp, 10, ks, kb, v0, target)
+        size = dict(ks=len(ks), kb=len(kb), x0=sp.num_vertices, v0=sp.num_vertices, final=sp.num_vertices)
+        part = {k: got[k][off[k]:off[k] + size[k]] for k in size}
+        assert np.abs(part["final"] - r["final"]).max() < 1e-5
+        for k in ("ks", "kb", "v0", "x0"):
+            assert rel_l2(part[k], r[k]) < 2e-3, f"{sp.params.solverIterations} iterations, {k}"
+        for k in size:
+            off[k] += size[k]
 
 
 def test_checkpointing_does_not_change_gradients():
