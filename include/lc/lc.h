@@ -121,7 +121,8 @@ typedef struct lc_batch_options {
     uint64_t cand_capacity;   /* narrowphase candidates kept per step after the AABB cull, per kind (VF, EE);
                                  default min(15 * pair capacity, max(32 * total triangles, 4 Mi)); at most
                                  2^31 - 16 */
-    int32_t adjoint;          /* 1: keep the tape lc_batch_adjoint_step needs (implies solver_variant 1) */
+    int32_t adjoint;          /* 1: keep the tape and decision records lc_batch_adjoint_step needs; every step,
+                                 recorded or not, runs on the batch's solver */
 } lc_batch_options;
 
 typedef struct lc_batch lc_batch;
